@@ -1,0 +1,1170 @@
+// Host engine implementation (see engine.h). Kernels are reached only through the C ABI.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <sstream>
+
+namespace gbe
+{
+
+void check(int rc, const char* what)
+    {
+    if (rc != GB_OK)
+        throw std::runtime_error(std::string(what) + ": " + gb_last_error());
+    }
+
+void cuda_check(cudaError_t e, const char* what)
+    {
+    if (e != cudaSuccess)
+        throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+    }
+
+static inline uint32_t f2u(float f)
+    {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+    }
+static inline float u2f(uint32_t u)
+    {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+    }
+
+// ------------------------------------------------------------------------------------------------
+// ParticleData
+// ------------------------------------------------------------------------------------------------
+ParticleData::ParticleData(unsigned int N_, unsigned int ntypes_, unsigned int ndim_,
+                           const std::vector<double>& b6, const std::vector<int>& per)
+    : N(N_), ntypes(ntypes_), ndim(ndim_)
+    {
+    if (b6.size() != 6)
+        throw std::invalid_argument("box must have 6 entries [Lx, Ly, Lz, xy, xz, yz]");
+    if (ntypes == 0)
+        throw std::invalid_argument("at least one particle type is required");
+    for (int d = 0; d < 6; d++)
+        box6[d] = b6[d];
+    for (int d = 0; d < 3; d++)
+        periodic[d] = per.size() == 3 ? per[d] : 1;
+    check(gb_box_make(box6, box6[3], box6[4], box6[5], periodic, &box), "gb_box_make");
+    cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    pos.resize(4 * (size_t)N);
+    vel.resize(4 * (size_t)N);
+    accel.resize(3 * (size_t)N);
+    image.resize(3 * (size_t)N);
+    tag.resize(N);
+    accel.zero(stream);
+    scratch.resize(std::max<size_t>(gb_thermo_scratch_bytes(N), 4096));
+    scratch.zero(stream);
+    }
+
+void ParticleData::set_particles(const double* p, const double* v, const double* m,
+                                 const uint32_t* t, const int32_t* img)
+    {
+    std::vector<float> hp(4 * (size_t)N), hv(4 * (size_t)N);
+    std::vector<int32_t> hi(3 * (size_t)N);
+    std::vector<uint32_t> ht(N);
+    for (unsigned int i = 0; i < N; i++)
+        {
+        if (t[i] >= ntypes)
+            throw std::invalid_argument("typeid out of range");
+        float x = (float)p[3 * i], y = (float)p[3 * i + 1], z = (float)p[3 * i + 2];
+        int ix = img ? img[3 * i] : 0, iy = img ? img[3 * i + 1] : 0, iz = img ? img[3 * i + 2] : 0;
+        // wrap into the box once, as ParticleData::initializeFromSnapshot does (orthorhombic
+        // and triclinic, one image at most)
+        for (int pass = 0; pass < 2; pass++)
+            {
+            if (periodic[2])
+                {
+                if (z >= box.hi[2])
+                    {
+                    z -= box.L[2];
+                    y -= box.L[2] * box.yz;
+                    x -= box.L[2] * box.xz;
+                    iz++;
+                    }
+                else if (z < box.lo[2])
+                    {
+                    z += box.L[2];
+                    y += box.L[2] * box.yz;
+                    x += box.L[2] * box.xz;
+                    iz--;
+                    }
+                }
+            if (periodic[1])
+                {
+                float ty = box.yz * z;
+                if (y >= box.hi[1] + ty)
+                    {
+                    y -= box.L[1];
+                    x -= box.L[1] * box.xy;
+                    iy++;
+                    }
+                else if (y < box.lo[1] + ty)
+                    {
+                    y += box.L[1];
+                    x += box.L[1] * box.xy;
+                    iy--;
+                    }
+                }
+            if (periodic[0])
+                {
+                float tx = (box.xz - box.xy * box.yz) * z + box.xy * y;
+                if (x >= box.hi[0] + tx)
+                    {
+                    x -= box.L[0];
+                    ix++;
+                    }
+                else if (x < box.lo[0] + tx)
+                    {
+                    x += box.L[0];
+                    ix--;
+                    }
+                }
+            }
+        hp[4 * i] = x;
+        hp[4 * i + 1] = y;
+        hp[4 * i + 2] = z;
+        hp[4 * i + 3] = u2f(t[i]);
+        hv[4 * i] = v ? (float)v[3 * i] : 0.0f;
+        hv[4 * i + 1] = v ? (float)v[3 * i + 1] : 0.0f;
+        hv[4 * i + 2] = v ? (float)v[3 * i + 2] : 0.0f;
+        hv[4 * i + 3] = m ? (float)m[i] : 1.0f;
+        hi[3 * i] = ix;
+        hi[3 * i + 1] = iy;
+        hi[3 * i + 2] = iz;
+        ht[i] = i;
+        }
+    pos.upload(hp.data(), hp.size(), stream);
+    vel.upload(hv.data(), hv.size(), stream);
+    image.upload(hi.data(), hi.size(), stream);
+    tag.upload(ht.data(), ht.size(), stream);
+    accel.zero(stream);
+    accel_set = false;
+    cuda_check(cudaStreamSynchronize(stream), "set_particles");
+    }
+
+std::vector<uint32_t> ParticleData::rtag()
+    {
+    std::vector<uint32_t> t(N), r(N);
+    tag.download(t.data(), N, stream);
+    cuda_check(cudaStreamSynchronize(stream), "rtag");
+    for (unsigned int i = 0; i < N; i++)
+        r[t[i]] = i;
+    return r;
+    }
+
+void ParticleData::get_particles(double* p, double* v, double* m, uint32_t* t, int32_t* img)
+    {
+    std::vector<float> hp(4 * (size_t)N), hv(4 * (size_t)N);
+    std::vector<int32_t> hi(3 * (size_t)N);
+    pos.download(hp.data(), hp.size(), stream);
+    vel.download(hv.data(), hv.size(), stream);
+    image.download(hi.data(), hi.size(), stream);
+    std::vector<uint32_t> r = rtag();
+    for (unsigned int tg = 0; tg < N; tg++)
+        {
+        const size_t i = r[tg];
+        if (p)
+            for (int d = 0; d < 3; d++)
+                p[3 * tg + d] = hp[4 * i + d];
+        if (v)
+            for (int d = 0; d < 3; d++)
+                v[3 * tg + d] = hv[4 * i + d];
+        if (m)
+            m[tg] = hv[4 * i + 3];
+        if (t)
+            t[tg] = f2u(hp[4 * i + 3]);
+        if (img)
+            for (int d = 0; d < 3; d++)
+                img[3 * tg + d] = hi[3 * i + d];
+        }
+    }
+
+void ParticleData::thermalize(double kT, uint64_t ts)
+    {
+    check(gb_thermalize(vel.get(), tag.get(), N, kT, ts, seed, ndim, scratch.get(), stream),
+          "gb_thermalize");
+    cuda_check(cudaStreamSynchronize(stream), "thermalize");
+    }
+
+// ------------------------------------------------------------------------------------------------
+// NeighborList (NeighborListGPUBinned + CellListGPU)
+// ------------------------------------------------------------------------------------------------
+NeighborList::NeighborList(std::shared_ptr<ParticleData> pd, double rb)
+    : pdata(std::move(pd)), r_buff((float)rb)
+    {
+    if (rb < 0.0)
+        throw std::invalid_argument("Requested buffer radius is less than zero.");
+    own_rcut.assign(pdata->ntypes * pdata->ntypes, 0.0f);
+    Nmax.assign(pdata->ntypes, 0);
+    cond.resize(3 + 64);
+    }
+
+void NeighborList::set_r_cut(unsigned int i, unsigned int j, double r)
+    {
+    const unsigned int nt = pdata->ntypes;
+    own_rcut[i * nt + j] = own_rcut[j * nt + i] = (float)r;
+    dirty = true;
+    }
+
+void NeighborList::add_consumer(const std::vector<float>* m)
+    {
+    consumers.push_back(m);
+    dirty = true;
+    }
+
+void NeighborList::clear_consumers()
+    {
+    consumers.clear();
+    dirty = true;
+    }
+
+// hoomd/md/NeighborList.cc:452-529
+void NeighborList::update_rlist()
+    {
+    const unsigned int nt = pdata->ntypes;
+    r_cut = own_rcut;
+    for (auto* m : consumers)
+        for (unsigned int k = 0; k < nt * nt; k++)
+            r_cut[k] = std::max(r_cut[k], (*m)[k]);
+    r_listsq.assign(nt * nt, 0.0f);
+    rcut_max.assign(nt, 0.0f);
+    for (unsigned int i = 0; i < nt; i++)
+        {
+        float mx = 0.0f;
+        for (unsigned int j = 0; j < nt; j++)
+            {
+            const float rc = r_cut[i * nt + j];
+            if (rc > mx)
+                mx = rc;
+            volatile float rl = (rc > 0.0f) ? rc + r_buff : 0.0f;
+            r_listsq[i * nt + j] = rl * rl;
+            }
+        rcut_max[i] = mx;
+        }
+    }
+
+void NeighborList::allocate()
+    {
+    ParticleData& pd = *pdata;
+    const unsigned int nt = pd.ntypes;
+    update_rlist();
+    float rmax = 0.0f;
+    for (float v : rcut_max)
+        rmax = std::max(rmax, v);
+    const float width = rmax + r_buff;
+    if (!(width > 0.0f))
+        throw std::runtime_error("Cell: cell width must be non-zero");
+    // NeighborList::checkBoxSize (hoomd/md/NeighborList.cc:535-561)
+    {
+    unsigned int d1[3];
+    check(gb_cell_dims(&pd.box, pd.ndim, 1.0f, d1), "gb_cell_dims");
+    float npd[3];
+    float a = pd.box.xy * pd.box.yz - pd.box.xz;
+    npd[0] = pd.box.L[0] / std::sqrt(1.0f + pd.box.xy * pd.box.xy + a * a);
+    npd[1] = pd.box.L[1] / std::sqrt(1.0f + pd.box.yz * pd.box.yz);
+    npd[2] = pd.box.L[2];
+    for (int d = 0; d < (pd.ndim == 3 ? 3 : 2); d++)
+        if (pd.periodic[d] && npd[d] <= width * 2.0f)
+            {
+            std::ostringstream oss;
+            oss << "nlist: Simulation box is too small, the neighbor list is searching beyond the "
+                   " minimum image: rmax="
+                << width;
+            throw std::runtime_error(oss.str());
+            }
+    }
+    check(gb_cell_dims(&pd.box, pd.ndim, width, dim), "gb_cell_dims");
+    const unsigned int ncell = dim[0] * dim[1] * dim[2];
+    adj.resize(27 * (size_t)ncell);
+    check(gb_cell_adj_build(dim, pd.ndim, adj.get(), &adj_w, pd.stream), "gb_cell_adj_build");
+    // capacities: the reference starts from ceil(N/ncell) and grows on overflow; start with
+    // headroom so that replayed runs rarely roll back
+    const double per_cell = double(pd.N) / ncell;
+    const unsigned int want_cell = (unsigned int)std::ceil(per_cell * 1.6) + 4;
+    if (!capacity_fixed)
+        Nmax_cell = std::max(Nmax_cell, want_cell);
+    const double vol = (pd.ndim == 3) ? double(pd.box.L[0]) * pd.box.L[1] * pd.box.L[2]
+                                      : double(pd.box.L[0]) * pd.box.L[1];
+    const double rho = pd.N / vol;
+    for (unsigned int t = 0; t < nt; t++)
+        {
+        float rl = 0.0f;
+        for (unsigned int j = 0; j < nt; j++)
+            rl = std::max(rl, r_listsq[t * nt + j]);
+        rl = std::sqrt(rl);
+        const double shell = (pd.ndim == 3) ? 4.0 / 3.0 * M_PI * rl * rl * rl : M_PI * rl * rl;
+        unsigned int want = (unsigned int)std::ceil(rho * shell * 1.35) + 8;
+        want = (want + 3) & ~3u;
+        if (!capacity_fixed)
+            Nmax[t] = std::max(Nmax[t], want);
+        }
+    capacity_fixed = false; // a fixed start applies to the first allocation only
+    stride = ((uint64_t)pd.N + 31) / 32 * 32;
+    const unsigned int nmax_all = *std::max_element(Nmax.begin(), Nmax.end());
+    cell_size.resize(ncell);
+    xyzf.resize(4 * (size_t)ncell * Nmax_cell);
+    cell_type.resize(nt > 1 ? (size_t)ncell * Nmax_cell : 0);
+    nlist.resize(std::max<uint64_t>(1, stride * nmax_all));
+    n_neigh.resize(std::max(1u, pd.N));
+    n_neigh.zero(pd.stream);
+    last_pos.resize(4 * (size_t)std::max(1u, pd.N));
+    d_Nmax.resize(nt);
+    d_Nmax.upload(Nmax.data(), nt, pd.stream);
+    d_r_cut.resize(nt * nt);
+    d_r_cut.upload(r_cut.data(), nt * nt, pd.stream);
+    d_r_listsq.resize(nt * nt);
+    d_r_listsq.upload(r_listsq.data(), nt * nt, pd.stream);
+    d_rcut_max.resize(nt);
+    d_rcut_max.upload(rcut_max.data(), nt, pd.stream);
+    cuda_check(cudaStreamSynchronize(pd.stream), "nlist allocate");
+    allocated = true;
+    dirty = false;
+    }
+
+void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count,
+                                 uint32_t* d_cell_cond, uint32_t* d_nl_cond, cudaStream_t s)
+    {
+    ParticleData& pd = *pdata;
+    gb_cell_list_args c {};
+    c.d_pos = pd.pos.get();
+    c.N = pd.N;
+    c.box = pd.box;
+    for (int d = 0; d < 3; d++)
+        c.dim[d] = dim[d];
+    c.Nmax = Nmax_cell;
+    c.d_cell_size = cell_size.get();
+    c.d_xyzf = xyzf.get();
+    c.d_cell_type = pd.ntypes > 1 ? cell_type.get() : nullptr;
+    c.d_conditions = d_cell_cond;
+    c.d_gate = d_gate;
+    c.deterministic = deterministic ? 1 : 0;
+    c.d_build_count = d_build_count;
+    check(gb_cell_list_build(&c, s), "gb_cell_list_build");
+    gb_nlist_args a {};
+    a.d_nlist = nlist.get();
+    a.d_n_neigh = n_neigh.get();
+    a.d_last_pos = last_pos.get();
+    a.d_conditions = d_nl_cond;
+    a.d_head_list = nullptr;
+    a.stride = stride;
+    a.d_Nmax = d_Nmax.get();
+    a.d_pos = pd.pos.get();
+    a.N = pd.N;
+    a.d_cell_size = cell_size.get();
+    a.d_xyzf = xyzf.get();
+    a.d_cell_type = pd.ntypes > 1 ? cell_type.get() : nullptr;
+    a.d_cell_adj = adj.get();
+    for (int d = 0; d < 3; d++)
+        a.dim[d] = dim[d];
+    a.Nmax_cell = Nmax_cell;
+    a.adj_width = adj_w;
+    a.box = pd.box;
+    a.d_r_cut = d_r_cut.get();
+    a.d_r_listsq = d_r_listsq.get();
+    a.ntypes = pd.ntypes;
+    a.d_gate = d_gate;
+    check(gb_nlist_build_binned(&a, s), "gb_nlist_build_binned");
+    }
+
+bool NeighborList::grow(const DevStatus& st)
+    {
+    bool grew = false;
+    if (st.cell_cond[0] > Nmax_cell)
+        {
+        Nmax_cell = st.cell_cond[0] + std::max(4u, st.cell_cond[0] / 8);
+        grew = true;
+        }
+    for (unsigned int t = 0; t < pdata->ntypes; t++)
+        if (st.nl_cond[t] > Nmax[t])
+            {
+            unsigned int want = st.nl_cond[t] + std::max(8u, st.nl_cond[t] / 8);
+            Nmax[t] = (want + 3) & ~3u;
+            grew = true;
+            }
+    if (grew)
+        {
+        allocated = false;
+        allocate();
+        }
+    return grew;
+    }
+
+static std::string tag_message(ParticleData& pd, uint32_t index_plus_one, const char* what)
+    {
+    std::vector<uint32_t> t(pd.N);
+    pd.tag.download(t.data(), pd.N, pd.stream);
+    cuda_check(cudaStreamSynchronize(pd.stream), "tag lookup");
+    std::ostringstream s;
+    s << "Particle with unique tag " << t[index_plus_one - 1] << " " << what;
+    return s.str();
+    }
+
+void NeighborList::build_sync()
+    {
+    ParticleData& pd = *pdata;
+    if (!allocated || dirty)
+        allocate();
+    for (int attempt = 0; attempt < 64; attempt++)
+        {
+        cond.zero(pd.stream);
+        enqueue_build(nullptr, nullptr, cond.get(), cond.get() + 3, pd.stream);
+        DevStatus st {};
+        std::vector<uint32_t> h(3 + 64);
+        cond.download(h.data(), h.size(), pd.stream);
+        cuda_check(cudaStreamSynchronize(pd.stream), "nlist build");
+        if (h[1])
+            throw std::runtime_error(tag_message(pd, h[1], "has NaN for its position."));
+        if (h[2])
+            throw std::runtime_error(tag_message(pd, h[2], "is no longer in the simulation box."));
+        for (int k = 0; k < 3; k++)
+            st.cell_cond[k] = h[k];
+        for (unsigned int t = 0; t < pd.ntypes; t++)
+            st.nl_cond[t] = h[3 + t];
+        if (!grow(st))
+            {
+            n_builds_host++;
+            return;
+            }
+        }
+    throw std::runtime_error("neighbour list build did not converge");
+    }
+
+std::vector<uint32_t> NeighborList::pair_list(bool full)
+    {
+    ParticleData& pd = *pdata;
+    std::vector<uint32_t> nn(pd.N), t(pd.N), nl(nlist.size());
+    n_neigh.download(nn.data(), pd.N, pd.stream);
+    nlist.download(nl.data(), nl.size(), pd.stream);
+    pd.tag.download(t.data(), pd.N, pd.stream);
+    cuda_check(cudaStreamSynchronize(pd.stream), "pair_list");
+    std::vector<uint32_t> out;
+    for (unsigned int i = 0; i < pd.N; i++)
+        for (unsigned int k = 0; k < nn[i]; k++)
+            {
+            uint32_t j = nl[i + (size_t)k * stride];
+            uint32_t a = t[i], b = t[j];
+            if (full || a < b)
+                {
+                out.push_back(a);
+                out.push_back(b);
+                }
+            }
+    return out;
+    }
+
+// ------------------------------------------------------------------------------------------------
+// PairForce (PotentialPair<Evaluator>GPU)
+// ------------------------------------------------------------------------------------------------
+PairForce::PairForce(std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborList> nl,
+                     PairKind k)
+    : pdata(std::move(pd)), nlist(std::move(nl)), kind(k)
+    {
+    ntypes = pdata->ntypes;
+    const unsigned int np = ntypes * ntypes;
+    r_cut.assign(np, 0.0f);
+    r_on.assign(np, 0.0f);
+    lj.assign(np, gb_lj_param {0.0f, 0.0f});
+    ex.assign(np, gb_example_param {0.0f, 0.0f});
+    t_rmin.assign(np, 0.0);
+    t_U.assign(np, std::vector<double>(1, 0.0));
+    t_F.assign(np, std::vector<double>(1, 0.0));
+    force.resize(4 * (size_t)std::max(1u, pdata->N));
+    force.zero(pdata->stream);
+    }
+
+// EvaluatorPairLJ::param_type(sigma, epsilon) at FP32 (hoomd/md/EvaluatorPairLJ.h:125-142)
+void PairForce::set_params_lj(unsigned int i, unsigned int j, double sigma, double epsilon)
+    {
+    const float s = (float)sigma;
+    gb_lj_param p;
+    p.sigma_6 = s * s * s * s * s * s;
+    p.epsilon_x_4 = 4.0f * (float)epsilon;
+    lj[i * ntypes + j] = lj[j * ntypes + i] = p;
+    params_dirty = true;
+    }
+
+void PairForce::set_params_example(unsigned int i, unsigned int j, double k, double sigma)
+    {
+    ex[i * ntypes + j] = ex[j * ntypes + i] = gb_example_param {(float)k, (float)sigma};
+    params_dirty = true;
+    }
+
+void PairForce::set_params_table(unsigned int i, unsigned int j, double r_min,
+                                 const std::vector<double>& U, const std::vector<double>& F)
+    {
+    if (U.size() != F.size())
+        throw std::runtime_error("The length of V and F arrays must be equal.");
+    if (U.empty())
+        throw std::runtime_error("The length of V and F must not be zero.");
+    for (auto idx : {i * ntypes + j, j * ntypes + i})
+        {
+        t_rmin[idx] = r_min;
+        t_U[idx] = U;
+        t_F[idx] = F;
+        }
+    params_dirty = true;
+    }
+
+// PotentialPair::setRCut / setROn (hoomd/md/PotentialPair.h:444-480): r^2 in Scalar.
+void PairForce::set_r_cut(unsigned int i, unsigned int j, double r)
+    {
+    r_cut[i * ntypes + j] = r_cut[j * ntypes + i] = (float)r;
+    params_dirty = true;
+    nlist->dirty = true;
+    }
+
+void PairForce::set_r_on(unsigned int i, unsigned int j, double r)
+    {
+    r_on[i * ntypes + j] = r_on[j * ntypes + i] = (float)r;
+    params_dirty = true;
+    }
+
+void PairForce::upload()
+    {
+    if (!params_dirty)
+        return;
+    cudaStream_t s = pdata->stream;
+    const unsigned int np = ntypes * ntypes;
+    std::vector<float> rc2(np), ro2(np);
+    for (unsigned int k = 0; k < np; k++)
+        {
+        rc2[k] = r_cut[k] * r_cut[k];
+        ro2[k] = r_on[k] * r_on[k];
+        }
+    d_rcutsq.resize(np);
+    d_rcutsq.upload(rc2.data(), np, s);
+    d_ronsq.resize(np);
+    d_ronsq.upload(ro2.data(), np, s);
+    if (kind == PairKind::LJ)
+        {
+        d_params.resize(np * sizeof(gb_lj_param));
+        cuda_check(cudaMemcpyAsync(d_params.get(), lj.data(), np * sizeof(gb_lj_param),
+                                   cudaMemcpyHostToDevice, s),
+                   "params");
+        }
+    else if (kind == PairKind::Example)
+        {
+        d_params.resize(np * sizeof(gb_example_param));
+        cuda_check(cudaMemcpyAsync(d_params.get(), ex.data(), np * sizeof(gb_example_param),
+                                   cudaMemcpyHostToDevice, s),
+                   "params");
+        }
+    else
+        {
+        std::vector<gb_table_param> tp(np);
+        std::vector<float> data;
+        std::map<std::pair<unsigned, unsigned>, uint32_t> seen;
+        for (unsigned int i = 0; i < ntypes; i++)
+            for (unsigned int j = 0; j < ntypes; j++)
+                {
+                const unsigned int a = std::min(i, j), b = std::max(i, j);
+                const unsigned int idx = i * ntypes + j;
+                auto it = seen.find({a, b});
+                uint32_t off;
+                if (it == seen.end())
+                    {
+                    off = (uint32_t)data.size();
+                    for (double v : t_U[idx])
+                        data.push_back((float)v);
+                    for (double v : t_F[idx])
+                        data.push_back((float)v);
+                    seen[{a, b}] = off;
+                    }
+                else
+                    off = it->second;
+                tp[idx] = gb_table_param {(float)t_rmin[idx], (uint32_t)t_U[idx].size(), off, 0u};
+                }
+        d_params.resize(np * sizeof(gb_table_param));
+        cuda_check(cudaMemcpyAsync(d_params.get(), tp.data(), np * sizeof(gb_table_param),
+                                   cudaMemcpyHostToDevice, s),
+                   "params");
+        d_table.resize(data.size());
+        d_table.upload(data.data(), data.size(), s);
+        }
+    cuda_check(cudaStreamSynchronize(s), "pair upload");
+    params_dirty = false;
+    }
+
+gb_pair_args PairForce::pair_args(bool with_virial)
+    {
+    ParticleData& pd = *pdata;
+    NeighborList& nl = *nlist;
+    gb_pair_args a {};
+    a.d_force = force.get();
+    if (with_virial)
+        {
+        virial.resize(6 * (size_t)std::max(1u, pd.N));
+        a.d_virial = virial.get();
+        a.virial_pitch = pd.N;
+        }
+    a.N = pd.N;
+    a.d_pos = pd.pos.get();
+    a.box = pd.box;
+    a.d_n_neigh = nl.n_neigh.get();
+    a.d_nlist = nl.nlist.get();
+    a.d_head_list = nullptr;
+    a.stride = nl.stride;
+    a.d_rcutsq = d_rcutsq.get();
+    a.d_ronsq = d_ronsq.get();
+    a.ntypes = ntypes;
+    a.shift_mode = (unsigned int)shift_mode;
+    a.compute_virial = with_virial ? 1 : 0;
+    return a;
+    }
+
+void PairForce::compute(cudaStream_t s, bool with_virial)
+    {
+    upload();
+    gb_pair_args a = pair_args(with_virial);
+    int rc;
+    if (kind == PairKind::LJ)
+        rc = gb_pair_forces_lj(&a, (const gb_lj_param*)d_params.get(), s);
+    else if (kind == PairKind::Example)
+        rc = gb_pair_forces_example(&a, (const gb_example_param*)d_params.get(), s);
+    else
+        rc = gb_pair_forces_table(&a, (const gb_table_param*)d_params.get(), d_table.get(), s);
+    check(rc, "pair force");
+    virial_valid = with_virial;
+    }
+
+int PairForce::launch_fused(const gb_pair_args& a, const gb_step_fuse& f, cudaStream_t s)
+    {
+    if (kind == PairKind::LJ)
+        return gb_md_pair_step_lj(&a, (const gb_lj_param*)d_params.get(), &f, s);
+    if (kind == PairKind::Example)
+        return gb_md_pair_step_example(&a, (const gb_example_param*)d_params.get(), &f, s);
+    return gb_md_pair_step_table(&a, (const gb_table_param*)d_params.get(), d_table.get(), &f, s);
+    }
+
+// ------------------------------------------------------------------------------------------------
+// Integrator (IntegratorTwoStep + TwoStepConstantVolume + BussiThermostat + ComputeThermo)
+// ------------------------------------------------------------------------------------------------
+Integrator::Integrator(std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborList> nl,
+                       double dt_)
+    : pdata(std::move(pd)), nlist(std::move(nl)), dt(dt_)
+    {
+    d_status.resize(1);
+    d_status.zero(pdata->stream);
+    }
+
+Integrator::~Integrator()
+    {
+    drop_graphs();
+    }
+
+void Integrator::add_force(std::shared_ptr<PairForce> f)
+    {
+    if (f->nlist != nlist)
+        throw std::invalid_argument("all pair forces of one integrator must share its nlist");
+    forces.push_back(std::move(f));
+    prepared = false;
+    drop_graphs();
+    }
+
+void Integrator::set_thermostat_bussi(double kT_, double tau_)
+    {
+    bussi = true;
+    kT = kT_;
+    tau = tau_;
+    prepared = false;
+    drop_graphs();
+    }
+
+void Integrator::set_thermostat_none()
+    {
+    bussi = false;
+    prepared = false;
+    drop_graphs();
+    }
+
+void Integrator::set_sorter(uint64_t period, int bits)
+    {
+    sort_period = period;
+    sort_bits = bits;
+    }
+
+// IntegratorTwoStep::getTranslationalDOF for one momentum-conserving method on all particles
+// (hoomd/md/IntegratorTwoStep.cc:154-199): D*N - D.
+double Integrator::dof() const
+    {
+    return double(pdata->ndim) * pdata->N - double(pdata->ndim);
+    }
+
+DevStatus Integrator::read_status()
+    {
+    DevStatus st;
+    cuda_check(cudaMemcpyAsync(&st, d_status.get(), sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                               pdata->stream),
+               "read status");
+    cuda_check(cudaStreamSynchronize(pdata->stream), "read status");
+    return st;
+    }
+
+void Integrator::drop_graphs()
+    {
+    for (auto& kv : graphs)
+        cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+    }
+
+// IntegratorTwoStep::prepRun (hoomd/md/IntegratorTwoStep.cc:226-298)
+void Integrator::prepare()
+    {
+    ParticleData& pd = *pdata;
+    cudaStream_t s = pd.stream;
+    if (forces.empty())
+        throw std::runtime_error("integrator has no forces");
+    if (pd.N == 0)
+        throw std::runtime_error("Empty integration group.");
+    nlist->clear_consumers();
+    for (auto& f : forces)
+        nlist->add_consumer(&f->r_cut);
+    nlist->build_sync();
+    drop_graphs();
+    for (auto& f : forces)
+        f->compute(s, compute_virial);
+    const float* net = forces[0]->force.get();
+    if (forces.size() > 1)
+        {
+        net_force.resize(4 * (size_t)pd.N);
+        std::vector<const float*> ptrs;
+        for (auto& f : forces)
+            ptrs.push_back(f->force.get());
+        check(gb_sum_net_force(net_force.get(), ptrs.data(), (unsigned)ptrs.size(), pd.N, s),
+              "gb_sum_net_force");
+        net = net_force.get();
+        }
+    if (!pd.accel_set)
+        {
+        // Integrator::computeAccelerations: a = F/m (a half step with dt = 0 leaves v as is)
+        check(gb_cv_step_two(pd.vel.get(), pd.accel.get(), net, pd.N, 0.0f, 1.0f, nullptr, s),
+              "accelerations");
+        pd.accel_set = true;
+        }
+    d_thermo_scratch.resize(gb_thermo_scratch_bytes(pd.N));
+    d_thermo_scratch.zero(s);
+    d_step_scratch.resize(gb_md_step_scratch_bytes(pd.N));
+    d_step_scratch.zero(s);
+    DevStatus st {};
+    st.timestep = pd.timestep;
+    st.n_builds = nlist->n_builds_host;
+    st.factor = 1.0;
+    cuda_check(cudaMemcpyAsync(d_status.get(), &st, sizeof(st), cudaMemcpyHostToDevice, s),
+               "status");
+    DevStatus* ds = d_status.get();
+    check(gb_thermo_reduce(pd.vel.get(), net, nullptr, 0, pd.N, d_thermo_scratch.get(),
+                           ds->thermo, s),
+          "thermo");
+    if (bussi)
+        check(gb_bussi_factor(&ds->thermo[0], dof(), dt, tau, kT, pd.timestep, pd.seed, 0u,
+                              &ds->factor, s),
+              "bussi");
+    DevStatus back = read_status();
+    if (bussi && dof() != 0 && back.thermo[0] == 0.0)
+        throw std::runtime_error("Bussi thermostat requires non-zero initial momenta.");
+    prepared = true;
+    }
+
+void Integrator::enqueue_step_fused(cudaStream_t s)
+    {
+    ParticleData& pd = *pdata;
+    DevStatus* ds = d_status.get();
+    gb_step_one_args o {};
+    o.d_pos = pd.pos.get();
+    o.d_vel = pd.vel.get();
+    o.d_accel = pd.accel.get();
+    o.d_image = pd.image.get();
+    o.N = pd.N;
+    o.box = pd.box;
+    o.dt = (float)dt;
+    o.scale = 1.0f;
+    o.d_scale = bussi ? &ds->factor : nullptr;
+    o.d_last_pos = nlist->last_pos.get();
+    o.d_rcut_max = nlist->d_rcut_max.get();
+    o.r_buff = nlist->r_buff;
+    o.d_rebuild = &ds->rebuild;
+    check(gb_md_step_one(&o, s), "gb_md_step_one");
+    nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
+    PairForce& f = *forces[0];
+    gb_pair_args a = f.pair_args(false);
+    gb_step_fuse fu {};
+    fu.d_vel = pd.vel.get();
+    fu.d_accel = pd.accel.get();
+    fu.dt = (float)dt;
+    fu.d_scale2 = nullptr;
+    fu.d_scratch = d_step_scratch.get();
+    fu.d_thermo = ds->thermo;
+    fu.bussi = bussi ? 1 : 0;
+    fu.dof = dof();
+    fu.tau = tau;
+    fu.kT = kT;
+    fu.seed = pd.seed;
+    fu.instance_id = 0;
+    fu.d_timestep = &ds->timestep;
+    fu.d_factor = &ds->factor;
+    fu.d_status = &ds->status;
+    fu.d_rebuild_reset = &ds->rebuild;
+    check(f.launch_fused(a, fu, s), "fused pair step");
+    }
+
+void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
+    {
+    ParticleData& pd = *pdata;
+    DevStatus* ds = d_status.get();
+    gb_step_one_args o {};
+    o.d_pos = pd.pos.get();
+    o.d_vel = pd.vel.get();
+    o.d_accel = pd.accel.get();
+    o.d_image = pd.image.get();
+    o.N = pd.N;
+    o.box = pd.box;
+    o.dt = (float)dt;
+    o.scale = 1.0f;
+    o.d_scale = bussi ? &ds->factor : nullptr;
+    o.d_last_pos = nlist->last_pos.get();
+    o.d_rcut_max = nlist->d_rcut_max.get();
+    o.r_buff = nlist->r_buff;
+    o.d_rebuild = &ds->rebuild;
+    check(gb_md_step_one(&o, s), "gb_md_step_one");
+    nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
+    for (auto& f : forces)
+        f->compute(s, compute_virial);
+    const float* net = forces[0]->force.get();
+    if (forces.size() > 1)
+        {
+        std::vector<const float*> ptrs;
+        for (auto& f : forces)
+            ptrs.push_back(f->force.get());
+        check(gb_sum_net_force(net_force.get(), ptrs.data(), (unsigned)ptrs.size(), pd.N, s),
+              "gb_sum_net_force");
+        net = net_force.get();
+        }
+    check(gb_cv_step_two(pd.vel.get(), pd.accel.get(), net, pd.N, (float)dt, 1.0f, nullptr, s),
+          "gb_cv_step_two");
+    check(gb_thermo_reduce(pd.vel.get(), net, nullptr, 0, pd.N, d_thermo_scratch.get(),
+                           ds->thermo, s),
+          "thermo");
+    if (bussi)
+        check(gb_bussi_factor(&ds->thermo[0], dof(), dt, tau, kT, step + 1, pd.seed, 0u,
+                              &ds->factor, s),
+              "bussi");
+    cuda_check(cudaMemsetAsync(&ds->rebuild, 0, sizeof(uint32_t), s), "reset rebuild");
+    }
+
+cudaGraphExec_t Integrator::graph_for(unsigned int k)
+    {
+    auto it = graphs.find(k);
+    if (it != graphs.end())
+        return it->second;
+    cudaStream_t s = pdata->stream;
+    cudaGraph_t g;
+    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    try
+        {
+        for (unsigned int i = 0; i < k; i++)
+            enqueue_step_fused(s);
+        }
+    catch (...)
+        {
+        cudaStreamEndCapture(s, &g);
+        throw;
+        }
+    cuda_check(cudaStreamEndCapture(s, &g), "end capture");
+    cudaGraphExec_t exec;
+    cuda_check(cudaGraphInstantiate(&exec, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    graphs[k] = exec;
+    return exec;
+    }
+
+void Integrator::checkpoint()
+    {
+    cudaStream_t s = pdata->stream;
+    ck_pos.copy_from(pdata->pos, s);
+    ck_vel.copy_from(pdata->vel, s);
+    ck_accel.copy_from(pdata->accel, s);
+    ck_image.copy_from(pdata->image, s);
+    ck_status.copy_from(d_status, s);
+    }
+
+void Integrator::restore()
+    {
+    cudaStream_t s = pdata->stream;
+    pdata->pos.copy_from(ck_pos, s);
+    pdata->vel.copy_from(ck_vel, s);
+    pdata->accel.copy_from(ck_accel, s);
+    pdata->image.copy_from(ck_image, s);
+    d_status.copy_from(ck_status, s);
+    }
+
+void Integrator::run_chunk(unsigned int k)
+    {
+    ParticleData& pd = *pdata;
+    cudaStream_t s = pd.stream;
+    const bool fused = forces.size() == 1 && !compute_virial;
+    for (int attempt = 0; attempt < 16; attempt++)
+        {
+        checkpoint();
+        DevStatus* ds = d_status.get();
+        cuda_check(cudaMemsetAsync(ds->cell_cond, 0, sizeof(ds->cell_cond), s), "zero cond");
+        cuda_check(cudaMemsetAsync(ds->nl_cond, 0, sizeof(ds->nl_cond), s), "zero cond");
+        cuda_check(cudaMemsetAsync(&ds->status, 0, sizeof(uint32_t), s), "zero status");
+        const uint64_t cell_kernels = nlist->deterministic ? 3 : 2;
+        if (fused && use_graph)
+            {
+            cuda_check(cudaGraphLaunch(graph_for(k), s), "graph launch");
+            launch_count += (uint64_t)k * (1 + cell_kernels + 1 + 1);
+            }
+        else if (fused)
+            {
+            for (unsigned int i = 0; i < k; i++)
+                enqueue_step_fused(s);
+            launch_count += (uint64_t)k * (1 + cell_kernels + 1 + 1);
+            }
+        else
+            {
+            if (forces.size() > 1)
+                net_force.resize(4 * (size_t)pd.N);
+            for (unsigned int i = 0; i < k; i++)
+                enqueue_step_general(s, pd.timestep + i);
+            launch_count += (uint64_t)k
+                            * (1 + cell_kernels + 1 + forces.size() + (forces.size() > 1 ? 1 : 0)
+                               + 2 + (bussi ? 1 : 0));
+            }
+        DevStatus st = read_status();
+        if (st.cell_cond[1])
+            throw std::runtime_error(tag_message(pd, st.cell_cond[1], "has NaN for its position."));
+        if (st.cell_cond[2])
+            throw std::runtime_error(
+                tag_message(pd, st.cell_cond[2], "is no longer in the simulation box."));
+        bool overflow = st.cell_cond[0] > nlist->Nmax_cell;
+        for (unsigned int t = 0; t < pd.ntypes; t++)
+            overflow = overflow || st.nl_cond[t] > nlist->Nmax[t];
+        if (overflow)
+            {
+            restore();
+            nlist->grow(st);
+            drop_graphs();
+            nlist->build_sync();
+            n_rollbacks++;
+            continue;
+            }
+        if (st.status & 1u)
+            throw std::runtime_error("Bussi thermostat requires non-zero initial momenta.");
+        pd.timestep += k;
+        steps_run += k;
+        if (!fused)
+            {
+            uint64_t ts = pd.timestep;
+            cuda_check(cudaMemcpyAsync(&ds->timestep, &ts, sizeof(ts), cudaMemcpyHostToDevice, s),
+                       "timestep");
+            cuda_check(cudaStreamSynchronize(s), "timestep");
+            }
+        return;
+        }
+    throw std::runtime_error("run: repeated neighbour-list overflow");
+    }
+
+// SFCPackTuner::update (hoomd/SFCPackTuner.cc:81-118): order, gather every per-particle array,
+// then force a neighbour-list rebuild (the reference's notifyParticleSort).
+void Integrator::sort_particles()
+    {
+    ParticleData& pd = *pdata;
+    cudaStream_t s = pd.stream;
+    const size_t need = gb_sfc_scratch_bytes(pd.N, sort_bits);
+    if (pd.scratch.size() < need + 4 * (size_t)pd.N + 256)
+        {
+        pd.scratch.resize(need + 4 * (size_t)pd.N + 256);
+        pd.scratch.zero(s);
+        }
+    uint32_t* order = reinterpret_cast<uint32_t*>(pd.scratch.get() + need);
+    check(gb_sfc_order(pd.pos.get(), pd.N, &pd.box, sort_bits, order, pd.scratch.get(), need, s),
+          "gb_sfc_order");
+    pd.alt.resize(4 * (size_t)pd.N);
+    auto apply = [&](void* arr, unsigned int bytes) {
+        check(gb_gather(pd.alt.get(), arr, order, pd.N, bytes, s), "gb_gather");
+        cuda_check(cudaMemcpyAsync(arr, pd.alt.get(), (size_t)bytes * pd.N,
+                                   cudaMemcpyDeviceToDevice, s),
+                   "sort copy");
+    };
+    apply(pd.pos.get(), 16);
+    apply(pd.vel.get(), 16);
+    apply(pd.accel.get(), 12);
+    apply(pd.image.get(), 12);
+    apply(pd.tag.get(), 4);
+    for (auto& f : forces)
+        {
+        apply(f->force.get(), 16);
+        f->virial_valid = false;
+        }
+    // the old scratch counter words may have been overwritten: re-zero the thermo scratch
+    pd.scratch.zero(s);
+    pd.sort_generation++;
+    nlist->build_sync();
+    DevStatus* ds = d_status.get();
+    uint64_t nb = 0;
+    cuda_check(cudaMemcpyAsync(&nb, &ds->n_builds, sizeof(nb), cudaMemcpyDeviceToHost, s), "nb");
+    cuda_check(cudaStreamSynchronize(s), "sort");
+    nb += 1;
+    cuda_check(cudaMemcpyAsync(&ds->n_builds, &nb, sizeof(nb), cudaMemcpyHostToDevice, s), "nb");
+    cuda_check(cudaStreamSynchronize(s), "sort");
+    }
+
+void Integrator::run(uint64_t nsteps)
+    {
+    ParticleData& pd = *pdata;
+    if (!prepared || nlist->dirty)
+        prepare();
+    for (auto& f : forces)
+        if (f->params_dirty)
+            {
+            f->upload();
+            drop_graphs();
+            }
+    uint64_t done = 0;
+    while (done < nsteps)
+        {
+        if (sort_period && pd.timestep % sort_period == 0)
+            sort_particles();
+        uint64_t k = std::min<uint64_t>(nsteps - done, chunk);
+        if (sort_period)
+            {
+            const uint64_t to_sort = sort_period - (pd.timestep % sort_period);
+            k = std::min(k, to_sort);
+            }
+        run_chunk((unsigned int)k);
+        done += k;
+        }
+    }
+
+double Integrator::sum_n_neigh()
+    {
+    ParticleData& pd = *pdata;
+    std::vector<uint32_t> h(pd.N);
+    nlist->n_neigh.download(h.data(), pd.N, pd.stream);
+    cuda_check(cudaStreamSynchronize(pd.stream), "n_neigh");
+    double s = 0;
+    for (uint32_t v : h)
+        s += v;
+    return s;
+    }
+
+std::vector<double> Integrator::time_phases(unsigned int reps)
+    {
+    ParticleData& pd = *pdata;
+    cudaStream_t s = pd.stream;
+    if (!prepared || nlist->dirty)
+        prepare();
+    if (forces.size() != 1)
+        throw std::runtime_error("time_phases: one pair force (the fused path) required");
+    checkpoint();
+    cudaEvent_t ev[4];
+    for (auto& e : ev)
+        cuda_check(cudaEventCreate(&e), "event");
+    std::vector<double> acc(3, 0.0);
+    DevStatus* ds = d_status.get();
+    for (unsigned int r = 0; r < reps; r++)
+        {
+        gb_step_one_args o {};
+        o.d_pos = pd.pos.get();
+        o.d_vel = pd.vel.get();
+        o.d_accel = pd.accel.get();
+        o.d_image = pd.image.get();
+        o.N = pd.N;
+        o.box = pd.box;
+        o.dt = (float)dt;
+        o.scale = 1.0f;
+        o.d_scale = bussi ? &ds->factor : nullptr;
+        o.d_last_pos = nlist->last_pos.get();
+        o.d_rcut_max = nlist->d_rcut_max.get();
+        o.r_buff = nlist->r_buff;
+        o.d_rebuild = &ds->rebuild;
+        cuda_check(cudaEventRecord(ev[0], s), "record");
+        check(gb_md_step_one(&o, s), "gb_md_step_one");
+        cuda_check(cudaEventRecord(ev[1], s), "record");
+        // time a real rebuild: open the gate (outside the timed interval)
+        uint32_t one = 1;
+        cuda_check(cudaMemcpyAsync(&ds->rebuild, &one, sizeof(one), cudaMemcpyHostToDevice, s),
+                   "gate");
+        cuda_check(cudaMemsetAsync(ds->cell_cond, 0, sizeof(ds->cell_cond), s), "cond");
+        cuda_check(cudaMemsetAsync(ds->nl_cond, 0, sizeof(ds->nl_cond), s), "cond");
+        cuda_check(cudaEventRecord(ev[2], s), "record");
+        nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
+        cuda_check(cudaEventRecord(ev[3], s), "record");
+        cuda_check(cudaEventSynchronize(ev[3]), "sync");
+        float t01, t23;
+        cudaEventElapsedTime(&t01, ev[0], ev[1]);
+        cudaEventElapsedTime(&t23, ev[2], ev[3]);
+        PairForce& f = *forces[0];
+        gb_pair_args a = f.pair_args(false);
+        gb_step_fuse fu {};
+        fu.d_vel = pd.vel.get();
+        fu.d_accel = pd.accel.get();
+        fu.dt = (float)dt;
+        fu.d_scratch = d_step_scratch.get();
+        fu.d_thermo = ds->thermo;
+        fu.bussi = bussi ? 1 : 0;
+        fu.dof = dof();
+        fu.tau = tau;
+        fu.kT = kT;
+        fu.seed = pd.seed;
+        fu.d_timestep = &ds->timestep;
+        fu.d_factor = &ds->factor;
+        fu.d_status = &ds->status;
+        fu.d_rebuild_reset = &ds->rebuild;
+        cuda_check(cudaEventRecord(ev[0], s), "record");
+        check(f.launch_fused(a, fu, s), "fused pair step");
+        cuda_check(cudaEventRecord(ev[1], s), "record");
+        cuda_check(cudaEventSynchronize(ev[1]), "sync");
+        float t_pair;
+        cudaEventElapsedTime(&t_pair, ev[0], ev[1]);
+        acc[0] += t01;
+        acc[1] += t23;
+        acc[2] += t_pair;
+        }
+    for (auto& e : ev)
+        cudaEventDestroy(e);
+    for (auto& v : acc)
+        v /= reps;
+    restore();
+    nlist->build_sync();
+    cuda_check(cudaStreamSynchronize(s), "time_phases");
+    return acc;
+    }
+
+std::vector<double> Integrator::thermo(bool with_virial)
+    {
+    ParticleData& pd = *pdata;
+    cudaStream_t s = pd.stream;
+    if (!prepared)
+        prepare();
+    if (with_virial)
+        for (auto& f : forces)
+            if (!f->virial_valid)
+                f->compute(s, true);
+    d_thermo_scratch.resize(gb_thermo_scratch_bytes(pd.N));
+    DeviceArray<double> out;
+    out.resize(3);
+    double ke = 0, pe = 0, w = 0;
+    for (size_t k = 0; k < forces.size(); k++)
+        {
+        PairForce& f = *forces[k];
+        check(gb_thermo_reduce(pd.vel.get(), f.force.get(), with_virial ? f.virial.get() : nullptr,
+                               pd.N, pd.N, d_thermo_scratch.get(), out.get(), s),
+              "thermo");
+        double h[3];
+        out.download(h, 3, s);
+        cuda_check(cudaStreamSynchronize(s), "thermo");
+        ke = h[0];
+        pe += h[1];
+        w += h[2];
+        }
+    return {ke, pe, w};
+    }
+
+} // namespace gbe

@@ -1,0 +1,293 @@
+// Host engine: the C++ operation classes of the short-range MD step on one GPU.
+//
+// These mirror the reference's host classes (ParticleData/SystemDefinition,
+// NeighborListGPUBinned + CellListGPU, PotentialPair<Evaluator>GPU, IntegratorTwoStep +
+// TwoStepConstantVolumeGPU + BussiThermostat + ComputeThermoGPU, SFCPackTunerGPU). They own the
+// device arrays (plain cudaMalloc buffers, the role GlobalArray plays in the reference) and
+// launch work only through the C ABI of include/hoomd_gb300.h.
+//
+// Differences from the reference's control flow, all invisible to the physics:
+//  * no host synchronisation per step: the rebuild decision, the overflow conditions and the
+//    Bussi factor live on the device; runs of steps are captured into a CUDA graph and replayed;
+//  * overflow of the cell list or neighbour list inside a replayed run is detected after the run
+//    from the device condition words; the state is then restored from a checkpoint taken before
+//    the run, capacities grow (with headroom) and the run is repeated. The reference instead
+//    re-runs the build immediately (hoomd/md/NeighborList.cc:412-427), which needs a host read
+//    after every build.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "hoomd_gb300.h"
+
+namespace gbe
+{
+
+void check(int rc, const char* what);
+void cuda_check(cudaError_t e, const char* what);
+
+template<class T> class DeviceArray
+    {
+    public:
+    DeviceArray() = default;
+    DeviceArray(const DeviceArray&) = delete;
+    DeviceArray& operator=(const DeviceArray&) = delete;
+    ~DeviceArray()
+        {
+        release();
+        }
+    void resize(size_t n)
+        {
+        if (n == m_n)
+            return;
+        release();
+        if (n)
+            cuda_check(cudaMalloc((void**)&m_ptr, n * sizeof(T)), "cudaMalloc");
+        m_n = n;
+        }
+    void release()
+        {
+        if (m_ptr)
+            cudaFree(m_ptr);
+        m_ptr = nullptr;
+        m_n = 0;
+        }
+    T* get() const
+        {
+        return m_ptr;
+        }
+    size_t size() const
+        {
+        return m_n;
+        }
+    size_t bytes() const
+        {
+        return m_n * sizeof(T);
+        }
+    void upload(const T* h, size_t n, cudaStream_t s)
+        {
+        if (n > m_n)
+            throw std::runtime_error("DeviceArray::upload: too many elements");
+        if (n)
+            cuda_check(cudaMemcpyAsync(m_ptr, h, n * sizeof(T), cudaMemcpyHostToDevice, s),
+                       "upload");
+        }
+    void download(T* h, size_t n, cudaStream_t s) const
+        {
+        if (n > m_n)
+            throw std::runtime_error("DeviceArray::download: too many elements");
+        if (n)
+            cuda_check(cudaMemcpyAsync(h, m_ptr, n * sizeof(T), cudaMemcpyDeviceToHost, s),
+                       "download");
+        }
+    void zero(cudaStream_t s)
+        {
+        if (m_n)
+            cuda_check(cudaMemsetAsync(m_ptr, 0, m_n * sizeof(T), s), "memset");
+        }
+    void copy_from(const DeviceArray& o, cudaStream_t s)
+        {
+        resize(o.m_n);
+        if (m_n)
+            cuda_check(cudaMemcpyAsync(m_ptr, o.m_ptr, m_n * sizeof(T), cudaMemcpyDeviceToDevice, s),
+                       "d2d copy");
+        }
+
+    private:
+    T* m_ptr = nullptr;
+    size_t m_n = 0;
+    };
+
+// Device-resident control block: one D2H copy per replayed run reads all of it.
+struct DevStatus
+    {
+    uint32_t cell_cond[3]; // needed Nmax, NaN index+1, out-of-box index+1
+    uint32_t rebuild;      // rebuild gate for the current step
+    uint32_t status;       // bit 0: Bussi with zero kinetic energy
+    uint32_t pad[3];
+    uint64_t timestep;
+    uint64_t n_builds;
+    double factor;         // Bussi rescale factor for the next step one
+    double thermo[3];      // KE, PE, W after the last step
+    uint32_t nl_cond[64];  // per-type neighbours needed on overflow
+    };
+
+class ParticleData
+    {
+    public:
+    ParticleData(unsigned int N, unsigned int ntypes, unsigned int ndim,
+                 const std::vector<double>& box6, const std::vector<int>& periodic);
+    // host arrays in tag order: pos xyz (3N), vel xyz (3N), mass (N), typeid (N), image (3N)
+    void set_particles(const double* pos, const double* vel, const double* mass,
+                       const uint32_t* typeid_, const int32_t* image);
+    void get_particles(double* pos, double* vel, double* mass, uint32_t* typeid_,
+                       int32_t* image);
+    std::vector<uint32_t> rtag(); // tag -> index
+    void thermalize(double kT, uint64_t timestep);
+
+    unsigned int N, ntypes, ndim;
+    double box6[6];
+    int periodic[3];
+    gb_box box;
+    uint16_t seed = 0;
+    uint64_t timestep = 0;
+    bool accel_set = false;
+    cudaStream_t stream = nullptr;
+    DeviceArray<float> pos, vel, accel, alt;
+    DeviceArray<int32_t> image;
+    DeviceArray<uint32_t> tag;
+    DeviceArray<char> scratch;
+    uint64_t sort_generation = 0;
+    };
+
+class NeighborList
+    {
+    public:
+    NeighborList(std::shared_ptr<ParticleData> pdata, double r_buff);
+    void set_r_cut(unsigned int i, unsigned int j, double r); // the nlist's own r_cut matrix
+    void add_consumer(const std::vector<float>* rcut_matrix);
+    void clear_consumers();
+    void update_rlist();        // NeighborList::updateRList
+    void allocate();            // cell grid, adjacency, capacities
+    void build_sync();          // forced build with host-side overflow retry
+    void enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count, uint32_t* d_cell_cond,
+                       uint32_t* d_nl_cond, cudaStream_t s);
+    bool grow(const DevStatus& st); // returns true when a capacity grew
+    std::vector<uint32_t> pair_list(bool full); // tag pairs, for tests
+    std::vector<uint32_t> dims() const
+        {
+        return {dim[0], dim[1], dim[2]};
+        }
+
+    std::shared_ptr<ParticleData> pdata;
+    float r_buff;
+    bool deterministic = false;
+    unsigned int rebuild_check_delay = 1;
+    bool check_dist = true;
+    std::vector<float> own_rcut;
+    std::vector<const std::vector<float>*> consumers;
+    std::vector<float> r_cut, r_listsq, rcut_max;
+    unsigned int dim[3] = {0, 0, 0};
+    unsigned int adj_w = 0, Nmax_cell = 0;
+    std::vector<uint32_t> Nmax;
+    uint64_t stride = 0;
+    uint64_t n_builds_host = 0;
+    bool allocated = false;
+    bool dirty = true; // r_cut or capacities changed: graphs must be rebuilt
+    bool capacity_fixed = false; // start from exactly Nmax_cell / Nmax (tests of the growth path)
+    DeviceArray<float> d_r_cut, d_r_listsq, d_rcut_max, xyzf, last_pos;
+    DeviceArray<uint32_t> cell_size, cell_type, adj, nlist, n_neigh, d_Nmax, cond;
+    };
+
+enum class PairKind
+    {
+    LJ = 0,
+    Table = 1,
+    Example = 2
+    };
+
+class PairForce
+    {
+    public:
+    PairForce(std::shared_ptr<ParticleData> pdata, std::shared_ptr<NeighborList> nlist,
+              PairKind kind);
+    void set_params_lj(unsigned int i, unsigned int j, double sigma, double epsilon);
+    void set_params_example(unsigned int i, unsigned int j, double k, double sigma);
+    void set_params_table(unsigned int i, unsigned int j, double r_min,
+                          const std::vector<double>& U, const std::vector<double>& F);
+    void set_r_cut(unsigned int i, unsigned int j, double r);
+    void set_r_on(unsigned int i, unsigned int j, double r);
+    void upload();
+    void compute(cudaStream_t s, bool virial);
+    int launch_fused(const gb_pair_args& a, const gb_step_fuse& f, cudaStream_t s);
+    gb_pair_args pair_args(bool virial);
+
+    std::shared_ptr<ParticleData> pdata;
+    std::shared_ptr<NeighborList> nlist;
+    PairKind kind;
+    int shift_mode = 0;
+    unsigned int ntypes;
+    std::vector<float> r_cut, r_on;
+    std::vector<gb_lj_param> lj;
+    std::vector<gb_example_param> ex;
+    std::vector<double> t_rmin;
+    std::vector<std::vector<double>> t_U, t_F;
+    bool params_dirty = true;
+    DeviceArray<char> d_params;
+    DeviceArray<float> d_rcutsq, d_ronsq, d_table, force, virial;
+    bool virial_valid = false;
+    };
+
+class Integrator
+    {
+    public:
+    Integrator(std::shared_ptr<ParticleData> pdata, std::shared_ptr<NeighborList> nlist,
+               double dt);
+    ~Integrator();
+    void add_force(std::shared_ptr<PairForce> f);
+    void set_thermostat_bussi(double kT, double tau);
+    void set_thermostat_none();
+    void set_sorter(uint64_t period, int grid_bits);
+    void set_chunk(unsigned int steps)
+        {
+        chunk = steps ? steps : 1;
+        }
+    void prepare();
+    void run(uint64_t nsteps);
+    std::vector<double> thermo(bool with_virial); // KE, PE, W (W only when with_virial)
+    double dof() const;
+    DevStatus read_status();
+
+    std::shared_ptr<ParticleData> pdata;
+    std::shared_ptr<NeighborList> nlist;
+    std::vector<std::shared_ptr<PairForce>> forces;
+    double dt;
+    bool bussi = false;
+    double kT = 1.0, tau = 0.0;
+    uint64_t sort_period = 0;
+    int sort_bits = 8;
+    unsigned int chunk = 50;
+    bool use_graph = true;
+    bool compute_virial = false;
+    bool prepared = false;
+    uint64_t n_rollbacks = 0;
+    uint64_t steps_run = 0;
+    uint64_t launch_count = 0; // kernels this engine launched (graph replays included)
+    // average device time (ms) of each phase of one fused step, launched outside the graph on
+    // the engine's stream with CUDA events: [step one + rebuild check, cell list + neighbour
+    // list build, fused pair step]; the state is checkpointed before and restored after
+    std::vector<double> time_phases(unsigned int reps);
+    uintptr_t stream_handle() const
+        {
+        return (uintptr_t)pdata->stream;
+        }
+    double sum_n_neigh();
+
+    private:
+    void sort_particles();
+    void enqueue_step_fused(cudaStream_t s);
+    void enqueue_step_general(cudaStream_t s, uint64_t step);
+    void run_chunk(unsigned int k);
+    void checkpoint();
+    void restore();
+    cudaGraphExec_t graph_for(unsigned int k);
+    void drop_graphs();
+
+    DeviceArray<DevStatus> d_status;
+    DeviceArray<char> d_step_scratch, d_thermo_scratch;
+    DeviceArray<float> net_force;
+    DeviceArray<float> ck_pos, ck_vel, ck_accel;
+    DeviceArray<int32_t> ck_image;
+    DeviceArray<DevStatus> ck_status;
+    std::map<unsigned int, cudaGraphExec_t> graphs;
+    uint64_t graph_sort_generation = ~0ull;
+    };
+
+} // namespace gbe

@@ -1,0 +1,386 @@
+// Integrator halves, thermodynamic reductions, Bussi factor and momentum thermalisation.
+//
+// The half steps use explicit round-to-nearest intrinsics in the order of the reference's CPU
+// path (hoomd/md/TwoStepConstantVolume.cc:7-80, 213-261), so one step is bit-identical to the
+// FP32 oracle. Reductions widen every per-particle term to double and sum in a fixed order.
+#include <cstdint>
+
+#include "fused_step.h"
+#include "gb_device.cuh"
+#include "gb_host.h"
+#include "rng.cuh"
+
+namespace gb
+{
+namespace
+{
+struct StepOneCheck
+    {
+    const float4* last_pos;
+    const float* rcut_max;
+    float r_buff;
+    uint32_t* rebuild;
+    };
+
+template<bool CHECK>
+__global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
+                           const float* __restrict__ accel, int* __restrict__ image,
+                           unsigned int N, gb_box box, float dt, float scale,
+                           const double* __restrict__ d_scale, StepOneCheck chk)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    bool moved = false;
+    if (j < N)
+        {
+        const float s = d_scale ? (float)*d_scale : scale;
+        float4 v = vel[j];
+        float4 p = pos[j];
+        const float ax = accel[3 * (size_t)j], ay = accel[3 * (size_t)j + 1],
+                    az = accel[3 * (size_t)j + 2];
+        // v = v + (1/2) a dt ; v *= s ; x += dt v   (TwoStepConstantVolume.cc:37-55)
+        v.x = fadd(v.x, fmul(fmul(0.5f, ax), dt));
+        v.y = fadd(v.y, fmul(fmul(0.5f, ay), dt));
+        v.z = fadd(v.z, fmul(fmul(0.5f, az), dt));
+        v.x = fmul(v.x, s);
+        v.y = fmul(v.y, s);
+        v.z = fmul(v.z, s);
+        p.x = fadd(p.x, fmul(dt, v.x));
+        p.y = fadd(p.y, fmul(dt, v.y));
+        p.z = fadd(p.z, fmul(dt, v.z));
+        int ix = 0, iy = 0, iz = 0;
+        wrap(box, p.x, p.y, p.z, ix, iy, iz);
+        if (ix | iy | iz)
+            {
+            image[3 * (size_t)j] += ix;
+            image[3 * (size_t)j + 1] += iy;
+            image[3 * (size_t)j + 2] += iz;
+            }
+        vel[j] = v;
+        pos[j] = p;
+        if (CHECK)
+            {
+            // hoomd/md/NeighborListGPU.cu:42-83 with lambda = 1 (fixed box)
+            const float4 lp = chk.last_pos[j];
+            float dx = fsub(p.x, lp.x), dy = fsub(p.y, lp.y), dz = fsub(p.z, lp.z);
+            min_image(box, dx, dy, dz);
+            const float rmin = chk.rcut_max[__float_as_uint(p.w)];
+            const float rmax = fadd(rmin, chk.r_buff);
+            const float delta_max = fmul(fsub(rmax, rmin), 0.5f);
+            const float maxsq = (delta_max > 0.0f) ? fmul(delta_max, delta_max) : 0.0f;
+            moved = dot3(dx, dy, dz) >= maxsq;
+            }
+        }
+    if (CHECK && __any_sync(0xffffffffu, moved) && (threadIdx.x % 32) == 0)
+        *chk.rebuild = 1u;
+    }
+
+__global__ void k_step_two(float4* __restrict__ vel, float* __restrict__ accel,
+                           const float4* __restrict__ net_force, unsigned int N, float dt,
+                           float scale, const double* __restrict__ d_scale)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N)
+        return;
+    const float s = d_scale ? (float)*d_scale : scale;
+    float4 v = vel[j];
+    const float4 f = net_force[j];
+    const float minv = __frcp_rn(v.w);
+    const float ax = fmul(f.x, minv), ay = fmul(f.y, minv), az = fmul(f.z, minv);
+    v.x = fmul(v.x, s);
+    v.y = fmul(v.y, s);
+    v.z = fmul(v.z, s);
+    const float hdt = fmul(0.5f, dt);
+    v.x = fadd(v.x, fmul(hdt, ax));
+    v.y = fadd(v.y, fmul(hdt, ay));
+    v.z = fadd(v.z, fmul(hdt, az));
+    vel[j] = v;
+    accel[3 * (size_t)j] = ax;
+    accel[3 * (size_t)j + 1] = ay;
+    accel[3 * (size_t)j + 2] = az;
+    }
+
+// Block sum of three doubles; result valid in thread 0.
+__device__ inline void block_sum3(double& a, double& b, double& c)
+    {
+    __shared__ double s[3][32];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    c = warp_sum(c);
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+    if (lane == 0)
+        {
+        s[0][warp] = a;
+        s[1][warp] = b;
+        s[2][warp] = c;
+        }
+    __syncthreads();
+    if (warp == 0)
+        {
+        const int nw = blockDim.x / 32;
+        a = lane < nw ? s[0][lane] : 0.0;
+        b = lane < nw ? s[1][lane] : 0.0;
+        c = lane < nw ? s[2][lane] : 0.0;
+        a = warp_sum(a);
+        b = warp_sum(b);
+        c = warp_sum(c);
+        }
+    __syncthreads();
+    }
+
+// Last-block-done reduction: partials[3*block + k]; returns true in the last block, whose
+// thread 0 then holds the totals in a, b, c.
+__device__ inline bool reduce3_last(double& a, double& b, double& c, unsigned int* counter,
+                                    double* partials)
+    {
+    __shared__ bool s_last;
+    block_sum3(a, b, c);
+    if (threadIdx.x == 0)
+        {
+        partials[3 * blockIdx.x] = a;
+        partials[3 * blockIdx.x + 1] = b;
+        partials[3 * blockIdx.x + 2] = c;
+        __threadfence();
+        s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+        }
+    __syncthreads();
+    if (!s_last)
+        return false;
+    __threadfence();
+    a = b = c = 0.0;
+    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x)
+        {
+        a += __ldcg(partials + 3 * k);
+        b += __ldcg(partials + 3 * k + 1);
+        c += __ldcg(partials + 3 * k + 2);
+        }
+    block_sum3(a, b, c);
+    if (threadIdx.x == 0)
+        *counter = 0;
+    return true;
+    }
+
+__global__ void k_thermo(const float4* __restrict__ vel, const float4* __restrict__ force,
+                         const float* __restrict__ virial, size_t pitch, unsigned int N,
+                         unsigned int* counter, double* partials, double* out)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double ke = 0.0, pe = 0.0, w = 0.0;
+    if (j < N)
+        {
+        const float4 v = vel[j];
+        ke = (double)v.w * ((double)v.x * (double)v.x + (double)v.y * (double)v.y
+                            + (double)v.z * (double)v.z);
+        if (force)
+            pe = (double)force[j].w;
+        if (virial)
+            w = (double)virial[j] + (double)virial[3 * pitch + j] + (double)virial[5 * pitch + j];
+        }
+    if (reduce3_last(ke, pe, w, counter, partials) && threadIdx.x == 0)
+        {
+        out[0] = 0.5 * ke;
+        out[1] = pe;
+        out[2] = w / 3.0;
+        }
+    }
+
+__global__ void k_bussi(const double* d_ke, double dof, double dt, double tau, double kT,
+                        uint64_t timestep, uint16_t seed, uint32_t instance_id, double* d_factor)
+    {
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        *d_factor = bussi_factor_d(*d_ke, dof, dt, tau, kT, timestep, seed, instance_id);
+    }
+
+// hoomd/ParticleGroup.cc:719-746: velocities from NormalDistribution<float>(sqrt(kT/m)) with
+// key Seed(35, timestep, seed) and counter = tag; momentum summed in double.
+__global__ void k_thermalize_draw(float4* __restrict__ vel, const uint32_t* __restrict__ tag,
+                                  unsigned int N, float kT, uint64_t timestep, uint16_t seed,
+                                  unsigned int ndim, unsigned int* counter, double* partials,
+                                  double* total)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double px = 0.0, py = 0.0, pz = 0.0;
+    if (j < N)
+        {
+        Philox rng(35, timestep, seed, tag[j]);
+        float4 v = vel[j];
+        const float sigma = sqrtf(kT / v.w);
+        v.x = normal_f(rng) * sigma + 0.0f;
+        v.y = normal_f(rng) * sigma + 0.0f;
+        v.z = (ndim > 2) ? normal_f(rng) * sigma + 0.0f : 0.0f;
+        vel[j] = v;
+        px = (double)v.w * v.x;
+        py = (double)v.w * v.y;
+        pz = (double)v.w * v.z;
+        }
+    if (reduce3_last(px, py, pz, counter, partials) && threadIdx.x == 0)
+        {
+        total[0] = px;
+        total[1] = py;
+        total[2] = pz;
+        }
+    }
+
+__global__ void k_thermalize_shift(float4* __restrict__ vel, unsigned int N, unsigned int ndim,
+                                   const double* __restrict__ total)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N)
+        return;
+    const float cx = (float)(total[0] / N), cy = (float)(total[1] / N),
+                cz = (float)(total[2] / N);
+    float4 v = vel[j];
+    v.x = v.x - cx / v.w;
+    v.y = v.y - cy / v.w;
+    if (ndim > 2)
+        v.z = v.z - cz / v.w;
+    vel[j] = v;
+    }
+struct ForcePtrs
+    {
+    const float4* f[8];
+    };
+
+__global__ void k_sum_net_force(float4* __restrict__ net, ForcePtrs fp, unsigned int nf,
+                                unsigned int N)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N)
+        return;
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (unsigned int k = 0; k < nf; k++)
+        {
+        const float4 v = fp.f[k][j];
+        s.x += v.x;
+        s.y += v.y;
+        s.z += v.z;
+        s.w += v.w;
+        }
+    net[j] = s;
+    }
+} // namespace
+} // namespace gb
+
+using namespace gb;
+
+extern "C"
+    {
+    int gb_cv_step_one(float* d_pos, float* d_vel, const float* d_accel, int* d_image,
+                       unsigned int N, const gb_box* box, float dt, float scale,
+                       const double* d_scale, void* stream)
+        {
+        GB_REQUIRE(box && (N == 0 || (d_pos && d_vel && d_accel && d_image)),
+                   "gb_cv_step_one: null argument");
+        if (N == 0)
+            return GB_OK;
+        StepOneCheck none {nullptr, nullptr, 0.0f, nullptr};
+        k_step_one<false><<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
+            reinterpret_cast<float4*>(d_pos), reinterpret_cast<float4*>(d_vel), d_accel, d_image,
+            N, *box, dt, scale, d_scale, none);
+        return check_launch("gb_cv_step_one");
+        }
+
+    int gb_md_step_one(const gb_step_one_args* a, void* stream)
+        {
+        GB_REQUIRE(a, "gb_md_step_one: null args");
+        GB_REQUIRE(a->N == 0 || (a->d_pos && a->d_vel && a->d_accel && a->d_image),
+                   "gb_md_step_one: null particle array");
+        GB_REQUIRE(!a->d_last_pos || (a->d_rcut_max && a->d_rebuild),
+                   "gb_md_step_one: rebuild check needs r_cut max and a flag");
+        if (a->N == 0)
+            return GB_OK;
+        StepOneCheck chk {reinterpret_cast<const float4*>(a->d_last_pos), a->d_rcut_max,
+                          a->r_buff, a->d_rebuild};
+        cudaStream_t s = (cudaStream_t)stream;
+        if (a->d_last_pos)
+            k_step_one<true><<<div_up(a->N, 256), 256, 0, s>>>(
+                reinterpret_cast<float4*>(a->d_pos), reinterpret_cast<float4*>(a->d_vel),
+                a->d_accel, a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk);
+        else
+            k_step_one<false><<<div_up(a->N, 256), 256, 0, s>>>(
+                reinterpret_cast<float4*>(a->d_pos), reinterpret_cast<float4*>(a->d_vel),
+                a->d_accel, a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk);
+        return check_launch("gb_md_step_one");
+        }
+
+    int gb_cv_step_two(float* d_vel, float* d_accel, const float* d_net_force, unsigned int N,
+                       float dt, float scale, const double* d_scale, void* stream)
+        {
+        GB_REQUIRE(N == 0 || (d_vel && d_accel && d_net_force), "gb_cv_step_two: null argument");
+        if (N == 0)
+            return GB_OK;
+        k_step_two<<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
+            reinterpret_cast<float4*>(d_vel), d_accel, reinterpret_cast<const float4*>(d_net_force),
+            N, dt, scale, d_scale);
+        return check_launch("gb_cv_step_two");
+        }
+
+    int gb_sum_net_force(float* d_net, const float* const* h_force_ptrs, unsigned int n_forces,
+                         unsigned int N, void* stream)
+        {
+        GB_REQUIRE(d_net && h_force_ptrs, "gb_sum_net_force: null argument");
+        GB_REQUIRE(n_forces >= 1 && n_forces <= 8, "gb_sum_net_force: 1 <= n_forces <= 8");
+        if (N == 0)
+            return GB_OK;
+        ForcePtrs fp {};
+        for (unsigned int k = 0; k < n_forces; k++)
+            {
+            GB_REQUIRE(h_force_ptrs[k], "gb_sum_net_force: null force array");
+            fp.f[k] = reinterpret_cast<const float4*>(h_force_ptrs[k]);
+            }
+        k_sum_net_force<<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
+            reinterpret_cast<float4*>(d_net), fp, n_forces, N);
+        return check_launch("gb_sum_net_force");
+        }
+
+    size_t gb_thermo_scratch_bytes(unsigned int N)
+        {
+        return 256 + 3 * sizeof(double) * (size_t)div_up(N > 0 ? N : 1, 256);
+        }
+
+    size_t gb_md_step_scratch_bytes(unsigned int N)
+        {
+        return step_scratch_bytes(N);
+        }
+
+    int gb_thermo_reduce(const float* d_vel, const float* d_force, const float* d_virial,
+                         size_t virial_pitch, unsigned int N, void* d_scratch, double* d_out,
+                         void* stream)
+        {
+        GB_REQUIRE(d_vel && d_scratch && d_out, "gb_thermo_reduce: null argument");
+        GB_REQUIRE(!d_virial || virial_pitch >= N, "gb_thermo_reduce: virial pitch < N");
+        const unsigned int nb = div_up(N > 0 ? N : 1, 256);
+        k_thermo<<<nb, 256, 0, (cudaStream_t)stream>>>(
+            reinterpret_cast<const float4*>(d_vel), reinterpret_cast<const float4*>(d_force),
+            d_virial, virial_pitch, N, reinterpret_cast<unsigned int*>(d_scratch),
+            reinterpret_cast<double*>(reinterpret_cast<char*>(d_scratch) + 256), d_out);
+        return check_launch("gb_thermo_reduce");
+        }
+
+    int gb_bussi_factor(const double* d_ke, double dof, double dt, double tau, double kT,
+                        uint64_t timestep, uint16_t seed, uint32_t instance_id, double* d_factor,
+                        void* stream)
+        {
+        GB_REQUIRE(d_ke && d_factor, "gb_bussi_factor: null argument");
+        k_bussi<<<1, 32, 0, (cudaStream_t)stream>>>(d_ke, dof, dt, tau, kT, timestep, seed,
+                                                     instance_id, d_factor);
+        return check_launch("gb_bussi_factor");
+        }
+
+    int gb_thermalize(float* d_vel, const uint32_t* d_tag, unsigned int N, double kT,
+                      uint64_t timestep, uint16_t seed, unsigned int ndim, void* d_scratch,
+                      void* stream)
+        {
+        GB_REQUIRE(d_vel && d_tag && d_scratch, "gb_thermalize: null argument");
+        if (N == 0)
+            return GB_OK;
+        cudaStream_t s = (cudaStream_t)stream;
+        const unsigned int nb = div_up(N, 256);
+        unsigned int* counter = reinterpret_cast<unsigned int*>(d_scratch);
+        double* total = reinterpret_cast<double*>(reinterpret_cast<char*>(d_scratch) + 64);
+        double* partials = reinterpret_cast<double*>(reinterpret_cast<char*>(d_scratch) + 256);
+        k_thermalize_draw<<<nb, 256, 0, s>>>(reinterpret_cast<float4*>(d_vel), d_tag, N, (float)kT,
+                                             timestep, seed, ndim, counter, partials, total);
+        k_thermalize_shift<<<nb, 256, 0, s>>>(reinterpret_cast<float4*>(d_vel), N, ndim, total);
+        return check_launch("gb_thermalize");
+        }
+    }

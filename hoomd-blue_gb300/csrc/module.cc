@@ -1,0 +1,234 @@
+// pybind11 module _hoomd_gb300: the host engine classes under the names of the reference's
+// C++ classes that the Python layer looks up (hoomd/md/pair/pair.py:126-146,
+// hoomd/md/nlist.py:390-397, hoomd/md/integrate.py:287-293).
+#include <pybind11/numpy.h>
+#include <pybind11/pybind11.h>
+#include <pybind11/stl.h>
+
+#include "engine.h"
+
+namespace py = pybind11;
+using namespace gbe;
+
+namespace
+{
+template<class T> py::array_t<T> make_array(std::vector<size_t> shape)
+    {
+    return py::array_t<T>(shape);
+    }
+
+// Per-particle float4 (or 6 x pitch) device array -> numpy in tag order.
+py::array_t<double> force_by_tag(PairForce& f, int what)
+    {
+    ParticleData& pd = *f.pdata;
+    const unsigned int N = pd.N;
+    std::vector<uint32_t> r = pd.rtag();
+    if (what == 2)
+        {
+        if (!f.virial_valid)
+            f.compute(pd.stream, true);
+        std::vector<float> h(6 * (size_t)N);
+        f.virial.download(h.data(), h.size(), pd.stream);
+        cuda_check(cudaStreamSynchronize(pd.stream), "virials");
+        auto out = make_array<double>({N, 6});
+        auto o = out.mutable_unchecked<2>();
+        for (unsigned int t = 0; t < N; t++)
+            for (int k = 0; k < 6; k++)
+                o(t, k) = h[(size_t)k * N + r[t]];
+        return out;
+        }
+    std::vector<float> h(4 * (size_t)N);
+    f.force.download(h.data(), h.size(), pd.stream);
+    cuda_check(cudaStreamSynchronize(pd.stream), "forces");
+    if (what == 0)
+        {
+        auto out = make_array<double>({N, 3});
+        auto o = out.mutable_unchecked<2>();
+        for (unsigned int t = 0; t < N; t++)
+            for (int k = 0; k < 3; k++)
+                o(t, k) = h[4 * (size_t)r[t] + k];
+        return out;
+        }
+    auto out = make_array<double>({N});
+    auto o = out.mutable_unchecked<1>();
+    for (unsigned int t = 0; t < N; t++)
+        o(t) = h[4 * (size_t)r[t] + 3];
+    return out;
+    }
+} // namespace
+
+PYBIND11_MODULE(_hoomd_gb300, m)
+    {
+    m.doc() = "GB300-native short-range MD engine (host classes over the C ABI)";
+    m.def("version", []() { return gb_version(); });
+
+    py::class_<ParticleData, std::shared_ptr<ParticleData>>(m, "ParticleData")
+        .def(py::init<unsigned int, unsigned int, unsigned int, std::vector<double>,
+                      std::vector<int>>())
+        .def("setParticles",
+             [](ParticleData& pd, py::array_t<double, py::array::c_style | py::array::forcecast> pos,
+                py::array_t<double, py::array::c_style | py::array::forcecast> vel,
+                py::array_t<double, py::array::c_style | py::array::forcecast> mass,
+                py::array_t<uint32_t, py::array::c_style | py::array::forcecast> typeid_,
+                py::array_t<int32_t, py::array::c_style | py::array::forcecast> image) {
+                 const size_t N = pd.N;
+                 if ((size_t)pos.size() != 3 * N || (size_t)vel.size() != 3 * N
+                     || (size_t)mass.size() != N || (size_t)typeid_.size() != N
+                     || (size_t)image.size() != 3 * N)
+                     throw std::invalid_argument("particle array sizes do not match N");
+                 pd.set_particles(pos.data(), vel.data(), mass.data(), typeid_.data(),
+                                  image.data());
+             })
+        .def("getParticles",
+             [](ParticleData& pd) {
+                 const size_t N = pd.N;
+                 auto pos = make_array<double>({N, 3});
+                 auto vel = make_array<double>({N, 3});
+                 auto mass = make_array<double>({N});
+                 auto tid = make_array<uint32_t>({N});
+                 auto img = make_array<int32_t>({N, 3});
+                 pd.get_particles(pos.mutable_data(), vel.mutable_data(), mass.mutable_data(),
+                                  tid.mutable_data(), img.mutable_data());
+                 py::dict d;
+                 d["position"] = pos;
+                 d["velocity"] = vel;
+                 d["mass"] = mass;
+                 d["typeid"] = tid;
+                 d["image"] = img;
+                 return d;
+             })
+        .def("thermalize", &ParticleData::thermalize)
+        .def_readwrite("seed", &ParticleData::seed)
+        .def_readwrite("timestep", &ParticleData::timestep)
+        .def_readonly("N", &ParticleData::N)
+        .def_readonly("ntypes", &ParticleData::ntypes)
+        .def_readonly("ndim", &ParticleData::ndim)
+        .def_readonly("sort_generation", &ParticleData::sort_generation)
+        .def("getBox",
+             [](ParticleData& pd) {
+                 return std::vector<double>(pd.box6, pd.box6 + 6);
+             });
+
+    py::class_<NeighborList, std::shared_ptr<NeighborList>>(m, "NeighborListGPUBinned")
+        .def(py::init<std::shared_ptr<ParticleData>, double>())
+        .def("setRCut", &NeighborList::set_r_cut)
+        .def_property(
+            "deterministic", [](NeighborList& n) { return n.deterministic; },
+            [](NeighborList& n, bool v) {
+                n.deterministic = v;
+                n.dirty = true;
+            })
+        .def_property(
+            "r_buff", [](NeighborList& n) { return n.r_buff; },
+            [](NeighborList& n, double v) {
+                if (v < 0)
+                    throw std::invalid_argument("Requested buffer radius is less than zero.");
+                n.r_buff = (float)v;
+                n.dirty = true;
+            })
+        .def_readwrite("check_dist", &NeighborList::check_dist)
+        .def_readwrite("rebuild_check_delay", &NeighborList::rebuild_check_delay)
+        .def("getDim", &NeighborList::dims)
+        .def("getNmax", [](NeighborList& n) { return n.Nmax_cell; })
+        .def("getNmaxPerType", [](NeighborList& n) { return n.Nmax; })
+        .def("getRList", [](NeighborList& n) { return n.r_listsq; })
+        .def("getPairList",
+             [](NeighborList& n, bool full) {
+                 std::vector<uint32_t> v = n.pair_list(full);
+                 auto out = make_array<uint32_t>({v.size() / 2, 2});
+                 std::copy(v.begin(), v.end(), out.mutable_data());
+                 return out;
+             })
+        .def("getNNeigh",
+             [](NeighborList& n) {
+                 ParticleData& pd = *n.pdata;
+                 std::vector<uint32_t> h(pd.N);
+                 n.n_neigh.download(h.data(), pd.N, pd.stream);
+                 std::vector<uint32_t> r = pd.rtag();
+                 auto out = make_array<uint32_t>({(size_t)pd.N});
+                 auto o = out.mutable_unchecked<1>();
+                 for (unsigned int t = 0; t < pd.N; t++)
+                     o(t) = h[r[t]];
+                 return out;
+             })
+        .def("buildNow", &NeighborList::build_sync)
+        .def("setStartCapacity",
+             [](NeighborList& n, unsigned int cell, std::vector<uint32_t> per_type) {
+                 if (per_type.size() != n.pdata->ntypes)
+                     throw std::invalid_argument("one capacity per particle type");
+                 n.Nmax_cell = cell;
+                 n.Nmax = per_type;
+                 n.capacity_fixed = true;
+                 n.allocated = false;
+                 n.dirty = true;
+             });
+
+    py::enum_<PairKind>(m, "PairKind")
+        .value("LJ", PairKind::LJ)
+        .value("Table", PairKind::Table)
+        .value("Example", PairKind::Example);
+
+    py::class_<PairForce, std::shared_ptr<PairForce>>(m, "PotentialPairGPU")
+        .def(py::init<std::shared_ptr<ParticleData>, std::shared_ptr<NeighborList>, PairKind>())
+        .def("setParamsLJ", &PairForce::set_params_lj)
+        .def("setParamsExample", &PairForce::set_params_example)
+        .def("setParamsTable", &PairForce::set_params_table)
+        .def("setRCut", &PairForce::set_r_cut)
+        .def("setROn", &PairForce::set_r_on)
+        .def_property(
+            "mode", [](PairForce& f) { return f.shift_mode; },
+            [](PairForce& f, int v) {
+                if (v < 0 || v > 2)
+                    throw std::invalid_argument("mode must be 0 (none), 1 (shift) or 2 (xplor)");
+                f.shift_mode = v;
+                f.params_dirty = true;
+            })
+        .def("compute",
+             [](PairForce& f, bool virial) {
+                 f.nlist->build_sync();
+                 f.compute(f.pdata->stream, virial);
+                 cuda_check(cudaStreamSynchronize(f.pdata->stream), "compute");
+             })
+        .def("getForces", [](PairForce& f) { return force_by_tag(f, 0); })
+        .def("getEnergies", [](PairForce& f) { return force_by_tag(f, 1); })
+        .def("getVirials", [](PairForce& f) { return force_by_tag(f, 2); });
+
+    py::class_<Integrator, std::shared_ptr<Integrator>>(m, "IntegratorTwoStep")
+        .def(py::init<std::shared_ptr<ParticleData>, std::shared_ptr<NeighborList>, double>())
+        .def("addForce", &Integrator::add_force)
+        .def("setBussi", &Integrator::set_thermostat_bussi)
+        .def("setNoThermostat", &Integrator::set_thermostat_none)
+        .def("setSorter", &Integrator::set_sorter)
+        .def("setChunk", &Integrator::set_chunk)
+        .def_readwrite("use_graph", &Integrator::use_graph)
+        .def_readwrite("compute_virial", &Integrator::compute_virial)
+        .def_readonly("n_rollbacks", &Integrator::n_rollbacks)
+        .def_readonly("steps_run", &Integrator::steps_run)
+        .def_readonly("launch_count", &Integrator::launch_count)
+        .def("timePhases", &Integrator::time_phases)
+        .def("streamHandle", &Integrator::stream_handle)
+        .def("sumNNeigh", &Integrator::sum_n_neigh)
+        .def_property(
+            "dt", [](Integrator& i) { return i.dt; },
+            [](Integrator& i, double v) {
+                i.dt = v;
+                i.prepared = false; // prepare() drops the captured graphs
+            })
+        .def("prepRun", &Integrator::prepare)
+        .def("run", &Integrator::run, py::call_guard<py::gil_scoped_release>())
+        .def("thermo", &Integrator::thermo)
+        .def("dof", &Integrator::dof)
+        .def("status",
+             [](Integrator& i) {
+                 DevStatus st = i.read_status();
+                 py::dict d;
+                 d["timestep"] = st.timestep;
+                 d["n_builds"] = st.n_builds;
+                 d["factor"] = st.factor;
+                 d["kinetic_energy"] = st.thermo[0];
+                 d["potential_energy"] = st.thermo[1];
+                 return d;
+             })
+        .def("synchronize",
+             [](Integrator& i) { cuda_check(cudaStreamSynchronize(i.pdata->stream), "sync"); });
+    }

@@ -1,0 +1,389 @@
+// The pair-force kernel template (PotentialPair<Evaluator> on GB300) and its launcher.
+//
+// Replaces gpu_compute_pair_forces_shared_kernel (hoomd/md/PotentialPairGPU.cuh:140-404).
+// Layouts: with a column-major neighbour list (head(i) = i, stride >= N) one thread owns one
+// particle and neighbour k of 32 consecutive particles is one 128-byte load, so the index stream
+// -- the dominant HBM traffic -- is read exactly once, coalesced, with no shuffle reductions.
+// With the reference's flat head-list layout, groups of TPP threads share a particle and reduce
+// with warp shuffles, as the reference does. Per-pair parameters, r_cut^2 and r_on^2 are staged
+// in shared memory when there is more than one type and held in registers otherwise.
+//
+// FUSE adds the integrator's second half step and the FP64 thermodynamic reductions to the
+// epilogue (TwoStepConstantVolume step two, hoomd/md/TwoStepConstantVolumeGPU.cu:166-205; thermo,
+// hoomd/md/ComputeThermo.cc:76-290): the force never makes a round trip through HBM before it is
+// used, and the last block to finish reduces the per-block partial sums in a fixed order and
+// draws the Bussi factor for the next step on the device (no host synchronisation per step).
+#pragma once
+
+#include <cstdint>
+
+#include "evaluators.cuh"
+#include "gb_device.cuh"
+#include "gb_host.h"
+#include "rng.cuh"
+
+namespace gb
+{
+
+// Epilogue state for the fused step (device pointers are caller-owned).
+struct FuseArgs
+    {
+    float4* vel;            // float4[N] in/out
+    float* accel;           // float3[N] out
+    float dt;
+    const double* d_scale2; // step-two rescale factor (NULL = 1)
+    double* partials;       // [3 * gridDim.x] scratch
+    unsigned int* counter;  // zero before the launch; left zero
+    double* out;            // [3]: KE, PE, W
+    int bussi;              // draw the factor for the next step into d_factor
+    double dof, tau, kT, dt_d;
+    uint16_t seed;
+    uint32_t instance_id;
+    uint64_t* d_timestep;   // current step; advanced by one by the last block
+    double* d_factor;
+    uint32_t* d_status;     // bit 0: Bussi with zero kinetic energy
+    uint32_t* d_rebuild_reset;
+    };
+
+template<int TPP> __device__ __forceinline__ double block_sum_d(double v, double* s_red)
+    {
+    v = warp_sum(v);
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+    if (lane == 0)
+        s_red[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (warp == 0)
+        {
+        const int nw = blockDim.x / 32;
+        r = (lane < nw) ? s_red[lane] : 0.0;
+        r = warp_sum(r);
+        }
+    __syncthreads();
+    return r; // valid in thread 0
+    }
+
+__device__ inline void fuse_finish(const FuseArgs& fz, double ke, double pe, double w)
+    {
+    __shared__ double s_red[32];
+    __shared__ bool s_last;
+    ke = block_sum_d<1>(ke, s_red);
+    pe = block_sum_d<1>(pe, s_red);
+    w = block_sum_d<1>(w, s_red);
+    if (threadIdx.x == 0)
+        {
+        fz.partials[3 * blockIdx.x + 0] = ke;
+        fz.partials[3 * blockIdx.x + 1] = pe;
+        fz.partials[3 * blockIdx.x + 2] = w;
+        __threadfence();
+        const unsigned int done = atomicAdd(fz.counter, 1u);
+        s_last = (done == gridDim.x - 1);
+        }
+    __syncthreads();
+    if (!s_last)
+        return;
+    __threadfence();
+    // last block: fixed-order reduction of the partials (deterministic)
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x)
+        {
+        a += __ldcg(fz.partials + 3 * k + 0);
+        b += __ldcg(fz.partials + 3 * k + 1);
+        c += __ldcg(fz.partials + 3 * k + 2);
+        }
+    a = block_sum_d<1>(a, s_red);
+    b = block_sum_d<1>(b, s_red);
+    c = block_sum_d<1>(c, s_red);
+    if (threadIdx.x == 0)
+        {
+        const double K = 0.5 * a;
+        fz.out[0] = K;
+        fz.out[1] = b;
+        fz.out[2] = c / 3.0;
+        if (fz.bussi)
+            {
+            const uint64_t next = *fz.d_timestep + 1;
+            if (K <= 0.0)
+                {
+                atomicOr(fz.d_status, 1u);
+                *fz.d_factor = 1.0;
+                }
+            else
+                *fz.d_factor = bussi_factor_d(K, fz.dof, fz.dt_d, fz.tau, fz.kT, next, fz.seed,
+                                              fz.instance_id);
+            }
+        if (fz.d_timestep)
+            *fz.d_timestep += 1;
+        if (fz.d_rebuild_reset)
+            *fz.d_rebuild_reset = 0u;
+        *fz.counter = 0;
+        }
+    }
+
+// Template parameters select the data path (evaluator, threads per particle, layout, type
+// tables, fused epilogue); shift mode, virial and box shape are uniform runtime branches.
+template<class Eval, int TPP, bool FLAT, bool MULTI, bool FUSE>
+__global__ void __launch_bounds__(256)
+    k_pair(float4* __restrict__ d_force, float* __restrict__ d_virial, size_t pitch,
+           unsigned int N, const float4* __restrict__ d_pos, gb_box box,
+           const unsigned int* __restrict__ d_n_neigh, const unsigned int* __restrict__ d_nlist,
+           const uint64_t* __restrict__ d_head_list, uint64_t stride,
+           const typename Eval::param_type* __restrict__ d_params,
+           const float* __restrict__ d_rcutsq, const float* __restrict__ d_ronsq,
+           unsigned int ntypes, const float* __restrict__ ext, int SHIFT, bool VIRIAL,
+           bool ORTHO, FuseArgs fz)
+    {
+    using P = typename Eval::param_type;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    P* s_params = reinterpret_cast<P*>(s_raw);
+    const unsigned int np = ntypes * ntypes;
+    float* s_rcutsq = reinterpret_cast<float*>(s_raw + sizeof(P) * np);
+    float* s_ronsq = s_rcutsq + np;
+    if (MULTI)
+        {
+        for (unsigned int t = threadIdx.x; t < np; t += blockDim.x)
+            {
+            s_params[t] = d_params[t];
+            s_rcutsq[t] = d_rcutsq[t];
+            if (SHIFT == 2)
+                s_ronsq[t] = d_ronsq[t];
+            }
+        __syncthreads();
+        }
+    P p0;
+    float rc0 = 0.0f, ro0 = 0.0f;
+    if (!MULTI)
+        {
+        p0 = d_params[0];
+        rc0 = d_rcutsq[0];
+        if (SHIFT == 2)
+            ro0 = d_ronsq[0];
+        }
+
+    const unsigned int gi = blockIdx.x * (blockDim.x / TPP) + threadIdx.x / TPP;
+    const unsigned int lane = threadIdx.x % TPP;
+    const bool active = gi < N;
+
+    float fx = 0.f, fy = 0.f, fz_ = 0.f, pe = 0.f;
+    float vxx = 0.f, vxy = 0.f, vxz = 0.f, vyy = 0.f, vyz = 0.f, vzz = 0.f;
+    float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active)
+        {
+        const unsigned int nn = d_n_neigh[gi];
+        pi = __ldg(d_pos + gi);
+        const unsigned int ti = __float_as_uint(pi.w);
+        const uint64_t head = FLAT ? d_head_list[gi] : (uint64_t)gi;
+        const uint64_t step = FLAT ? 1ull : stride;
+        auto pair = [&](unsigned int j) {
+            const float4 pj = __ldg(d_pos + j);
+            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            if (ORTHO)
+                min_image_ortho(box, dx, dy, dz);
+            else
+                min_image(box, dx, dy, dz);
+            const float rsq = dx * dx + dy * dy + dz * dz;
+            const P* param;
+            float rcutsq, ronsq = 0.0f;
+            if (MULTI)
+                {
+                const unsigned int tp = ti * ntypes + __float_as_uint(pj.w);
+                param = s_params + tp;
+                rcutsq = s_rcutsq[tp];
+                if (SHIFT == 2)
+                    ronsq = s_ronsq[tp];
+                }
+            else
+                {
+                param = &p0;
+                rcutsq = rc0;
+                ronsq = ro0;
+                }
+            bool energy_shift = (SHIFT == 1) || (SHIFT == 2 && ronsq > rcutsq);
+            float force_divr = 0.0f, pair_eng = 0.0f;
+            Eval eval(rsq, rcutsq, *param, ext);
+            eval.evalForceAndEnergy(force_divr, pair_eng, energy_shift);
+            if (SHIFT == 2)
+                {
+                if (rsq >= ronsq && rsq < rcutsq)
+                    {
+                    // XPLOR smoothing (hoomd/md/PotentialPairGPU.cuh:318-338)
+                    const float old_pair_eng = pair_eng;
+                    const float old_force_divr = force_divr;
+                    const float xplor_denom_inv
+                        = 1.0f / ((rcutsq - ronsq) * (rcutsq - ronsq) * (rcutsq - ronsq));
+                    const float rsq_minus_r_cut_sq = rsq - rcutsq;
+                    const float s = rsq_minus_r_cut_sq * rsq_minus_r_cut_sq
+                                    * (rcutsq + 2.0f * rsq - 3.0f * ronsq) * xplor_denom_inv;
+                    const float ds_dr_divr
+                        = 12.0f * (rsq - ronsq) * rsq_minus_r_cut_sq * xplor_denom_inv;
+                    pair_eng = old_pair_eng * s;
+                    force_divr = s * old_force_divr - ds_dr_divr * old_pair_eng;
+                    }
+                }
+            if (VIRIAL)
+                {
+                const float force_div2r = 0.5f * force_divr;
+                vxx += dx * dx * force_div2r;
+                vxy += dx * dy * force_div2r;
+                vxz += dx * dz * force_div2r;
+                vyy += dy * dy * force_div2r;
+                vyz += dy * dz * force_div2r;
+                vzz += dz * dz * force_div2r;
+                }
+            fx += dx * force_divr;
+            fy += dy * force_divr;
+            fz_ += dz * force_divr;
+            pe += pair_eng;
+        };
+        unsigned int k = lane;
+        // four independent index loads and gathers in flight per thread
+        for (; k + 3 * TPP < nn; k += 4 * TPP)
+            {
+            const unsigned int j0 = __ldg(d_nlist + head + (uint64_t)k * step);
+            const unsigned int j1 = __ldg(d_nlist + head + (uint64_t)(k + TPP) * step);
+            const unsigned int j2 = __ldg(d_nlist + head + (uint64_t)(k + 2 * TPP) * step);
+            const unsigned int j3 = __ldg(d_nlist + head + (uint64_t)(k + 3 * TPP) * step);
+            pair(j0);
+            pair(j1);
+            pair(j2);
+            pair(j3);
+            }
+        for (; k < nn; k += TPP)
+            pair(__ldg(d_nlist + head + (uint64_t)k * step));
+        pe *= 0.5f;
+        }
+    if (TPP > 1)
+        {
+        fx = group_sum<TPP>(fx);
+        fy = group_sum<TPP>(fy);
+        fz_ = group_sum<TPP>(fz_);
+        pe = group_sum<TPP>(pe);
+        if (VIRIAL)
+            {
+            vxx = group_sum<TPP>(vxx);
+            vxy = group_sum<TPP>(vxy);
+            vxz = group_sum<TPP>(vxz);
+            vyy = group_sum<TPP>(vyy);
+            vyz = group_sum<TPP>(vyz);
+            vzz = group_sum<TPP>(vzz);
+            }
+        }
+    double ke_d = 0.0, pe_d = 0.0, w_d = 0.0;
+    if (active && lane == 0)
+        {
+        d_force[gi] = make_float4(fx, fy, fz_, pe);
+        if (VIRIAL)
+            {
+            d_virial[0 * pitch + gi] = vxx;
+            d_virial[1 * pitch + gi] = vxy;
+            d_virial[2 * pitch + gi] = vxz;
+            d_virial[3 * pitch + gi] = vyy;
+            d_virial[4 * pitch + gi] = vyz;
+            d_virial[5 * pitch + gi] = vzz;
+            w_d = (double)vxx + (double)vyy + (double)vzz;
+            }
+        if (FUSE)
+            {
+            // step two: a = F/m, v = v*s + dt/2 * a (TwoStepConstantVolume.cc:213-261 order)
+            float4 v = fz.vel[gi];
+            const float minv = __frcp_rn(v.w);
+            const float ax = __fmul_rn(fx, minv), ay = __fmul_rn(fy, minv),
+                        az = __fmul_rn(fz_, minv);
+            const float s2 = fz.d_scale2 ? (float)*fz.d_scale2 : 1.0f;
+            const float hdt = __fmul_rn(0.5f, fz.dt);
+            v.x = __fadd_rn(__fmul_rn(v.x, s2), __fmul_rn(hdt, ax));
+            v.y = __fadd_rn(__fmul_rn(v.y, s2), __fmul_rn(hdt, ay));
+            v.z = __fadd_rn(__fmul_rn(v.z, s2), __fmul_rn(hdt, az));
+            fz.vel[gi] = v;
+            fz.accel[3 * (size_t)gi + 0] = ax;
+            fz.accel[3 * (size_t)gi + 1] = ay;
+            fz.accel[3 * (size_t)gi + 2] = az;
+            ke_d = (double)v.w
+                   * ((double)v.x * (double)v.x + (double)v.y * (double)v.y
+                      + (double)v.z * (double)v.z);
+            pe_d = (double)pe;
+            }
+        }
+    if (FUSE)
+        fuse_finish(fz, ke_d, pe_d, w_d);
+    }
+
+template<class Eval, int TPP, bool FLAT, bool MULTI, bool FUSE>
+int launch_pair_inst(const gb_pair_args& a, const typename Eval::param_type* d_params,
+                     const float* ext, const FuseArgs& fz, unsigned int block,
+                     cudaStream_t s)
+    {
+    const unsigned int per_block = block / TPP;
+    const unsigned int grid = div_up(a.N, per_block);
+    size_t smem = 0;
+    if (MULTI)
+        smem = (sizeof(typename Eval::param_type) + 2 * sizeof(float)) * a.ntypes * a.ntypes;
+    auto kern = k_pair<Eval, TPP, FLAT, MULTI, FUSE>;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const bool ortho = a.box.xy == 0.0f && a.box.xz == 0.0f && a.box.yz == 0.0f;
+    kern<<<grid, block, smem, s>>>(reinterpret_cast<float4*>(a.d_force), a.d_virial,
+                                   a.virial_pitch, a.N, reinterpret_cast<const float4*>(a.d_pos),
+                                   a.box, a.d_n_neigh, a.d_nlist, a.d_head_list, a.stride,
+                                   d_params, a.d_rcutsq, a.d_ronsq, a.ntypes, ext,
+                                   (int)a.shift_mode, a.compute_virial != 0, ortho, fz);
+    return check_launch("pair force kernel");
+    }
+
+template<class Eval, int TPP, bool FLAT, bool FUSE>
+int dispatch_pair_flags(const gb_pair_args& a, const typename Eval::param_type* d_params,
+                        const float* ext, const FuseArgs& fz, unsigned int block,
+                        cudaStream_t s)
+    {
+    GB_REQUIRE(a.shift_mode <= 2, "pair force: shift_mode must be 0, 1 or 2");
+    if (a.ntypes > 1)
+        return launch_pair_inst<Eval, TPP, FLAT, true, FUSE>(a, d_params, ext, fz, block, s);
+    return launch_pair_inst<Eval, TPP, FLAT, false, FUSE>(a, d_params, ext, fz, block, s);
+    }
+
+// Entry for one evaluator: validates and picks the layout / TPP instantiation.
+template<class Eval, bool FUSE>
+int launch_pair(const gb_pair_args* a, const typename Eval::param_type* d_params,
+                const float* ext, const FuseArgs& fz, cudaStream_t s)
+    {
+    GB_REQUIRE(a, "pair force: null args");
+    GB_REQUIRE(a->d_force && a->d_pos && a->d_n_neigh && a->d_nlist && a->d_rcutsq && d_params,
+               "pair force: null device pointer");
+    GB_REQUIRE(!a->compute_virial || (a->d_virial && a->virial_pitch >= a->N),
+               "pair force: virial requested without a buffer of pitch >= N");
+    GB_REQUIRE(a->shift_mode != 2 || a->d_ronsq, "pair force: xplor needs r_on^2");
+    GB_REQUIRE(a->ntypes >= 1 && a->ntypes <= 64, "pair force: 1 <= ntypes <= 64");
+    GB_REQUIRE(a->d_head_list || a->stride >= a->N, "pair force: column-major stride < N");
+    if (a->N == 0)
+        return GB_OK;
+    unsigned int block = a->block_size ? a->block_size : 256;
+    GB_REQUIRE(block % 32 == 0 && block <= 256, "pair force: block size multiple of 32, <= 256");
+    const bool flat = a->d_head_list != nullptr;
+    unsigned int tpp = a->threads_per_particle;
+    if (!flat)
+        {
+        GB_REQUIRE(tpp <= 1, "pair force: column-major lists use one thread per particle");
+        return dispatch_pair_flags<Eval, 1, false, FUSE>(*a, d_params, ext, fz, block, s);
+        }
+    if (tpp == 0)
+        tpp = 8;
+    switch (tpp)
+        {
+    case 1:
+        return dispatch_pair_flags<Eval, 1, true, FUSE>(*a, d_params, ext, fz, block, s);
+    case 2:
+        return dispatch_pair_flags<Eval, 2, true, FUSE>(*a, d_params, ext, fz, block, s);
+    case 4:
+        return dispatch_pair_flags<Eval, 4, true, FUSE>(*a, d_params, ext, fz, block, s);
+    case 8:
+        return dispatch_pair_flags<Eval, 8, true, FUSE>(*a, d_params, ext, fz, block, s);
+    case 16:
+        return dispatch_pair_flags<Eval, 16, true, FUSE>(*a, d_params, ext, fz, block, s);
+    case 32:
+        return dispatch_pair_flags<Eval, 32, true, FUSE>(*a, d_params, ext, fz, block, s);
+    default:
+        return fail(GB_ERR_INVALID, "pair force: threads_per_particle must be a power of two <= 32");
+        }
+    }
+
+} // namespace gb

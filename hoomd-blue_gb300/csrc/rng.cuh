@@ -1,0 +1,170 @@
+// Counter-based random numbers on the device, following the wrappers of hoomd/RandomNumbers.h
+// around Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11; the random123 library is not part of
+// the reference checkout, so the generator is written here from the published description), and
+// the Bussi rescale factor of hoomd/md/Thermostat.h:416-446, all in double as the reference does.
+#pragma once
+
+#include <cstdint>
+
+namespace gb
+{
+
+struct Philox
+    {
+    uint32_t key[2];
+    uint32_t ctr[4];
+
+    // Seed (hoomd/RandomNumbers.h:136-168) + Counter(a, b, c, d) (:175-197)
+    __host__ __device__ Philox(uint8_t id, uint64_t timestep, uint16_t seed, uint32_t a,
+                               uint32_t b = 0, uint32_t c = 0, uint16_t d = 0)
+        {
+        key[0] = uint32_t(id) << 24 | uint32_t(seed) << 8
+                 | uint32_t((timestep & 0x000000ff00000000ull) >> 32);
+        key[1] = uint32_t(timestep & 0x00000000ffffffffull);
+        ctr[0] = uint32_t(d) << 16;
+        ctr[1] = c;
+        ctr[2] = b;
+        ctr[3] = a;
+        }
+
+    // Ten rounds of (c0,c1,c2,c3) -> (hi(M1*c2)^c1^k0, lo(M1*c2), hi(M0*c0)^c3^k1, lo(M0*c0)),
+    // key bumped by the Weyl constants between rounds.
+    __host__ __device__ void block(uint32_t out[4]) const
+        {
+        uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+        uint32_t k0 = key[0], k1 = key[1];
+#pragma unroll
+        for (int r = 0; r < 10; r++)
+            {
+            if (r > 0)
+                {
+                k0 += 0x9E3779B9u;
+                k1 += 0xBB67AE85u;
+                }
+            const uint64_t p0 = uint64_t(0xD2511F53u) * c0;
+            const uint64_t p1 = uint64_t(0xCD9E8D57u) * c2;
+            const uint32_t n0 = uint32_t(p1 >> 32) ^ c1 ^ k0;
+            const uint32_t n1 = uint32_t(p1);
+            const uint32_t n2 = uint32_t(p0 >> 32) ^ c3 ^ k1;
+            const uint32_t n3 = uint32_t(p0);
+            c0 = n0;
+            c1 = n1;
+            c2 = n2;
+            c3 = n3;
+            }
+        out[0] = c0;
+        out[1] = c1;
+        out[2] = c2;
+        out[3] = c3;
+        }
+
+    // RandomGenerator::operator() (hoomd/RandomNumbers.h:264-270): draw, then bump counter word 0.
+    __host__ __device__ void next(uint32_t out[4])
+        {
+        block(out);
+        ctr[0] += 1;
+        }
+    __host__ __device__ uint64_t u64()
+        {
+        uint32_t o[4];
+        next(o);
+        return uint64_t(o[0]) << 32 | o[1];
+        }
+    __host__ __device__ void two_u64(uint64_t& a, uint64_t& b)
+        {
+        uint32_t o[4];
+        next(o);
+        a = uint64_t(o[0]) << 32 | o[1];
+        b = uint64_t(o[2]) << 32 | o[3];
+        }
+    };
+
+// Published random123 conversions: u01 -> (0,1], uneg11 -> [-1,1] (half-step offset).
+template<class R> __host__ __device__ inline R u01(uint64_t in)
+    {
+    const R factor = R(1.) / (R(18446744073709551615.0) + R(1.));
+    return R(in) * factor + R(0.5) * factor;
+    }
+template<class R> __host__ __device__ inline R uneg11(uint64_t in)
+    {
+    const R factor = R(1.) / (R(9223372036854775807.0) + R(1.));
+    return R(int64_t(in)) * factor + R(0.5) * factor;
+    }
+
+// Box-Muller, one value per draw (hoomd/RandomNumbers.h:346-372).
+__device__ inline double normal_d(Philox& rng)
+    {
+    uint64_t u0, u1;
+    rng.two_u64(u0, u1);
+    double s, c;
+    sincospi(uneg11<double>(u0), &s, &c);
+    const double r = sqrt(-2.0 * log(u01<double>(u1)));
+    return s * r;
+    }
+
+__device__ inline float normal_f(Philox& rng)
+    {
+    uint64_t u0, u1;
+    rng.two_u64(u0, u1);
+    float s, c;
+    sincospif(uneg11<float>(u0), &s, &c);
+    const float r = sqrtf(-2.0f * logf(u01<float>(u1)));
+    return s * r;
+    }
+
+// Marsaglia-Tsang gamma with squeeze test (hoomd/RandomNumbers.h:454-534). The rejection loop is
+// bounded (acceptance is > 95% per iteration for alpha >= 1); after 64 rejections the last
+// candidate is returned rather than spinning.
+__device__ inline double gamma_d(Philox& rng, double m_alpha, double m_b)
+    {
+    double alpha = m_alpha;
+    if (m_alpha < 1.0)
+        alpha += 1.0;
+    const double d = alpha - 1. / 3.;
+    const double c = (1.0 / sqrt(d)) / 3.;
+    double v = 1.0;
+    for (int it = 0; it < 64; it++)
+        {
+        double x;
+        int tries = 0;
+        do
+            {
+            x = normal_d(rng);
+            v = 1.0 + c * x;
+            } while (v <= 0. && ++tries < 64);
+        v = v * v * v;
+        const double x2 = x * x;
+        const double u = u01<double>(rng.u64());
+        if (u < 1.0 - 0.0331 * x2 * x2)
+            break;
+        if (log(u) < 0.5 * x2 + d * (1.0 - v + log(v)))
+            break;
+        }
+    v *= d * m_b;
+    if (m_alpha < 1.0)
+        v *= pow(u01<double>(rng.u64()), 1.0 / m_alpha);
+    return v;
+    }
+
+// hoomd/md/Thermostat.h:357-391 (key id 45, counter = first member tag) and :416-446.
+__device__ inline double bussi_factor_d(double K, double dof, double dt, double tau, double set_T,
+                                        uint64_t timestep, uint16_t seed, uint32_t instance_id)
+    {
+    if (dt == 0.0 || dof == 0.0 || K <= 0.0)
+        return 1.0;
+    Philox rng(45, timestep, seed, instance_id);
+    double time_decay_factor = 0.0;
+    if (tau != 0.0)
+        time_decay_factor = exp(-dt / tau);
+    const double r_normal_one = normal_d(rng);
+    double r_gamma = 0.0;
+    if (dof > 1.0)
+        r_gamma = 2.0 * gamma_d(rng, (dof - 1.0) / 2.0, 1.0);
+    const double v = set_T / 2.0 / K;
+    const double term1 = v * (1.0 - time_decay_factor) * (r_gamma + r_normal_one * r_normal_one);
+    const double term2
+        = 2.0 * r_normal_one * sqrt(v * (1.0 - time_decay_factor) * time_decay_factor);
+    return sqrt(time_decay_factor + term1 + term2);
+    }
+
+} // namespace gb

@@ -1,0 +1,155 @@
+"""Pair forces (hoomd/md/pair/pair.py): ``Pair`` with ``LJ`` and ``Table``, plus ``ExamplePair``,
+the evaluator of the reference's pair-plugin template
+(example_plugins/pair_plugin/EvaluatorPairExample.h), as a worked plugin.
+
+Attribute names, parameter keys, accepted modes and the per-particle outputs (``forces``,
+``energies``, ``virials``, ``energy``) follow the reference. On attach each force becomes a
+PotentialPairGPU engine object; its kernels are instantiated per evaluator
+(gb_pair_forces_lj / _table / _example in include/hoomd_gb300.h).
+"""
+
+import numpy as np
+
+from hoomd_gb300._native import _hoomd_gb300
+from hoomd_gb300.md.data import TypePairDict, dict_validator, nonnegative_real
+
+_MODES = {"none": 0, "shift": 1, "xplor": 2}
+
+
+class Pair:
+    """Base pair force (hoomd/md/pair/pair.py:18-161)."""
+
+    _accepted_modes = ("none", "shift", "xplor")
+    _kind = None
+
+    def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
+        self.r_cut = TypePairDict(default=None if default_r_cut is None else float(default_r_cut),
+                                  validator=nonnegative_real)
+        self.r_on = TypePairDict(default=float(default_r_on), validator=nonnegative_real)
+        if mode not in self._accepted_modes:
+            raise ValueError(f"mode must be one of {self._accepted_modes}")
+        self._mode = mode
+        self.nlist = nlist
+        self._cpp_obj = None
+        self._simulation = None
+
+    @property
+    def mode(self):
+        return self._mode
+
+    @mode.setter
+    def mode(self, m):
+        if m not in self._accepted_modes:
+            raise ValueError(f"mode must be one of {self._accepted_modes}")
+        self._mode = m
+        if self._cpp_obj is not None:
+            self._cpp_obj.mode = _MODES[m]
+
+    def _set_pair_params(self, cpp, i, j, value):
+        raise NotImplementedError
+
+    def _attach(self, simulation, cpp_nlist):
+        self._simulation = simulation
+        state = simulation.state
+        self._cpp_obj = _hoomd_gb300.PotentialPairGPU(state._cpp_pdata, cpp_nlist, self._kind)
+        self._cpp_obj.mode = _MODES[self._mode]
+        types = state.particle_types
+        for i, a in enumerate(types):
+            for j, b in enumerate(types):
+                if j < i:
+                    continue
+                try:
+                    value = self.params[(a, b)]
+                except KeyError:
+                    raise RuntimeError(f"{type(self).__name__}: params[({a!r}, {b!r})] is not set")
+                self._set_pair_params(self._cpp_obj, i, j, value)
+                try:
+                    rc = self.r_cut[(a, b)]
+                except KeyError:
+                    raise RuntimeError(f"{type(self).__name__}: r_cut[({a!r}, {b!r})] is not set")
+                self._cpp_obj.setRCut(i, j, float(rc))
+                self._cpp_obj.setROn(i, j, float(self.r_on[(a, b)]))
+        return self._cpp_obj
+
+    def _detach(self):
+        self._cpp_obj = None
+
+    def _require_run(self):
+        if self._cpp_obj is None or self._simulation is None:
+            raise RuntimeError("forces are available after Simulation.run")
+        self._simulation._attach()
+
+    @property
+    def forces(self):
+        """(N, 3) forces in tag order."""
+        self._require_run()
+        return self._cpp_obj.getForces()
+
+    @property
+    def energies(self):
+        """(N,) per-particle energies (half of each pair energy) in tag order."""
+        self._require_run()
+        return self._cpp_obj.getEnergies()
+
+    @property
+    def virials(self):
+        """(N, 6) per-particle virials (xx, xy, xz, yy, yz, zz) in tag order."""
+        self._require_run()
+        return self._cpp_obj.getVirials()
+
+    @property
+    def energy(self):
+        """Total energy of this force (summed in double)."""
+        return float(np.sum(self.energies, dtype=np.float64))
+
+
+class LJ(Pair):
+    """Lennard-Jones (hoomd/md/pair/pair.py:163-228); params: epsilon, sigma."""
+
+    _kind = _hoomd_gb300.PairKind.LJ
+
+    def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none',
+                 tail_correction=False):
+        super().__init__(nlist, default_r_cut, default_r_on, mode)
+        if tail_correction:
+            raise NotImplementedError("tail_correction is not implemented")
+        self.tail_correction = False
+        self.params = TypePairDict(validator=dict_validator(("epsilon", "sigma")))
+
+    def _set_pair_params(self, cpp, i, j, v):
+        cpp.setParamsLJ(i, j, v["sigma"], v["epsilon"])
+
+
+class Table(Pair):
+    """Tabulated potential (hoomd/md/pair/pair.py:520-619); params: r_min, U, F. Mode 'none'."""
+
+    _kind = _hoomd_gb300.PairKind.Table
+    _accepted_modes = ("none",)
+
+    def __init__(self, nlist, default_r_cut=None):
+        super().__init__(nlist, default_r_cut=default_r_cut, default_r_on=0, mode='none')
+        self.params = TypePairDict(validator=dict_validator(("r_min", "U", "F"),
+                                                            arrays=("U", "F")))
+
+    def _set_pair_params(self, cpp, i, j, v):
+        U = np.asarray(v["U"], np.float64)
+        F = np.asarray(v["F"], np.float64)
+        if U.shape != F.shape or U.ndim != 1:
+            raise RuntimeError("The length of V and F arrays must be equal.")
+        if len(U) == 0:
+            raise RuntimeError("The length of V and F must not be zero.")
+        cpp.setParamsTable(i, j, float(v["r_min"]), U.tolist(), F.tolist())
+
+
+class ExamplePair(Pair):
+    """The reference's pair-plugin example evaluator: V = k/2 (sigma - r)^2 inside r_cut
+    (example_plugins/pair_plugin/pair.py:15-28); params: k, sigma."""
+
+    _kind = _hoomd_gb300.PairKind.Example
+
+    def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
+        super().__init__(nlist, default_r_cut, default_r_on, mode)
+        self.params = TypePairDict(validator=dict_validator(("k", "sigma")))
+
+    def _set_pair_params(self, cpp, i, j, v):
+        cpp.setParamsExample(i, j, v["k"], v["sigma"])

@@ -1,0 +1,80 @@
+"""System state (hoomd/state.py), held on the GPU by the engine's ParticleData."""
+
+import numpy as np
+
+from hoomd_gb300._native import _hoomd_gb300
+from hoomd_gb300.box import Box
+from hoomd_gb300.snapshot import Snapshot
+
+
+class State:
+    def __init__(self, simulation, snapshot):
+        snapshot.validate()
+        self._simulation = simulation
+        self._types = list(snapshot.particles.types)
+        self._dimensions = snapshot.configuration.dimensions
+        p = snapshot.particles
+        self._cpp_pdata = _hoomd_gb300.ParticleData(
+            int(p.N), len(self._types), int(self._dimensions),
+            [float(x) for x in snapshot.configuration.box], [1, 1, 1])
+        self._cpp_pdata.seed = simulation.seed & 0xFFFF
+        self._cpp_pdata.timestep = simulation._initial_timestep
+        self._upload(snapshot)
+
+    def _upload(self, snapshot):
+        p = snapshot.particles
+        self._cpp_pdata.setParticles(
+            np.ascontiguousarray(p.position, np.float64),
+            np.ascontiguousarray(p.velocity, np.float64),
+            np.ascontiguousarray(p.mass, np.float64),
+            np.ascontiguousarray(p.typeid, np.uint32),
+            np.ascontiguousarray(p.image, np.int32))
+        self._simulation._state_changed()
+
+    @property
+    def N_particles(self):
+        return self._cpp_pdata.N
+
+    @property
+    def particle_types(self):
+        return list(self._types)
+
+    @property
+    def types(self):
+        return dict(particle_types=self.particle_types)
+
+    @property
+    def box(self):
+        return Box.from_box(self._cpp_pdata.getBox())
+
+    @property
+    def dimensions(self):
+        return self._dimensions
+
+    def get_snapshot(self):
+        d = self._cpp_pdata.getParticles()
+        s = Snapshot()
+        s.configuration.box = self._cpp_pdata.getBox()
+        s.particles.N = self.N_particles
+        s.particles.types = self.particle_types
+        s.particles.position[:] = d["position"]
+        s.particles.velocity[:] = d["velocity"]
+        s.particles.mass[:] = d["mass"]
+        s.particles.typeid[:] = d["typeid"]
+        s.particles.image[:] = d["image"]
+        return s
+
+    def set_snapshot(self, snapshot):
+        if snapshot.particles.N != self.N_particles:
+            raise RuntimeError("set_snapshot: the number of particles may not change")
+        if list(snapshot.particles.types) != self._types:
+            raise RuntimeError("set_snapshot: particle types may not change")
+        if list(snapshot.configuration.box) != list(self._cpp_pdata.getBox()):
+            raise RuntimeError("set_snapshot: box changes are not supported")
+        snapshot.validate()
+        self._upload(snapshot)
+
+    def thermalize_particle_momenta(self, filter, kT):
+        """Gaussian velocities at kT with zero total momentum (hoomd/state.py:759)."""
+        self._cpp_pdata.thermalize(float(kT), self._simulation.timestep)
+        self._simulation._state_changed(velocities_only=True)

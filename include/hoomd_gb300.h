@@ -1,0 +1,328 @@
+/* hoomd_gb300.h -- C ABI of the GB300-native short-range MD step.
+ *
+ * One shared library (libhoomd_gb300.so) exports the kernel drivers of HOOMD-blue's short-range
+ * MD hot path -- cell list, binned neighbour list, distance check, PotentialPair<Evaluator> force
+ * loop, ConstantVolume/NVE integrator halves, thermodynamic reductions, Bussi factor, momentum
+ * thermalisation and the space-filling-curve particle sort -- as extern "C" functions with POD
+ * argument structs and plain device pointers. Each entry point names the reference kernel driver
+ * it replaces (paths relative to the HOOMD-blue source tree).
+ *
+ * Conventions
+ *  - All pointers named d_* (or documented as device) are device pointers owned by the caller.
+ *  - Per-particle arrays keep HOOMD's FP32 layouts: positions float4 (x, y, z, type bits in w),
+ *    velocities float4 (vx, vy, vz, mass), accelerations float3, images int3, forces float4
+ *    (fx, fy, fz, energy), virials 6 x pitch floats (xx, xy, xz, yy, yz, zz).
+ *  - Every call is ordered on `stream` (a cudaStream_t passed as void*; NULL = legacy default)
+ *    and never synchronises the host. Functions return GB_OK or a gb_status error code and never
+ *    throw across the boundary; gb_last_error() returns a message for the last failure on the
+ *    calling host thread.
+ *  - Device-side conditions (overflow, NaN, particle outside the box) are written to caller
+ *    buffers, as the reference's m_conditions arrays are, for the host to read when it chooses.
+ */
+#ifndef HOOMD_GB300_H
+#define HOOMD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gb_status
+    {
+    GB_OK = 0,
+    GB_ERR_INVALID = 1,     /* bad argument (null pointer, zero size, unsupported option) */
+    GB_ERR_CUDA = 2,        /* a CUDA launch or runtime call failed */
+    GB_ERR_TOO_LARGE = 3,   /* size beyond a documented maximum */
+    GB_ERR_UNSUPPORTED = 4  /* combination not implemented */
+    } gb_status;
+
+/* Simulation box at FP32, field for field the reference's BoxDim (hoomd/BoxDim.h:69-840). Build
+ * it with gb_box_make so that lo, hi and Linv round exactly as BoxDim::setL does at FP32. */
+typedef struct gb_box
+    {
+    float lo[3];
+    float hi[3];
+    float L[3];
+    float Linv[3];
+    float xy, xz, yz;
+    uint32_t periodic[3];
+    } gb_box;
+
+/* BoxDim(Lx, Ly, Lz) + setTiltFactors + setPeriodic (hoomd/BoxDim.h:103-180), host only. */
+int gb_box_make(const double L[3], double xy, double xz, double yz, const int periodic[3],
+                gb_box* out);
+
+/* Nearest plane distances (hoomd/BoxDim.h:552-567) and cell-grid dimensions
+ * floor(npd / nominal_width), at least 1 (hoomd/CellList.cc:83-131), host only. */
+int gb_cell_dims(const gb_box* box, unsigned int ndim, float nominal_width, unsigned int dim[3]);
+
+const char* gb_last_error(void);
+int gb_version(void);
+
+/* ---------------------------------------------------------------------------------------------
+ * Cell list. Replaces gpu_compute_cell_list (hoomd/CellListGPU.cuh:21-43, kernel
+ * hoomd/CellListGPU.cu:42-170) with flag = particle index (NeighborListBinned.cc:25-28).
+ * Slot layout: xyzf[cell * Nmax + slot] (Index2D(Nmax, ncell), hoomd/CellList.cc:241).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct gb_cell_list_args
+    {
+    const float* d_pos;          /* float4[N] */
+    unsigned int N;
+    gb_box box;
+    unsigned int dim[3];
+    unsigned int Nmax;           /* slots per cell */
+    unsigned int* d_cell_size;   /* [ncell], zeroed by the call */
+    float* d_xyzf;               /* float4[ncell * Nmax]: x, y, z, particle index bits */
+    unsigned int* d_cell_type;   /* optional [ncell * Nmax] particle type per slot (NULL = skip) */
+    unsigned int* d_conditions;  /* [3]: needed Nmax on overflow, NaN index+1, out-of-box
+                                    index+1 (max over offenders); the caller zeroes it */
+    const uint32_t* d_gate;      /* optional: when non-NULL and *d_gate == 0 the call is a no-op
+                                    on the device (rebuild decided on the GPU, no host sync) */
+    int deterministic;           /* sort each cell's slots by particle index
+                                    (nlist.Cell(deterministic=True), hoomd/CellListGPU.cu:478-540) */
+    uint64_t* d_build_count;     /* optional: incremented once per (non-gated-off) call */
+    } gb_cell_list_args;
+
+int gb_cell_list_build(const gb_cell_list_args* args, void* stream);
+
+/* Cell adjacency (hoomd/CellList.cc:346-402): per cell the (2r+1)^3 stencil (r = 1), wrapped,
+ * sorted and deduplicated; computed on the device. width = 27 unless a dimension has < 3 cells.
+ * d_adj must hold ncell * 27 entries. */
+int gb_cell_adj_build(const unsigned int dim[3], unsigned int ndim, unsigned int* d_adj,
+                      unsigned int* width_out, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Neighbour list. Replaces gpu_compute_nlist_binned (hoomd/md/NeighborListGPUBinned.cuh,
+ * kernel hoomd/md/NeighborListGPUBinned.cu:52-298): full storage, dr^2 <= r_list^2 inclusive,
+ * self and r_cut <= 0 pairs skipped, overflow recorded per type as the count needed. Unlike
+ * the reference, d_n_neigh holds the stored count, min(found, Nmax[type]), so that a consumer
+ * launched before the host has read the overflow condition never reads past a particle's list.
+ * Layout: neighbour k of particle i lives at d_nlist[head(i) + k * stride], where
+ * head(i) = d_head_list[i] when d_head_list is non-NULL (the reference's flat layout, stride 1)
+ * and head(i) = i otherwise (column-major layout, stride >= N, coalesced across particles).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct gb_nlist_args
+    {
+    unsigned int* d_nlist;
+    unsigned int* d_n_neigh;          /* [N] */
+    float* d_last_pos;                /* optional float4[N]: positions at build (distance check) */
+    unsigned int* d_conditions;       /* [ntypes]: max neighbours needed where Nmax overflowed */
+    const uint64_t* d_head_list;      /* NULL = column-major */
+    uint64_t stride;
+    const unsigned int* d_Nmax;       /* [ntypes] capacity per particle type */
+    const float* d_pos;               /* float4[N] */
+    unsigned int N;
+    const unsigned int* d_cell_size;
+    const float* d_xyzf;
+    const unsigned int* d_cell_type;  /* required when ntypes > 1 */
+    const unsigned int* d_cell_adj;
+    unsigned int dim[3];
+    unsigned int Nmax_cell;
+    unsigned int adj_width;
+    gb_box box;
+    const float* d_r_cut;             /* [ntypes^2] */
+    const float* d_r_listsq;          /* [ntypes^2] (r_cut + r_buff)^2, 0 where r_cut <= 0 */
+    unsigned int ntypes;
+    const uint32_t* d_gate;           /* optional no-op gate, as for the cell list */
+    } gb_nlist_args;
+
+int gb_nlist_build_binned(const gb_nlist_args* args, void* stream);
+
+/* Rebuild check. Replaces gpu_nlist_needs_update_check_new (hoomd/md/NeighborListGPU.cu:42-83):
+ * sets *d_result = checkn when any particle moved at least (r_list*lambda_min - r_cut)/2 since
+ * the last build. */
+int gb_nlist_needs_update(uint32_t* d_result, const float* d_last_pos, const float* d_pos,
+                          unsigned int N, const gb_box* box, const float* d_rcut_max,
+                          float r_buff, unsigned int ntypes, float lambda_min,
+                          const float lambda[3], uint32_t checkn, void* stream);
+
+/* Head list for the flat layout: head[i] = sum_{k<i} Nmax[type k]
+ * (NeighborListGPU.cu:355-448). d_total must hold 1 + ceil(N/1024) elements: element 0
+ * receives the total, the rest is the scan's block-sum scratch. */
+int gb_nlist_head_list(uint64_t* d_head_list, uint64_t* d_total, const float* d_pos,
+                       unsigned int N, const unsigned int* d_Nmax, unsigned int ntypes,
+                       void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Pair forces. Replaces gpu_compute_pair_forces<Evaluator> (hoomd/md/PotentialPairGPU.cuh:
+ * 44-98 pair_args_t, 140-404 kernel, 579-656 driver). shift_mode: 0 none, 1 shift, 2 xplor.
+ * The evaluator parameter structs below are byte-for-byte the FP32 param_type of the reference
+ * evaluators. threads_per_particle 0 picks the layout's default (1 for column-major lists).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct gb_pair_args
+    {
+    float* d_force;                   /* float4[N]: fx, fy, fz, energy (half of each pair) */
+    float* d_virial;                  /* 6 x virial_pitch, written when compute_virial */
+    size_t virial_pitch;
+    unsigned int N;
+    const float* d_pos;
+    const float* d_charge;            /* unused by LJ, Table, Example */
+    gb_box box;
+    const unsigned int* d_n_neigh;
+    const unsigned int* d_nlist;
+    const uint64_t* d_head_list;      /* NULL = column-major */
+    uint64_t stride;
+    const float* d_rcutsq;            /* [ntypes^2] */
+    const float* d_ronsq;             /* [ntypes^2], read when shift_mode == 2 */
+    unsigned int ntypes;
+    unsigned int shift_mode;
+    unsigned int compute_virial;
+    unsigned int block_size;          /* 0 = default */
+    unsigned int threads_per_particle;
+    } gb_pair_args;
+
+/* EvaluatorPairLJ::param_type at FP32 (hoomd/md/EvaluatorPairLJ.h:99-155). */
+typedef struct gb_lj_param
+    {
+    float sigma_6;
+    float epsilon_x_4;
+    } gb_lj_param;
+
+/* EvaluatorPairTable::param_type (hoomd/md/EvaluatorPairTable.h:45-118) with the tables held in
+ * one flat device array: V at d_table[offset .. offset+width), F at d_table[offset+width ..). */
+typedef struct gb_table_param
+    {
+    float rmin;
+    uint32_t width;
+    uint32_t offset;
+    uint32_t pad;
+    } gb_table_param;
+
+/* EvaluatorPairExample::param_type (example_plugins/pair_plugin/EvaluatorPairExample.h:30-60). */
+typedef struct gb_example_param
+    {
+    float k;
+    float sigma;
+    } gb_example_param;
+
+int gb_pair_forces_lj(const gb_pair_args* args, const gb_lj_param* d_params, void* stream);
+int gb_pair_forces_table(const gb_pair_args* args, const gb_table_param* d_params,
+                         const float* d_table, void* stream);
+int gb_pair_forces_example(const gb_pair_args* args, const gb_example_param* d_params,
+                           void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Integrator halves. Replace gpu_nvt_rescale_step_one / _two
+ * (hoomd/md/TwoStepConstantVolumeGPU.cu:35-89, 166-205; with scale 1 these are the NVE halves of
+ * hoomd/md/TwoStepNVEGPU.cu:46-124, 383-453). The rescale factor is read on the device from
+ * d_scale (a double, e.g. written by gb_bussi_factor) or taken as `scale` when d_scale is NULL.
+ * ------------------------------------------------------------------------------------------- */
+int gb_cv_step_one(float* d_pos, float* d_vel, const float* d_accel, int* d_image,
+                   unsigned int N, const gb_box* box, float dt, float scale,
+                   const double* d_scale, void* stream);
+int gb_cv_step_two(float* d_vel, float* d_accel, const float* d_net_force, unsigned int N,
+                   float dt, float scale, const double* d_scale, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Thermodynamic reductions in FP64. Replace gpu_compute_thermo_partial_sums / final_sums
+ * (hoomd/md/ComputeThermoGPU.cu:46-120, 326-...), whose partial sums are in Scalar; here every
+ * per-particle term is widened to double before it is summed, in a fixed order (deterministic).
+ * d_out receives [0] translational KE, [1] potential energy, [2] W = sum(virial xx+yy+zz)/3
+ * (0 when d_virial is NULL).
+ * d_scratch is caller-provided global scratch of gb_thermo_scratch_bytes(N) bytes; its counter
+ * word must be zero before the first call (cudaMemset once); the kernel leaves it zero.
+ * ------------------------------------------------------------------------------------------- */
+size_t gb_thermo_scratch_bytes(unsigned int N);
+int gb_thermo_reduce(const float* d_vel, const float* d_force, const float* d_virial,
+                     size_t virial_pitch, unsigned int N, void* d_scratch, double* d_out,
+                     void* stream);
+
+/* Bussi stochastic velocity rescaling factor on the device (hoomd/md/Thermostat.h:357-446):
+ * reads K = d_ke[0], draws with Philox4x32-10 key Seed(45, timestep, seed) and counter
+ * instance_id, writes the factor (double) to d_factor. */
+int gb_bussi_factor(const double* d_ke, double dof, double dt, double tau, double kT,
+                    uint64_t timestep, uint16_t seed, uint32_t instance_id, double* d_factor,
+                    void* stream);
+
+/* ParticleGroup::thermalizeParticleMomenta for point particles (hoomd/ParticleGroup.cc:690-760):
+ * per-particle Gaussian velocities (Philox key Seed(35, timestep, seed), counter = tag) and
+ * removal of the centre-of-mass momentum (summed in double). d_scratch as for thermo. */
+int gb_thermalize(float* d_vel, const uint32_t* d_tag, unsigned int N, double kT,
+                  uint64_t timestep, uint16_t seed, unsigned int ndim, void* d_scratch,
+                  void* stream);
+
+
+/* ---------------------------------------------------------------------------------------------
+ * Fused whole-step kernels (GB300 design; no single reference counterpart). One MD step of
+ * IntegratorTwoStep::update (hoomd/md/IntegratorTwoStep.cc:51-139) for one ConstantVolume method
+ * and one pair force runs as two kernels plus the rebuild kernels:
+ *   gb_md_step_one      step one (gpu_nvt_rescale_step_one) + the rebuild check
+ *                       (gpu_nlist_needs_update_check_new) in one pass over the particles;
+ *   [gb_cell_list_build + gb_nlist_build_binned, gated on the device by the rebuild flag]
+ *   gb_md_pair_step_*   pair forces + step two (gpu_nvt_rescale_step_two) + FP64 kinetic and
+ *                       potential energy reductions + the Bussi factor for the next step.
+ * No host synchronisation is needed between steps, so a run of steps can be captured into a
+ * CUDA graph and replayed.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct gb_step_one_args
+    {
+    float* d_pos;
+    float* d_vel;
+    const float* d_accel;       /* float3[N] */
+    int* d_image;               /* int3[N] */
+    unsigned int N;
+    gb_box box;
+    float dt;
+    float scale;                /* used when d_scale is NULL */
+    const double* d_scale;      /* device rescale factor (Bussi) or NULL */
+    /* rebuild check, skipped when d_last_pos is NULL */
+    const float* d_last_pos;    /* float4[N] positions at the last build */
+    const float* d_rcut_max;    /* [ntypes] */
+    float r_buff;
+    uint32_t* d_rebuild;        /* set to 1 when any particle moved >= (r_buff)/2 */
+    } gb_step_one_args;
+
+int gb_md_step_one(const gb_step_one_args* args, void* stream);
+
+typedef struct gb_step_fuse
+    {
+    float* d_vel;               /* float4[N] in/out */
+    float* d_accel;             /* float3[N] out */
+    float dt;
+    const double* d_scale2;     /* step-two rescale factor or NULL (= 1) */
+    void* d_scratch;            /* gb_md_step_scratch_bytes(N); zeroed once before first use */
+    double* d_thermo;           /* [3] out: translational KE, potential energy, W */
+    int bussi;                  /* draw the next step's Bussi factor into d_factor */
+    double dof, tau, kT;
+    uint32_t seed;              /* low 16 bits used, as the reference's Seed */
+    uint32_t instance_id;       /* tag of the first group member */
+    uint64_t* d_timestep;       /* current step; incremented by one per call */
+    double* d_factor;
+    uint32_t* d_status;         /* bit 0 set: Bussi factor requested with zero kinetic energy */
+    uint32_t* d_rebuild_reset;  /* optional: set to 0 once the step is complete (clears the
+                                   rebuild flag that gated this step's neighbour-list build) */
+    } gb_step_fuse;
+
+/* Net force (hoomd/Integrator.cu:68-170 gpu_integrator_sum_net_force): d_net[i] = sum over the
+ * n_forces force arrays (float4; energy in w), n_forces <= 8. */
+int gb_sum_net_force(float* d_net, const float* const* h_force_ptrs, unsigned int n_forces,
+                     unsigned int N, void* stream);
+
+size_t gb_md_step_scratch_bytes(unsigned int N);
+int gb_md_pair_step_lj(const gb_pair_args* args, const gb_lj_param* d_params,
+                       const gb_step_fuse* fuse, void* stream);
+int gb_md_pair_step_table(const gb_pair_args* args, const gb_table_param* d_params,
+                          const float* d_table, const gb_step_fuse* fuse, void* stream);
+int gb_md_pair_step_example(const gb_pair_args* args, const gb_example_param* d_params,
+                            const gb_step_fuse* fuse, void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Space-filling-curve sort. Replaces SFCPackTunerGPU (hoomd/SFCPackTunerGPU.cu:26-160): a
+ * Hilbert order over a 2^grid_bits per side lattice of the box (the reference's default grid is
+ * 256 = 2^8). d_order[new] = old index; deterministic. d_scratch of gb_sfc_scratch_bytes().
+ * gb_gather applies the order to one per-particle array (dst[i] = src[order[i]]; elements of
+ * 4, 8, 12 or 16 bytes; dst and src must differ), as gpu_apply_sorted_order does.
+ * ------------------------------------------------------------------------------------------- */
+size_t gb_sfc_scratch_bytes(unsigned int N, int grid_bits);
+int gb_sfc_order(const float* d_pos, unsigned int N, const gb_box* box, int grid_bits,
+                 uint32_t* d_order, void* d_scratch, size_t scratch_bytes, void* stream);
+int gb_gather(void* d_dst, const void* d_src, const uint32_t* d_order, unsigned int N,
+              unsigned int elem_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HOOMD_GB300_H */

@@ -1,0 +1,200 @@
+"""Helpers for the GPU parity tests: device buffers from torch, calls through the C ABI
+(hoomd_gb300.abi), and conversion of the results for comparison with the oracle."""
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from hoomd_gb300 import abi
+from oracle import oracle as O
+
+c_void = ctypes.c_void_p
+
+
+def dev(a, dtype=None):
+    a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype))
+    return torch.from_numpy(a.copy()).cuda()
+
+
+def zeros(n, dtype=torch.int32):
+    return torch.zeros(int(n), dtype=dtype, device="cuda")
+
+
+def p(t):
+    return c_void(t.data_ptr()) if t is not None else None
+
+
+def stream():
+    return c_void(torch.cuda.current_stream().cuda_stream)
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def r_matrices(r_cut, r_buff):
+    """(r_cut, r_list^2, r_cut max per type) at FP32, as updateRList computes them."""
+    rc = np.atleast_2d(np.asarray(r_cut, np.float32))
+    rl = np.where(rc > 0, rc + np.float32(r_buff), np.float32(0)).astype(np.float32)
+    return rc, (rl * rl).astype(np.float32), rc.max(axis=1).astype(np.float32)
+
+
+class GpuNlist:
+    """Cell list + neighbour list through the C ABI, with the reference's overflow retries."""
+
+    def __init__(self, pos4, box6, r_cut, r_buff, layout="col", deterministic=False, ndim=3):
+        L = abi.load()
+        self.N = N = len(pos4)
+        self.box = abi.make_box(box6[:3], box6[3:6])
+        self.pos = dev(np.asarray(pos4, np.float32))
+        rc, rlsq, rcmax = r_matrices(r_cut, r_buff)
+        self.ntypes = nt = rc.shape[0]
+        self.d_rc, self.d_rl, self.d_rcmax = dev(rc.ravel()), dev(rlsq.ravel()), dev(rcmax)
+        width = float(np.float32(rc.max()) + np.float32(r_buff))
+        self.dim = abi.cell_dims(self.box, ndim, width)
+        ncell = int(np.prod(self.dim))
+        self.adj = zeros(27 * ncell)
+        w = ctypes.c_uint32()
+        dims = (ctypes.c_uint32 * 3)(*self.dim)
+        abi.check(L.gb_cell_adj_build(dims, ndim, p(self.adj), ctypes.byref(w), stream()), "adj")
+        self.adj_w = w.value
+        types = O.pos_index_bits(np.asarray(pos4, np.float32)[:, 3], 32)
+        self.types = types
+        Nmax_cell = max(1, math.ceil(N / ncell))
+        while True:
+            self.cell_size = zeros(ncell)
+            self.xyzf = zeros(4 * ncell * Nmax_cell, torch.float32)
+            self.cell_type = zeros(ncell * Nmax_cell) if nt > 1 else None
+            self.ccond = zeros(3)
+            a = abi.CellListArgs(d_pos=p(self.pos), N=N, box=self.box,
+                                 dim=(ctypes.c_uint32 * 3)(*self.dim), Nmax=Nmax_cell,
+                                 d_cell_size=p(self.cell_size), d_xyzf=p(self.xyzf),
+                                 d_cell_type=p(self.cell_type), d_conditions=p(self.ccond),
+                                 deterministic=int(deterministic))
+            abi.check(L.gb_cell_list_build(ctypes.byref(a), stream()), "cell list")
+            cc = host(self.ccond)
+            assert cc[1] == 0 and cc[2] == 0, cc
+            if cc[0] > Nmax_cell:
+                Nmax_cell = int(cc[0])
+                continue
+            break
+        self.Nmax_cell = Nmax_cell
+        Nmax = np.full(nt, 4, np.uint32)
+        while True:
+            self.d_Nmax = dev(Nmax)
+            self.n_neigh = zeros(N)
+            self.last_pos = zeros(4 * N, torch.float32)
+            self.ncond = zeros(nt)
+            if layout == "col":
+                self.stride = (N + 31) // 32 * 32
+                self.head = None
+                self.nlist = zeros(self.stride * int(Nmax.max()))
+            else:
+                self.stride = 1
+                nb = (N + 1023) // 1024
+                self.head = zeros(N, torch.int64)
+                total = zeros(1 + nb, torch.int64)
+                abi.check(L.gb_nlist_head_list(p(self.head), p(total), p(self.pos), N,
+                                               p(self.d_Nmax), nt, stream()), "head")
+                self.nlist = zeros(max(1, int(host(total)[0])))
+            a = abi.NlistArgs(d_nlist=p(self.nlist), d_n_neigh=p(self.n_neigh),
+                              d_last_pos=p(self.last_pos), d_conditions=p(self.ncond),
+                              d_head_list=p(self.head), stride=self.stride, d_Nmax=p(self.d_Nmax),
+                              d_pos=p(self.pos), N=N, d_cell_size=p(self.cell_size),
+                              d_xyzf=p(self.xyzf), d_cell_type=p(self.cell_type),
+                              d_cell_adj=p(self.adj), dim=(ctypes.c_uint32 * 3)(*self.dim),
+                              Nmax_cell=self.Nmax_cell, adj_width=self.adj_w, box=self.box,
+                              d_r_cut=p(self.d_rc), d_r_listsq=p(self.d_rl), ntypes=nt)
+            abi.check(L.gb_nlist_build_binned(ctypes.byref(a), stream()), "nlist")
+            cond = host(self.ncond)
+            over = cond > Nmax
+            if not over.any():
+                break
+            Nmax = np.where(over, np.where(cond > 4, (cond + 3) & ~np.uint32(3), 4),
+                            Nmax).astype(np.uint32)
+        self.Nmax = Nmax
+
+    def sets(self):
+        nn = host(self.n_neigh).astype(np.int64)
+        nl = host(self.nlist).astype(np.int64)
+        if self.head is None:
+            return [np.sort(nl[i + np.arange(nn[i]) * self.stride]) for i in range(self.N)]
+        hd = host(self.head)
+        return [np.sort(nl[hd[i]: hd[i] + nn[i]]) for i in range(self.N)]
+
+    def pair_args(self, force, virial, rcutsq, ronsq=None, shift=0, tpp=0):
+        a = abi.PairArgs(d_force=p(force), d_virial=p(virial),
+                         virial_pitch=self.N if virial is not None else 0, N=self.N,
+                         d_pos=p(self.pos), box=self.box, d_n_neigh=p(self.n_neigh),
+                         d_nlist=p(self.nlist), d_head_list=p(self.head), stride=self.stride,
+                         d_rcutsq=p(rcutsq), d_ronsq=p(ronsq), ntypes=self.ntypes,
+                         shift_mode=shift, compute_virial=int(virial is not None),
+                         threads_per_particle=tpp)
+        return a
+
+
+def lj_params_dev(par):
+    """(ntypes^2, 2) (sigma, epsilon) -> gb_lj_param array at FP32 (EvaluatorPairLJ.h:125-142)."""
+    par = np.asarray(par, np.float64).reshape(-1, 2)
+    s = par[:, 0].astype(np.float32)
+    out = np.zeros((len(par), 2), np.float32)
+    out[:, 0] = s * s * s * s * s * s
+    out[:, 1] = np.float32(4.0) * par[:, 1].astype(np.float32)
+    return dev(out.ravel())
+
+
+def gpu_pair_forces(nl, kind, params, r_cut, virial=True, shift=0, r_on=None, tables=None, tpp=0):
+    """Run one pair kernel through the C ABI; returns (force (N,4), virial (6,N) or None)."""
+    L = abi.load()
+    rc = np.atleast_2d(np.asarray(r_cut, np.float32))
+    rcutsq = dev((rc * rc).ravel())
+    ro = np.zeros_like(rc) if r_on is None else np.atleast_2d(np.asarray(r_on, np.float32))
+    ronsq = dev((ro * ro).ravel())
+    force = zeros(4 * nl.N, torch.float32)
+    vir = zeros(6 * nl.N, torch.float32) if virial else None
+    a = nl.pair_args(force, vir, rcutsq, ronsq, shift, tpp)
+    if kind == "lj":
+        d = lj_params_dev(params)
+        rc_ = L.gb_pair_forces_lj(ctypes.byref(a), p(d), stream())
+    elif kind == "example":
+        d = dev(np.asarray(params, np.float32).ravel())
+        rc_ = L.gb_pair_forces_example(ctypes.byref(a), p(d), stream())
+    else:
+        tp, data = tables
+        d = dev(np.asarray(tp, np.uint32).ravel())
+        td = dev(np.asarray(data, np.float32))
+        rc_ = L.gb_pair_forces_table(ctypes.byref(a), p(d), p(td), stream())
+    abi.check(rc_, "pair forces")
+    f = host(force).reshape(-1, 4)
+    v = host(vir).reshape(6, -1) if virial else None
+    return f, v
+
+
+def table_params(ntypes, tables):
+    """tables: {(i, j): (r_min, U, F)} for i <= j -> (gb_table_param records as uint32 words,
+    flat [V, F] FP32 data, oracle params (ntypes^2, 3), oracle tdata FP64)."""
+    recs = np.zeros((ntypes * ntypes, 4), np.uint32)
+    data, odata = [], []
+    opar = np.zeros((ntypes * ntypes, 3))
+    offs = {}
+    off = 0
+    for (i, j), (rmin, U, F) in sorted(tables.items()):
+        offs[(i, j)] = off
+        data.append(np.asarray(U, np.float32))
+        data.append(np.asarray(F, np.float32))
+        odata.append(np.asarray(U, np.float64))
+        odata.append(np.asarray(F, np.float64))
+        off += 2 * len(U)
+    for i in range(ntypes):
+        for j in range(ntypes):
+            a, b = min(i, j), max(i, j)
+            rmin, U, F = tables[(a, b)]
+            k = i * ntypes + j
+            recs[k, 0] = np.float32(rmin).view(np.uint32)
+            recs[k, 1] = len(U)
+            recs[k, 2] = offs[(a, b)]
+            opar[k] = (rmin, len(U), offs[(a, b)])
+    return recs, np.concatenate(data), opar, np.concatenate(odata)

@@ -1,0 +1,58 @@
+"""CPU checks of the drop-in boundary: the C-ABI library loads, exports every symbol that
+include/hoomd_gb300.h declares, and its host-only helpers (box construction, cell-grid
+dimensions) round exactly as the reference's BoxDim / CellList do at FP32. No GPU calls."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_library_exports_every_declared_symbol():
+    from hoomd_gb300 import abi
+    names = abi.declared_functions()
+    assert len(names) >= 25
+    lib = ctypes.CDLL(str(abi.LIB_PATH))
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # every declared function has a ctypes prototype in the binding
+    assert set(names) <= set(abi._PROTOS), set(names) - set(abi._PROTOS)
+    abi.load()
+
+
+def test_engine_module_imports():
+    import hoomd_gb300
+    assert hoomd_gb300._hoomd_gb300.version() == 1
+    for cls in ("ParticleData", "NeighborListGPUBinned", "PotentialPairGPU", "IntegratorTwoStep"):
+        assert hasattr(hoomd_gb300._hoomd_gb300, cls)
+
+
+@pytest.mark.parametrize("box6", [(16.957, 16.957, 16.957, 0, 0, 0), (10, 11, 12, 0.3, -0.2, 0.1),
+                                  (107.67, 107.67, 107.67, 0, 0, 0)])
+def test_box_make_matches_oracle_fp32(box6):
+    from hoomd_gb300 import abi
+    b = abi.make_box(box6[:3], box6[3:])
+    L = np.array(b.L[:], np.float32)
+    assert np.array_equal(L, np.asarray(box6[:3], np.float32))
+    assert np.array_equal(np.array(b.hi[:], np.float32), L / np.float32(2))
+    assert np.array_equal(np.array(b.Linv[:], np.float32), np.float32(1) / L)
+    # cell dims identical to the oracle's CellList::computeDimensions at FP32
+    for w in (2.9, 2.8, 1.1, 3.4, 0.5):
+        assert abi.cell_dims(b, 3, w) == O.cell_dims(box6, w, 3, 32).tolist()
+
+
+def test_c_abi_rejects_bad_arguments_without_gpu():
+    from hoomd_gb300 import abi
+    lib = abi.load()
+    # null arguments are rejected before any CUDA call
+    assert lib.gb_cell_list_build(None, None) == abi.GB_ERR_INVALID
+    assert b"null" in lib.gb_last_error()
+    assert lib.gb_nlist_build_binned(None, None) == abi.GB_ERR_INVALID
+    assert lib.gb_pair_forces_lj(None, None, None) == abi.GB_ERR_INVALID
+    args = abi.PairArgs()
+    args.N = 10
+    assert lib.gb_pair_forces_lj(ctypes.byref(args), None, None) == abi.GB_ERR_INVALID
+    b = abi.make_box((10, 10, 10))
+    assert lib.gb_cell_dims(ctypes.byref(b), 3, 0.0, (ctypes.c_uint32 * 3)()) == abi.GB_ERR_INVALID

@@ -1,0 +1,261 @@
+"""End-to-end GPU tests through the hoomd-style Python API, written like the reference's own tests
+(hoomd/md/pytest/test_potential.py, test_nlist.py, example_plugins/pair_plugin/pytest), checked
+against the golden fixtures and the CPU oracle."""
+
+import itertools
+import json
+import pathlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+import hoomd_gb300 as hoomd  # noqa: E402
+from hoomd_gb300 import md, workloads  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+GOLD = pathlib.Path(__file__).resolve().parent / "golden"
+
+
+def two_particle_snapshot(d=1.0, L=20.0):
+    s = hoomd.Snapshot()
+    s.configuration.box = [L, L, L, 0, 0, 0]
+    s.particles.N = 2
+    s.particles.position[:] = [[-d / 2, 0, 0.1], [d / 2, 0, 0.1]]
+    s.particles.types = ["A"]
+    return s
+
+
+def make_sim(snap, seed=22765):
+    sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=seed)
+    sim.create_state_from_snapshot(snap)
+    return sim
+
+
+@pytest.mark.parametrize("pot", ["LJ", "Table"])
+def test_force_energy_accuracy(pot):
+    """hoomd/md/pytest/test_potential.py:952-1058 on the golden fixture."""
+    fe = json.load(open(GOLD / "forces_and_energies_lj_table.json"))[pot]
+    for i, params in enumerate(fe["params"]):
+        cls = getattr(md.pair, pot)
+        f = cls(nlist=md.nlist.Cell(buffer=0.4), default_r_cut=2.5)
+        f.params[("A", "A")] = params
+        sim = make_sim(two_particle_snapshot(d=0.75))
+        sim.operations.integrator = md.Integrator(
+            dt=0.005, forces=[f], methods=[md.methods.ConstantVolume(hoomd.filter.All())])
+        sim.run(0)
+        for k, d in enumerate([0.75, 1.5]):
+            snap = sim.state.get_snapshot()
+            snap.particles.position[0] = [0, 0, 0.1]
+            snap.particles.position[1] = [0, 0, d + 0.1]
+            sim.state.set_snapshot(snap)
+            e = f.energies
+            forces = f.forces
+            ref_e = fe["energies"][i][k]
+            assert np.isclose(e.sum(), ref_e, rtol=2e-5, atol=1e-6 if ref_e == 0 else 0)
+            assert np.allclose(forces[0], np.array([0, 0, 1.0]) * fe["forces"][i][k], rtol=2e-5,
+                               atol=1e-5)
+
+
+def test_true_pair_list():
+    """hoomd/md/pytest/test_nlist.py:221-372 (standalone Cell compute, r_cut 1.1, buffer 0)."""
+    truth = set(frozenset(p) for p in json.load(open(GOLD / "true_pair_list_sc7.json")))
+    s = hoomd.Snapshot()
+    s.configuration.box = [7, 7, 7, 0, 0, 0]
+    s.particles.N = 343
+    s.particles.position[:] = workloads.sc_positions(7, 1.0)
+    sim = make_sim(s)
+    nlist = md.nlist.Cell(buffer=0.0, default_r_cut=1.1)
+    sim.operations.computes.append(nlist)
+    sim.run(0)
+    got = set(frozenset(map(int, p)) for p in nlist.pair_list())
+    assert got == truth
+
+
+def harm_force_and_energy(dx, k, sigma, r_cut, shift=False):
+    dr = np.linalg.norm(dx)
+    if dr >= r_cut:
+        return np.zeros(3), 0.0
+    f = k * (sigma - dr) * np.asarray(dx, np.float64) / dr
+    e = 0.5 * k * (sigma - dr) ** 2
+    if shift:
+        e -= 0.5 * k * (r_cut - sigma) ** 2
+    return f, e
+
+
+@pytest.mark.parametrize("distance, k, sigma, mode",
+                         list(itertools.product(np.linspace(0.1, 2.0, 3), [0.5, 2.0, 5.0],
+                                                [0.5, 1.0, 1.5], ["none", "shift"])))
+def test_example_pair_plugin(distance, k, sigma, mode):
+    """example_plugins/pair_plugin/pytest/test_example_pair.py."""
+    sim = make_sim(two_particle_snapshot(d=distance))
+    cell = md.nlist.Cell(buffer=0.4)
+    ex = md.pair.ExamplePair(cell, default_r_cut=sigma, mode=mode)
+    ex.params[("A", "A")] = dict(k=k, sigma=sigma)
+    sim.operations.integrator = md.Integrator(
+        dt=0.001, forces=[ex], methods=[md.methods.ConstantVolume(hoomd.filter.All())])
+    sim.run(0)
+    snap = sim.state.get_snapshot()
+    vec = snap.particles.position[1] - snap.particles.position[0]
+    f, e = harm_force_and_energy(vec, k, sigma, sigma, mode == "shift")
+    np.testing.assert_array_almost_equal(ex.forces, [-f, f], decimal=5)
+    np.testing.assert_array_almost_equal(ex.energies, [e / 2, e / 2], decimal=5)
+
+
+def lj_sim(snap, kT=None, dt=0.005, mode="none", sorter=None, seed=5, thermalize=1.5):
+    sim = make_sim(snap, seed)
+    if thermalize:
+        sim.state.thermalize_particle_momenta(hoomd.filter.All(), thermalize)
+    cell = md.nlist.Cell(buffer=0.4)
+    lj = md.pair.LJ(nlist=cell, default_r_cut=2.5, mode=mode)
+    lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+    th = None if kT is None else md.methods.thermostats.Bussi(kT=kT)
+    sim.operations.integrator = md.Integrator(
+        dt=dt, forces=[lj], methods=[md.methods.ConstantVolume(hoomd.filter.All(), th)])
+    if sorter:
+        sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=sorter))
+    thermo = md.compute.ThermodynamicQuantities(hoomd.filter.All())
+    sim.operations.computes.append(thermo)
+    return sim, lj, cell, thermo
+
+
+def test_run0_forces_match_fp64_oracle():
+    snap = workloads.lj_fluid_sc(16)
+    sim, lj, cell, thermo = lj_sim(snap, thermalize=None)
+    sim.run(0)
+    pos4 = O.make_pos4(sim.state.get_snapshot().particles.position, np.zeros(4096), 64)
+    box = tuple(snap.configuration.box)
+    n, l, h, _ = O.build_nlist(pos4, box, [[2.5]], 0.4, full=False, prec=64)
+    fo, vo = O.pair_forces("lj", pos4, box, [[1.0, 1.0]], [[6.25]], n, l, h, third_law=True,
+                           compute_virial=True, prec=64)
+    F = lj.forces
+    floor = 1e-5 * np.abs(fo[:, :3]).max()
+    assert np.all(np.abs(F - fo[:, :3]) <= 1e-5 * np.abs(fo[:, :3]) + floor)
+    assert np.isclose(lj.energy, fo[:, 3].sum(), rtol=1e-5)
+    V = lj.virials
+    assert np.all(np.abs(V - vo.T) <= 1e-5 * np.abs(vo.T) + 1e-5 * np.abs(vo).max())
+    assert np.isclose(thermo.potential_energy, fo[:, 3].sum(), rtol=1e-5)
+
+
+def test_trajectory_matches_oracle_short_nve():
+    """20 NVE steps: GPU FP32 vs the oracle's FP32 CPU run from the same state (per-particle
+    positions agree to FP32 round-off amplified by the dynamics)."""
+    snap = workloads.lj_fluid_sc(12, density=0.84)
+    N = snap.particles.N
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0)
+    s0 = sim.state.get_snapshot()
+    sim.run(20)
+    s1 = sim.state.get_snapshot()
+    pos4 = O.make_pos4(s0.particles.position, np.zeros(N), 32)
+    vel4 = np.zeros((N, 4), np.float32)
+    vel4[:, :3] = s0.particles.velocity
+    vel4[:, 3] = 1.0
+    ref = O.Sim(pos4, vel4, np.zeros((N, 3), np.int32), np.arange(N), snap.configuration.box,
+                [[2.5]], 0.4, 0.005, params=[[1.0, 1.0]], full=True, prec=32)
+    ref.run(20)
+    r = ref.get()
+    box = np.array(snap.configuration.box[:3])
+    unwrapped_gpu = s1.particles.position + s1.particles.image * box
+    unwrapped_ref = r["pos"][:, :3] + r["image"] * box
+    assert np.abs(unwrapped_gpu - unwrapped_ref).max() < 1e-3
+    assert np.abs(s1.particles.velocity - r["vel"][:, :3]).max() < 1e-2
+
+
+def test_nve_energy_conservation():
+    snap = workloads.lj_fluid_sc(16)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, mode="shift", thermalize=1.5, dt=0.004)
+    sim.run(50)
+    e0 = thermo.kinetic_energy + thermo.potential_energy
+    sim.run(2000)
+    e1 = thermo.kinetic_energy + thermo.potential_energy
+    assert cell.num_builds > 10
+    assert abs(e1 - e0) / snap.particles.N < 2e-3
+
+
+def test_bussi_thermostat_temperature():
+    snap = workloads.lj_fluid_sc(16)
+    sim, lj, cell, thermo = lj_sim(snap, kT=1.5, thermalize=0.5)
+    sim.run(300)
+    Ts = []
+    for _ in range(20):
+        sim.run(20)
+        Ts.append(thermo.kinetic_temperature)
+    assert abs(np.mean(Ts) - 1.5) < 0.05
+    assert thermo.degrees_of_freedom == 3 * snap.particles.N - 3
+
+
+def test_sorter_does_not_change_physics():
+    snap = workloads.lj_fluid_sc(14)
+    out = []
+    for sorter in (None, 7):
+        sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0, sorter=sorter)
+        sim.run(30)
+        out.append((sim.state.get_snapshot(), lj.forces))
+    (s_a, f_a), (s_b, f_b) = out
+    box = np.array(snap.configuration.box[:3])
+    ua = s_a.particles.position + s_a.particles.image * box
+    ub = s_b.particles.position + s_b.particles.image * box
+    assert np.abs(ua - ub).max() < 1e-3
+    assert np.abs(f_a - f_b).max() < 1e-2 * max(1.0, np.abs(f_a).max())
+
+
+def test_overflow_rolls_back_and_matches():
+    """Start the cell list and neighbour list exactly full: the melting lattice overflows inside
+    a replayed run, the engine restores its checkpoint, grows and repeats the run. The result
+    must equal a run that never overflowed."""
+    snap = workloads.lj_fluid_sc(14)
+    res = []
+    for tight in (False, True):
+        sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=2.0)
+        sim.run(0)
+        if tight:
+            pos4 = O.make_pos4(sim.state.get_snapshot().particles.position, np.zeros(14 ** 3), 32)
+            box = tuple(snap.configuration.box)
+            n, _, _, info = O.build_nlist(pos4, box, [[2.5]], 0.4, full=True, prec=32)
+            need = int(n.max())
+            cell._cpp_obj.setStartCapacity(int(info["cell_size"].max()), [need])
+            sim._needs_prep = True
+        sim.run(200)
+        integ = sim._cpp_integrator
+        res.append((sim.state.get_snapshot(), integ.n_rollbacks))
+    (a, rb_a), (b, rb_b) = res
+    assert rb_a == 0 and rb_b >= 1
+    assert np.abs(a.particles.position - b.particles.position).max() < 5e-2
+
+
+def test_nan_position_raises_with_tag():
+    snap = workloads.lj_fluid_sc(8)
+    snap.particles.position[17] = [np.nan, 0, 0]
+    sim, lj, cell, thermo = lj_sim(snap, thermalize=None)
+    with pytest.raises(RuntimeError, match="tag 17 has NaN"):
+        sim.run(0)
+
+
+def test_bussi_requires_momenta():
+    snap = workloads.lj_fluid_sc(8)
+    sim, lj, cell, thermo = lj_sim(snap, kT=1.0, thermalize=None)
+    with pytest.raises(RuntimeError, match="non-zero initial momenta"):
+        sim.run(1)
+
+
+def test_multiple_forces_general_path():
+    """Two LJ forces sharing one list run through the unfused path; their sum equals one LJ with
+    epsilon doubled."""
+    snap = workloads.lj_fluid_sc(10)
+    sim1, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0, seed=3)
+    lj.params[("A", "A")] = dict(epsilon=2.0, sigma=1.0)
+    sim1.run(10)
+    sim2 = make_sim(snap, 3)
+    sim2.state.thermalize_particle_momenta(hoomd.filter.All(), 1.0)
+    cell2 = md.nlist.Cell(buffer=0.4)
+    a = md.pair.LJ(nlist=cell2, default_r_cut=2.5)
+    b = md.pair.LJ(nlist=cell2, default_r_cut=2.5)
+    a.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+    b.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+    sim2.operations.integrator = md.Integrator(
+        dt=0.005, forces=[a, b], methods=[md.methods.ConstantVolume(hoomd.filter.All())])
+    sim2.run(10)
+    p1 = sim1.state.get_snapshot().particles.position
+    p2 = sim2.state.get_snapshot().particles.position
+    assert np.abs(p1 - p2).max() < 1e-4
