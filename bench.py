@@ -179,9 +179,11 @@ def run_gb300(args):
 
     rank, world, local = dist_init()
     torch.cuda.set_device(local)
-    snap = workloads.lj_fluid_fcc(m=64, density=WORKLOAD["density"], jitter=0.05,
+    snap = workloads.lj_fluid_fcc(m=args.fcc_m, density=WORKLOAD["density"], jitter=0.05,
                                   seed=1 + rank)
     N = snap.particles.N
+    if args.fcc_m != 64:
+        WORKLOAD.update(workload=f"lj_fluid_fcc_{N}", N=N, lattice=f"fcc {args.fcc_m}^3")
     sim, lj, cell, method = make_sim(snap, seed=1 + rank)
     # warm-up / equilibration (Bussi)
     sim.run(max(3, args.warmup))
@@ -302,6 +304,9 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fcc-m", type=int, default=64,
+                    help="FCC cells per side (64 = the 1,048,576-particle workload; smaller "
+                         "values are for profiling captures only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
