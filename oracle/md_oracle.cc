@@ -535,8 +535,14 @@ void nlist_binned(unsigned int N,
                   unsigned int* nlist,
                   unsigned int* n_neigh,
                   unsigned int* conditions, // per type
-                  bool rint_min_image)
+                  bool rint_min_image,
+                  int nthreads = 1)
     {
+    // each particle's list is built by one thread in the reference's order, so the result does
+    // not depend on the thread count
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 512) num_threads(std::max(nthreads, 1))
+#endif
     for (int i = 0; i < (int)N; i++)
         {
         unsigned int cur_n_neigh = 0;
@@ -583,7 +589,12 @@ void nlist_binned(unsigned int N,
                         if (cur_n_neigh < Nmax_i)
                             nlist[head_i + cur_n_neigh] = j;
                         else
+                            {
+#ifdef _OPENMP
+#pragma omp critical(orc_nlist_cond)
+#endif
                             conditions[type_i] = std::max(conditions[type_i], cur_n_neigh + 1);
+                            }
                         cur_n_neigh++;
                         }
                     }
@@ -729,8 +740,11 @@ void pair_forces(unsigned int N,
 // ------------------------------------------------------------------------------------------------
 template<class R>
 void cv_step_one(unsigned int N, R* pos, R* vel, const R* accel, int* image, const Box<R>& box,
-                 R dt, R s)
+                 R dt, R s, int nthreads = 1)
     {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(std::max(nthreads, 1))
+#endif
     for (unsigned int j = 0; j < N; j++)
         {
         R vx = vel[4 * j], vy = vel[4 * j + 1], vz = vel[4 * j + 2];
@@ -755,8 +769,12 @@ void cv_step_one(unsigned int N, R* pos, R* vel, const R* accel, int* image, con
     }
 
 template<class R>
-void cv_step_two(unsigned int N, R* vel, R* accel, const R* net_force, R dt, R s)
+void cv_step_two(unsigned int N, R* vel, R* accel, const R* net_force, R dt, R s,
+                 int nthreads = 1)
     {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(std::max(nthreads, 1))
+#endif
     for (unsigned int j = 0; j < N; j++)
         {
         R vx = vel[4 * j], vy = vel[4 * j + 1], vz = vel[4 * j + 2];
@@ -1069,6 +1087,10 @@ template<class R> struct Sim
         box.nearest_plane_distance(Lg);
         R lam[3] = {Lg[0] / last_L[0], Lg[1] / last_L[1], Lg[2] / last_L[2]};
         R lmin = std::min(std::min(lam[0], lam[1]), lam[2]);
+        int moved = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(| : moved) num_threads(std::max(nthreads, 1))
+#endif
         for (unsigned int i = 0; i < N; i++)
             {
             unsigned int ti = as_uint(pos[4 * i + 3]);
@@ -1081,9 +1103,9 @@ template<class R> struct Sim
             R dz = pos[4 * i + 2] - lam[2] * last_pos[4 * i + 2];
             box.min_image_rint(dx, dy, dz);
             if (dx * dx + dy * dy + dz * dz >= maxsq)
-                return true;
+                moved = 1;
             }
-        return false;
+        return moved != 0;
         }
 
     bool build()
@@ -1132,7 +1154,8 @@ template<class R> struct Sim
             nl_cond.assign(ntypes, 0);
             nlist_binned(N, pos.data(), box, ntypes, r_cut.data(), r_listsq.data(), full, dim,
                          cell_size.data(), xyzf.data(), Nmax_cell, adj.data(), adj_w, Nmax.data(),
-                         head_list.data(), nlist.data(), n_neigh.data(), nl_cond.data(), false);
+                         head_list.data(), nlist.data(), n_neigh.data(), nl_cond.data(), false,
+                         nthreads);
             bool overflow = false;
             for (unsigned int t = 0; t < ntypes; t++)
                 if (nl_cond[t] > Nmax[t])
@@ -1227,10 +1250,10 @@ template<class R> struct Sim
                 }
             s = R(bussi_factor(K, dof(), double(dt), tau, kT, timestep, seed, tags[0]));
             }
-        cv_step_one(N, pos.data(), vel.data(), accel.data(), image.data(), box, dt, s);
+        cv_step_one(N, pos.data(), vel.data(), accel.data(), image.data(), box, dt, s, nthreads);
         if (!compute_forces())
             return false;
-        cv_step_two(N, vel.data(), accel.data(), force.data(), dt, R(1.0));
+        cv_step_two(N, vel.data(), accel.data(), force.data(), dt, R(1.0), nthreads);
         timestep++;
         return true;
         }
