@@ -88,6 +88,7 @@ _PROTOS = {
     "gb_cv_step_two": (c_int, [c_void, c_void, c_void, c_uint, c_float, c_float, c_void, c_void]),
     "gb_thermo_scratch_bytes": (c_size, [c_uint]),
     "gb_thermo_reduce": (c_int, [c_void, c_void, c_void, c_size, c_uint, c_void, c_void, c_void]),
+    "gb_thermo_reduce_noalloc": (c_int, [c_void, c_void, c_void, c_size, c_uint, c_void, c_void]),
     "gb_bussi_factor": (c_int, [c_void, c_double, c_double, c_double, c_double, c_u64,
                                 ctypes.c_uint16, c_uint, c_void, c_void]),
     "gb_thermalize": (c_int, [c_void, c_void, c_uint, c_double, c_u64, ctypes.c_uint16, c_uint,

@@ -229,6 +229,19 @@ int gb_thermo_reduce(const float* d_vel, const float* d_force, const float* d_vi
                      size_t virial_pitch, unsigned int N, void* d_scratch, double* d_out,
                      void* stream);
 
+/* Allocation-free variant of gb_thermo_reduce; it has no counterpart in the reference. It is for
+ * callers that cannot allocate device memory: a host that has given all device memory to its own
+ * pool and forbids side allocations, or one that must not stall the GPU (cudaFree synchronises
+ * the device), and so cannot pass the d_scratch buffer gb_thermo_reduce needs. Its scratch is a
+ * fixed array inside the library (GB_NOALLOC_MAX_N particles' worth, 384.25 KiB), resident on
+ * every GPU that loads the library until the process exits. N > GB_NOALLOC_MAX_N returns
+ * GB_ERR_TOO_LARGE. The first call on a device looks up the array's address with that device
+ * current; make it before any stream capture. All calls share the array: calls that overlap on
+ * the GPU race. Outputs as gb_thermo_reduce; no cudaMalloc or cudaFree is ever called. */
+#define GB_NOALLOC_MAX_N 4194304u
+int gb_thermo_reduce_noalloc(const float* d_vel, const float* d_force, const float* d_virial,
+                             size_t virial_pitch, unsigned int N, double* d_out, void* stream);
+
 /* Bussi stochastic velocity rescaling factor on the device (hoomd/md/Thermostat.h:357-446):
  * reads K = d_ke[0], draws with Philox4x32-10 key Seed(45, timestep, seed) and counter
  * instance_id, writes the factor (double) to d_factor. */
