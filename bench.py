@@ -8,6 +8,13 @@ engine's own stream. Warm-up runs W Bussi (kT = 1.5) equilibration steps from a 
 lattice; the K timed steps are NVE (ConstantVolume without thermostat) with the Hilbert-curve
 particle sort every 100 steps, as the 1M-particle configuration prescribes.
 
+Other configurations (``--workload``): ``lj_sc_4096`` (the 4096-particle LJ fluid, Bussi
+kT = 1.5), ``ka_262k`` (Kob-Andersen 80:20 mixture, N = 262,144, density 1.2, Bussi kT = 0.8,
+dt 0.003, buffer 0.3, started from a jittered lattice instead of random positions plus capped
+relaxation), ``table32_524k`` (32 types, 528 tabulated pair potentials, N = 524,288, density
+0.8, Bussi kT = 1.5, dt 0.004, buffer 0.4). Those configurations keep their thermostat in the
+timed steps.
+
 --impl reference times the CPU restatement of the reference's path (oracle/, FP64 Scalar, full
 neighbour list over all host threads) on a bounded sample of the same workload.
 Multi-GPU: the path is run as independent replicas, one per GPU (no collective on the data path).
@@ -28,15 +35,114 @@ for _p in (REPO, REPO / "hoomd-blue_gb300"):
     if str(_p) not in sys.path:
         sys.path.insert(0, str(_p))
 
-METRIC = "LJ MD timesteps/s at N=1M"
 UNIT = "timesteps/s"
-WORKLOAD = {"workload": "lj_fluid_fcc_1M", "N": 1048576, "lattice": "fcc 64^3",
-            "density": 0.84, "r_cut": 2.5, "buffer": 0.4, "dt": 0.005,
-            "integrator": "ConstantVolume NVE after Bussi kT=1.5 warm-up",
-            "sort_period": 100, "precision": "fp32 positions/forces, fp64 reductions",
-            "l2": "working set > L2 (neighbour list ~0.35 GB read per step)"}
 
 
+# ------------------------------------------------------------------------------------------------
+# workloads
+# ------------------------------------------------------------------------------------------------
+def _lj_forces(md, cell, types, pairs, r_cut):
+    lj = md.pair.LJ(nlist=cell, default_r_cut=r_cut)
+    for (a, b), (eps, sig, rc) in pairs.items():
+        lj.params[(a, b)] = dict(epsilon=eps, sigma=sig)
+        lj.r_cut[(a, b)] = rc
+    return lj
+
+
+class Workload:
+    """One benchmark configuration: its snapshot, pair force, thermostat and oracle inputs."""
+
+    def __init__(self, name, metric, config, make_snap, kind, pairs=None, tables=None,
+                 timed_thermostat=False):
+        self.name, self.metric, self.config = name, metric, config
+        self.make_snap, self.kind = make_snap, kind
+        self.pairs, self.tables = pairs, tables
+        self.timed_thermostat = timed_thermostat
+
+    def force(self, md, cell, snap):
+        types = snap.particles.types
+        if self.kind == "lj":
+            return _lj_forces(md, cell, types, self.pairs, self.config["r_cut"])
+        tab = md.pair.Table(nlist=cell, default_r_cut=self.config["r_cut"])
+        for (i, j), v in self.tables().items():
+            tab.params[(types[i], types[j])] = dict(r_min=v["r_min"], U=v["U"], F=v["F"])
+        return tab
+
+    def oracle_inputs(self, snap):
+        """(kind, params, tdata, r_cut matrix) in the oracle's formats."""
+        import numpy as np
+        types = snap.particles.types
+        nt = len(types)
+        rc = np.zeros((nt, nt))
+        if self.kind == "lj":
+            par = np.zeros((nt * nt, 2))
+            for (a, b), (eps, sig, r) in self.pairs.items():
+                i, j = types.index(a), types.index(b)
+                for x, y in ((i, j), (j, i)):
+                    par[x * nt + y] = (sig, eps)
+                    rc[x, y] = r
+            return "lj", par, None, rc
+        tabs = self.tables()
+        par = np.zeros((nt * nt, 3))
+        data, offs, off = [], {}, 0
+        for (i, j), v in sorted(tabs.items()):
+            offs[(i, j)] = off
+            data += [v["U"], v["F"]]
+            off += 2 * len(v["U"])
+        for i in range(nt):
+            for j in range(nt):
+                a, b = min(i, j), max(i, j)
+                par[i * nt + j] = (tabs[(a, b)]["r_min"], len(tabs[(a, b)]["U"]), offs[(a, b)])
+                rc[i, j] = self.config["r_cut"]
+        return "table", par, np.concatenate(data), rc
+
+
+def workloads_registry(fcc_m=64):
+    from hoomd_gb300 import workloads as W
+    N_fcc = 4 * fcc_m ** 3
+    reg = {}
+    reg["lj_fcc_1m"] = Workload(
+        "lj_fcc_1m", "LJ MD timesteps/s at N=1M",
+        {"workload": "lj_fluid_fcc_1M" if fcc_m == 64 else f"lj_fluid_fcc_{N_fcc}", "N": N_fcc,
+         "lattice": f"fcc {fcc_m}^3", "density": 0.84, "r_cut": 2.5, "buffer": 0.4, "dt": 0.005,
+         "kT": 1.5, "integrator": "ConstantVolume NVE after Bussi kT=1.5 warm-up",
+         "sort_period": 100, "precision": "fp32 positions/forces, fp64 reductions",
+         "l2": "working set > L2 (neighbour list ~0.35 GB read per step)"},
+        lambda seed: W.lj_fluid_fcc(m=fcc_m, density=0.84, jitter=0.05, seed=seed), "lj",
+        pairs={("A", "A"): (1.0, 1.0, 2.5)})
+    reg["lj_sc_4096"] = Workload(
+        "lj_sc_4096", "LJ MD timesteps/s at N=4096",
+        {"workload": "lj_fluid_sc_4096", "N": 4096, "lattice": "sc 16^3", "density": 0.84,
+         "r_cut": 2.5, "buffer": 0.4, "dt": 0.005, "kT": 1.5,
+         "integrator": "ConstantVolume + Bussi kT=1.5", "sort_period": 0,
+         "precision": "fp32 positions/forces, fp64 reductions", "l2": "fits in L2"},
+        lambda seed: W.lj_fluid_sc(16, density=0.84, jitter=0.05, seed=seed), "lj",
+        pairs={("A", "A"): (1.0, 1.0, 2.5)}, timed_thermostat=True)
+    reg["ka_262k"] = Workload(
+        "ka_262k", "Kob-Andersen LJ timesteps/s at N=262144",
+        {"workload": "kob_andersen_262k", "N": 262144, "lattice": "jittered sc 64^3, 80:20 A:B",
+         "density": 1.2, "r_cut": 2.5, "buffer": 0.3, "dt": 0.003, "kT": 0.8,
+         "integrator": "ConstantVolume + Bussi kT=0.8", "sort_period": 100,
+         "precision": "fp32 positions/forces, fp64 reductions", "l2": "working set > L2"},
+        lambda seed: W.binary_mixture(N=262144, density=1.2, seed=seed), "lj",
+        pairs={("A", "A"): (1.0, 1.0, 2.5), ("A", "B"): (1.5, 0.8, 2.0),
+               ("B", "B"): (0.5, 0.88, 2.2)}, timed_thermostat=True)
+    reg["table32_524k"] = Workload(
+        "table32_524k", "32-type Table timesteps/s at N=524288",
+        {"workload": "table_32types_524k", "N": 524288, "types": 32, "table_pairs": 528,
+         "table_width": 1000, "density": 0.8, "r_min": 0.8, "r_cut": 3.0, "buffer": 0.4,
+         "dt": 0.004, "kT": 1.5, "integrator": "ConstantVolume + Bussi kT=1.5",
+         "sort_period": 100, "precision": "fp32 positions/forces/tables, fp64 reductions",
+         "l2": "working set > L2; tables (4.2 MB) L2-resident"},
+        lambda seed: W.multitype_system(N=524288, ntypes=32, density=0.8, seed=seed), "table",
+        tables=lambda: W.mixture_tables(32, r_min=0.8, r_cut=3.0, width=1000, seed=2),
+        timed_thermostat=True)
+    return reg
+
+
+# ------------------------------------------------------------------------------------------------
+# harness
+# ------------------------------------------------------------------------------------------------
 def peaks():
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
@@ -116,79 +222,78 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
-def make_sim(snap, kT=1.5, seed=1, sort_period=100, thermostat=True):
+def make_sim(wl, snap, seed=1):
     import hoomd_gb300 as hoomd
     from hoomd_gb300 import md
+    c = wl.config
     sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=seed)
     sim.create_state_from_snapshot(snap)
-    sim.state.thermalize_particle_momenta(hoomd.filter.All(), kT)
-    cell = md.nlist.Cell(buffer=WORKLOAD["buffer"])
-    lj = md.pair.LJ(nlist=cell, default_r_cut=WORKLOAD["r_cut"])
-    lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
-    method = md.methods.ConstantVolume(
-        hoomd.filter.All(), md.methods.thermostats.Bussi(kT=kT) if thermostat else None)
-    sim.operations.integrator = md.Integrator(dt=WORKLOAD["dt"], forces=[lj], methods=[method])
-    if sort_period:
-        sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=sort_period))
-    return sim, lj, cell, method
+    sim.state.thermalize_particle_momenta(hoomd.filter.All(), c["kT"])
+    cell = md.nlist.Cell(buffer=c["buffer"])
+    force = wl.force(md, cell, snap)
+    method = md.methods.ConstantVolume(hoomd.filter.All(),
+                                       md.methods.thermostats.Bussi(kT=c["kT"]))
+    sim.operations.integrator = md.Integrator(dt=c["dt"], forces=[force], methods=[method])
+    if c.get("sort_period"):
+        sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=c["sort_period"]))
+    return sim, force, cell, method
 
 
-def traffic_per_launch():
+def traffic_per_launch(wl):
     """DRAM bytes (read + write) per launch of the fused pair kernel from the committed ncu
-    summary, when one exists."""
+    summary of this workload, when one exists."""
     p = REPO / "profiles" / "pair_step_lj_traffic.json"
-    if p.exists():
+    if wl.name == "lj_fcc_1m" and p.exists():
         d = json.loads(p.read_text())
         return d.get("dram_bytes_per_launch_scaled_to_1M")
     return None
 
 
-def cpu_baseline_sample(snap, max_seconds=20.0):
-    """The oracle (single thread, FP64 Scalar, half list + third law: the reference's CPU path)
-    on the same 1M-particle system: one untimed step, then as many timed steps as fit in
-    ~max_seconds (at least 2)."""
+def oracle_sim(wl, snap, full, nthreads):
     import numpy as np
     from oracle import oracle as O
     p = snap.particles
     N = p.N
+    kind, par, tdata, rc = wl.oracle_inputs(snap)
     pos4 = O.make_pos4(p.position, p.typeid, 64)
     vel4 = np.zeros((N, 4))
     vel4[:, 3] = 1.0
-    vel4 = O.thermalize(vel4, np.arange(N), 1.5, 0, 1, prec=64)
-    sim = O.Sim(pos4, vel4, np.zeros((N, 3), np.int32), np.arange(N), snap.configuration.box,
-                [[WORKLOAD["r_cut"]]], WORKLOAD["buffer"], WORKLOAD["dt"], params=[[1.0, 1.0]],
-                full=False, prec=64, nthreads=1)
+    vel4 = O.thermalize(vel4, np.arange(N), wl.config["kT"], 0, 1, prec=64)
+    return O.Sim(pos4, vel4, np.zeros((N, 3), np.int32), np.arange(N), snap.configuration.box,
+                 rc, wl.config["buffer"], wl.config["dt"], kind=kind, params=par, tdata=tdata,
+                 full=full, prec=64, nthreads=nthreads, bussi=wl.timed_thermostat,
+                 kT=wl.config["kT"], seed=1)
+
+
+def cpu_baseline_sample(wl, snap, max_seconds=20.0):
+    """The oracle (single thread, FP64 Scalar, half list + third law: the reference's CPU path)
+    on the same system: one untimed step, then as many timed steps as fit in ~max_seconds."""
+    sim = oracle_sim(wl, snap, full=False, nthreads=1)
     t0 = time.perf_counter()
     sim.run(1)
-    t1 = time.perf_counter()
-    per = max(1e-3, t1 - t0)
+    per = max(1e-3, time.perf_counter() - t0)
     n = max(2, int(max_seconds / per))
     t0 = time.perf_counter()
     sim.run(n)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{n} timesteps of the 1,048,576-particle LJ system after one untimed "
-                      f"step; oracle FP64, half list, single thread"}
+            "sample": f"{n} timesteps of the {snap.particles.N}-particle {wl.name} system after "
+                      f"one untimed step; oracle FP64, half list, single thread"}
 
 
 def run_gb300(args):
-    import numpy as np
     import torch
 
-    from hoomd_gb300 import workloads
-
+    wl = workloads_registry(args.fcc_m)[args.workload]
     rank, world, local = dist_init()
     torch.cuda.set_device(local)
-    snap = workloads.lj_fluid_fcc(m=args.fcc_m, density=WORKLOAD["density"], jitter=0.05,
-                                  seed=1 + rank)
+    snap = wl.make_snap(1 + rank)
     N = snap.particles.N
-    if args.fcc_m != 64:
-        WORKLOAD.update(workload=f"lj_fluid_fcc_{N}", N=N, lattice=f"fcc {args.fcc_m}^3")
-    sim, lj, cell, method = make_sim(snap, seed=1 + rank)
-    # warm-up / equilibration (Bussi)
-    sim.run(max(3, args.warmup))
-    method.thermostat = None  # NVE for the timed steps
-    sim._needs_prep = True
+    sim, force, cell, method = make_sim(wl, snap, seed=1 + rank)
+    sim.run(max(3, args.warmup))  # warm-up / equilibration (Bussi)
+    if not wl.timed_thermostat:
+        method.thermostat = None  # NVE for the timed steps
+        sim._needs_prep = True
     sim.run(3)
     integ = sim._cpp_integrator
     stream = torch.cuda.ExternalStream(integ.streamHandle())
@@ -214,14 +319,14 @@ def run_gb300(args):
     tps = args.steps / (ms_max / 1e3)
 
     # end to end through the public API: host snapshot in (H2D), K steps, snapshot and
-    # energies out (D2H), wall clock
+    # energy out (D2H), wall clock
     snap_now = sim.state.get_snapshot()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim.state.set_snapshot(snap_now)
     sim.run(args.steps)
     out = sim.state.get_snapshot()
-    e_pot = lj.energy
+    e_pot = force.energy
     t_e2e = time.perf_counter() - t0
     h2d = N * (16 + 16 + 12 + 4)  # positions+type, velocities+mass, images, tags (FP32/int)
     d2h = N * (16 + 16 + 12 + 4) + N * 16  # state back + per-particle force/energy for E_pot
@@ -235,23 +340,25 @@ def run_gb300(args):
     bytes_pair = N * (16 + 4 + 16 + 16 + 16 + 12) + 4.0 * sum_n
     achieved = bytes_pair / t_pair / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic_per_launch(),
-                "kernel": "k_pair<EvalLJ,1,col,single-type,fused step two + fp64 thermo>",
+                "frac": achieved / peak, "traffic": traffic_per_launch(wl),
+                "kernel": "k_pair_i4 (gb_md_pair_step_*: pair forces + step two + fp64 thermo)",
                 "algorithmic_bytes_per_launch": bytes_pair,
+                "bytes_formula": "N*(16 pos + 4 n_neigh + 16 force + 16+16 vel r/w + 12 accel) "
+                                 "+ 4*sum(n_neigh)",
                 "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind ==
                 "measured" else "fallback 6.8 TB/s",
                 "kernel_ms": phases[2], "step_one_ms": phases[0], "rebuild_ms": phases[1]}
 
-    line = {"metric": METRIC, "value": tps * world, "unit": UNIT, "n_gpus": world,
+    line = {"metric": wl.metric, "value": tps * world, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-            "data": "synthetic (seeded FCC lattice, jittered, thermalised)",
-            "config": dict(WORKLOAD, parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
+            "data": "synthetic (seeded lattice, jittered, thermalised)",
+            "config": dict(wl.config, parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
             "pair_evals_per_s": sum_n * tps * world, "nlist_builds": builds,
             "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk}
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline_sample(snap, args.cpu_seconds)
+            line["cpu_baseline"] = cpu_baseline_sample(wl, snap, args.cpu_seconds)
         print(json.dumps(line), flush=True)
 
 
@@ -260,21 +367,12 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import numpy as np
-    from hoomd_gb300 import workloads
-    from oracle import oracle as O
+    wl = workloads_registry(args.fcc_m)[args.workload]
     cores = os.cpu_count() or 1
-    snap = workloads.lj_fluid_fcc(m=64, density=WORKLOAD["density"], jitter=0.05, seed=1)
-    p = snap.particles
-    N = p.N
-    pos4 = O.make_pos4(p.position, p.typeid, 64)
-    vel4 = np.zeros((N, 4))
-    vel4[:, 3] = 1.0
-    vel4 = O.thermalize(vel4, np.arange(N), 1.5, 0, 1, prec=64)
-    sim = O.Sim(pos4, vel4, np.zeros((N, 3), np.int32), np.arange(N), snap.configuration.box,
-                [[WORKLOAD["r_cut"]]], WORKLOAD["buffer"], WORKLOAD["dt"], params=[[1.0, 1.0]],
-                full=True, prec=64, nthreads=cores)
-    sim.run(max(1, min(args.warmup, 3)))  # includes the first neighbour-list build
+    snap = wl.make_snap(1)
+    sim = oracle_sim(wl, snap, full=True, nthreads=cores)
+    warm = max(1, min(args.warmup, 3))
+    sim.run(warm)  # includes the first neighbour-list build
     t0 = time.perf_counter()
     sim.run(1)
     per = time.perf_counter() - t0
@@ -284,15 +382,15 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     v = n / dt
     print(json.dumps({
-        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": n,
-        "warmup": max(1, min(args.warmup, 3)), "ms_per_step": 1e3 * dt / n,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
-        "data": "synthetic (seeded FCC lattice, jittered, thermalised)", "config": WORKLOAD,
+        "metric": wl.metric, "value": v, "unit": UNIT, "n_gpus": 0, "steps": n, "warmup": warm,
+        "ms_per_step": 1e3 * dt / n, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic (seeded lattice, jittered, thermalised)", "config": wl.config,
         "impl": "reference",
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{n} of the {args.steps} requested timesteps (bounded to a "
-                                   f"few minutes) of the 1,048,576-particle LJ system; oracle "
-                                   f"FP64, full list, {cores} OpenMP threads"},
+                                   f"few minutes) of the {snap.particles.N}-particle {wl.name} "
+                                   f"system; oracle FP64, full list, {cores} OpenMP threads"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
         flush=True)
 
@@ -303,11 +401,13 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=200)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", default="lj_fcc_1m",
+                    choices=["lj_fcc_1m", "lj_sc_4096", "ka_262k", "table32_524k"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fcc-m", type=int, default=64,
-                    help="FCC cells per side (64 = the 1,048,576-particle workload; smaller "
-                         "values are for profiling captures only)")
+                    help="FCC cells per side of lj_fcc_1m (64 = the 1,048,576-particle workload; "
+                         "smaller values are for profiling captures only)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

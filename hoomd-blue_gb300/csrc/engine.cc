@@ -352,6 +352,7 @@ void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count
     a.d_conditions = d_nl_cond;
     a.d_head_list = nullptr;
     a.stride = stride;
+    a.interleave = 4;
     a.d_Nmax = d_Nmax.get();
     a.d_pos = pd.pos.get();
     a.N = pd.N;
@@ -446,7 +447,7 @@ std::vector<uint32_t> NeighborList::pair_list(bool full)
     for (unsigned int i = 0; i < pd.N; i++)
         for (unsigned int k = 0; k < nn[i]; k++)
             {
-            uint32_t j = nl[i + (size_t)k * stride];
+            uint32_t j = nl[((size_t)(k >> 2) * stride + i) * 4 + (k & 3)];
             uint32_t a = t[i], b = t[j];
             if (full || a < b)
                 {
@@ -609,6 +610,7 @@ gb_pair_args PairForce::pair_args(bool with_virial)
     a.d_nlist = nl.nlist.get();
     a.d_head_list = nullptr;
     a.stride = nl.stride;
+    a.interleave = 4;
     a.d_rcutsq = d_rcutsq.get();
     a.d_ronsq = d_ronsq.get();
     a.ntypes = ntypes;

@@ -183,7 +183,9 @@ class NeighborList
     bool dirty = true; // r_cut or capacities changed: graphs must be rebuilt
     bool capacity_fixed = false; // start from exactly Nmax_cell / Nmax (tests of the growth path)
     DeviceArray<float> d_r_cut, d_r_listsq, d_rcut_max, xyzf, last_pos;
-    DeviceArray<uint32_t> cell_size, cell_type, adj, nlist, n_neigh, d_Nmax, cond;
+    DeviceArray<uint32_t> cell_size, cell_type, adj, n_neigh, d_Nmax, cond;
+    // column-major, interleaved by 4: neighbour k of particle i at ((k/4)*stride + i)*4 + k%4
+    DeviceArray<uint32_t> nlist;
     };
 
 enum class PairKind

@@ -148,9 +148,18 @@ __global__ void k_cell_adj(uint3 dim, unsigned int ndim, unsigned int width, uns
         }
     }
 
-// The build: see the file comment. MULTI: per-pair r_cut / r_list tables (ntypes > 1);
-// ORTHO: zero tilt factors; FLAT: reference head-list layout instead of column-major.
-template<bool MULTI, bool ORTHO, bool FLAT>
+// The build: see the file comment. Template parameters:
+//  MULTI  per-pair r_cut / r_list tables (ntypes > 1)
+//  LAYOUT 0 = reference flat head-list layout, 1 = column-major, 4 = column-major interleaved by 4
+//  MI     minimum-image method: 0 = BoxDim::minImage (rint) general, 1 = rint orthorhombic,
+//         2 = exact image shift of the adjacent cell (every dimension has >= 4 cells and is
+//         periodic). In case 2 each candidate cell appears once in the 27-cell stencil, so a
+//         candidate within r_list of particle i is the minimum image and the rint image equals the
+//         cell's image; subtracting the cell's L*img terms in minImage's order (z, then y, then x)
+//         reproduces minImage's roundings exactly for every pair that can be in the list, so the
+//         dr^2 <= r_list^2 decisions are unchanged while three multiplies and three rints per
+//         candidate disappear.
+template<bool MULTI, int LAYOUT, int MI>
 __global__ void __launch_bounds__(NL_WARPS * 32)
     k_nlist_binned(unsigned int* __restrict__ nlist, unsigned int* __restrict__ n_neigh,
                    float4* __restrict__ last_pos, unsigned int* __restrict__ cond,
@@ -158,7 +167,7 @@ __global__ void __launch_bounds__(NL_WARPS * 32)
                    const unsigned int* __restrict__ Nmax_t,
                    const unsigned int* __restrict__ cell_size, const float4* __restrict__ xyzf,
                    const unsigned int* __restrict__ cell_type,
-                   const unsigned int* __restrict__ cell_adj, unsigned int ncell,
+                   const unsigned int* __restrict__ cell_adj, uint3 dim, unsigned int ncell,
                    unsigned int Nmax_cell, unsigned int adj_w, gb_box box,
                    const float* __restrict__ r_cut, const float* __restrict__ r_listsq,
                    unsigned int ntypes, const uint32_t* gate)
@@ -185,6 +194,7 @@ __global__ void __launch_bounds__(NL_WARPS * 32)
     const unsigned int cell = blockIdx.x * NL_WARPS + warp;
     if (cell >= ncell)
         return;
+    const int ci = cell % dim.x, cj = (cell / dim.x) % dim.y, ck = cell / (dim.x * dim.y);
     const unsigned int csize = min(cell_size[cell], Nmax_cell);
     for (unsigned int base = 0; base < csize; base += 32)
         {
@@ -200,13 +210,40 @@ __global__ void __launch_bounds__(NL_WARPS * 32)
                 ti = cell_type[(size_t)cell * Nmax_cell + own];
             }
         const unsigned int Nmax_i = MULTI ? (active ? Nmax_t[ti] : 0u) : Nmax0;
-        const uint64_t head = FLAT ? (active ? head_list[i] : 0ull) : (uint64_t)i;
-        const uint64_t step = FLAT ? 1ull : stride;
+        const uint64_t head = (LAYOUT == 0) ? (active ? head_list[i] : 0ull) : (uint64_t)i;
         unsigned int cnt = 0;
+        auto store = [&](unsigned int j) {
+            if (cnt < Nmax_i)
+                {
+                if (LAYOUT == 0)
+                    nlist[head + cnt] = j;
+                else if (LAYOUT == 1)
+                    nlist[head + (uint64_t)cnt * stride] = j;
+                else
+                    nlist[((uint64_t)(cnt >> 2) * stride + i) * 4 + (cnt & 3)] = j;
+                }
+            cnt++;
+        };
         for (unsigned int a = 0; a < adj_w; a++)
             {
             const unsigned int nc = __ldg(cell_adj + (size_t)cell * adj_w + a);
             const unsigned int nsz = min(__ldg(cell_size + nc), Nmax_cell);
+            // image of the adjacent cell relative to this one (MI == 2)
+            float sz = 0.f, syz = 0.f, sxz = 0.f, sy = 0.f, sxy = 0.f, sx = 0.f;
+            if (MI == 2)
+                {
+                const int ni = nc % dim.x, nj = (nc / dim.x) % dim.y, nk = nc / (dim.x * dim.y);
+                const int dx_c = ni - ci, dy_c = nj - cj, dz_c = nk - ck;
+                const float ix = dx_c == (int)dim.x - 1 ? -1.f : (dx_c == 1 - (int)dim.x ? 1.f : 0.f);
+                const float iy = dy_c == (int)dim.y - 1 ? -1.f : (dy_c == 1 - (int)dim.y ? 1.f : 0.f);
+                const float iz = dz_c == (int)dim.z - 1 ? -1.f : (dz_c == 1 - (int)dim.z ? 1.f : 0.f);
+                sz = fmul(box.L[2], iz);
+                syz = fmul(fmul(box.L[2], box.yz), iz);
+                sxz = fmul(fmul(box.L[2], box.xz), iz);
+                sy = fmul(box.L[1], iy);
+                sxy = fmul(fmul(box.L[1], box.xy), iy);
+                sx = fmul(box.L[0], ix);
+                }
             for (unsigned int cb = 0; cb < nsz; cb += 32)
                 {
                 if (cb + lane < nsz)
@@ -219,12 +256,22 @@ __global__ void __launch_bounds__(NL_WARPS * 32)
                 const unsigned int m = min(32u, nsz - cb);
                 if (active)
                     {
+#pragma unroll 2
                     for (unsigned int t = 0; t < m; t++)
                         {
                         const float4 c = s_cand[warp][t];
                         const unsigned int j = __float_as_uint(c.w);
                         float dx = fsub(pi.x, c.x), dy = fsub(pi.y, c.y), dz = fsub(pi.z, c.z);
-                        if (ORTHO)
+                        if (MI == 2)
+                            {
+                            dz = fsub(dz, sz);
+                            dy = fsub(dy, syz);
+                            dx = fsub(dx, sxz);
+                            dy = fsub(dy, sy);
+                            dx = fsub(dx, sxy);
+                            dx = fsub(dx, sx);
+                            }
+                        else if (MI == 1)
                             min_image_ortho(box, dx, dy, dz);
                         else
                             min_image(box, dx, dy, dz);
@@ -242,11 +289,7 @@ __global__ void __launch_bounds__(NL_WARPS * 32)
                             rl = rl0;
                             }
                         if (rsq <= rl && j != i && rc > 0.0f)
-                            {
-                            if (cnt < Nmax_i)
-                                nlist[head + (uint64_t)cnt * step] = j;
-                            cnt++;
-                            }
+                            store(j);
                         }
                     }
                 __syncwarp();
@@ -265,15 +308,285 @@ __global__ void __launch_bounds__(NL_WARPS * 32)
         }
     }
 
-template<bool MULTI, bool ORTHO, bool FLAT>
+// Tiled build for the common case (every dimension >= 4 cells and periodic, column-major list):
+// one warp per cell. For each z-plane of the 3x3x3 stencil the warp stages the nine adjacent
+// cells' particles in shared memory together with each cell's exact image shift (the MI == 2
+// argument above), then every lane takes one staged candidate and the warp walks the cell's own
+// particles. For own particle o, the lanes whose candidate is within r_list form a ballot; each
+// writes its candidate at position count(o) + rank, and count(o) (held by lane o) advances by the
+// ballot's population. All 32 lanes test a distinct pair in every iteration, the store path is
+// one predicated store per lane, and neighbours appear in a fixed order (stencil plane, cell,
+// slot), so the list is as deterministic as the cell list it is built from.
+constexpr int TILE_WARPS_MAX = 4;
+
+__device__ __forceinline__ unsigned int wrap_cell(int c, int n)
+    {
+    return (unsigned int)(c < 0 ? c + n : (c >= n ? c - n : c));
+    }
+
+template<bool MULTI, int LAYOUT, bool ORTHO>
+__global__ void __launch_bounds__(TILE_WARPS_MAX * 32)
+    k_nlist_tile(unsigned int* __restrict__ nlist, unsigned int* __restrict__ n_neigh,
+                 float4* __restrict__ last_pos, unsigned int* __restrict__ cond, uint64_t stride,
+                 const unsigned int* __restrict__ Nmax_t,
+                 const unsigned int* __restrict__ cell_size, const float4* __restrict__ xyzf,
+                 const unsigned int* __restrict__ cell_type, uint3 dim, unsigned int ncell,
+                 unsigned int Nmax_cell, gb_box box, const float* __restrict__ r_cut,
+                 const float* __restrict__ r_listsq, unsigned int ntypes, const uint32_t* gate)
+    {
+    if (gate && *gate == 0)
+        return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wpb = blockDim.x / 32;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    // block-wide: type tables (MULTI)
+    float* s_tab = reinterpret_cast<float*>(smem);
+    const size_t tab_bytes = MULTI ? ((2 * sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
+    if (MULTI)
+        {
+        for (unsigned int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x)
+            {
+            s_tab[t] = r_cut[t];
+            s_tab[ntypes * ntypes + t] = r_listsq[t];
+            }
+        __syncthreads();
+        }
+    // per-warp region
+    const size_t per_warp = (size_t)Nmax_cell * (16 + 16 * 9 + 4 * 9 + 4) + 9 * 6 * 4;
+    unsigned char* base = smem + tab_bytes + (size_t)warp * ((per_warp + 15) / 16 * 16);
+    float4* s_own = reinterpret_cast<float4*>(base);
+    float4* s_cand = s_own + Nmax_cell;
+    unsigned int* s_meta = reinterpret_cast<unsigned int*>(s_cand + 9 * Nmax_cell);
+    unsigned int* s_otype = s_meta + 9 * Nmax_cell;
+    float* s_shift = reinterpret_cast<float*>(s_otype + Nmax_cell);
+
+    const unsigned int cell = blockIdx.x * wpb + warp;
+    if (cell >= ncell)
+        return;
+    const int ci = cell % dim.x, cj = (cell / dim.x) % dim.y, ck = cell / (dim.x * dim.y);
+    const unsigned int csize = min(cell_size[cell], Nmax_cell);
+    if (csize == 0)
+        return;
+    for (unsigned int a = lane; a < csize; a += 32)
+        {
+        s_own[a] = xyzf[(size_t)cell * Nmax_cell + a];
+        if (MULTI)
+            s_otype[a] = cell_type[(size_t)cell * Nmax_cell + a];
+        }
+    __syncwarp();
+    const float rc0 = MULTI ? 0.0f : r_cut[0];
+    const float rl0 = MULTI ? 0.0f : r_listsq[0];
+    const unsigned int Nmax0 = MULTI ? 0u : Nmax_t[0];
+    const unsigned int lt_mask = (1u << lane) - 1u;
+    const size_t row4 = (size_t)stride * 4u; // entries between consecutive groups of four
+
+    for (unsigned int ob = 0; ob < csize; ob += 32)
+        {
+        const unsigned int nown = min(32u, csize - ob);
+        unsigned int my_cnt = 0; // count of own particle ob + lane
+        for (int pz = -1; pz <= 1; pz++)
+            {
+            // stage the nine cells of this plane; lane q < 9 describes cell q
+            unsigned int q_cell = 0, q_n = 0;
+            if (lane < 9)
+                {
+                const int ox = lane % 3 - 1, oy = lane / 3 - 1;
+                const unsigned int ni = wrap_cell(ci + ox, dim.x);
+                const unsigned int nj = wrap_cell(cj + oy, dim.y);
+                const unsigned int nk = wrap_cell(ck + pz, dim.z);
+                q_cell = (nk * dim.y + nj) * dim.x + ni;
+                q_n = min(__ldg(cell_size + q_cell), Nmax_cell);
+                // minImage's image rint((x_i - x_j)/L) for this cell: +1 when the stencil wraps
+                // past the high face (x_j near the low face, x_i near the high face), -1 past
+                // the low face, 0 otherwise
+                const float ix = (ci + ox >= (int)dim.x) ? 1.f : (ci + ox < 0 ? -1.f : 0.f);
+                const float iy = (cj + oy >= (int)dim.y) ? 1.f : (cj + oy < 0 ? -1.f : 0.f);
+                const float iz = (ck + pz >= (int)dim.z) ? 1.f : (ck + pz < 0 ? -1.f : 0.f);
+                s_shift[lane * 6 + 0] = fmul(box.L[2], iz);
+                s_shift[lane * 6 + 1] = fmul(fmul(box.L[2], box.yz), iz);
+                s_shift[lane * 6 + 2] = fmul(fmul(box.L[2], box.xz), iz);
+                s_shift[lane * 6 + 3] = fmul(box.L[1], iy);
+                s_shift[lane * 6 + 4] = fmul(fmul(box.L[1], box.xy), iy);
+                s_shift[lane * 6 + 5] = fmul(box.L[0], ix);
+                }
+            // exclusive prefix of the nine counts
+            unsigned int incl = q_n;
+#pragma unroll
+            for (int o = 1; o < 16; o <<= 1)
+                {
+                const unsigned int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                    incl += y;
+                }
+            const unsigned int ncand = __shfl_sync(0xffffffffu, incl, 8);
+            for (int q = 0; q < 9; q++)
+                {
+                const unsigned int qc = __shfl_sync(0xffffffffu, q_cell, q);
+                const unsigned int qn = __shfl_sync(0xffffffffu, q_n, q);
+                const unsigned int qo = __shfl_sync(0xffffffffu, incl - q_n, q);
+                for (unsigned int t = lane; t < qn; t += 32)
+                    {
+                    s_cand[qo + t] = __ldg(xyzf + (size_t)qc * Nmax_cell + t);
+                    s_meta[qo + t] = (unsigned int)q
+                                     | (MULTI ? (__ldg(cell_type + (size_t)qc * Nmax_cell + t) << 8)
+                                              : 0u);
+                    }
+                }
+            __syncwarp();
+            for (unsigned int cb = 0; cb < ncand; cb += 32)
+                {
+                const unsigned int t = cb + lane;
+                const bool has = t < ncand;
+                float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+                unsigned int meta = 0;
+                if (has)
+                    {
+                    c = s_cand[t];
+                    meta = s_meta[t];
+                    }
+                const unsigned int j = __float_as_uint(c.w);
+                const float* sh = s_shift + (meta & 0xffu) * 6;
+                const float sz = sh[0], syz = sh[1], sxz = sh[2], sy = sh[3], sxy = sh[4], sx = sh[5];
+                const unsigned int tj = meta >> 8;
+                for (unsigned int o = 0; o < nown; o++)
+                    {
+                    const float4 pi = s_own[ob + o];
+                    const unsigned int i = __float_as_uint(pi.w);
+                    float dx = fsub(pi.x, c.x), dy = fsub(pi.y, c.y), dz = fsub(pi.z, c.z);
+                    dz = fsub(dz, sz);
+                    if (!ORTHO)
+                        {
+                        dy = fsub(dy, syz); // tilt terms; exactly zero in an orthorhombic box
+                        dx = fsub(dx, sxz);
+                        }
+                    dy = fsub(dy, sy);
+                    if (!ORTHO)
+                        dx = fsub(dx, sxy);
+                    dx = fsub(dx, sx);
+                    const float rsq = dot3(dx, dy, dz);
+                    float rc, rl;
+                    unsigned int nmax_o;
+                    if (MULTI)
+                        {
+                        const unsigned int ti = s_otype[ob + o];
+                        rc = s_tab[ti * ntypes + tj];
+                        rl = s_tab[ntypes * ntypes + ti * ntypes + tj];
+                        nmax_o = __ldg(Nmax_t + ti);
+                        }
+                    else
+                        {
+                        rc = rc0;
+                        rl = rl0;
+                        nmax_o = Nmax0;
+                        }
+                    const bool hit = has && rsq <= rl && j != i && rc > 0.0f;
+                    const unsigned int bal = __ballot_sync(0xffffffffu, hit);
+                    if (bal)
+                        {
+                        const unsigned int cnt_o = __shfl_sync(0xffffffffu, my_cnt, o);
+                        const unsigned int k = cnt_o + __popc(bal & lt_mask);
+                        if (hit && k < nmax_o)
+                            {
+                            if (LAYOUT == 4)
+                                nlist[(size_t)(k >> 2) * row4 + (size_t)i * 4u + (k & 3u)] = j;
+                            else
+                                nlist[(size_t)k * stride + i] = j;
+                            }
+                        if (lane == (int)o)
+                            my_cnt += __popc(bal);
+                        }
+                    }
+                }
+            __syncwarp();
+            }
+        if (lane < (int)nown)
+            {
+            const float4 pi = s_own[ob + lane];
+            const unsigned int i = __float_as_uint(pi.w);
+            const unsigned int nmax_i = MULTI ? Nmax_t[s_otype[ob + lane]] : Nmax0;
+            n_neigh[i] = min(my_cnt, nmax_i);
+            if (my_cnt > nmax_i)
+                atomicMax(&cond[MULTI ? s_otype[ob + lane] : 0u], my_cnt);
+            if (last_pos)
+                last_pos[i] = make_float4(pi.x, pi.y, pi.z, 0.0f);
+            }
+        __syncwarp();
+        }
+    }
+
+size_t tile_smem_bytes(unsigned int Nmax_cell, unsigned int ntypes, bool multi, int wpb)
+    {
+    const size_t tab = multi ? ((2 * sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
+    const size_t per_warp = (size_t)Nmax_cell * (16 + 16 * 9 + 4 * 9 + 4) + 9 * 6 * 4;
+    return tab + (size_t)wpb * ((per_warp + 15) / 16 * 16);
+    }
+
+template<bool MULTI, int LAYOUT>
+bool launch_nlist_tile(const gb_nlist_args& a, unsigned int ncell, cudaStream_t s)
+    {
+    const bool ortho = a.box.xy == 0.0f && a.box.xz == 0.0f && a.box.yz == 0.0f;
+    int wpb = TILE_WARPS_MAX;
+    size_t smem = tile_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, wpb);
+    while (smem > 96 * 1024 && wpb > 1)
+        smem = tile_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, --wpb);
+    if (smem > 200 * 1024)
+        return false;
+    auto kern = ortho ? k_nlist_tile<MULTI, LAYOUT, true> : k_nlist_tile<MULTI, LAYOUT, false>;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<div_up(ncell, wpb), wpb * 32, smem, s>>>(
+        a.d_nlist, a.d_n_neigh, reinterpret_cast<float4*>(a.d_last_pos), a.d_conditions, a.stride,
+        a.d_Nmax, a.d_cell_size, reinterpret_cast<const float4*>(a.d_xyzf), a.d_cell_type,
+        make_uint3(a.dim[0], a.dim[1], a.dim[2]), ncell, a.Nmax_cell, a.box, a.d_r_cut,
+        a.d_r_listsq, a.ntypes, a.d_gate);
+    return true;
+    }
+
+template<bool MULTI, int LAYOUT, int MI>
 void launch_nlist(const gb_nlist_args& a, unsigned int ncell, cudaStream_t s)
     {
     size_t smem = MULTI ? 2 * sizeof(float) * a.ntypes * a.ntypes : 0;
-    k_nlist_binned<MULTI, ORTHO, FLAT><<<div_up(ncell, NL_WARPS), NL_WARPS * 32, smem, s>>>(
+    k_nlist_binned<MULTI, LAYOUT, MI><<<div_up(ncell, NL_WARPS), NL_WARPS * 32, smem, s>>>(
         a.d_nlist, a.d_n_neigh, reinterpret_cast<float4*>(a.d_last_pos), a.d_conditions,
         a.d_head_list, a.stride, a.d_Nmax, a.d_cell_size,
-        reinterpret_cast<const float4*>(a.d_xyzf), a.d_cell_type, a.d_cell_adj, ncell,
-        a.Nmax_cell, a.adj_width, a.box, a.d_r_cut, a.d_r_listsq, a.ntypes, a.d_gate);
+        reinterpret_cast<const float4*>(a.d_xyzf), a.d_cell_type, a.d_cell_adj,
+        make_uint3(a.dim[0], a.dim[1], a.dim[2]), ncell, a.Nmax_cell, a.adj_width, a.box,
+        a.d_r_cut, a.d_r_listsq, a.ntypes, a.d_gate);
+    }
+
+template<bool MULTI, int LAYOUT>
+void launch_nlist_mi(const gb_nlist_args& a, unsigned int ncell, cudaStream_t s)
+    {
+    const bool ortho = a.box.xy == 0.0f && a.box.xz == 0.0f && a.box.yz == 0.0f;
+    const bool all_periodic = a.box.periodic[0] && a.box.periodic[1] && a.box.periodic[2];
+    // four or more cells per side: an index difference of +-(dim-1) can only be a wrapped
+    // neighbour, and rint(dx/L) agrees with the cell image whenever |dx| <= L/2 could matter
+    if (a.adj_width == 27 && all_periodic && a.dim[0] >= 4 && a.dim[1] >= 4 && a.dim[2] >= 4)
+        launch_nlist<MULTI, LAYOUT, 2>(a, ncell, s);
+    else if (ortho)
+        launch_nlist<MULTI, LAYOUT, 1>(a, ncell, s);
+    else
+        launch_nlist<MULTI, LAYOUT, 0>(a, ncell, s);
+    }
+
+template<bool MULTI>
+void launch_nlist_layout(const gb_nlist_args& a, unsigned int ncell, cudaStream_t s)
+    {
+    const bool all_periodic = a.box.periodic[0] && a.box.periodic[1] && a.box.periodic[2];
+    const bool tiled = !a.d_head_list && a.adj_width == 27 && all_periodic && a.dim[0] >= 4
+                       && a.dim[1] >= 4 && a.dim[2] >= 4;
+    if (tiled)
+        {
+        if (a.interleave == 4 ? launch_nlist_tile<MULTI, 4>(a, ncell, s)
+                              : launch_nlist_tile<MULTI, 1>(a, ncell, s))
+            return;
+        }
+    if (a.d_head_list)
+        launch_nlist_mi<MULTI, 0>(a, ncell, s);
+    else if (a.interleave == 4)
+        launch_nlist_mi<MULTI, 4>(a, ncell, s);
+    else
+        launch_nlist_mi<MULTI, 1>(a, ncell, s);
     }
 
 __global__ void k_needs_update(uint32_t* result, const float4* __restrict__ last_pos,
@@ -419,28 +732,13 @@ extern "C"
         const unsigned int ncell = a->dim[0] * a->dim[1] * a->dim[2];
         if (ncell == 0 || a->N == 0)
             return GB_OK;
+        GB_REQUIRE(a->d_head_list || a->interleave <= 1 || a->interleave == 4,
+                   "gb_nlist_build_binned: interleave must be 1 or 4");
         cudaStream_t s = (cudaStream_t)stream;
-        const bool multi = a->ntypes > 1;
-        const bool ortho = a->box.xy == 0.0f && a->box.xz == 0.0f && a->box.yz == 0.0f;
-        const bool flat = a->d_head_list != nullptr;
-        if (multi)
-            {
-            if (ortho)
-                flat ? launch_nlist<true, true, true>(*a, ncell, s)
-                     : launch_nlist<true, true, false>(*a, ncell, s);
-            else
-                flat ? launch_nlist<true, false, true>(*a, ncell, s)
-                     : launch_nlist<true, false, false>(*a, ncell, s);
-            }
+        if (a->ntypes > 1)
+            launch_nlist_layout<true>(*a, ncell, s);
         else
-            {
-            if (ortho)
-                flat ? launch_nlist<false, true, true>(*a, ncell, s)
-                     : launch_nlist<false, true, false>(*a, ncell, s);
-            else
-                flat ? launch_nlist<false, false, true>(*a, ncell, s)
-                     : launch_nlist<false, false, false>(*a, ncell, s);
-            }
+            launch_nlist_layout<false>(*a, ncell, s);
         return check_launch("gb_nlist_build_binned");
         }
 

@@ -308,6 +308,276 @@ __global__ void __launch_bounds__(256)
         fuse_finish(fz, ke_d, pe_d, w_d);
     }
 
+// Fast path for the column-major list interleaved by 4 (gb_nlist_args.interleave = 4): one thread
+// per particle reads four neighbour indices with one 16-byte streaming load (a warp reads 512
+// contiguous bytes), keeps the next two index batches in flight while the current four position
+// gathers and pair evaluations run, and masks the tail of the list by substituting the particle
+// itself (a valid address) and discarding its result.
+__device__ __forceinline__ uint4 ld_stream_u4(const uint4* p)
+    {
+    return __ldcs(p);
+    }
+
+// bytes of the per-type tables at the start of the kernel's dynamic shared memory, rounded to 16
+template<class P> __host__ __device__ inline size_t i4_param_bytes(unsigned int ntypes, bool multi)
+    {
+    return multi ? ((sizeof(P) + 2 * sizeof(float)) * ntypes * ntypes + 15) / 16 * 16 : 0;
+    }
+
+template<class Eval, bool MULTI, bool ORTHO, bool FUSE, bool VIRIAL, bool XPLOR>
+__global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
+    k_pair_i4(float4* __restrict__ d_force, float* __restrict__ d_virial, size_t pitch,
+              unsigned int N, const float4* __restrict__ d_pos, gb_box box,
+              const unsigned int* __restrict__ d_n_neigh, const uint4* __restrict__ d_nlist4,
+              uint64_t stride, const typename Eval::param_type* __restrict__ d_params,
+              const float* __restrict__ d_rcutsq, const float* __restrict__ d_ronsq,
+              unsigned int ntypes, const float* __restrict__ ext, bool SHIFT1, FuseArgs fz)
+    {
+    using P = typename Eval::param_type;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    P* s_params = reinterpret_cast<P*>(s_raw);
+    const unsigned int np = ntypes * ntypes;
+    float* s_rcutsq = reinterpret_cast<float*>(s_raw + sizeof(P) * np);
+    float* s_ronsq = s_rcutsq + np;
+    if (MULTI)
+        {
+        for (unsigned int t = threadIdx.x; t < np; t += blockDim.x)
+            {
+            s_params[t] = d_params[t];
+            s_rcutsq[t] = d_rcutsq[t];
+            if (XPLOR)
+                s_ronsq[t] = d_ronsq[t];
+            }
+        __syncthreads();
+        }
+    P p0;
+    float rc0 = 0.0f, ro0 = 0.0f;
+    if (!MULTI)
+        {
+        p0 = d_params[0];
+        rc0 = d_rcutsq[0];
+        if (XPLOR)
+            ro0 = d_ronsq[0];
+        }
+
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < N;
+    float fx = 0.f, fy = 0.f, fz_ = 0.f, pe = 0.f;
+    float vxx = 0.f, vxy = 0.f, vxz = 0.f, vyy = 0.f, vyz = 0.f, vzz = 0.f;
+    if (active)
+        {
+        const unsigned int nn = d_n_neigh[i];
+        const float4 pi = __ldg(d_pos + i);
+        const unsigned int ti = __float_as_uint(pi.w);
+        // minimum image with fused multiply-adds (forces are held to a tolerance; only the
+        // neighbour-list build needs minImage's exact roundings); every direction periodic
+        const float Lx = box.L[0], Ly = box.L[1], Lz = box.L[2];
+        const float Lix = box.Linv[0], Liy = box.Linv[1], Liz = box.Linv[2];
+        const float Lzxz = box.L[2] * box.xz, Lzyz = box.L[2] * box.yz, Lyxy = box.L[1] * box.xy;
+        auto pair = [&](const float4 pj, bool valid) {
+            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            if (ORTHO)
+                {
+                dx -= Lx * rintf(dx * Lix);
+                dy -= Ly * rintf(dy * Liy);
+                dz -= Lz * rintf(dz * Liz);
+                }
+            else
+                {
+                const float iz = rintf(dz * Liz);
+                dz -= Lz * iz;
+                dy -= Lzyz * iz;
+                dx -= Lzxz * iz;
+                const float iy = rintf(dy * Liy);
+                dy -= Ly * iy;
+                dx -= Lyxy * iy;
+                dx -= Lx * rintf(dx * Lix);
+                }
+            const float rsq = dx * dx + dy * dy + dz * dz;
+            const P* param;
+            float rcutsq, ronsq = 0.0f;
+            if (MULTI)
+                {
+                const unsigned int tp = ti * ntypes + __float_as_uint(pj.w);
+                param = s_params + tp;
+                rcutsq = s_rcutsq[tp];
+                if (XPLOR)
+                    ronsq = s_ronsq[tp];
+                }
+            else
+                {
+                param = &p0;
+                rcutsq = rc0;
+                ronsq = ro0;
+                }
+            const bool energy_shift = XPLOR ? (ronsq > rcutsq) : SHIFT1;
+            float force_divr = 0.0f, pair_eng = 0.0f;
+            Eval eval(rsq, rcutsq, *param, ext);
+            eval.evalForceAndEnergy(force_divr, pair_eng, energy_shift);
+            if (XPLOR && rsq >= ronsq && rsq < rcutsq)
+                {
+                const float old_pair_eng = pair_eng;
+                const float old_force_divr = force_divr;
+                const float xplor_denom_inv
+                    = 1.0f / ((rcutsq - ronsq) * (rcutsq - ronsq) * (rcutsq - ronsq));
+                const float rsq_minus_r_cut_sq = rsq - rcutsq;
+                const float s = rsq_minus_r_cut_sq * rsq_minus_r_cut_sq
+                                * (rcutsq + 2.0f * rsq - 3.0f * ronsq) * xplor_denom_inv;
+                const float ds_dr_divr = 12.0f * (rsq - ronsq) * rsq_minus_r_cut_sq * xplor_denom_inv;
+                pair_eng = old_pair_eng * s;
+                force_divr = s * old_force_divr - ds_dr_divr * old_pair_eng;
+                }
+            if (!valid)
+                {
+                force_divr = 0.0f;
+                pair_eng = 0.0f;
+                }
+            if (VIRIAL)
+                {
+                const float force_div2r = 0.5f * force_divr;
+                vxx += dx * dx * force_div2r;
+                vxy += dx * dy * force_div2r;
+                vxz += dx * dz * force_div2r;
+                vyy += dy * dy * force_div2r;
+                vyz += dy * dz * force_div2r;
+                vzz += dz * dz * force_div2r;
+                }
+            fx += dx * force_divr;
+            fy += dy * force_divr;
+            fz_ += dz * force_divr;
+            pe += pair_eng;
+        };
+        // full groups of four with no per-pair masking, then the partial last group; index
+        // loads run two groups ahead of the four independent position gathers
+        const unsigned int nfull = nn >> 2;
+        const unsigned int rem = nn & 3u;
+        const uint4* p4 = d_nlist4 + i;
+        const uint4 self = make_uint4(i, i, i, i);
+        uint4 jA = self, jB = self;
+        if (nfull > 0)
+            jA = ld_stream_u4(p4);
+        if (nfull > 1)
+            jB = ld_stream_u4(p4 + stride);
+        for (unsigned int b = 0; b < nfull; b++)
+            {
+            const uint4 jc = jA;
+            jA = jB;
+            if (b + 2 < nfull)
+                jB = ld_stream_u4(p4 + (uint64_t)(b + 2) * stride);
+            const float4 q0 = __ldg(d_pos + jc.x);
+            const float4 q1 = __ldg(d_pos + jc.y);
+            const float4 q2 = __ldg(d_pos + jc.z);
+            const float4 q3 = __ldg(d_pos + jc.w);
+            pair(q0, true);
+            pair(q1, true);
+            pair(q2, true);
+            pair(q3, true);
+            }
+        if (rem)
+            {
+            const uint4 jc = ld_stream_u4(p4 + (uint64_t)nfull * stride);
+            const float4 q0 = __ldg(d_pos + jc.x);
+            const float4 q1 = __ldg(d_pos + (rem > 1 ? jc.y : i));
+            const float4 q2 = __ldg(d_pos + (rem > 2 ? jc.z : i));
+            pair(q0, true);
+            pair(q1, rem > 1);
+            pair(q2, rem > 2);
+            }
+        pe *= 0.5f;
+        }
+    double ke_d = 0.0, pe_d = 0.0, w_d = 0.0;
+    if (active)
+        {
+        d_force[i] = make_float4(fx, fy, fz_, pe);
+        if (VIRIAL)
+            {
+            d_virial[0 * pitch + i] = vxx;
+            d_virial[1 * pitch + i] = vxy;
+            d_virial[2 * pitch + i] = vxz;
+            d_virial[3 * pitch + i] = vyy;
+            d_virial[4 * pitch + i] = vyz;
+            d_virial[5 * pitch + i] = vzz;
+            w_d = (double)vxx + (double)vyy + (double)vzz;
+            }
+        if (FUSE)
+            {
+            float4 v = fz.vel[i];
+            const float minv = __frcp_rn(v.w);
+            const float ax = __fmul_rn(fx, minv), ay = __fmul_rn(fy, minv),
+                        az = __fmul_rn(fz_, minv);
+            const float s2 = fz.d_scale2 ? (float)*fz.d_scale2 : 1.0f;
+            const float hdt = __fmul_rn(0.5f, fz.dt);
+            v.x = __fadd_rn(__fmul_rn(v.x, s2), __fmul_rn(hdt, ax));
+            v.y = __fadd_rn(__fmul_rn(v.y, s2), __fmul_rn(hdt, ay));
+            v.z = __fadd_rn(__fmul_rn(v.z, s2), __fmul_rn(hdt, az));
+            fz.vel[i] = v;
+            fz.accel[3 * (size_t)i + 0] = ax;
+            fz.accel[3 * (size_t)i + 1] = ay;
+            fz.accel[3 * (size_t)i + 2] = az;
+            ke_d = (double)v.w
+                   * ((double)v.x * (double)v.x + (double)v.y * (double)v.y
+                      + (double)v.z * (double)v.z);
+            pe_d = (double)pe;
+            }
+        }
+    if (FUSE)
+        fuse_finish(fz, ke_d, pe_d, w_d);
+    }
+
+template<class Eval, bool MULTI, bool ORTHO, bool FUSE, bool VIRIAL, bool XPLOR>
+int launch_pair_i4_inst(const gb_pair_args& a, const typename Eval::param_type* d_params,
+                        const float* ext, const FuseArgs& fz, cudaStream_t s)
+    {
+    const unsigned int block = 256;
+    const unsigned int grid = div_up(a.N, block);
+    const size_t smem = i4_param_bytes<typename Eval::param_type>(a.ntypes, MULTI);
+    auto kern = k_pair_i4<Eval, MULTI, ORTHO, FUSE, VIRIAL, XPLOR>;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<grid, block, smem, s>>>(reinterpret_cast<float4*>(a.d_force), a.d_virial,
+                                   a.virial_pitch, a.N, reinterpret_cast<const float4*>(a.d_pos),
+                                   a.box, a.d_n_neigh, reinterpret_cast<const uint4*>(a.d_nlist),
+                                   a.stride, d_params, a.d_rcutsq, a.d_ronsq, a.ntypes, ext,
+                                   a.shift_mode == 1, fz);
+    return check_launch("pair force kernel (interleaved list)");
+    }
+
+template<class Eval, bool MULTI, bool ORTHO, bool FUSE>
+int dispatch_pair_i4_vx(const gb_pair_args& a, const typename Eval::param_type* d_params,
+                        const float* ext, const FuseArgs& fz, cudaStream_t s)
+    {
+    const bool xplor = a.shift_mode == 2;
+    if (FUSE)
+        {
+        // the fused step never needs the virial
+        return xplor ? launch_pair_i4_inst<Eval, MULTI, ORTHO, FUSE, false, true>(a, d_params, ext, fz, s)
+                     : launch_pair_i4_inst<Eval, MULTI, ORTHO, FUSE, false, false>(a, d_params, ext, fz, s);
+        }
+    if (a.compute_virial)
+        return xplor ? launch_pair_i4_inst<Eval, MULTI, ORTHO, false, true, true>(a, d_params, ext, fz, s)
+                     : launch_pair_i4_inst<Eval, MULTI, ORTHO, false, true, false>(a, d_params, ext, fz, s);
+    return xplor ? launch_pair_i4_inst<Eval, MULTI, ORTHO, false, false, true>(a, d_params, ext, fz, s)
+                 : launch_pair_i4_inst<Eval, MULTI, ORTHO, false, false, false>(a, d_params, ext, fz, s);
+    }
+
+template<class Eval, bool FUSE>
+int dispatch_pair_i4(const gb_pair_args& a, const typename Eval::param_type* d_params,
+                     const float* ext, const FuseArgs& fz, cudaStream_t s)
+    {
+    GB_REQUIRE(a.shift_mode <= 2, "pair force: shift_mode must be 0, 1 or 2");
+    GB_REQUIRE(a.block_size == 0 || a.block_size == 256,
+               "pair force: the interleaved-list kernel runs 256-thread blocks");
+    GB_REQUIRE(!(FUSE && a.compute_virial), "fused step: the virial is not computed");
+    GB_REQUIRE(a.box.periodic[0] && a.box.periodic[1] && a.box.periodic[2],
+               "pair force: the interleaved-list kernel needs a box periodic in every direction");
+    const bool ortho = a.box.xy == 0.0f && a.box.xz == 0.0f && a.box.yz == 0.0f;
+    if (a.ntypes > 1)
+        return ortho ? dispatch_pair_i4_vx<Eval, true, true, FUSE>(a, d_params, ext, fz, s)
+                     : dispatch_pair_i4_vx<Eval, true, false, FUSE>(a, d_params, ext, fz, s);
+    return ortho ? dispatch_pair_i4_vx<Eval, false, true, FUSE>(a, d_params, ext, fz, s)
+                 : dispatch_pair_i4_vx<Eval, false, false, FUSE>(a, d_params, ext, fz, s);
+    }
+
 template<class Eval, int TPP, bool FLAT, bool MULTI, bool FUSE>
 int launch_pair_inst(const gb_pair_args& a, const typename Eval::param_type* d_params,
                      const float* ext, const FuseArgs& fz, unsigned int block,
@@ -363,6 +633,10 @@ int launch_pair(const gb_pair_args* a, const typename Eval::param_type* d_params
     if (!flat)
         {
         GB_REQUIRE(tpp <= 1, "pair force: column-major lists use one thread per particle");
+        GB_REQUIRE(a->interleave <= 1 || a->interleave == 4,
+                   "pair force: interleave must be 1 or 4");
+        if (a->interleave == 4)
+            return dispatch_pair_i4<Eval, FUSE>(*a, d_params, ext, fz, s);
         return dispatch_pair_flags<Eval, 1, false, FUSE>(*a, d_params, ext, fz, block, s);
         }
     if (tpp == 0)

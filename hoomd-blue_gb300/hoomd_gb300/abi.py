@@ -37,7 +37,7 @@ class CellListArgs(ctypes.Structure):
 class NlistArgs(ctypes.Structure):
     _fields_ = [("d_nlist", c_void), ("d_n_neigh", c_void), ("d_last_pos", c_void),
                 ("d_conditions", c_void), ("d_head_list", c_void), ("stride", c_u64),
-                ("d_Nmax", c_void), ("d_pos", c_void), ("N", c_uint), ("d_cell_size", c_void),
+                ("interleave", c_uint), ("d_Nmax", c_void), ("d_pos", c_void), ("N", c_uint), ("d_cell_size", c_void),
                 ("d_xyzf", c_void), ("d_cell_type", c_void), ("d_cell_adj", c_void),
                 ("dim", c_uint * 3), ("Nmax_cell", c_uint), ("adj_width", c_uint), ("box", Box),
                 ("d_r_cut", c_void), ("d_r_listsq", c_void), ("ntypes", c_uint),
@@ -48,7 +48,7 @@ class PairArgs(ctypes.Structure):
     _fields_ = [("d_force", c_void), ("d_virial", c_void), ("virial_pitch", c_size),
                 ("N", c_uint), ("d_pos", c_void), ("d_charge", c_void), ("box", Box),
                 ("d_n_neigh", c_void), ("d_nlist", c_void), ("d_head_list", c_void),
-                ("stride", c_u64), ("d_rcutsq", c_void), ("d_ronsq", c_void), ("ntypes", c_uint),
+                ("stride", c_u64), ("interleave", c_uint), ("d_rcutsq", c_void), ("d_ronsq", c_void), ("ntypes", c_uint),
                 ("shift_mode", c_uint), ("compute_virial", c_uint), ("block_size", c_uint),
                 ("threads_per_particle", c_uint)]
 

@@ -99,9 +99,11 @@ int gb_cell_adj_build(const unsigned int dim[3], unsigned int ndim, unsigned int
  * self and r_cut <= 0 pairs skipped, overflow recorded per type as the count needed. Unlike
  * the reference, d_n_neigh holds the stored count, min(found, Nmax[type]), so that a consumer
  * launched before the host has read the overflow condition never reads past a particle's list.
- * Layout: neighbour k of particle i lives at d_nlist[head(i) + k * stride], where
- * head(i) = d_head_list[i] when d_head_list is non-NULL (the reference's flat layout, stride 1)
- * and head(i) = i otherwise (column-major layout, stride >= N, coalesced across particles).
+ * Layouts: with d_head_list non-NULL, neighbour k of particle i lives at
+ * d_nlist[d_head_list[i] + k] (the reference's flat layout). With d_head_list NULL the list is
+ * column-major with stride >= N: interleave 1 puts neighbour k at d_nlist[k * stride + i];
+ * interleave 4 puts it at d_nlist[((k / 4) * stride + i) * 4 + k % 4], so one 16-byte load gives
+ * a particle four consecutive neighbours and a warp reads 512 contiguous bytes.
  * ------------------------------------------------------------------------------------------- */
 typedef struct gb_nlist_args
     {
@@ -111,6 +113,7 @@ typedef struct gb_nlist_args
     unsigned int* d_conditions;       /* [ntypes]: max neighbours needed where Nmax overflowed */
     const uint64_t* d_head_list;      /* NULL = column-major */
     uint64_t stride;
+    uint32_t interleave;              /* column-major only: 1 or 4 (0 means 1) */
     const unsigned int* d_Nmax;       /* [ntypes] capacity per particle type */
     const float* d_pos;               /* float4[N] */
     unsigned int N;
@@ -164,6 +167,7 @@ typedef struct gb_pair_args
     const unsigned int* d_nlist;
     const uint64_t* d_head_list;      /* NULL = column-major */
     uint64_t stride;
+    uint32_t interleave;              /* column-major only: 1 or 4 (0 means 1), as gb_nlist_args */
     const float* d_rcutsq;            /* [ntypes^2] */
     const float* d_ronsq;             /* [ntypes^2], read when shift_mode == 2 */
     unsigned int ntypes;

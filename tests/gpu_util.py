@@ -88,10 +88,11 @@ class GpuNlist:
             self.n_neigh = zeros(N)
             self.last_pos = zeros(4 * N, torch.float32)
             self.ncond = zeros(nt)
-            if layout == "col":
+            self.interleave = 4 if layout == "col4" else 1
+            if layout in ("col", "col4"):
                 self.stride = (N + 31) // 32 * 32
                 self.head = None
-                self.nlist = zeros(self.stride * int(Nmax.max()))
+                self.nlist = zeros(self.stride * int((Nmax.max() + 3) // 4 * 4))
             else:
                 self.stride = 1
                 nb = (N + 1023) // 1024
@@ -102,7 +103,8 @@ class GpuNlist:
                 self.nlist = zeros(max(1, int(host(total)[0])))
             a = abi.NlistArgs(d_nlist=p(self.nlist), d_n_neigh=p(self.n_neigh),
                               d_last_pos=p(self.last_pos), d_conditions=p(self.ncond),
-                              d_head_list=p(self.head), stride=self.stride, d_Nmax=p(self.d_Nmax),
+                              d_head_list=p(self.head), stride=self.stride,
+                              interleave=self.interleave, d_Nmax=p(self.d_Nmax),
                               d_pos=p(self.pos), N=N, d_cell_size=p(self.cell_size),
                               d_xyzf=p(self.xyzf), d_cell_type=p(self.cell_type),
                               d_cell_adj=p(self.adj), dim=(ctypes.c_uint32 * 3)(*self.dim),
@@ -120,6 +122,12 @@ class GpuNlist:
     def sets(self):
         nn = host(self.n_neigh).astype(np.int64)
         nl = host(self.nlist).astype(np.int64)
+        if self.head is None and self.interleave == 4:
+            out = []
+            for i in range(self.N):
+                k = np.arange(nn[i])
+                out.append(np.sort(nl[((k >> 2) * self.stride + i) * 4 + (k & 3)]))
+            return out
         if self.head is None:
             return [np.sort(nl[i + np.arange(nn[i]) * self.stride]) for i in range(self.N)]
         hd = host(self.head)
@@ -130,6 +138,7 @@ class GpuNlist:
                          virial_pitch=self.N if virial is not None else 0, N=self.N,
                          d_pos=p(self.pos), box=self.box, d_n_neigh=p(self.n_neigh),
                          d_nlist=p(self.nlist), d_head_list=p(self.head), stride=self.stride,
+                         interleave=self.interleave,
                          d_rcutsq=p(rcutsq), d_ronsq=p(ronsq), ntypes=self.ntypes,
                          shift_mode=shift, compute_virial=int(virial is not None),
                          threads_per_particle=tpp)

@@ -80,7 +80,7 @@ NLIST_CASES = {
 
 
 @pytest.mark.parametrize("case", sorted(NLIST_CASES))
-@pytest.mark.parametrize("layout", ["col", "flat"])
+@pytest.mark.parametrize("layout", ["col", "col4", "flat"])
 def test_nlist_bitexact_vs_oracle(case, layout):
     pos4, box6, rc, rb = NLIST_CASES[case]()
     nl = GpuNlist(pos4, box6, rc, rb, layout=layout)
@@ -127,8 +127,8 @@ def oracle_forces_f64(pos4, box6, kind, params, rc, shift=0, r_on=None, tdata=No
                          compute_virial=True, shift_mode=shift, ronsq=ro, tdata=tdata, prec=64)
 
 
-@pytest.mark.parametrize("layout,tpp", [("col", 0), ("flat", 1), ("flat", 4), ("flat", 8),
-                                        ("flat", 32)])
+@pytest.mark.parametrize("layout,tpp", [("col", 0), ("col4", 0), ("flat", 1), ("flat", 4),
+                                        ("flat", 8), ("flat", 32)])
 def test_lj_forces_vs_fp64_oracle(layout, tpp):
     pos4, box6, rc, rb = NLIST_CASES["lj4096"]()
     nl = GpuNlist(pos4, box6, rc, rb, layout=layout)
@@ -140,13 +140,14 @@ def test_lj_forces_vs_fp64_oracle(layout, tpp):
     assert_close_f64(v, vo, what="virial")
 
 
+@pytest.mark.parametrize("layout", ["col", "col4"])
 @pytest.mark.parametrize("shift", [0, 1, 2])
-def test_lj_binary_shift_modes_vs_fp64_oracle(shift):
+def test_lj_binary_shift_modes_vs_fp64_oracle(shift, layout):
     pos4, box6, rc, rb = NLIST_CASES["binary3000"]()
     rc = np.array([[2.5, 2.0], [2.0, 2.2]])
     ron = np.array([[2.0, 1.5], [1.5, 1.8]])
     par = np.array([[1.0, 1.0], [0.8, 1.5], [0.8, 1.5], [0.88, 0.5]])
-    nl = GpuNlist(pos4, box6, rc, rb)
+    nl = GpuNlist(pos4, box6, rc, rb, layout=layout)
     f, v = gpu_pair_forces(nl, "lj", par, rc, shift=shift, r_on=ron)
     fo, vo = oracle_forces_f64(pos4, box6, "lj", par, rc, shift=shift, r_on=ron)
     assert_close_f64(f[:, :3], fo[:, :3], what="force")
@@ -154,18 +155,20 @@ def test_lj_binary_shift_modes_vs_fp64_oracle(shift):
     assert_close_f64(v, vo, what="virial")
 
 
-def test_lj_triclinic_vs_fp64_oracle():
+@pytest.mark.parametrize("layout", ["col", "col4"])
+def test_lj_triclinic_vs_fp64_oracle(layout):
     pos4, box6, rc, rb = NLIST_CASES["triclinic1728"]()
     rc = np.array([[2.5, 1.5], [1.5, 2.0]])
     par = np.array([[1.0, 0.5], [0.9, 1.0], [0.9, 1.0], [1.1, 0.7]])
-    nl = GpuNlist(pos4, box6, rc, rb)
+    nl = GpuNlist(pos4, box6, rc, rb, layout=layout)
     f, v = gpu_pair_forces(nl, "lj", par, rc)
     fo, vo = oracle_forces_f64(pos4, box6, "lj", par, rc)
     assert_close_f64(f[:, :3], fo[:, :3], what="force")
     assert_close_f64(f[:, 3], fo[:, 3], what="energy")
 
 
-def test_table_multitype_vs_fp64_oracle():
+@pytest.mark.parametrize("layout", ["col", "col4"])
+def test_table_multitype_vs_fp64_oracle(layout):
     nt = 4
     snap = workloads.multitype_system(N=4096, ntypes=nt, density=0.8)
     pos4, box6 = snap_pos4(snap)
@@ -173,7 +176,7 @@ def test_table_multitype_vs_fp64_oracle():
     tables = {k: (v["r_min"], v["U"], v["F"]) for k, v in tabs.items()}
     recs, data, opar, odata = table_params(nt, tables)
     rc = np.full((nt, nt), 3.0)
-    nl = GpuNlist(pos4, box6, rc, 0.4)
+    nl = GpuNlist(pos4, box6, rc, 0.4, layout=layout)
     f, v = gpu_pair_forces(nl, "table", None, rc, tables=(recs, data))
     fo, vo = oracle_forces_f64(pos4, box6, "table", opar, rc, tdata=odata)
     assert_close_f64(f[:, :3], fo[:, :3], what="force")
@@ -200,10 +203,11 @@ def test_forces_and_energies_golden_through_abi(kind):
                                atol=1e-5)
 
 
-def test_example_evaluator_vs_oracle():
+@pytest.mark.parametrize("layout", ["col", "col4"])
+def test_example_evaluator_vs_oracle(layout):
     pos4, box6, rc, rb = NLIST_CASES["random700_dims332"]()
     par = np.array([[2.0, 1.2]])
-    nl = GpuNlist(pos4, box6, [[1.5]], rb)
+    nl = GpuNlist(pos4, box6, [[1.5]], rb, layout=layout)
     for shift in (0, 1):
         f, v = gpu_pair_forces(nl, "example", par, [[1.5]], shift=shift)
         fo, vo = oracle_forces_f64(pos4, box6, "example", par, [[1.5]], shift=shift)
