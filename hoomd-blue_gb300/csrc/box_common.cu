@@ -64,6 +64,20 @@ extern "C"
         return GB_OK;
         }
 
+    int gb_table_pack(const double* U, const double* F, uint32_t width, float* out)
+        {
+        GB_REQUIRE(U && F && out, "gb_table_pack: null argument");
+        GB_REQUIRE(width > 0, "The length of V and F must not be zero.");
+        for (uint32_t k = 0; k < width; k++)
+            {
+            out[4 * k + 0] = (float)U[k];
+            out[4 * k + 1] = (float)F[k];
+            out[4 * k + 2] = (k + 1 < width) ? (float)U[k + 1] : 0.0f;
+            out[4 * k + 3] = (k + 1 < width) ? (float)F[k + 1] : 0.0f;
+            }
+        return GB_OK;
+        }
+
     // hoomd/BoxDim.h:552-567 (host rsqrt = 1/sqrt) and hoomd/CellList.cc:83-131.
     int gb_cell_dims(const gb_box* box, unsigned int ndim, float nominal_width,
                      unsigned int dim[3])

@@ -569,11 +569,13 @@ void PairForce::upload()
                 uint32_t off;
                 if (it == seen.end())
                     {
-                    off = (uint32_t)data.size();
-                    for (double v : t_U[idx])
-                        data.push_back((float)v);
-                    for (double v : t_F[idx])
-                        data.push_back((float)v);
+                    // packed bins (V[k], F[k], V[k+1], F[k+1]); offsets count quads
+                    off = (uint32_t)(data.size() / 4);
+                    const uint32_t w = (uint32_t)t_U[idx].size();
+                    std::vector<float> q(4 * (size_t)w);
+                    check(gb_table_pack(t_U[idx].data(), t_F[idx].data(), w, q.data()),
+                          "gb_table_pack");
+                    data.insert(data.end(), q.begin(), q.end());
                     seen[{a, b}] = off;
                     }
                 else
@@ -684,6 +686,14 @@ void Integrator::set_thermostat_none()
     drop_graphs();
     }
 
+// Bussi draws for the next k timesteps, in parallel, ahead of a run of fused steps.
+static void enqueue_bussi_draws(const Integrator& in, DevStatus* ds, double* ring,
+                                unsigned int ring_size, unsigned int k, cudaStream_t s)
+    {
+    check(gb_bussi_draws(&ds->timestep, k, in.dof(), in.pdata->seed, 0u, ring, ring_size, s),
+          "gb_bussi_draws");
+    }
+
 void Integrator::set_sorter(uint64_t period, int bits)
     {
     sort_period = period;
@@ -752,6 +762,7 @@ void Integrator::prepare()
     d_thermo_scratch.zero(s);
     d_step_scratch.resize(gb_md_step_scratch_bytes(pd.N));
     d_step_scratch.zero(s);
+    d_bussi_ring.resize(2 * (size_t)BUSSI_RING);
     DevStatus st {};
     st.timestep = pd.timestep;
     st.n_builds = nlist->n_builds_host;
@@ -811,6 +822,11 @@ void Integrator::enqueue_step_fused(cudaStream_t s)
     fu.d_factor = &ds->factor;
     fu.d_status = &ds->status;
     fu.d_rebuild_reset = &ds->rebuild;
+    if (bussi)
+        {
+        fu.d_bussi_ring = d_bussi_ring.get();
+        fu.bussi_ring_size = BUSSI_RING;
+        }
     check(f.launch_fused(a, fu, s), "fused pair step");
     }
 
@@ -865,9 +881,13 @@ cudaGraphExec_t Integrator::graph_for(unsigned int k)
         return it->second;
     cudaStream_t s = pdata->stream;
     cudaGraph_t g;
+    if (k > BUSSI_RING)
+        throw std::runtime_error("chunk longer than the Bussi draw ring");
     cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
     try
         {
+        if (bussi)
+            enqueue_bussi_draws(*this, d_status.get(), d_bussi_ring.get(), BUSSI_RING, k, s);
         for (unsigned int i = 0; i < k; i++)
             enqueue_step_fused(s);
         }
@@ -920,13 +940,15 @@ void Integrator::run_chunk(unsigned int k)
         if (fused && use_graph)
             {
             cuda_check(cudaGraphLaunch(graph_for(k), s), "graph launch");
-            launch_count += (uint64_t)k * (1 + cell_kernels + 1 + 1);
+            launch_count += (uint64_t)k * (1 + cell_kernels + 1 + 1) + (bussi ? 1 : 0);
             }
         else if (fused)
             {
+            if (bussi)
+                enqueue_bussi_draws(*this, ds, d_bussi_ring.get(), BUSSI_RING, k, s);
             for (unsigned int i = 0; i < k; i++)
                 enqueue_step_fused(s);
-            launch_count += (uint64_t)k * (1 + cell_kernels + 1 + 1);
+            launch_count += (uint64_t)k * (1 + cell_kernels + 1 + 1) + (bussi ? 1 : 0);
             }
         else
             {
@@ -1119,6 +1141,12 @@ std::vector<double> Integrator::time_phases(unsigned int reps)
         fu.d_factor = &ds->factor;
         fu.d_status = &ds->status;
         fu.d_rebuild_reset = &ds->rebuild;
+        if (bussi)
+            {
+            enqueue_bussi_draws(*this, ds, d_bussi_ring.get(), BUSSI_RING, 1, s);
+            fu.d_bussi_ring = d_bussi_ring.get();
+            fu.bussi_ring_size = BUSSI_RING;
+            }
         cuda_check(cudaEventRecord(ev[0], s), "record");
         check(f.launch_fused(a, fu, s), "fused pair step");
         cuda_check(cudaEventRecord(ev[1], s), "record");

@@ -239,7 +239,7 @@ class Integrator
     void set_sorter(uint64_t period, int grid_bits);
     void set_chunk(unsigned int steps)
         {
-        chunk = steps ? steps : 1;
+        chunk = steps ? (steps > 1024 ? 1024 : steps) : 1;
         }
     void prepare();
     void run(uint64_t nsteps);
@@ -284,6 +284,8 @@ class Integrator
 
     DeviceArray<DevStatus> d_status;
     DeviceArray<char> d_step_scratch, d_thermo_scratch;
+    static constexpr unsigned int BUSSI_RING = 1024; // >= the longest chunk
+    DeviceArray<double> d_bussi_ring;                // (normal, 2*gamma) per timestep % RING
     DeviceArray<float> net_force;
     DeviceArray<float> ck_pos, ck_vel, ck_accel;
     DeviceArray<int32_t> ck_image;

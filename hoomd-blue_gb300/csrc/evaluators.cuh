@@ -2,9 +2,11 @@
 // (example_plugins/pair_plugin/EvaluatorPairExample.h): a POD param_type per type pair, a
 // constructor from (rsq, rcutsq, param), needsCharge/setCharge, and
 // evalForceAndEnergy(force_divr, pair_eng, energy_shift) returning false when the pair does not
-// interact. One addition: the constructor also receives `ext`, a device pointer to shared
-// read-only data (the flat table array for Table; unused by LJ and Example), because the
-// reference's ManagedArray members have no equivalent in a plain C-ABI parameter struct.
+// interact. Two additions: the constructor also receives `ext`, a device pointer to shared
+// read-only data (the packed table bins for Table; unused by LJ and Example), because the
+// reference's ManagedArray members have no equivalent in a plain C-ABI parameter struct; and a
+// static prepare_param(param, rcutsq) that a kernel applies once per type pair when it stages
+// the parameters (derived constants, e.g. the Table's 1/dr).
 //
 // A plugin evaluator is added by writing a struct with this interface and instantiating
 // gb::launch_pair<Evaluator>() from pair_kernel.cuh.
@@ -29,6 +31,7 @@ __device__ __forceinline__ float rcp_approx(float x)
 struct EvalLJ
     {
     using param_type = gb_lj_param;
+    __device__ __forceinline__ static void prepare_param(param_type&, float) { }
     float rsq, rcutsq, lj1, lj2;
     __device__ __forceinline__ EvalLJ(float rsq_, float rcutsq_, const param_type& p,
                                       const float*)
@@ -61,22 +64,31 @@ struct EvalLJ
         }
     };
 
-// hoomd/md/EvaluatorPairTable.h:151-194. Linear interpolation on width points spaced
-// (r_cut - r_min)/width; V1 = F1 = 0 in the last bin. value_i is clamped to width-1: at FP32, r
-// just below r_cut can round (r - rmin)/dr up to width, where the reference reads one past the
-// end of its table.
+// hoomd/md/EvaluatorPairTable.h:151-194: linear interpolation on width points spaced
+// dr = (r_cut - r_min)/width, V1 = F1 = 0 in the last bin. Each bin is one packed quad
+// (V[k], F[k], V[k+1], F[k+1]), so a pair reads 16 bytes. 1/dr is derived once per type pair
+// (prepare_param) and r, 1/r come from one reciprocal square root; value_i is clamped to width-1
+// (at FP32, r just below r_cut can round (r - rmin)/dr up to width, where the reference reads one
+// past the end of its table). Branch free: out-of-range lanes read a valid bin and are discarded.
 struct EvalTable
     {
     using param_type = gb_table_param;
-    float rsq, rcutsq, rmin;
+    float rsq, rcutsq, rmin, inv_dr;
     unsigned int width;
-    const float* V;
-    const float* F;
+    const float4* bins;
+    // per type pair, once per block: keep 1/dr in the reserved word
+    __device__ __forceinline__ static void prepare_param(param_type& p, float rcutsq)
+        {
+        const float rcut = sqrtf(rcutsq);
+        const float inv = (float)p.width / (rcut - p.rmin);
+        p.reserved = __float_as_uint(inv);
+        }
     __device__ __forceinline__ EvalTable(float rsq_, float rcutsq_, const param_type& p,
                                          const float* table)
-        : rsq(rsq_), rcutsq(rcutsq_), rmin(p.rmin), width(p.width), V(table + p.offset),
-          F(table + p.offset + p.width)
+        : rsq(rsq_), rcutsq(rcutsq_), rmin(p.rmin), width(p.width),
+          bins(reinterpret_cast<const float4*>(table) + p.offset)
         {
+        inv_dr = __uint_as_float(p.reserved);
         }
     static constexpr bool needsCharge()
         {
@@ -86,30 +98,19 @@ struct EvalTable
     __device__ __forceinline__ bool evalForceAndEnergy(float& force_divr, float& pair_eng,
                                                        bool) const
         {
-        const float r = sqrtf(rsq);
-        if (rsq >= rcutsq || r < rmin)
-            return false;
-        const float rcut = sqrtf(rcutsq);
-        const float delta_r = (rcut - rmin) / (float)width;
-        const float value_f = (r - rmin) / delta_r;
-        unsigned int value_i = (unsigned int)floorf(value_f);
-        if (value_i >= width)
-            value_i = width - 1;
-        const float V0 = __ldg(V + value_i);
-        const float F0 = __ldg(F + value_i);
-        float V1 = 0.0f, F1 = 0.0f;
-        if (value_i + 1 < width)
-            {
-            V1 = __ldg(V + value_i + 1);
-            F1 = __ldg(F + value_i + 1);
-            }
+        const float rinv = rsqrtf(rsq);
+        const float r = rsq * rinv;
+        const bool in = rsq < rcutsq && r >= rmin && rsq > 0.0f;
+        const float value_f = fmaxf((r - rmin) * inv_dr, 0.0f);
+        unsigned int value_i = (unsigned int)value_f;
+        value_i = min(value_i, width - 1);
+        const float4 q = __ldg(bins + value_i);
         const float f = value_f - (float)value_i;
-        const float Vr = V0 + f * (V1 - V0);
-        const float Fr = F0 + f * (F1 - F0);
-        if (rsq > 0.0f)
-            force_divr = Fr / r;
-        pair_eng = Vr;
-        return true;
+        const float Vr = q.x + f * (q.z - q.x);
+        const float Fr = q.y + f * (q.w - q.y);
+        force_divr = in ? Fr * rinv : force_divr;
+        pair_eng = in ? Vr : pair_eng;
+        return in;
         }
     };
 
@@ -117,6 +118,7 @@ struct EvalTable
 struct EvalExample
     {
     using param_type = gb_example_param;
+    __device__ __forceinline__ static void prepare_param(param_type&, float) { }
     float rsq, rcutsq, k, sigma;
     __device__ __forceinline__ EvalExample(float rsq_, float rcutsq_, const param_type& p,
                                            const float*)

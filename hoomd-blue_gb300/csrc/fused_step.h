@@ -38,6 +38,9 @@ inline int make_fuse_args(const gb_pair_args* a, const gb_step_fuse* f, FuseArgs
     fz.d_factor = f->d_factor;
     fz.d_status = f->d_status;
     fz.d_rebuild_reset = f->d_rebuild_reset;
+    GB_REQUIRE(!f->d_bussi_ring || f->bussi_ring_size > 0, "fused step: empty Bussi ring");
+    fz.d_ring = reinterpret_cast<const double2*>(f->d_bussi_ring);
+    fz.ring_size = f->bussi_ring_size;
     return GB_OK;
     }
 } // namespace gb

@@ -183,6 +183,17 @@ __global__ void k_thermo(const float4* __restrict__ vel, const float4* __restric
         }
     }
 
+__global__ void k_bussi_draws(const uint64_t* d_timestep, unsigned int count, double dof,
+                              uint16_t seed, uint32_t instance_id, double2* ring,
+                              unsigned int ring_size)
+    {
+    const unsigned int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count)
+        return;
+    const uint64_t ts = *d_timestep + 1 + k;
+    ring[ts % ring_size] = bussi_draws_d(dof, ts, seed, instance_id);
+    }
+
 __global__ void k_bussi(const double* d_ke, double dof, double dt, double tau, double kT,
                         uint64_t timestep, uint16_t seed, uint32_t instance_id, double* d_factor)
     {
@@ -364,6 +375,19 @@ extern "C"
         k_bussi<<<1, 32, 0, (cudaStream_t)stream>>>(d_ke, dof, dt, tau, kT, timestep, seed,
                                                      instance_id, d_factor);
         return check_launch("gb_bussi_factor");
+        }
+
+    int gb_bussi_draws(const uint64_t* d_timestep, unsigned int count, double dof, uint16_t seed,
+                       uint32_t instance_id, double* d_ring, unsigned int ring_size, void* stream)
+        {
+        GB_REQUIRE(d_timestep && d_ring, "gb_bussi_draws: null argument");
+        GB_REQUIRE(ring_size > 0 && count <= ring_size, "gb_bussi_draws: count > ring_size");
+        if (count == 0)
+            return GB_OK;
+        k_bussi_draws<<<div_up(count, 64), 64, 0, (cudaStream_t)stream>>>(
+            d_timestep, count, dof, seed, instance_id, reinterpret_cast<double2*>(d_ring),
+            ring_size);
+        return check_launch("gb_bussi_draws");
         }
 
     int gb_thermalize(float* d_vel, const uint32_t* d_tag, unsigned int N, double kT,

@@ -43,6 +43,8 @@ struct FuseArgs
     double* d_factor;
     uint32_t* d_status;     // bit 0: Bussi with zero kinetic energy
     uint32_t* d_rebuild_reset;
+    const double2* d_ring;  // optional pre-drawn Bussi draws, indexed by timestep % ring_size
+    unsigned int ring_size;
     };
 
 template<int TPP> __device__ __forceinline__ double block_sum_d(double v, double* s_red)
@@ -108,6 +110,9 @@ __device__ inline void fuse_finish(const FuseArgs& fz, double ke, double pe, dou
                 atomicOr(fz.d_status, 1u);
                 *fz.d_factor = 1.0;
                 }
+            else if (fz.d_ring)
+                *fz.d_factor = bussi_factor_from_draws(K, fz.dof, fz.dt_d, fz.tau, fz.kT,
+                                                       fz.d_ring[next % fz.ring_size]);
             else
                 *fz.d_factor = bussi_factor_d(K, fz.dof, fz.dt_d, fz.tau, fz.kT, next, fz.seed,
                                               fz.instance_id);
@@ -143,7 +148,9 @@ __global__ void __launch_bounds__(256)
         {
         for (unsigned int t = threadIdx.x; t < np; t += blockDim.x)
             {
-            s_params[t] = d_params[t];
+            P pt = d_params[t];
+            Eval::prepare_param(pt, d_rcutsq[t]);
+            s_params[t] = pt;
             s_rcutsq[t] = d_rcutsq[t];
             if (SHIFT == 2)
                 s_ronsq[t] = d_ronsq[t];
@@ -156,6 +163,7 @@ __global__ void __launch_bounds__(256)
         {
         p0 = d_params[0];
         rc0 = d_rcutsq[0];
+        Eval::prepare_param(p0, rc0);
         if (SHIFT == 2)
             ro0 = d_ronsq[0];
         }
@@ -343,7 +351,9 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
         {
         for (unsigned int t = threadIdx.x; t < np; t += blockDim.x)
             {
-            s_params[t] = d_params[t];
+            P pt = d_params[t];
+            Eval::prepare_param(pt, d_rcutsq[t]);
+            s_params[t] = pt;
             s_rcutsq[t] = d_rcutsq[t];
             if (XPLOR)
                 s_ronsq[t] = d_ronsq[t];
@@ -356,6 +366,7 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
         {
         p0 = d_params[0];
         rc0 = d_rcutsq[0];
+        Eval::prepare_param(p0, rc0);
         if (XPLOR)
             ro0 = d_ronsq[0];
         }

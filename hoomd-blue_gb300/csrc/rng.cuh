@@ -146,25 +146,45 @@ __device__ inline double gamma_d(Philox& rng, double m_alpha, double m_b)
     return v;
     }
 
-// hoomd/md/Thermostat.h:357-391 (key id 45, counter = first member tag) and :416-446.
-__device__ inline double bussi_factor_d(double K, double dof, double dt, double tau, double set_T,
-                                        uint64_t timestep, uint16_t seed, uint32_t instance_id)
+// hoomd/md/Thermostat.h:357-391 (key id 45, counter = first member tag) and :416-446, split in
+// two: the random draws of a timestep (one normal, then 2 * Gamma((dof-1)/2, 1)) depend only on
+// the timestep, seed, counter and dof, so they can be drawn ahead for a run of steps, in
+// parallel; the factor then needs only the kinetic energy and a few FP64 operations.
+__device__ inline double2 bussi_draws_d(double dof, uint64_t timestep, uint16_t seed,
+                                        uint32_t instance_id)
     {
-    if (dt == 0.0 || dof == 0.0 || K <= 0.0)
-        return 1.0;
     Philox rng(45, timestep, seed, instance_id);
-    double time_decay_factor = 0.0;
-    if (tau != 0.0)
-        time_decay_factor = exp(-dt / tau);
     const double r_normal_one = normal_d(rng);
     double r_gamma = 0.0;
     if (dof > 1.0)
         r_gamma = 2.0 * gamma_d(rng, (dof - 1.0) / 2.0, 1.0);
+    return make_double2(r_normal_one, r_gamma);
+    }
+
+__device__ inline double bussi_factor_from_draws(double K, double dof, double dt, double tau,
+                                                 double set_T, double2 draws)
+    {
+    if (dt == 0.0 || dof == 0.0 || K <= 0.0)
+        return 1.0;
+    double time_decay_factor = 0.0;
+    if (tau != 0.0)
+        time_decay_factor = exp(-dt / tau);
+    const double r_normal_one = draws.x;
+    const double r_gamma = draws.y;
     const double v = set_T / 2.0 / K;
     const double term1 = v * (1.0 - time_decay_factor) * (r_gamma + r_normal_one * r_normal_one);
     const double term2
         = 2.0 * r_normal_one * sqrt(v * (1.0 - time_decay_factor) * time_decay_factor);
     return sqrt(time_decay_factor + term1 + term2);
+    }
+
+__device__ inline double bussi_factor_d(double K, double dof, double dt, double tau, double set_T,
+                                        uint64_t timestep, uint16_t seed, uint32_t instance_id)
+    {
+    if (dt == 0.0 || dof == 0.0 || K <= 0.0)
+        return 1.0;
+    return bussi_factor_from_draws(K, dof, dt, tau, set_T,
+                                   bussi_draws_d(dof, timestep, seed, instance_id));
     }
 
 } // namespace gb

@@ -65,7 +65,8 @@ class StepFuse(ctypes.Structure):
                 ("d_scratch", c_void), ("d_thermo", c_void), ("bussi", c_int), ("dof", c_double),
                 ("tau", c_double), ("kT", c_double), ("seed", c_uint), ("instance_id", c_uint),
                 ("d_timestep", c_void), ("d_factor", c_void), ("d_status", c_void),
-                ("d_rebuild_reset", c_void)]
+                ("d_rebuild_reset", c_void), ("d_bussi_ring", c_void),
+                ("bussi_ring_size", c_uint)]
 
 
 _P = ctypes.POINTER
@@ -82,6 +83,7 @@ _PROTOS = {
     "gb_nlist_head_list": (c_int, [c_void, c_void, c_void, c_uint, c_void, c_uint, c_void]),
     "gb_pair_forces_lj": (c_int, [_P(PairArgs), c_void, c_void]),
     "gb_pair_forces_table": (c_int, [_P(PairArgs), c_void, c_void, c_void]),
+    "gb_table_pack": (c_int, [_P(c_double), _P(c_double), c_uint, _P(c_float)]),
     "gb_pair_forces_example": (c_int, [_P(PairArgs), c_void, c_void]),
     "gb_cv_step_one": (c_int, [c_void, c_void, c_void, c_void, c_uint, _P(Box), c_float, c_float,
                                c_void, c_void]),
@@ -91,6 +93,8 @@ _PROTOS = {
     "gb_thermo_reduce_noalloc": (c_int, [c_void, c_void, c_void, c_size, c_uint, c_void, c_void]),
     "gb_bussi_factor": (c_int, [c_void, c_double, c_double, c_double, c_double, c_u64,
                                 ctypes.c_uint16, c_uint, c_void, c_void]),
+    "gb_bussi_draws": (c_int, [c_void, c_uint, c_double, ctypes.c_uint16, c_uint, c_void, c_uint,
+                               c_void]),
     "gb_thermalize": (c_int, [c_void, c_void, c_uint, c_double, c_u64, ctypes.c_uint16, c_uint,
                               c_void, c_void]),
     "gb_md_step_one": (c_int, [_P(StepOneArgs), c_void]),

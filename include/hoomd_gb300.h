@@ -184,15 +184,21 @@ typedef struct gb_lj_param
     float epsilon_x_4;
     } gb_lj_param;
 
-/* EvaluatorPairTable::param_type (hoomd/md/EvaluatorPairTable.h:45-118) with the tables held in
- * one flat device array: V at d_table[offset .. offset+width), F at d_table[offset+width ..). */
+/* EvaluatorPairTable::param_type (hoomd/md/EvaluatorPairTable.h:45-118). The tables of all type
+ * pairs share one device array of bins: bin k of a pair is the float quad
+ * (V[k], F[k], V[k+1], F[k+1]) with V[width] = F[width] = 0 (the reference's last-bin rule), so
+ * an evaluation reads one 16-byte quad. `offset` is the pair's first bin, in quads.
+ * gb_table_pack writes a pair's quads from its U and F arrays. `reserved` must be 0. */
 typedef struct gb_table_param
     {
     float rmin;
     uint32_t width;
     uint32_t offset;
-    uint32_t pad;
+    uint32_t reserved;
     } gb_table_param;
+
+/* Host helper: pack width points of U and F into width quads (4 * width floats) at out. */
+int gb_table_pack(const double* U, const double* F, uint32_t width, float* out);
 
 /* EvaluatorPairExample::param_type (example_plugins/pair_plugin/EvaluatorPairExample.h:30-60). */
 typedef struct gb_example_param
@@ -310,7 +316,19 @@ typedef struct gb_step_fuse
     uint32_t* d_status;         /* bit 0 set: Bussi factor requested with zero kinetic energy */
     uint32_t* d_rebuild_reset;  /* optional: set to 0 once the step is complete (clears the
                                    rebuild flag that gated this step's neighbour-list build) */
+    const double* d_bussi_ring; /* optional: pairs (normal, 2*gamma) drawn ahead by
+                                   gb_bussi_draws, at index timestep % bussi_ring_size; NULL =
+                                   draw in the kernel's last block */
+    uint32_t bussi_ring_size;
     } gb_step_fuse;
+
+/* Pre-draws the random numbers of the Bussi factor (hoomd/md/Thermostat.h:416-446) for timesteps
+ * *d_timestep + 1 ... *d_timestep + count, one thread per timestep, into
+ * d_ring[t % ring_size] as (normal, 2 * Gamma((dof - 1)/2, 1)). The draws depend only on the
+ * timestep, seed, counter and dof, so the factor computed from them later equals the one drawn
+ * at that step. count <= ring_size. */
+int gb_bussi_draws(const uint64_t* d_timestep, unsigned int count, double dof, uint16_t seed,
+                   uint32_t instance_id, double* d_ring, unsigned int ring_size, void* stream);
 
 /* Net force (hoomd/Integrator.cu:68-170 gpu_integrator_sum_net_force): d_net[i] = sum over the
  * n_forces force arrays (float4; energy in w), n_forces <= 8. */

@@ -182,21 +182,34 @@ def gpu_pair_forces(nl, kind, params, r_cut, virial=True, shift=0, r_on=None, ta
     return f, v
 
 
+def pack_table(U, F):
+    """Packed bins through the C ABI's host helper gb_table_pack: (width, 4) FP32 quads."""
+    U = np.ascontiguousarray(U, np.float64)
+    F = np.ascontiguousarray(F, np.float64)
+    out = np.zeros((len(U), 4), np.float32)
+    abi.check(abi.load().gb_table_pack(U.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       F.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       len(U), out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+              "gb_table_pack")
+    return out
+
+
 def table_params(ntypes, tables):
     """tables: {(i, j): (r_min, U, F)} for i <= j -> (gb_table_param records as uint32 words,
-    flat [V, F] FP32 data, oracle params (ntypes^2, 3), oracle tdata FP64)."""
+    packed FP32 bins, oracle params (ntypes^2, 3), oracle tdata FP64 [U, F] per pair)."""
     recs = np.zeros((ntypes * ntypes, 4), np.uint32)
     data, odata = [], []
     opar = np.zeros((ntypes * ntypes, 3))
-    offs = {}
-    off = 0
+    offs, ooffs = {}, {}
+    off = ooff = 0
     for (i, j), (rmin, U, F) in sorted(tables.items()):
         offs[(i, j)] = off
-        data.append(np.asarray(U, np.float32))
-        data.append(np.asarray(F, np.float32))
+        ooffs[(i, j)] = ooff
+        data.append(pack_table(U, F).ravel())
         odata.append(np.asarray(U, np.float64))
         odata.append(np.asarray(F, np.float64))
-        off += 2 * len(U)
+        off += len(U)
+        ooff += 2 * len(U)
     for i in range(ntypes):
         for j in range(ntypes):
             a, b = min(i, j), max(i, j)
@@ -205,5 +218,5 @@ def table_params(ntypes, tables):
             recs[k, 0] = np.float32(rmin).view(np.uint32)
             recs[k, 1] = len(U)
             recs[k, 2] = offs[(a, b)]
-            opar[k] = (rmin, len(U), offs[(a, b)])
+            opar[k] = (rmin, len(U), ooffs[(a, b)])
     return recs, np.concatenate(data), opar, np.concatenate(odata)

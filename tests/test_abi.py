@@ -56,3 +56,15 @@ def test_c_abi_rejects_bad_arguments_without_gpu():
     assert lib.gb_pair_forces_lj(ctypes.byref(args), None, None) == abi.GB_ERR_INVALID
     b = abi.make_box((10, 10, 10))
     assert lib.gb_cell_dims(ctypes.byref(b), 3, 0.0, (ctypes.c_uint32 * 3)()) == abi.GB_ERR_INVALID
+
+
+def test_table_pack_layout():
+    """gb_table_pack: bin k = (U[k], F[k], U[k+1], F[k+1]) with zeros past the last point (the
+    reference's V1 = F1 = 0 in the last bin, hoomd/md/EvaluatorPairTable.h:172-178)."""
+    from gpu_util_cpu import pack_table_cpu
+    U = np.array([5.0, 4.0, 3.0, 2.0])
+    F = np.array([2.0, 2.5, 3.0, 3.5])
+    q = pack_table_cpu(U, F)
+    assert q.shape == (4, 4)
+    assert np.array_equal(q[0], np.float32([5.0, 2.0, 4.0, 2.5]))
+    assert np.array_equal(q[3], np.float32([2.0, 3.5, 0.0, 0.0]))

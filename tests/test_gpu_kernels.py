@@ -364,3 +364,22 @@ def test_needs_update_kernel():
     abi.check(L_.gb_nlist_needs_update(p(flag), p(last), p(dev(moved)), N, ctypes.byref(box),
                                        p(rcmax), 0.4, 1, 1.0, lam, 7, stream()), "check")
     assert int(host(flag)[0]) == 7
+
+
+def test_bussi_predrawn_ring_gives_the_same_factor():
+    """gb_bussi_draws fills the ring with each timestep's (normal, 2*gamma); the factor formed
+    from them equals the oracle's per-step Bussi factor (same Philox stream, same algorithm)."""
+    L_ = abi.load()
+    ring_size, count, t0 = 64, 40, 1000
+    ring = zeros(2 * ring_size, torch.float64)
+    ts = dev(np.array([t0], np.int64))
+    dof, seed, K, dt, kT = 3.0 * 4096 - 3, 22765, 5000.0, 0.005, 1.5
+    abi.check(L_.gb_bussi_draws(p(ts), count, dof, seed, 0, p(ring), ring_size, stream()),
+              "draws")
+    r = host(ring).reshape(-1, 2)
+    for k in range(count):
+        t = t0 + 1 + k
+        n, g = r[t % ring_size]
+        v = kT / 2.0 / K
+        factor = np.sqrt(v * (g + n * n))  # tau = 0: time_decay_factor = 0
+        assert np.isclose(factor, O.bussi_factor(K, dof, dt, 0.0, kT, t, seed, 0), rtol=1e-9)
