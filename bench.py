@@ -13,7 +13,9 @@ kT = 1.5), ``ka_262k`` (Kob-Andersen 80:20 mixture, N = 262,144, density 1.2, Bu
 dt 0.003, buffer 0.3, started from a jittered lattice instead of random positions plus capped
 relaxation), ``table32_524k`` (32 types, 528 tabulated pair potentials, N = 524,288, density
 0.8, Bussi kT = 1.5, dt 0.004, buffer 0.4). Those configurations keep their thermostat in the
-timed steps.
+timed steps. ``replicas_256``: 256 independent LJ systems (N ~ U[500, 20000], density ~
+U[0.7, 0.9], Bussi kT ~ U[0.8, 2.0], dt 0.005) advanced by one persistent launch per run, with the
+launch shape chosen by the ensemble's tuner during warm-up; reported in particle-timesteps/s.
 
 --impl reference times the CPU restatement of the reference's path (oracle/, FP64 Scalar, full
 neighbour list over all host threads) on a bounded sample of the same workload.
@@ -362,10 +364,164 @@ def run_gb300(args):
         print(json.dumps(line), flush=True)
 
 
+def replica_systems():
+    from hoomd_gb300 import workloads as W
+    return W.replica_systems(count=256, n_min=500, n_max=20000, seed=4)
+
+
+REPLICA_CONFIG = {"workload": "lj_replicas_256", "replicas": 256, "N_range": [500, 20000],
+                  "density_range": [0.7, 0.9], "kT_range": [0.8, 2.0], "r_cut": 2.5,
+                  "buffer": 0.4, "dt": 0.005, "integrator": "ConstantVolume + Bussi per replica",
+                  "launch": "one persistent kernel per run, CUDA graph",
+                  "precision": "fp32 positions/forces, fp64 reductions",
+                  "l2": "working set > L2 (neighbour lists ~1.4 GB)"}
+REPLICA_UNIT = "particle-timesteps/s"
+
+
+def run_replicas(args):
+    """256 uneven LJ replicas advanced together (one persistent launch per run)."""
+    import torch
+    import hoomd_gb300 as hoomd
+    import numpy as np
+    rank, world, local = dist_init()
+    torch.cuda.set_device(local)
+    systems = replica_systems()
+
+    def build():
+        ens = hoomd.ReplicaEnsemble(dt=0.005, r_cut=2.5, buffer=0.4)
+        for snap, kT, seed in systems:
+            ens.add_replica(snap, kT=kT, seed=seed + 1000 * rank)
+        return ens
+
+    ens = build()
+    Ntot = ens.total_particles
+    ens.run(0)
+    tune = ens.autotune(steps=10, repeats=1)
+    ens.run(max(3, args.warmup))
+    stream = torch.cuda.ExternalStream(ens._cpp.streamHandle())
+    sum_n = sum(int(np.sum(ens._cpp.neighborCounts(r))) for r in range(ens.count))
+    builds0 = sum(ens.thermo(r)["n_builds"] for r in range(ens.count))
+    launches0 = ens.launch_count
+    cyc0 = np.asarray(ens._cpp.phaseClocks(), np.float64).reshape(-1, 4)
+    clocks = ClockSampler(local) if rank == 0 else None
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    ens.run(args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    clk = clocks.stop() if clocks else None
+    builds = sum(ens.thermo(r)["n_builds"] for r in range(ens.count)) - builds0
+    cyc = np.asarray(ens._cpp.phaseClocks(), np.float64).reshape(-1, 4) - cyc0
+    big = int(np.argmax([ens.record(r)["N"] for r in range(ens.count)]))
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    phase_names = ["step_one", "nlist_build", "pair_step", "bussi_draws"]
+    phase_split = {
+        "all_replicas_fraction": dict(zip(phase_names, (cyc.sum(0) / cyc.sum()).round(4).tolist())),
+        "largest_replica": {"N": ens.record(big)["N"], "us_per_step": dict(zip(
+            phase_names, (cyc[big] / mhz / args.steps).round(2).tolist()))},
+        "sm_cycles_total": float(cyc.sum()), "note": "clock64 at phase boundaries, thread 0"}
+    launches = ens.launch_count - launches0
+    value = Ntot * args.steps / (ms / 1e3) * world
+
+    # end to end through the public API: build the ensemble from host snapshots (H2D), run K
+    # steps, read every replica's snapshot and energies back (D2H), wall clock
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2 = build()
+    e2.run(args.steps)
+    out = [e2.get_snapshot(r) for r in range(e2.count)]
+    th = [e2.thermo(r) for r in range(e2.count)]
+    t_e2e = time.perf_counter() - t0
+    del out, th, e2
+    e2e = {"value": Ntot * args.steps / t_e2e, "unit": REPLICA_UNIT,
+           "h2d_bytes_per_step": Ntot * (16 + 16 + 16) / args.steps,
+           "d2h_bytes_per_step": (Ntot * (16 + 16 + 16 + 16) + 256 * 240) / args.steps,
+           "note": "256 host snapshots -> ReplicaEnsemble -> run(K) (prep included) -> "
+                   "get_snapshot + thermo of every replica, wall clock"}
+
+    peak, peak_kind = peaks()
+    # per particle and step: step one (pos, vel, accel, last_pos read; pos, vel write) + pair
+    # step (n_neigh, own pos, vel r/w, force and accel write) + 4 bytes per neighbour index
+    bytes_step = Ntot * (96 + 84) + 4.0 * sum_n
+    achieved = bytes_step * args.steps / (ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None,
+                "kernel": "k_replicas (gb_replicas_run: every step of every replica)",
+                "algorithmic_bytes_per_step": bytes_step,
+                "bytes_formula": "Ntot*(96 step one + 84 pair step) + 4*sum(n_neigh); "
+                                 "neighbour-list builds not counted",
+                "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"}
+    best = min(tune, key=lambda t: t["ms_per_step"])
+    line = {"metric": "LJ replica ensemble particle-timesteps/s (256 replicas, N 500-20000)",
+            "value": value, "unit": REPLICA_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded sizes, densities, kT; jittered lattices, MB velocities)",
+            "config": dict(REPLICA_CONFIG, total_particles=Ntot,
+                           launch_shape=ens.launch, tuned_from=len(tune),
+                           parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
+            "timesteps_per_s": args.steps / (ms / 1e3), "pair_evals_per_s":
+            sum_n * args.steps / (ms / 1e3) * world, "nlist_builds": builds,
+            "autotune_best": best, "phases": phase_split, "e2e": e2e, "roofline": roofline,
+            "gpu_launches": int(launches), "clocks": clk}
+    if rank == 0:
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = replica_cpu_sample(systems, args.cpu_seconds, 1)
+        print(json.dumps(line), flush=True)
+
+
+def replica_cpu_sample(systems, seconds, nthreads):
+    """The oracle on a sample of the replicas, one after another (as separate reference runs
+    would be): steps until about ``seconds`` have passed, in particle-timesteps/s."""
+    import numpy as np
+    from oracle import oracle as O
+    done, t_tot, k, names = 0, 0.0, 0, []
+    for snap, kT, seed in systems[::17]:
+        N = snap.particles.N
+        pos4 = O.make_pos4(snap.particles.position, np.zeros(N), 64)
+        vel4 = np.ones((N, 4))
+        vel4[:, :3] = snap.particles.velocity
+        sim = O.Sim(pos4, vel4, np.zeros((N, 3), np.int32), np.arange(N),
+                    snap.configuration.box, [[2.5]], 0.4, 0.005, params=[[1.0, 1.0]],
+                    full=nthreads > 1, prec=64, nthreads=nthreads, bussi=True, kT=kT, seed=seed)
+        sim.run(1)
+        t0 = time.perf_counter()
+        sim.run(10)
+        t_tot += time.perf_counter() - t0
+        done += 10 * N
+        k += 1
+        names.append(N)
+        if t_tot > seconds:
+            break
+    return {"value": done / t_tot, "unit": REPLICA_UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"10 timesteps of each of {k} replicas (N = {names}) one after another, "
+                      f"after one untimed step; oracle FP64, "
+                      + ("half list, single thread" if nthreads == 1 else
+                         f"full list, {nthreads} OpenMP threads")}
+
+
 def run_reference(args):
     """The CPU restatement of the reference's path over all host threads (FP64, full list)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.workload == "replicas_256":
+        cores = os.cpu_count() or 1
+        cb = replica_cpu_sample(replica_systems(), args.cpu_seconds * 3, cores)
+        v = cb["value"]
+        print(json.dumps({
+            "metric": "LJ replica ensemble particle-timesteps/s (256 replicas, N 500-20000)",
+            "value": v, "unit": REPLICA_UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic (seeded sizes, densities, kT; jittered lattices, MB velocities)",
+            "config": REPLICA_CONFIG, "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": REPLICA_UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
         return
     wl = workloads_registry(args.fcc_m)[args.workload]
     cores = os.cpu_count() or 1
@@ -402,7 +558,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=200)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", default="lj_fcc_1m",
-                    choices=["lj_fcc_1m", "lj_sc_4096", "ka_262k", "table32_524k"])
+                    choices=["lj_fcc_1m", "lj_sc_4096", "ka_262k", "table32_524k",
+                             "replicas_256"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fcc-m", type=int, default=64,
@@ -413,6 +570,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "replicas_256":
+        run_replicas(args)
     else:
         run_gb300(args)
 

@@ -21,6 +21,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -86,6 +87,20 @@ template<class T> class DeviceArray
         if (n)
             cuda_check(cudaMemcpyAsync(h, m_ptr, n * sizeof(T), cudaMemcpyDeviceToHost, s),
                        "download");
+        }
+    void download_at(T* h, size_t offset, size_t n, cudaStream_t s) const
+        {
+        if (offset + n > m_n)
+            throw std::runtime_error("DeviceArray::download_at: out of range");
+        if (n)
+            cuda_check(cudaMemcpyAsync(h, m_ptr + offset, n * sizeof(T), cudaMemcpyDeviceToHost,
+                                       s),
+                       "download");
+        }
+    void swap(DeviceArray& o)
+        {
+        std::swap(m_ptr, o.m_ptr);
+        std::swap(m_n, o.m_n);
         }
     void zero(cudaStream_t s)
         {

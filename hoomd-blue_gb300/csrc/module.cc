@@ -6,6 +6,7 @@
 #include <pybind11/stl.h>
 
 #include "engine.h"
+#include "ensemble.h"
 
 namespace py = pybind11;
 using namespace gbe;
@@ -231,4 +232,86 @@ PYBIND11_MODULE(_hoomd_gb300, m)
              })
         .def("synchronize",
              [](Integrator& i) { cuda_check(cudaStreamSynchronize(i.pdata->stream), "sync"); });
+
+    using darr = py::array_t<double, py::array::c_style | py::array::forcecast>;
+    py::class_<ReplicaEnsemble, std::shared_ptr<ReplicaEnsemble>>(m, "ReplicaEnsembleGPU")
+        .def(py::init<double, double, double, double, double, int>())
+        .def("addReplica",
+             [](ReplicaEnsemble& e, darr pos, darr vel, darr mass,
+                py::array_t<int32_t, py::array::c_style | py::array::forcecast> image, darr L,
+                darr tilt, bool bussi, double kT, double tau, uint32_t seed, uint64_t timestep) {
+                 const size_t N = (size_t)mass.size();
+                 if ((size_t)pos.size() != 3 * N || (size_t)vel.size() != 3 * N
+                     || (size_t)image.size() != 3 * N || L.size() != 3 || tilt.size() != 3)
+                     throw std::invalid_argument("replica array sizes do not match N");
+                 return e.add((unsigned int)N, pos.data(), vel.data(), mass.data(), image.data(),
+                              L.data(), tilt.data(), bussi, kT, tau, seed, timestep);
+             })
+        .def("run", &ReplicaEnsemble::run, py::call_guard<py::gil_scoped_release>())
+        .def("autotune",
+             [](ReplicaEnsemble& e, uint32_t steps, uint32_t repeats) {
+                 py::list out;
+                 for (const TuneResult& t : e.autotune(steps, repeats))
+                     out.append(py::make_tuple(t.block_size, t.grid_size, t.ms_per_step));
+                 return out;
+             })
+        .def("setLaunch", &ReplicaEnsemble::set_launch)
+        .def("setStartCapacity", &ReplicaEnsemble::set_start_capacity)
+        .def("setStencil", &ReplicaEnsemble::set_stencil)
+        .def("getParticles",
+             [](ReplicaEnsemble& e, uint32_t r) {
+                 const size_t N = e.record(r).N;
+                 auto pos = make_array<double>({N, 3});
+                 auto vel = make_array<double>({N, 4});
+                 auto img = make_array<int32_t>({N, 3});
+                 auto frc = make_array<double>({N, 4});
+                 e.get_particles(r, pos.mutable_data(), vel.mutable_data(), img.mutable_data(),
+                                 frc.mutable_data());
+                 py::dict d;
+                 d["position"] = pos;
+                 d["velocity"] = vel;
+                 d["image"] = img;
+                 d["force"] = frc;
+                 return d;
+             })
+        .def("neighborCounts", &ReplicaEnsemble::neighbor_counts)
+        .def("phaseClocks", &ReplicaEnsemble::phase_clocks)
+        .def("neighborList",
+             [](ReplicaEnsemble& e, uint32_t r) {
+                 std::vector<uint32_t> v = e.neighbor_list(r);
+                 const gb_replica rec = e.record(r);
+                 auto out = make_array<int64_t>({(size_t)rec.N, (size_t)rec.Nmax});
+                 int64_t* o = out.mutable_data();
+                 for (size_t k = 0; k < v.size(); k++)
+                     o[k] = v[k] == 0xffffffffu ? -1 : (int64_t)v[k];
+                 return out;
+             })
+        .def("record",
+             [](ReplicaEnsemble& e, uint32_t r) {
+                 const gb_replica x = e.record(r);
+                 py::dict d;
+                 d["N"] = x.N;
+                 d["timestep"] = x.timestep;
+                 d["kinetic_energy"] = x.ke;
+                 d["potential_energy"] = x.pe;
+                 d["factor"] = x.factor;
+                 d["n_builds"] = x.n_builds;
+                 d["Nmax"] = x.Nmax;
+                 d["dim"] = std::vector<uint32_t>(x.dim, x.dim + 3);
+                 d["stencil"] = x.stencil;
+                 d["dof"] = x.dof;
+                 d["kT"] = x.kT;
+                 d["box"] = std::vector<float>(x.box.L, x.box.L + 3);
+                 d["prepared"] = x.prepared;
+                 return d;
+             })
+        .def_property_readonly("count", &ReplicaEnsemble::count)
+        .def_property_readonly("total_particles", &ReplicaEnsemble::total_particles)
+        .def_readonly("block_size", &ReplicaEnsemble::block_size)
+        .def_readonly("grid_size", &ReplicaEnsemble::grid_size)
+        .def_readonly("launch_count", &ReplicaEnsemble::launch_count)
+        .def_readonly("n_regrowths", &ReplicaEnsemble::n_regrowths)
+        .def_readonly("last_run_ms", &ReplicaEnsemble::last_run_ms)
+        .def_readwrite("use_graph", &ReplicaEnsemble::use_graph)
+        .def("streamHandle", &ReplicaEnsemble::stream_handle);
     }

@@ -106,6 +106,10 @@ _PROTOS = {
     "gb_sfc_scratch_bytes": (c_size, [c_uint, c_int]),
     "gb_sfc_order": (c_int, [c_void, c_uint, _P(Box), c_int, c_void, c_void, c_size, c_void]),
     "gb_gather": (c_int, [c_void, c_void, c_void, c_uint, c_uint, c_void]),
+    "gb_replica_scratch_bytes": (c_size, [ctypes.c_uint64]),
+    "gb_replica_smem_bytes": (c_size, [ctypes.c_uint32, ctypes.c_uint32]),
+    "gb_replica_ctas_per_sm": (c_int, [ctypes.c_uint32, ctypes.c_uint32]),
+    "gb_replicas_run": (c_int, [c_void, c_void]),
 }
 
 _lib = None

@@ -7,6 +7,10 @@
   m = 64, density 0.84, jitter 0.05).
 * ``binary_mixture``: N particles, 80 % A / 20 % B by seeded shuffle, on a jittered simple-cubic
   lattice at the given density (a Kob-Andersen start that needs no overlap removal).
+* ``replica_systems``: independent single-type LJ systems with N ~ U[n_min, n_max], density
+  ~ U[0.7, 0.9] and kT ~ U[0.8, 2.0]; particles on randomly chosen sites of the smallest simple-
+  cubic lattice with at least N sites, jittered, Maxwell-Boltzmann velocities at kT with zero
+  net momentum (the 256-replica ensemble: count 256, N in [500, 20000]).
 * ``multitype_system`` and ``mixture_tables``: N particles of uniformly random types and the
   per-pair tabulated potentials (LJ + Yukawa + Gaussian, F = -dU/dr analytic) on HOOMD's table
   grid r_k = r_min + k (r_cut - r_min)/width.
@@ -115,3 +119,24 @@ def table_potential(r, eps, sig, A, kappa, G, w):
     U = 4 * eps * (sr6 * sr6 - sr6) + A * ey / r + G * eg
     F = 4 * eps * (12 * sr6 * sr6 - 6 * sr6) / r + A * ey * (kappa * r + 1) / (r * r) + G * eg * r / (w * w)
     return U, F
+
+
+def replica_systems(count=256, n_min=500, n_max=20000, rho=(0.7, 0.9), kT=(0.8, 2.0),
+                    jitter=0.05, seed=4):
+    """[(snapshot, kT, seed)] for ``count`` replicas drawn from one seeded generator."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(count):
+        N = int(rng.integers(n_min, n_max + 1))
+        density = float(rng.uniform(*rho))
+        kt = float(rng.uniform(*kT))
+        L = (N / density) ** (1.0 / 3.0)
+        m = int(np.ceil(N ** (1.0 / 3.0) - 1e-9))
+        sites = np.sort(rng.choice(m ** 3, N, replace=False))
+        pos = sc_positions(m, L / m)[sites] + rng.uniform(-jitter, jitter, (N, 3))
+        vel = rng.normal(0.0, np.sqrt(kt), (N, 3))
+        vel -= vel.mean(axis=0)
+        s = _snapshot(pos, L, ("A",), np.zeros(N, np.uint32))
+        s.particles.velocity[:] = vel
+        out.append((s, kt, r + 1))
+    return out

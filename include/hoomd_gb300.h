@@ -356,6 +356,99 @@ int gb_sfc_order(const float* d_pos, unsigned int N, const gb_box* box, int grid
 int gb_gather(void* d_dst, const void* d_src, const uint32_t* d_order, unsigned int N,
               unsigned int elem_bytes, void* stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Replica ensembles (GB300 design; the reference runs one Simulation per process, so a batch of
+ * R systems is R separate runs of the path above: IntegratorTwoStep::update with
+ * TwoStepConstantVolume + BussiThermostat, NeighborListGPUBinned and PotentialPairGPU<LJ>).
+ * Many independent single-type LJ systems of uneven size advance in ONE persistent launch. Each
+ * CTA takes the next replica from a device queue (the caller orders it, largest first) and runs
+ * all of that replica's steps with block barriers only -- step one with the rebuild check, an
+ * in-CTA cell list (counting sort, deterministic order) and neighbour-list build when the check
+ * fires, then pair forces + step two + FP64 kinetic/potential energy sums + the Bussi factor for
+ * the next step -- before it takes the next replica. No CTA ever waits for another.
+ *
+ * A replica's results do not depend on the launch shape: its neighbour order follows the
+ * deterministic cell list, each particle sums its own forces, and the energy sums run over fixed
+ * 32-particle chunks in a fixed order. block_size and grid_size can therefore be tuned on live
+ * steps without changing any trajectory.
+ *
+ * Per-particle arrays are shared by all replicas: replica r owns elements [first, first + N).
+ * Positions float4 (x, y, z, type bits = 0), velocities float4 (vx, vy, vz, mass),
+ * accelerations float4 (ax, ay, az, 0), images int4 (ix, iy, iz, 0), forces float4 (fx, fy, fz,
+ * energy), last-build positions float4. The neighbour list of replica r starts at word
+ * nlist_offset of d_nlist: element k of its particle i is at word
+ * nlist_offset + ((k / 4) * stride + i) * 4 + k % 4.
+ * ------------------------------------------------------------------------------------------- */
+#define GB_REPLICA_OVERFLOW 1u      /* the neighbour list needs `needed` > Nmax slots */
+#define GB_REPLICA_NAN 2u           /* a position is NaN (hoomd/CellListGPU.cu:89-94) */
+#define GB_REPLICA_OUTSIDE 4u       /* a particle left the box (hoomd/CellListGPU.cu:96-110) */
+#define GB_REPLICA_ZERO_KE 8u       /* Bussi factor requested with zero kinetic energy */
+#define GB_REPLICA_CONFIG 16u       /* the cell grid exceeds the launch's max_cells */
+#define GB_REPLICA_MAX_BLOCK 1024u
+
+typedef struct gb_replica
+    {
+    /* set by the caller */
+    gb_box box;                 /* fully periodic; every perpendicular width >= 2 r_list */
+    uint32_t N;
+    uint32_t stride;            /* neighbour-list column stride: >= N, multiple of 32 */
+    uint64_t first;             /* first particle in the shared arrays: multiple of 32 */
+    uint64_t nlist_offset;      /* in uint32 words, multiple of 4 */
+    uint32_t Nmax;              /* neighbour capacity per particle: multiple of 4 */
+    uint32_t dim[3];            /* cell grid: width >= r_list / stencil in every direction */
+    gb_lj_param lj;             /* EvaluatorPairLJ parameters of the one type pair */
+    float r_cut;
+    float r_buff;
+    uint32_t shift_mode;        /* 0 none, 1 shift (hoomd/md/PotentialPair.h:255-341) */
+    uint32_t bussi;             /* 1: ConstantVolume + Bussi; 0: NVE */
+    uint32_t seed;              /* low 16 bits, as the reference's Seed */
+    uint32_t stencil;           /* cells searched on each side of a particle's cell: 1 or 2 */
+    double dt;                  /* rounded to float for the half steps, as a double for Bussi */
+    double kT, tau, dof;
+    uint64_t target;            /* advance until timestep == target */
+    /* state: initialised by the caller (zeros, timestep, factor 1), then owned by the kernel */
+    uint64_t timestep;
+    double factor;              /* Bussi factor of the step that starts at `timestep` */
+    double ke, pe;              /* translational kinetic and potential energy after the last step */
+    uint64_t n_builds;
+    uint32_t prepared;          /* forces and accelerations at `timestep` are current */
+    uint32_t pending_build;     /* step one of the step at `timestep` is done; its neighbour
+                                   list must be built before the step can finish */
+    uint32_t status;            /* GB_REPLICA_* bits; the replica stops when any is set */
+    uint32_t needed;            /* with GB_REPLICA_OVERFLOW: the neighbour count to fit */
+    } gb_replica;
+
+typedef struct gb_replica_batch
+    {
+    gb_replica* d_replicas;     /* [n_replicas], device */
+    uint32_t n_replicas;
+    const uint32_t* d_order;    /* [n_replicas] queue order (replica ids), device */
+    uint32_t* d_queue;          /* two words, zero before the first launch; left zero */
+    float* d_pos;
+    float* d_vel;
+    float* d_accel;
+    int* d_image;
+    float* d_force;
+    float* d_last_pos;
+    uint32_t* d_n_neigh;
+    uint32_t* d_nlist;
+    void* d_scratch;            /* gb_replica_scratch_bytes(total particle slots) */
+    uint64_t n_slots;           /* length of the per-particle arrays (>= every first + N) */
+    uint32_t max_cells;         /* largest dim[0] * dim[1] * dim[2] among the replicas */
+    uint32_t block_size;        /* threads per CTA: multiple of 32, 64 ... 1024 */
+    uint32_t grid_size;         /* persistent CTAs; 0 = every CTA that fits at once */
+    uint64_t* d_phase_clocks;   /* optional [4 * n_replicas]: SM clock cycles the replica's CTA
+                                   spent in step one, list builds, pair step, Bussi draws;
+                                   accumulated (NULL = not recorded) */
+    } gb_replica_batch;
+
+size_t gb_replica_scratch_bytes(uint64_t n_slots);
+/* Dynamic shared memory of one CTA; also the check that max_cells fits (0 = does not fit). */
+size_t gb_replica_smem_bytes(uint32_t max_cells, uint32_t block_size);
+/* CTAs of block_size threads resident per SM (0 = the shape cannot launch). */
+int gb_replica_ctas_per_sm(uint32_t max_cells, uint32_t block_size);
+int gb_replicas_run(const gb_replica_batch* batch, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

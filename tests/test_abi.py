@@ -68,3 +68,15 @@ def test_table_pack_layout():
     assert q.shape == (4, 4)
     assert np.array_equal(q[0], np.float32([5.0, 2.0, 4.0, 2.5]))
     assert np.array_equal(q[3], np.float32([2.0, 3.5, 0.0, 0.0]))
+
+
+def test_replica_host_helpers():
+    """Host-only sizes of the replica-ensemble launch; no GPU call."""
+    from hoomd_gb300 import abi
+    lib = abi.load()
+    n = 1000
+    assert lib.gb_replica_scratch_bytes(n) >= n * (4 + 16) + (n + 31) // 32 * 16
+    # double2 Bussi draws per thread, cell starts and counters, 16-byte rounded
+    assert lib.gb_replica_smem_bytes(1000, 512) == (512 * 16 + 2001 * 4 + 15) // 16 * 16
+    assert lib.gb_replica_smem_bytes(100000, 1024) == 0  # beyond 227 KB of shared memory
+    assert lib.gb_replicas_run(None, None) == abi.GB_ERR_INVALID
