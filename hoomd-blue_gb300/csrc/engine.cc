@@ -1,5 +1,6 @@
 // Host engine implementation (see engine.h). Kernels are reached only through the C ABI.
 #include "engine.h"
+#include "surrogate.h"
 
 #include <algorithm>
 #include <cmath>
@@ -555,7 +556,7 @@ void PairForce::upload()
                                    cudaMemcpyHostToDevice, s),
                    "params");
         }
-    else
+    else if (kind == PairKind::Table)
         {
         std::vector<gb_table_param> tp(np);
         std::vector<float> data;
@@ -624,6 +625,37 @@ gb_pair_args PairForce::pair_args(bool with_virial)
 void PairForce::compute(cudaStream_t s, bool with_virial)
     {
     upload();
+    if (kind == PairKind::MLP)
+        {
+        if (!mlp)
+            throw std::runtime_error("the surrogate pair force has no network");
+        if (with_virial)
+            throw std::runtime_error("the surrogate pair force does not compute virials");
+        if (mlp->ntypes != ntypes)
+            throw std::runtime_error("the surrogate was built for another number of types");
+        ParticleData& pd = *pdata;
+        NeighborList& nl = *nlist;
+        const unsigned int nmax = *std::max_element(nl.Nmax.begin(), nl.Nmax.end());
+        mlp_scratch.resize(gb_mlp_forces_scratch_bytes(pd.N, nmax));
+        gb_mlp_force_args m {};
+        m.d_force = force.get();
+        m.d_pos = pd.pos.get();
+        m.N = pd.N;
+        m.box = pd.box;
+        m.d_n_neigh = nl.n_neigh.get();
+        m.d_nlist = nl.nlist.get();
+        m.stride = nl.stride;
+        m.Nmax = nmax;
+        m.ntypes = ntypes;
+        m.r_min = mlp->r_min;
+        m.r_cut = mlp->r_cut;
+        m.act_split = mlp->act_split;
+        m.d_infer = mlp->infer_block();
+        m.d_scratch = mlp_scratch.get();
+        check(gb_mlp_forces(&m, s), "gb_mlp_forces");
+        virial_valid = false;
+        return;
+        }
     gb_pair_args a = pair_args(with_virial);
     int rc;
     if (kind == PairKind::LJ)
@@ -928,7 +960,7 @@ void Integrator::run_chunk(unsigned int k)
     {
     ParticleData& pd = *pdata;
     cudaStream_t s = pd.stream;
-    const bool fused = forces.size() == 1 && !compute_virial;
+    const bool fused = forces.size() == 1 && !compute_virial && forces[0]->kind != PairKind::MLP;
     for (int attempt = 0; attempt < 16; attempt++)
         {
         checkpoint();
@@ -1148,7 +1180,23 @@ std::vector<double> Integrator::time_phases(unsigned int reps)
             fu.bussi_ring_size = BUSSI_RING;
             }
         cuda_check(cudaEventRecord(ev[0], s), "record");
-        check(f.launch_fused(a, fu, s), "fused pair step");
+        if (f.kind == PairKind::MLP)
+            {
+            // unfused: forces, step two, thermo and the Bussi factor as enqueue_step_general
+            f.compute(s, false);
+            check(gb_cv_step_two(pd.vel.get(), pd.accel.get(), f.force.get(), pd.N, (float)dt,
+                                 1.0f, nullptr, s),
+                  "gb_cv_step_two");
+            check(gb_thermo_reduce(pd.vel.get(), f.force.get(), nullptr, 0, pd.N,
+                                   d_thermo_scratch.get(), ds->thermo, s),
+                  "thermo");
+            if (bussi)
+                check(gb_bussi_factor(&ds->thermo[0], dof(), dt, tau, kT, pd.timestep + 1,
+                                      pd.seed, 0u, &ds->factor, s),
+                      "bussi");
+            }
+        else
+            check(f.launch_fused(a, fu, s), "fused pair step");
         cuda_check(cudaEventRecord(ev[1], s), "record");
         cuda_check(cudaEventSynchronize(ev[1]), "sync");
         float t_pair;

@@ -207,8 +207,11 @@ enum class PairKind
     {
     LJ = 0,
     Table = 1,
-    Example = 2
+    Example = 2,
+    MLP = 3 // radial MLP surrogate of Table (unfused path: pair list + tensor-core tiles)
     };
+
+class MlpSurrogate;
 
 class PairForce
     {
@@ -237,7 +240,8 @@ class PairForce
     std::vector<double> t_rmin;
     std::vector<std::vector<double>> t_U, t_F;
     bool params_dirty = true;
-    DeviceArray<char> d_params;
+    std::shared_ptr<MlpSurrogate> mlp;
+    DeviceArray<char> d_params, mlp_scratch;
     DeviceArray<float> d_rcutsq, d_ronsq, d_table, force, virial;
     bool virial_valid = false;
     };

@@ -7,6 +7,7 @@
 
 #include "engine.h"
 #include "ensemble.h"
+#include "surrogate.h"
 
 namespace py = pybind11;
 using namespace gbe;
@@ -167,7 +168,8 @@ PYBIND11_MODULE(_hoomd_gb300, m)
     py::enum_<PairKind>(m, "PairKind")
         .value("LJ", PairKind::LJ)
         .value("Table", PairKind::Table)
-        .value("Example", PairKind::Example);
+        .value("Example", PairKind::Example)
+        .value("MLP", PairKind::MLP);
 
     py::class_<PairForce, std::shared_ptr<PairForce>>(m, "PotentialPairGPU")
         .def(py::init<std::shared_ptr<ParticleData>, std::shared_ptr<NeighborList>, PairKind>())
@@ -176,6 +178,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setParamsTable", &PairForce::set_params_table)
         .def("setRCut", &PairForce::set_r_cut)
         .def("setROn", &PairForce::set_r_on)
+        .def("setSurrogate", [](PairForce& f, std::shared_ptr<MlpSurrogate> m) { f.mlp = m; })
         .def_property(
             "mode", [](PairForce& f) { return f.shift_mode; },
             [](PairForce& f, int v) {
@@ -232,6 +235,44 @@ PYBIND11_MODULE(_hoomd_gb300, m)
              })
         .def("synchronize",
              [](Integrator& i) { cuda_check(cudaStreamSynchronize(i.pdata->stream), "sync"); });
+
+    using farr = py::array_t<float, py::array::c_style | py::array::forcecast>;
+    using uarr = py::array_t<uint32_t, py::array::c_style | py::array::forcecast>;
+    auto fvec = [](const farr& a) { return std::vector<float>(a.data(), a.data() + a.size()); };
+    auto uvec = [](const uarr& a) { return std::vector<uint32_t>(a.data(), a.data() + a.size()); };
+    py::class_<MlpSurrogate, std::shared_ptr<MlpSurrogate>>(m, "MlpSurrogate")
+        .def(py::init<unsigned int, double, double, uint64_t>())
+        .def_property_readonly("n_pairs", &MlpSurrogate::n_pairs)
+        .def_readonly("ntypes", &MlpSurrogate::ntypes)
+        .def_readonly("r_min", &MlpSurrogate::r_min)
+        .def_readonly("r_cut", &MlpSurrogate::r_cut)
+        .def_readwrite("act_split", &MlpSurrogate::act_split)
+        .def_readonly("train_steps", &MlpSurrogate::train_steps)
+        .def_readonly("train_ms", &MlpSurrogate::train_ms)
+        .def("setParams", [fvec](MlpSurrogate& s, farr th) { s.set_params(fvec(th)); })
+        .def("getParams",
+             [](MlpSurrogate& s) {
+                 std::vector<float> v = s.params();
+                 auto out = make_array<float>({v.size()});
+                 std::copy(v.begin(), v.end(), out.mutable_data());
+                 return out;
+             })
+        .def("setSamples",
+             [fvec, uvec](MlpSurrogate& s, uarr pair, farr r, farr U, farr F) {
+                 s.set_samples(uvec(pair), fvec(r), fvec(U), fvec(F));
+             })
+        .def("train", &MlpSurrogate::train, py::call_guard<py::gil_scoped_release>())
+        .def("loss", &MlpSurrogate::loss)
+        .def("eval",
+             [fvec, uvec](MlpSurrogate& s, uarr pair, farr r) {
+                 std::vector<float> U, dU;
+                 s.eval(uvec(pair), fvec(r), U, dU);
+                 auto a = make_array<float>({U.size()});
+                 auto b = make_array<float>({dU.size()});
+                 std::copy(U.begin(), U.end(), a.mutable_data());
+                 std::copy(dU.begin(), dU.end(), b.mutable_data());
+                 return py::make_tuple(a, b);
+             });
 
     using darr = py::array_t<double, py::array::c_style | py::array::forcecast>;
     py::class_<ReplicaEnsemble, std::shared_ptr<ReplicaEnsemble>>(m, "ReplicaEnsembleGPU")

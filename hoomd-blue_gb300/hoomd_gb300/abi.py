@@ -69,6 +69,13 @@ class StepFuse(ctypes.Structure):
                 ("bussi_ring_size", c_uint)]
 
 
+class MlpForceArgs(ctypes.Structure):
+    _fields_ = [("d_force", c_void), ("d_pos", c_void), ("N", c_uint), ("box", Box),
+                ("d_n_neigh", c_void), ("d_nlist", c_void), ("stride", c_u64), ("Nmax", c_uint),
+                ("ntypes", c_uint), ("r_min", c_float), ("r_cut", c_float), ("act_split", c_int),
+                ("d_infer", c_void), ("d_scratch", c_void)]
+
+
 _P = ctypes.POINTER
 _PROTOS = {
     "gb_box_make": (c_int, [_P(c_double), c_double, c_double, c_double, _P(c_int), _P(Box)]),
@@ -110,6 +117,19 @@ _PROTOS = {
     "gb_replica_smem_bytes": (c_size, [ctypes.c_uint32, ctypes.c_uint32]),
     "gb_replica_ctas_per_sm": (c_int, [ctypes.c_uint32, ctypes.c_uint32]),
     "gb_replicas_run": (c_int, [c_void, c_void]),
+    "gb_mlp_param_count": (c_size, [ctypes.c_uint32]),
+    "gb_mlp_train_scratch_bytes": (c_size, [ctypes.c_uint32]),
+    "gb_mlp_loss_grad": (c_int, [c_void, ctypes.c_uint32, c_float, c_float, c_void, c_void, c_void,
+                                 c_void, ctypes.c_uint32, c_float, c_int, c_void, c_void, c_void,
+                                 c_void]),
+    "gb_mlp_adam": (c_int, [c_void, c_void, c_void, c_void, c_size, c_float, c_float, c_float,
+                            c_float, ctypes.c_uint32, c_void]),
+    "gb_mlp_infer_bytes": (c_size, [ctypes.c_uint32]),
+    "gb_mlp_prepare": (c_int, [c_void, ctypes.c_uint32, c_void, c_void]),
+    "gb_mlp_eval": (c_int, [c_void, ctypes.c_uint32, c_float, c_float, c_int, c_void, c_void,
+                            ctypes.c_uint32, c_void, c_void, c_void]),
+    "gb_mlp_forces_scratch_bytes": (c_size, [c_uint, c_uint]),
+    "gb_mlp_forces": (c_int, [c_void, c_void]),
 }
 
 _lib = None

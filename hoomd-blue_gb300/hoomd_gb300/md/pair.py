@@ -153,3 +153,36 @@ class ExamplePair(Pair):
 
     def _set_pair_params(self, cpp, i, j, v):
         cpp.setParamsExample(i, j, v["k"], v["sigma"])
+
+
+class TableSurrogate(Pair):
+    """Radial MLP stand-in for a multi-type ``Table`` (the reference has no counterpart; it
+    replaces hoomd/md/EvaluatorPairTable.h's spline gathers). ``surrogate`` is a trained
+    :class:`hoomd_gb300.surrogate.Surrogate`; its r_cut applies to every type pair and pairs
+    closer than its r_min feel no force, as in ``Table``. Mode 'none', no virials. On attach the
+    force becomes a PotentialPairGPU of kind MLP (gb_mlp_forces in include/hoomd_gb300.h)."""
+
+    _kind = _hoomd_gb300.PairKind.MLP
+    _accepted_modes = ("none",)
+
+    def __init__(self, nlist, surrogate):
+        super().__init__(nlist, default_r_cut=surrogate.r_cut, default_r_on=0, mode='none')
+        self.surrogate = surrogate
+
+    def _attach(self, simulation, cpp_nlist):
+        self._simulation = simulation
+        state = simulation.state
+        ntypes = len(state.particle_types)
+        if ntypes != self.surrogate.ntypes:
+            raise RuntimeError(f"the surrogate was trained for {self.surrogate.ntypes} types, "
+                               f"the state has {ntypes}")
+        self._cpp_obj = _hoomd_gb300.PotentialPairGPU(state._cpp_pdata, cpp_nlist, self._kind)
+        self._cpp_obj.setSurrogate(self.surrogate._cpp)
+        for i in range(ntypes):
+            for j in range(i, ntypes):
+                self._cpp_obj.setRCut(i, j, float(self.surrogate.r_cut))
+        return self._cpp_obj
+
+    @property
+    def virials(self):
+        raise RuntimeError("TableSurrogate does not compute virials")

@@ -449,6 +449,73 @@ size_t gb_replica_smem_bytes(uint32_t max_cells, uint32_t block_size);
 int gb_replica_ctas_per_sm(uint32_t max_cells, uint32_t block_size);
 int gb_replicas_run(const gb_replica_batch* batch, void* stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Radial MLP surrogate of the Table pair potential (GB300 design; it stands in for
+ * EvaluatorPairTable, hoomd/md/EvaluatorPairTable.h, on many type pairs at once). Per unordered
+ * type pair p = (a <= b), index a*ntypes - a(a-1)/2 + (b - a), and distance r in [r_min, r_cut):
+ *   phi_k(r) = exp(-gamma (r - mu_k)^2), mu_k = r_min + k h, h = (r_cut - r_min)/31,
+ *              gamma = 1/(2 h^2), k = 0..31
+ *   z1 = W1e E[p] + W1r phi + b1, h1 = silu(z1);  z2 = W2 h1 + b2, h2 = silu(z2);
+ *   U = w3 . h2 + b3,  F(r) = -dU/dr (analytic, forward-mode through the same layers).
+ * Parameters are one float array (offsets in floats; P = ntypes (ntypes + 1) / 2):
+ *   W1e[64][16] @ 0, W1r[64][32] @ 1024, b1[64] @ 3072, W2[64][64] @ 3136, b2[64] @ 7232,
+ *   w3[64] @ 7296, b3 @ 7360, E[P][16] @ 7424; gb_mlp_param_count(P) floats in all.
+ * Inference (gb_mlp_prepare / gb_mlp_eval / gb_mlp_forces) runs the two 64-wide layers and their
+ * derivative on BF16 tensor cores with FP32 accumulation: E, W1e, W1r, W2, w3 are rounded to
+ * bfloat16; phi, dphi/dr, h1, dh1/dr enter the products as bfloat16 (act_split 0) or as the sum
+ * of two bfloat16 numbers (act_split 1). Training (gb_mlp_loss_grad) evaluates the same function
+ * in FP32 and returns the gradient of
+ *   L = (1/B) sum_s [ (dU/dr_s + F_s)^2 + lam (U_s - U_s^target)^2 ]
+ * with the rounding (quant = 0 none, 1 bfloat16, 2 two-term bfloat16) applied straight-through.
+ * ------------------------------------------------------------------------------------------- */
+#define GB_MLP_EMB 16u
+#define GB_MLP_RBF 32u
+#define GB_MLP_HID 64u
+
+size_t gb_mlp_param_count(uint32_t n_pairs);
+size_t gb_mlp_train_scratch_bytes(uint32_t batch);
+/* d_grad (param_count floats) is overwritten; *d_loss (double) receives L. */
+int gb_mlp_loss_grad(const float* d_theta, uint32_t n_pairs, float r_min, float r_cut,
+                     const uint32_t* d_pair, const float* d_r, const float* d_U,
+                     const float* d_F, uint32_t batch, float lam, int quant, float* d_grad,
+                     double* d_loss, void* d_scratch, void* stream);
+/* Adam (Kingma & Ba 2015) with bias correction; step counts from 1. */
+int gb_mlp_adam(float* d_theta, const float* d_grad, float* d_m, float* d_v, size_t n, float lr,
+                float beta1, float beta2, float eps, uint32_t step, void* stream);
+
+/* Inference block: per-pair first-layer offsets C[p] = W1e E[p] + b1 (FP32) and the bfloat16
+ * weights laid out as tensor-core operand fragments. */
+size_t gb_mlp_infer_bytes(uint32_t n_pairs);
+int gb_mlp_prepare(const float* d_theta, uint32_t n_pairs, void* d_infer, void* stream);
+/* U and dU/dr of n samples (pair index, r) on the tensor-core path (tests). */
+int gb_mlp_eval(const void* d_infer, uint32_t n_pairs, float r_min, float r_cut, int act_split,
+                const uint32_t* d_pair, const float* d_r, uint32_t n, float* d_U, float* d_dU,
+                void* stream);
+
+/* Pair forces of the surrogate over a column-major interleaved-by-4 full neighbour list (the
+ * layout of gb_nlist_build_binned with interleave 4): each unordered pair within
+ * [r_min, r_cut) is evaluated once and its force added to both particles with atomics.
+ * d_force (float4[N]: fx, fy, fz, energy) is overwritten. Orthorhombic or triclinic periodic
+ * boxes. d_scratch: gb_mlp_forces_scratch_bytes(N, Nmax). */
+typedef struct gb_mlp_force_args
+    {
+    float* d_force;
+    const float* d_pos;               /* float4[N], type bits in w */
+    unsigned int N;
+    gb_box box;
+    const unsigned int* d_n_neigh;
+    const unsigned int* d_nlist;
+    uint64_t stride;
+    unsigned int Nmax;                /* capacity per particle (largest over types) */
+    unsigned int ntypes;
+    float r_min, r_cut;
+    int act_split;
+    const void* d_infer;
+    void* d_scratch;
+    } gb_mlp_force_args;
+size_t gb_mlp_forces_scratch_bytes(unsigned int N, unsigned int Nmax);
+int gb_mlp_forces(const gb_mlp_force_args* args, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,216 @@
+"""The Table surrogate's GPU kernels through the C ABI, against the FP64 oracle
+(oracle/mlp_oracle.py): the training loss gradient, the tensor-core forward (energy and dU/dr),
+and the pair forces over a neighbour list."""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+from hoomd_gb300 import abi  # noqa: E402
+from oracle import mlp_oracle as M  # noqa: E402
+from gpu_util import GpuNlist, dev, p, stream, host  # noqa: E402
+
+RMIN, RCUT = 0.8, 3.0
+
+
+def params(n_pairs, seed=5):
+    rng = np.random.default_rng(seed)
+    th = M.init_params(n_pairs, seed)
+    th[3072:3136] = rng.normal(0, 0.3, 64)
+    th[7232:7296] = rng.normal(0, 0.3, 64)
+    th[7360] = 0.2
+    return th.astype(np.float32)
+
+
+def samples(n_pairs, B, seed=9):
+    rng = np.random.default_rng(seed)
+    return (rng.integers(0, n_pairs, B).astype(np.uint32),
+            rng.uniform(RMIN, RCUT, B).astype(np.float32),
+            rng.normal(0, 1, B).astype(np.float32), rng.normal(0, 3, B).astype(np.float32))
+
+
+def gpu_loss_grad(th, pr, r, Ut, Ft, n_pairs, lam, quant):
+    L = abi.load()
+    B = len(r)
+    d_th, d_p, d_r, d_U, d_F = dev(th), dev(pr), dev(r), dev(Ut), dev(Ft)
+    grad = torch.zeros(len(th), dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    scr = torch.empty(L.gb_mlp_train_scratch_bytes(B), dtype=torch.uint8, device="cuda")
+    abi.check(L.gb_mlp_loss_grad(p(d_th), n_pairs, RMIN, RCUT, p(d_p), p(d_r), p(d_U), p(d_F), B,
+                                 lam, quant, p(grad), p(loss), p(scr), stream()), "loss_grad")
+    return host(loss)[0], host(grad).astype(np.float64)
+
+
+@pytest.mark.parametrize("quant", [0, 1])
+def test_loss_gradient_matches_oracle(quant):
+    n_pairs = 10
+    th = params(n_pairs)
+    pr, r, Ut, Ft = samples(n_pairs, 3000)
+    Lg, gg = gpu_loss_grad(th, pr, r, Ut, Ft, n_pairs, 0.3, quant)
+    Lo, go = M.loss_and_grad(th.astype(np.float64), pr, r.astype(np.float64), Ut, Ft, 0.3, RMIN,
+                             RCUT, n_pairs, quant=None if quant == 0 else "bf16")
+    tol = 1e-4 if quant == 0 else 2e-2
+    assert abs(Lg - Lo) <= tol * abs(Lo)
+    scale = np.abs(go).max()
+    assert np.abs(gg - go).max() <= tol * scale, (np.abs(gg - go).max(), scale)
+    # every parameter block is exercised
+    for a, b in [(0, 1024), (1024, 3072), (3072, 3136), (3136, 7232), (7232, 7296), (7296, 7360),
+                 (7424, len(th))]:
+        assert np.abs(go[a:b]).max() > 0
+
+
+def prepared(th, n_pairs):
+    L = abi.load()
+    inf = torch.empty(L.gb_mlp_infer_bytes(n_pairs), dtype=torch.uint8, device="cuda")
+    d_th = dev(th)
+    abi.check(L.gb_mlp_prepare(p(d_th), n_pairs, p(inf), stream()), "prepare")
+    torch.cuda.synchronize()
+    return inf
+
+
+@pytest.mark.parametrize("split", [0, 1])
+def test_tensor_core_forward_matches_oracle(split):
+    n_pairs = 528
+    th = params(n_pairs, 7)
+    pr, r, _, _ = samples(n_pairs, 5003, 4)
+    inf = prepared(th, n_pairs)
+    U = torch.zeros(len(r), dtype=torch.float32, device="cuda")
+    dU = torch.zeros_like(U)
+    L = abi.load()
+    d_pr, d_r = dev(pr), dev(r)  # held: a freed temporary's block would be reused at once
+    abi.check(L.gb_mlp_eval(p(inf), n_pairs, RMIN, RCUT, split, p(d_pr), p(d_r), len(r), p(U),
+                            p(dU), stream()), "eval")
+    Uo, dUo, _ = M.forward(th, pr, r.astype(np.float64), RMIN, RCUT, n_pairs,
+                           quant="bf16x2" if split else "bf16")
+    Ug, dUg = host(U), host(dU)
+    tol = 2e-3 if split else 3e-2
+    assert np.abs(Ug - Uo).max() <= tol * max(1.0, np.abs(Uo).max())
+    assert np.abs(dUg - dUo).max() <= tol * max(1.0, np.abs(dUo).max())
+    # against the unrounded network: the two-term activations remove the activation rounding
+    Ux, dUx, _ = M.forward(th, pr, r.astype(np.float64), RMIN, RCUT, n_pairs, quant=None)
+    err = np.sqrt(np.mean((dUg - dUx) ** 2)) / np.sqrt(np.mean(dUx ** 2))
+    assert err < (0.01 if split else 0.05)
+
+
+def test_pair_forces_match_oracle():
+    rng = np.random.default_rng(3)
+    ntypes, N, Lb = 3, 600, 9.0
+    pos = rng.uniform(-Lb / 2, Lb / 2, (N, 3))
+    types = rng.integers(0, ntypes, N)
+    n_pairs = ntypes * (ntypes + 1) // 2
+    th = params(n_pairs, 11)
+    pos4 = np.zeros((N, 4), np.float32)
+    pos4[:, :3] = pos
+    pos4[:, 3] = types.astype(np.uint32).view(np.float32)
+    box = (Lb, Lb, Lb, 0, 0, 0)
+    nl = GpuNlist(pos4, box, np.full((ntypes, ntypes), RCUT), 0.3, layout="col4")
+    inf = prepared(th, n_pairs)
+    L = abi.load()
+    Nmax = int(nl.Nmax.max())
+    force = torch.zeros(4 * N, dtype=torch.float32, device="cuda")
+    scr = torch.empty(L.gb_mlp_forces_scratch_bytes(N, Nmax), dtype=torch.uint8, device="cuda")
+    a = abi.MlpForceArgs(d_force=p(force), d_pos=p(nl.pos), N=N, box=nl.box,
+                         d_n_neigh=p(nl.n_neigh), d_nlist=p(nl.nlist), stride=nl.stride,
+                         Nmax=Nmax, ntypes=ntypes, r_min=RMIN, r_cut=RCUT, act_split=1,
+                         d_infer=p(inf), d_scratch=p(scr))
+    abi.check(L.gb_mlp_forces(ctypes.byref(a), stream()), "forces")
+    F = host(force).reshape(N, 4)
+    Fo, Eo = M.pair_forces(th, pos4[:, :3].astype(np.float64), types, (Lb, Lb, Lb), ntypes, RMIN,
+                           RCUT, quant="bf16x2")
+    scale = np.abs(Fo).max()
+    assert np.abs(F[:, :3] - Fo).max() <= 3e-3 * scale
+    assert np.abs(F[:, 3] - Eo).max() <= 3e-3 * max(1.0, np.abs(Eo).max())
+    assert abs(F[:, :3].sum(0)).max() < 1e-3 * scale  # Newton's third law
+
+
+def test_training_reduces_the_loss():
+    """A few hundred Adam steps of the GPU kernels on a smooth two-pair target."""
+    n_pairs = 3
+    th = params(n_pairs, 2)
+    rng = np.random.default_rng(1)
+    B = 4096
+    pr = rng.integers(0, n_pairs, B).astype(np.uint32)
+    r = rng.uniform(0.9, 3.0, B).astype(np.float32)
+    eps = 1.0 + 0.5 * pr
+    Ut = (4 * eps * (r ** -12 - r ** -6)).astype(np.float32)
+    Ft = (4 * eps * (12 * r ** -13 - 6 * r ** -7)).astype(np.float32)
+    L = abi.load()
+    d_th, d_p, d_r, d_U, d_F = dev(th), dev(pr), dev(r), dev(Ut), dev(Ft)
+    n = len(th)
+    grad = torch.zeros(n, dtype=torch.float32, device="cuda")
+    m, v = torch.zeros_like(grad), torch.zeros_like(grad)
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    scr = torch.empty(L.gb_mlp_train_scratch_bytes(B), dtype=torch.uint8, device="cuda")
+    losses = []
+    for step in range(1, 401):
+        abi.check(L.gb_mlp_loss_grad(p(d_th), n_pairs, RMIN, RCUT, p(d_p), p(d_r), p(d_U),
+                                     p(d_F), B, 0.1, 1, p(grad), p(loss), p(scr), stream()), "lg")
+        abi.check(L.gb_mlp_adam(p(d_th), p(grad), p(m), p(v), n, 3e-3, 0.9, 0.999, 1e-8, step,
+                                stream()), "adam")
+        if step in (1, 400):
+            losses.append(host(loss)[0])
+    assert losses[1] < 0.05 * losses[0], losses
+
+
+def test_surrogate_pipeline_learns_the_table():
+    """Plain-Table NVT frames -> pair samples -> GPU training -> TableSurrogate run; per-particle
+    forces of the trained surrogate against the FP64 oracle's Table forces on a fresh frame."""
+    import hoomd_gb300 as hoomd
+    from hoomd_gb300 import md, workloads
+    from hoomd_gb300.surrogate import Surrogate
+    ntypes = 3
+    snap = workloads.multitype_system(N=4096, ntypes=ntypes, density=0.8, seed=2)
+    tabs = workloads.mixture_tables(ntypes, r_min=RMIN, r_cut=RCUT, width=1000, seed=2)
+    types = snap.particles.types
+    params = {(types[i], types[j]): dict(r_min=v["r_min"], U=v["U"], F=v["F"])
+              for (i, j), v in tabs.items()}
+    sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=1)
+    sim.create_state_from_snapshot(snap)
+    sim.state.thermalize_particle_momenta(hoomd.filter.All(), 1.5)
+    cell = md.nlist.Cell(buffer=0.4)
+    tab = md.pair.Table(nlist=cell, default_r_cut=RCUT)
+    for k, v in params.items():
+        tab.params[k] = v
+    sim.operations.integrator = md.Integrator(
+        dt=0.004, forces=[tab], methods=[md.methods.ConstantVolume(
+            hoomd.filter.All(), thermostat=md.methods.thermostats.Bussi(kT=1.5))])
+    frames = []
+    box = np.array(snap.configuration.box[:3])
+    for _ in range(4):
+        sim.run(100)
+        s = sim.state.get_snapshot()
+        frames.append((s.particles.position.copy(), s.particles.typeid.copy(), box))
+    sur = Surrogate.from_table(params, types, RMIN, RCUT, seed=3)
+    samples = sur.sample_pairs(frames[:3], anchors=3000)
+    losses = sur.fit(samples, steps=3000, batch=4096, report=1000)
+    assert losses[-1] < 0.2 * losses[0], losses
+    # per-particle forces on the held-out frame: surrogate (GPU) vs Table (FP64 oracle)
+    pos, typeid, _ = frames[3]
+    s2 = hoomd.Simulation(device=hoomd.device.GPU(), seed=1)
+    snap2 = sim.state.get_snapshot()
+    s2.create_state_from_snapshot(snap2)
+    cell2 = md.nlist.Cell(buffer=0.4)
+    sf = md.pair.TableSurrogate(nlist=cell2, surrogate=sur)
+    s2.operations.integrator = md.Integrator(
+        dt=0.004, forces=[sf], methods=[md.methods.ConstantVolume(hoomd.filter.All())])
+    s2.run(0)
+    Fs = sf.forces
+    from oracle import oracle as O
+    N = len(pos)
+    pos64 = O.make_pos4(snap2.particles.position, snap2.particles.typeid, 64)
+    tp, _, opar, odata = __import__("gpu_util").table_params(
+        ntypes, {k: (v["r_min"], v["U"], v["F"]) for k, v in tabs.items()})
+    n, l, h, _ = O.build_nlist(pos64, tuple(snap2.configuration.box), np.full((ntypes, ntypes), RCUT),
+                               0.4, full=False, prec=64)
+    fo, _ = O.pair_forces("table", pos64, tuple(snap2.configuration.box), opar,
+                          np.full((ntypes, ntypes), RCUT * RCUT), n, l, h, third_law=True,
+                          compute_virial=False, tdata=odata, prec=64)
+    rmse = np.sqrt(np.mean((Fs - fo[:, :3]) ** 2))
+    frms = np.sqrt(np.mean(fo[:, :3] ** 2))
+    assert rmse < 0.1 * frms, (rmse, frms)
+    s2.run(20)  # the surrogate drives dynamics through the unfused integrator path
+    assert np.isfinite(s2.state.get_snapshot().particles.position).all()
