@@ -364,6 +364,139 @@ def run_gb300(args):
         print(json.dumps(line), flush=True)
 
 
+def peak_bf16():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("bf16_tflops_sustained") or d.get("bf16_tflops")), "measured sustained"
+    return 1700.0, "fallback sustained"
+
+
+def run_mlp(args):
+    """The 32-type Table system (N = 524,288) with the plain Table force and with the radial MLP
+    surrogate trained on pairs from the plain-Table NVT run: timesteps/s of both, force RMSE."""
+    import numpy as np
+    import torch
+    import hoomd_gb300 as hoomd
+    from hoomd_gb300 import md
+    from hoomd_gb300.surrogate import Surrogate
+    rank, world, local = dist_init()
+    torch.cuda.set_device(local)
+    wl = workloads_registry()["table32_524k"]
+    c = wl.config
+    snap = wl.make_snap(1 + rank)
+    types = snap.particles.types
+    tabs = wl.tables()
+    params = {(types[i], types[j]): dict(r_min=v["r_min"], U=v["U"], F=v["F"])
+              for (i, j), v in tabs.items()}
+
+    def make(force_fn, snapshot, thermalize):
+        sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=1 + rank)
+        sim.create_state_from_snapshot(snapshot)
+        if thermalize:
+            sim.state.thermalize_particle_momenta(hoomd.filter.All(), c["kT"])
+        cell = md.nlist.Cell(buffer=c["buffer"])
+        f = force_fn(cell)
+        sim.operations.integrator = md.Integrator(dt=c["dt"], forces=[f], methods=[
+            md.methods.ConstantVolume(hoomd.filter.All(),
+                                      md.methods.thermostats.Bussi(kT=c["kT"]))])
+        sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=c["sort_period"]))
+        return sim, f, cell
+
+    def table_force(cell):
+        t = md.pair.Table(nlist=cell, default_r_cut=c["r_cut"])
+        for k, v in params.items():
+            t.params[k] = v
+        return t
+
+    def timed(sim, steps):
+        integ = sim._cpp_integrator
+        stream = torch.cuda.ExternalStream(integ.streamHandle())
+        launches0 = integ.launch_count
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        sim.run(steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1), integ.launch_count - launches0
+
+    # plain Table: equilibrate, collect training frames, time
+    sim_t, tab, cell_t = make(table_force, snap, True)
+    sim_t.run(max(3, args.warmup))
+    box = np.array(snap.configuration.box[:3])
+    frames = []
+    for _ in range(args.mlp_frames):
+        sim_t.run(100)
+        st = sim_t.state.get_snapshot()
+        frames.append((st.particles.position.copy(), st.particles.typeid.copy(), box))
+    clocks = ClockSampler(local) if rank == 0 else None
+    ms_t, launches_t = timed(sim_t, args.steps)
+    clk = clocks.stop() if clocks else None
+    phases_t = sim_t._cpp_integrator.timePhases(10)
+
+    # surrogate: sample pairs from the frames, train with the GPU kernels
+    t0 = time.perf_counter()
+    sur = Surrogate.from_table(params, types, c["r_min"], c["r_cut"], seed=7)
+    sur._cpp.act_split = args.mlp_act_split
+    samples = sur.sample_pairs(frames, anchors=args.mlp_anchors)
+    t_sample = time.perf_counter() - t0
+    losses = sur.fit(samples, steps=args.mlp_train_steps, batch=8192, report=1000)
+    t_train = sur._cpp.train_ms / 1e3
+
+    # accuracy on the state the timed Table run ended in
+    snap_eval = sim_t.state.get_snapshot()
+    tab._cpp_obj.compute(False)
+    F_table = tab.forces
+    sim_m, sf, cell_m = make(lambda cell: md.pair.TableSurrogate(nlist=cell, surrogate=sur),
+                             snap_eval, False)
+    sim_m.run(0)
+    F_mlp = sf.forces
+    rmse = float(np.sqrt(np.mean((F_mlp - F_table) ** 2)))
+    frms = float(np.sqrt(np.mean(F_table ** 2)))
+    sim_m.run(max(3, args.warmup // 4))
+    clocks = ClockSampler(local) if rank == 0 else None
+    ms_m, launches_m = timed(sim_m, args.steps)
+    clk_m = clocks.stop() if clocks else None
+    phases_m = sim_m._cpp_integrator.timePhases(10)
+    tps_t = args.steps / (ms_t / 1e3)
+    tps_m = args.steps / (ms_m / 1e3)
+    # tensor-pipe roofline of the surrogate force: FLOPs of the per-pair products
+    # (2 x (32x64 + 64x64) multiply-adds for value and derivative) per evaluated pair
+    sum_n = sim_m._cpp_integrator.sumNNeigh()
+    N = snap.particles.N
+    R = sur.r_cut
+    pairs_in_cut = 0.5 * N * c["density"] * 4.0 / 3.0 * np.pi * (R ** 3 - sur.r_min ** 3)
+    flops_pair = 2.0 * 2.0 * (32 * 64 + 64 * 64)
+    peak, pk = peak_bf16()
+    t_force = phases_m[2] / 1e3
+    achieved = flops_pair * pairs_in_cut / t_force / 1e12
+    line = {"metric": "MLP-surrogate vs plain Table TPS at <=1e-3 force err (32 types, N=524288)",
+            "value": tps_m, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_m / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 tensor / fp32",
+            "data": "synthetic (seeded 32-type tables, random types, jittered lattice)",
+            "config": dict(c, workload="table32_mlp_524k", mlp="16 emb + 32 RBF -> 64 -> 64 SiLU"
+                           " -> 1, force = -dU/dr", act_split=sur._cpp.act_split,
+                           train_steps=args.mlp_train_steps, train_batch=8192,
+                           train_samples=int(len(samples["r"])), train_frames=args.mlp_frames),
+            "table_tps": tps_t, "mlp_over_table": tps_m / tps_t,
+            "force_rmse": rmse, "force_rms": frms, "force_rmse_target": 1e-3,
+            "force_rmse_ref": "GPU Table path (FP32; within 1e-5 of the FP64 oracle)",
+            "train_s": t_train, "sample_s": t_sample, "train_loss": losses[-3:],
+            "phases_ms": {"table": dict(zip(["step_one", "rebuild", "pair_step"], phases_t)),
+                          "mlp": dict(zip(["step_one", "rebuild", "force+step_two"], phases_m))},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                         "kernel": "k_mlp_forces (+ pair list, step two, thermo)",
+                         "flops_formula": "pairs in [r_min, r_cut) (0.5 N rho 4/3 pi (rc^3 - "
+                                          "rmin^3)) x 2 x 2 x (32x64 + 64x64)",
+                         "peak_kind": pk},
+            "gpu_launches": int(launches_m), "clocks": clk_m, "clocks_table": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def replica_systems():
     from hoomd_gb300 import workloads as W
     return W.replica_systems(count=256, n_min=500, n_max=20000, seed=4)
@@ -559,7 +692,12 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", default="lj_fcc_1m",
                     choices=["lj_fcc_1m", "lj_sc_4096", "ka_262k", "table32_524k",
-                             "replicas_256"])
+                             "replicas_256", "table32_mlp_524k"])
+    ap.add_argument("--mlp-train-steps", type=int, default=20000)
+    ap.add_argument("--mlp-frames", type=int, default=3)
+    ap.add_argument("--mlp-anchors", type=int, default=20000)
+    ap.add_argument("--mlp-act-split", type=int, default=1, choices=[0, 1],
+                    help="activations as one bfloat16 (0) or the sum of two (1)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fcc-m", type=int, default=64,
@@ -572,6 +710,8 @@ def main():
         run_reference(args)
     elif args.workload == "replicas_256":
         run_replicas(args)
+    elif args.workload == "table32_mlp_524k":
+        run_mlp(args)
     else:
         run_gb300(args)
 

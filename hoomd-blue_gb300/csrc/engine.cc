@@ -1211,6 +1211,9 @@ std::vector<double> Integrator::time_phases(unsigned int reps)
         v /= reps;
     restore();
     nlist->build_sync();
+    // the force arrays belong to the restored positions again
+    for (auto& f : forces)
+        f->compute(s, false);
     cuda_check(cudaStreamSynchronize(s), "time_phases");
     return acc;
     }
