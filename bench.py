@@ -497,9 +497,9 @@ def run_mlp(args):
         print(json.dumps(line), flush=True)
 
 
-def replica_systems():
+def replica_systems(count=256):
     from hoomd_gb300 import workloads as W
-    return W.replica_systems(count=256, n_min=500, n_max=20000, seed=4)
+    return W.replica_systems(count=count, n_min=500, n_max=20000, seed=4)
 
 
 REPLICA_CONFIG = {"workload": "lj_replicas_256", "replicas": 256, "N_range": [500, 20000],
@@ -518,7 +518,7 @@ def run_replicas(args):
     import numpy as np
     rank, world, local = dist_init()
     torch.cuda.set_device(local)
-    systems = replica_systems()
+    systems = replica_systems(args.replicas)
 
     def build():
         ens = hoomd.ReplicaEnsemble(dt=0.005, r_cut=2.5, buffer=0.4)
@@ -529,7 +529,11 @@ def run_replicas(args):
     ens = build()
     Ntot = ens.total_particles
     ens.run(0)
-    tune = ens.autotune(steps=10, repeats=1)
+    if args.no_tune:
+        ens.set_launch(1024, 0)
+        tune = [dict(block_size=1024, grid_size=0, ms_per_step=float("nan"))]
+    else:
+        tune = ens.autotune(steps=10, repeats=1)
     ens.run(max(3, args.warmup))
     stream = torch.cuda.ExternalStream(ens._cpp.streamHandle())
     sum_n = sum(int(np.sum(ens._cpp.neighborCounts(r))) for r in range(ens.count))
@@ -594,7 +598,7 @@ def run_replicas(args):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic (seeded sizes, densities, kT; jittered lattices, MB velocities)",
-            "config": dict(REPLICA_CONFIG, total_particles=Ntot,
+            "config": dict(REPLICA_CONFIG, replicas=len(systems), total_particles=Ntot,
                            launch_shape=ens.launch, tuned_from=len(tune),
                            parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
             "timesteps_per_s": args.steps / (ms / 1e3), "pair_evals_per_s":
@@ -696,6 +700,10 @@ def main():
     ap.add_argument("--mlp-train-steps", type=int, default=20000)
     ap.add_argument("--mlp-frames", type=int, default=3)
     ap.add_argument("--mlp-anchors", type=int, default=20000)
+    ap.add_argument("--replicas", type=int, default=256,
+                    help="replica count of replicas_256 (256 = the benchmark; fewer for profiling)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="replicas_256: fixed 1024-thread launch instead of the tuner (profiling)")
     ap.add_argument("--mlp-act-split", type=int, default=1, choices=[0, 1],
                     help="activations as one bfloat16 (0) or the sum of two (1)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
