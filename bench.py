@@ -245,7 +245,7 @@ def traffic_per_launch(wl):
     """DRAM bytes (read + write) per launch of the fused pair kernel from the committed ncu
     summary of this workload, when one exists."""
     p = REPO / "profiles" / "pair_step_lj_traffic.json"
-    if wl.name == "lj_fcc_1m" and p.exists():
+    if wl.name == "lj_fcc_1m" and wl.config["N"] == 1048576 and p.exists():
         d = json.loads(p.read_text())
         return d.get("dram_bytes_per_launch_scaled_to_1M")
     return None
