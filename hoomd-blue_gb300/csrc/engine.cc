@@ -310,7 +310,9 @@ void NeighborList::allocate()
     cell_size.resize(ncell);
     xyzf.resize(4 * (size_t)ncell * Nmax_cell);
     cell_type.resize(nt > 1 ? (size_t)ncell * Nmax_cell : 0);
-    nlist.resize(std::max<uint64_t>(1, stride * nmax_all));
+    // the interleaved layout writes whole groups of four: a capacity that is not a multiple of
+    // four (a fixed start capacity) still needs its last group allocated
+    nlist.resize(std::max<uint64_t>(1, stride * ((nmax_all + 3u) & ~3u)));
     n_neigh.resize(std::max(1u, pd.N));
     n_neigh.zero(pd.stream);
     last_pos.resize(4 * (size_t)std::max(1u, pd.N));

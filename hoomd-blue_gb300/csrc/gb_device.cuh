@@ -61,6 +61,37 @@ __device__ __forceinline__ void min_image_ortho(const gb_box& b, float& x, float
         x = fsub(x, fmul(b.L[0], rintf(fmul(x, b.Linv[0]))));
     }
 
+// Packed FP32 pairs (add/sub/mul.rn.f32x2): two independent IEEE round-to-nearest operations
+// per instruction, so each half is bit-identical to the scalar __f*_rn form.
+__device__ __forceinline__ uint64_t f2pack(float lo, float hi)
+    {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+    }
+__device__ __forceinline__ void f2unpack(uint64_t v, float& lo, float& hi)
+    {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    }
+__device__ __forceinline__ uint64_t f2sub(uint64_t a, uint64_t b)
+    {
+    uint64_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+    }
+__device__ __forceinline__ uint64_t f2add(uint64_t a, uint64_t b)
+    {
+    uint64_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+    }
+__device__ __forceinline__ uint64_t f2mul(uint64_t a, uint64_t b)
+    {
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+    }
+
 __device__ __forceinline__ float dot3(float x, float y, float z)
     {
     return fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z));

@@ -448,7 +448,68 @@ __global__ void __launch_bounds__(TILE_WARPS_MAX * 32)
                 const float* sh = s_shift + (meta & 0xffu) * 6;
                 const float sz = sh[0], syz = sh[1], sxz = sh[2], sy = sh[3], sxy = sh[4], sx = sh[5];
                 const unsigned int tj = meta >> 8;
-                for (unsigned int o = 0; o < nown; o++)
+                // r_cut, r_list^2 and capacity of own particle o
+                auto limits = [&](unsigned int o, float& rc, float& rl, unsigned int& nmax_o) {
+                    if (MULTI)
+                        {
+                        const unsigned int ti = s_otype[ob + o];
+                        rc = s_tab[ti * ntypes + tj];
+                        rl = s_tab[ntypes * ntypes + ti * ntypes + tj];
+                        nmax_o = __ldg(Nmax_t + ti);
+                        }
+                    else
+                        {
+                        rc = rc0;
+                        rl = rl0;
+                        nmax_o = Nmax0;
+                        }
+                };
+                // the lanes holding a hit for own particle o write it at count(o) + rank
+                auto emit = [&](unsigned int o, unsigned int i, bool hit, unsigned int nmax_o) {
+                    const unsigned int bal = __ballot_sync(0xffffffffu, hit);
+                    if (bal)
+                        {
+                        const unsigned int cnt_o = __shfl_sync(0xffffffffu, my_cnt, o);
+                        const unsigned int k = cnt_o + __popc(bal & lt_mask);
+                        if (hit && k < nmax_o)
+                            {
+                            if (LAYOUT == 4)
+                                nlist[(size_t)(k >> 2) * row4 + (size_t)i * 4u + (k & 3u)] = j;
+                            else
+                                nlist[(size_t)k * stride + i] = j;
+                            }
+                        if (lane == (int)o)
+                            my_cnt += __popc(bal);
+                        }
+                };
+                unsigned int o = 0;
+                if (ORTHO)
+                    {
+                    // two own particles per step in packed FP32 pairs; each half rounds as the
+                    // scalar fsub / fmul / fadd sequence below, so the decisions are identical
+                    const uint64_t cx2 = f2pack(c.x, c.x), cy2 = f2pack(c.y, c.y),
+                                   cz2 = f2pack(c.z, c.z);
+                    const uint64_t sx2 = f2pack(sx, sx), sy2 = f2pack(sy, sy), sz2 = f2pack(sz, sz);
+                    for (; o + 1 < nown; o += 2)
+                        {
+                        const float4 p0 = s_own[ob + o], p1 = s_own[ob + o + 1];
+                        const uint64_t dx = f2sub(f2sub(f2pack(p0.x, p1.x), cx2), sx2);
+                        const uint64_t dy = f2sub(f2sub(f2pack(p0.y, p1.y), cy2), sy2);
+                        const uint64_t dz = f2sub(f2sub(f2pack(p0.z, p1.z), cz2), sz2);
+                        const uint64_t r2
+                            = f2add(f2add(f2mul(dx, dx), f2mul(dy, dy)), f2mul(dz, dz));
+                        float rsq0, rsq1;
+                        f2unpack(r2, rsq0, rsq1);
+                        const unsigned int i0 = __float_as_uint(p0.w), i1 = __float_as_uint(p1.w);
+                        float rc, rl;
+                        unsigned int nmax_o;
+                        limits(o, rc, rl, nmax_o);
+                        emit(o, i0, has && rsq0 <= rl && j != i0 && rc > 0.0f, nmax_o);
+                        limits(o + 1, rc, rl, nmax_o);
+                        emit(o + 1, i1, has && rsq1 <= rl && j != i1 && rc > 0.0f, nmax_o);
+                        }
+                    }
+                for (; o < nown; o++)
                     {
                     const float4 pi = s_own[ob + o];
                     const unsigned int i = __float_as_uint(pi.w);
@@ -466,35 +527,8 @@ __global__ void __launch_bounds__(TILE_WARPS_MAX * 32)
                     const float rsq = dot3(dx, dy, dz);
                     float rc, rl;
                     unsigned int nmax_o;
-                    if (MULTI)
-                        {
-                        const unsigned int ti = s_otype[ob + o];
-                        rc = s_tab[ti * ntypes + tj];
-                        rl = s_tab[ntypes * ntypes + ti * ntypes + tj];
-                        nmax_o = __ldg(Nmax_t + ti);
-                        }
-                    else
-                        {
-                        rc = rc0;
-                        rl = rl0;
-                        nmax_o = Nmax0;
-                        }
-                    const bool hit = has && rsq <= rl && j != i && rc > 0.0f;
-                    const unsigned int bal = __ballot_sync(0xffffffffu, hit);
-                    if (bal)
-                        {
-                        const unsigned int cnt_o = __shfl_sync(0xffffffffu, my_cnt, o);
-                        const unsigned int k = cnt_o + __popc(bal & lt_mask);
-                        if (hit && k < nmax_o)
-                            {
-                            if (LAYOUT == 4)
-                                nlist[(size_t)(k >> 2) * row4 + (size_t)i * 4u + (k & 3u)] = j;
-                            else
-                                nlist[(size_t)k * stride + i] = j;
-                            }
-                        if (lane == (int)o)
-                            my_cnt += __popc(bal);
-                        }
+                    limits(o, rc, rl, nmax_o);
+                    emit(o, i, has && rsq <= rl && j != i && rc > 0.0f, nmax_o);
                     }
                 }
             __syncwarp();

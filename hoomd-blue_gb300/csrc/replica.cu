@@ -146,37 +146,6 @@ __device__ __forceinline__ uint32_t wrap_index(int c, int n)
     return (uint32_t)(c < 0 ? c + n : (c >= n ? c - n : c));
     }
 
-// Packed FP32 pairs (add/sub/mul.rn.f32x2): two independent IEEE round-to-nearest operations
-// per instruction, so each half is bit-identical to the scalar __f*_rn form.
-__device__ __forceinline__ uint64_t f2pack(float lo, float hi)
-    {
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-    }
-__device__ __forceinline__ void f2unpack(uint64_t v, float& lo, float& hi)
-    {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-    }
-__device__ __forceinline__ uint64_t f2sub(uint64_t a, uint64_t b)
-    {
-    uint64_t r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-    }
-__device__ __forceinline__ uint64_t f2add(uint64_t a, uint64_t b)
-    {
-    uint64_t r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-    }
-__device__ __forceinline__ uint64_t f2mul(uint64_t a, uint64_t b)
-    {
-    uint64_t r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-    }
-
 // Cell list + neighbour list of the replica in sh.rep. Sets sh.err / sh.maxcnt; ends synced.
 // Not inlined (nor are the other phases): each phase gets its own register allocation.
 template<int MAXT>
