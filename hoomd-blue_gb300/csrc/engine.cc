@@ -474,6 +474,7 @@ PairForce::PairForce(std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborL
     r_on.assign(np, 0.0f);
     lj.assign(np, gb_lj_param {0.0f, 0.0f});
     ex.assign(np, gb_example_param {0.0f, 0.0f});
+    rad.assign(np, gb_radial_param {});
     t_rmin.assign(np, 0.0);
     t_U.assign(np, std::vector<double>(1, 0.0));
     t_F.assign(np, std::vector<double>(1, 0.0));
@@ -495,6 +496,21 @@ void PairForce::set_params_lj(unsigned int i, unsigned int j, double sigma, doub
 void PairForce::set_params_example(unsigned int i, unsigned int j, double k, double sigma)
     {
     ex[i * ntypes + j] = ex[j * ntypes + i] = gb_example_param {(float)k, (float)sigma};
+    params_dirty = true;
+    }
+
+void PairForce::set_params_radial(unsigned int i, unsigned int j, unsigned int kind,
+                                  const std::vector<double>& v)
+    {
+    if (kind >= GB_RADIAL_KINDS)
+        throw std::invalid_argument("unknown radial potential kind");
+    if (v.size() > 6)
+        throw std::invalid_argument("at most six parameters per type pair");
+    gb_radial_param p {};
+    for (size_t k = 0; k < v.size(); k++)
+        p.v[k] = (float)v[k];
+    p.kind = kind;
+    rad[i * ntypes + j] = rad[j * ntypes + i] = p;
     params_dirty = true;
     }
 
@@ -548,6 +564,13 @@ void PairForce::upload()
         {
         d_params.resize(np * sizeof(gb_lj_param));
         cuda_check(cudaMemcpyAsync(d_params.get(), lj.data(), np * sizeof(gb_lj_param),
+                                   cudaMemcpyHostToDevice, s),
+                   "params");
+        }
+    else if (kind == PairKind::Radial)
+        {
+        d_params.resize(np * sizeof(gb_radial_param));
+        cuda_check(cudaMemcpyAsync(d_params.get(), rad.data(), np * sizeof(gb_radial_param),
                                    cudaMemcpyHostToDevice, s),
                    "params");
         }
@@ -664,6 +687,8 @@ void PairForce::compute(cudaStream_t s, bool with_virial)
         rc = gb_pair_forces_lj(&a, (const gb_lj_param*)d_params.get(), s);
     else if (kind == PairKind::Example)
         rc = gb_pair_forces_example(&a, (const gb_example_param*)d_params.get(), s);
+    else if (kind == PairKind::Radial)
+        rc = gb_pair_forces_radial(&a, (const gb_radial_param*)d_params.get(), s);
     else
         rc = gb_pair_forces_table(&a, (const gb_table_param*)d_params.get(), d_table.get(), s);
     check(rc, "pair force");
@@ -676,6 +701,8 @@ int PairForce::launch_fused(const gb_pair_args& a, const gb_step_fuse& f, cudaSt
         return gb_md_pair_step_lj(&a, (const gb_lj_param*)d_params.get(), &f, s);
     if (kind == PairKind::Example)
         return gb_md_pair_step_example(&a, (const gb_example_param*)d_params.get(), &f, s);
+    if (kind == PairKind::Radial)
+        return gb_md_pair_step_radial(&a, (const gb_radial_param*)d_params.get(), &f, s);
     return gb_md_pair_step_table(&a, (const gb_table_param*)d_params.get(), d_table.get(), &f, s);
     }
 

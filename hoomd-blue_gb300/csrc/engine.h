@@ -208,7 +208,8 @@ enum class PairKind
     LJ = 0,
     Table = 1,
     Example = 2,
-    MLP = 3 // radial MLP surrogate of Table (unfused path: pair list + tensor-core tiles)
+    MLP = 3, // radial MLP surrogate of Table (unfused path: pair list + tensor-core tiles)
+    Radial = 4 // the other radial evaluators (gb_radial_param.kind)
     };
 
 class MlpSurrogate;
@@ -220,6 +221,8 @@ class PairForce
               PairKind kind);
     void set_params_lj(unsigned int i, unsigned int j, double sigma, double epsilon);
     void set_params_example(unsigned int i, unsigned int j, double k, double sigma);
+    void set_params_radial(unsigned int i, unsigned int j, unsigned int kind,
+                           const std::vector<double>& v);
     void set_params_table(unsigned int i, unsigned int j, double r_min,
                           const std::vector<double>& U, const std::vector<double>& F);
     void set_r_cut(unsigned int i, unsigned int j, double r);
@@ -237,6 +240,7 @@ class PairForce
     std::vector<float> r_cut, r_on;
     std::vector<gb_lj_param> lj;
     std::vector<gb_example_param> ex;
+    std::vector<gb_radial_param> rad;
     std::vector<double> t_rmin;
     std::vector<std::vector<double>> t_U, t_F;
     bool params_dirty = true;

@@ -152,4 +152,190 @@ struct EvalExample
         }
     };
 
+// The reference's other radial evaluators (hoomd/md/EvaluatorPair{Gauss,Yukawa,Morse,
+// ForceShiftedLJ,Mie,ExpandedMie,ExpandedLJ,Buckingham,LJ1208,LJ0804,LJGauss,ExpandedGaussian,
+// OPP,TWF}.h) as one evaluator: the kind is uniform per force, so the switch costs one
+// non-divergent branch per pair and the whole family shares one set of kernel instantiations.
+// Each kind writes V(r) and F(r) = -dV/dr from its closed form; shift mode subtracts V(r_cut).
+// The closed forms are one out-of-line function, so every kernel variant shares its code.
+struct EvalRadial
+    {
+    using param_type = gb_radial_param;
+    // derived per type pair: the Mie prefactor, or F(r_cut) of the force-shifted LJ
+    __device__ __forceinline__ static void prepare_param(param_type& p, float rcutsq)
+        {
+        if (p.kind == GB_RADIAL_MIE || p.kind == GB_RADIAL_EXPANDED_MIE)
+            {
+            const float n = p.v[2], m = p.v[3];
+            p.aux = (n / (n - m)) * powf(n / m, m / (n - m)) * p.v[0];
+            }
+        else if (p.kind == GB_RADIAL_FORCE_SHIFTED_LJ)
+            {
+            float V, F;
+            p.aux = 0.0f;
+            eval(p, sqrtf(rcutsq), V, F);
+            p.aux = F;
+            }
+        }
+    float rsq, rcutsq;
+    param_type p;
+    __device__ __forceinline__ EvalRadial(float rsq_, float rcutsq_, const param_type& p_,
+                                          const float*)
+        : rsq(rsq_), rcutsq(rcutsq_), p(p_)
+        {
+        }
+    static constexpr bool needsCharge()
+        {
+        return false;
+        }
+    __device__ __forceinline__ void setCharge(float, float) { }
+
+    // (s/x)^n - style LJ of exponents (n, m) with prefactor c: V and F at distance x = r - delta
+    __device__ __forceinline__ static void lj_nm(float c, float sigma, float x, int n, int m,
+                                                 float& V, float& F)
+        {
+        const float q = sigma / x;
+        const float q2 = q * q, q4 = q2 * q2;
+        float qn, qm;
+        if (n == 12)
+            {
+            const float q6 = q4 * q2;
+            qn = q6 * q6;
+            qm = m == 6 ? q6 : q4 * q4;
+            }
+        else // n == 8, m == 4
+            {
+            qn = q4 * q4;
+            qm = q4;
+            }
+        V = c * (qn - qm);
+        F = c * ((float)n * qn - (float)m * qm) / x;
+        }
+
+    __device__ __noinline__ static void eval(const param_type& p, float r, float& V, float& F)
+        {
+        const float* v = p.v;
+        switch (p.kind)
+            {
+            case GB_RADIAL_GAUSS:
+                {
+                const float is2 = 1.0f / (v[1] * v[1]);
+                const float e = v[0] * expf(-0.5f * r * r * is2);
+                V = e;
+                F = e * r * is2;
+                break;
+                }
+            case GB_RADIAL_YUKAWA:
+                {
+                const float e = v[0] * expf(-v[1] * r) / r;
+                V = e;
+                F = e * (v[1] * r + 1.0f) / r;
+                break;
+                }
+            case GB_RADIAL_MORSE:
+                {
+                const float e1 = expf(-v[1] * (r - v[2]));
+                V = v[0] * (e1 * e1 - 2.0f * e1);
+                F = 2.0f * v[0] * v[1] * (e1 * e1 - e1);
+                break;
+                }
+            case GB_RADIAL_FORCE_SHIFTED_LJ:
+                {
+                // F = F_LJ(r) - F_LJ(r_cut); aux = F_LJ(r_cut) (0 while it is being derived).
+                // The energy's (r - r_cut) F_LJ(r_cut) term is added by evalForceAndEnergy.
+                lj_nm(4.0f * v[1], v[0], r, 12, 6, V, F);
+                F -= p.aux;
+                break;
+                }
+            case GB_RADIAL_MIE:
+            case GB_RADIAL_EXPANDED_MIE:
+                {
+                const float x = p.kind == GB_RADIAL_EXPANDED_MIE ? r - v[4] : r;
+                const float q = v[1] / x;
+                const float qn = powf(q, v[2]), qm = powf(q, v[3]);
+                V = p.aux * (qn - qm);
+                F = p.aux * (v[2] * qn - v[3] * qm) / x;
+                break;
+                }
+            case GB_RADIAL_EXPANDED_LJ:
+                lj_nm(4.0f * v[1], v[0], r - v[2], 12, 6, V, F);
+                break;
+            case GB_RADIAL_BUCKINGHAM:
+                {
+                const float ir2 = 1.0f / (r * r), ir6 = ir2 * ir2 * ir2;
+                const float e = v[0] * expf(-r / v[1]);
+                V = e - v[2] * ir6;
+                F = e / v[1] - 6.0f * v[2] * ir6 / r;
+                break;
+                }
+            case GB_RADIAL_LJ1208:
+                lj_nm(4.0f * v[1], v[0], r, 12, 8, V, F);
+                break;
+            case GB_RADIAL_LJ0804:
+                lj_nm(4.0f * v[1], v[0], r, 8, 4, V, F);
+                break;
+            case GB_RADIAL_LJ_GAUSS:
+                {
+                const float ir2 = 1.0f / (r * r), ir6 = ir2 * ir2 * ir2;
+                const float d = r - v[2];
+                const float is2 = 1.0f / (v[1] * v[1]);
+                const float g = v[0] * expf(-0.5f * d * d * is2);
+                V = ir6 * ir6 - 2.0f * ir6 - g;
+                F = (12.0f * ir6 * ir6 - 12.0f * ir6) / r - g * d * is2;
+                break;
+                }
+            case GB_RADIAL_EXPANDED_GAUSS:
+                {
+                const float d = r - v[2];
+                const float is2 = 1.0f / (v[1] * v[1]);
+                const float e = v[0] * expf(-0.5f * d * d * is2);
+                V = e;
+                F = e * d * is2;
+                break;
+                }
+            case GB_RADIAL_OPP:
+                {
+                const float a = v[0] * powf(r, -v[2]);
+                const float b = v[1] * powf(r, -v[3]);
+                const float arg = v[4] * r - v[5];
+                const float c = cosf(arg), s = sinf(arg);
+                V = a + b * c;
+                F = (v[2] * a + v[3] * b * c) / r + v[4] * b * s;
+                break;
+                }
+            default: // GB_RADIAL_TWF
+                {
+                const float is2 = 1.0f / (v[0] * v[0]);
+                const float t = r * r * is2 - 1.0f;
+                const float it3 = 1.0f / (t * t * t);
+                const float pre = 4.0f * v[1] / (v[2] * v[2]);
+                V = pre * (it3 * it3 - v[2] * it3);
+                F = pre * (6.0f * it3 * it3 - 3.0f * v[2] * it3) / t * 2.0f * r * is2;
+                break;
+                }
+            }
+        }
+
+    __device__ __forceinline__ bool evalForceAndEnergy(float& force_divr, float& pair_eng,
+                                                       bool energy_shift) const
+        {
+        if (!(rsq < rcutsq))
+            return false;
+        const float r = sqrtf(rsq);
+        float V, F;
+        eval(p, r, V, F);
+        if (p.kind == GB_RADIAL_FORCE_SHIFTED_LJ)
+            V += (r - sqrtf(rcutsq)) * p.aux;
+        if (energy_shift)
+            {
+            float Vc, Fc;
+            eval(p, sqrtf(rcutsq), Vc, Fc);
+            V -= Vc;
+            }
+        force_divr = F / r;
+        pair_eng = V;
+        return true;
+        }
+    };
+
 } // namespace gb

@@ -169,13 +169,15 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .value("LJ", PairKind::LJ)
         .value("Table", PairKind::Table)
         .value("Example", PairKind::Example)
-        .value("MLP", PairKind::MLP);
+        .value("MLP", PairKind::MLP)
+        .value("Radial", PairKind::Radial);
 
     py::class_<PairForce, std::shared_ptr<PairForce>>(m, "PotentialPairGPU")
         .def(py::init<std::shared_ptr<ParticleData>, std::shared_ptr<NeighborList>, PairKind>())
         .def("setParamsLJ", &PairForce::set_params_lj)
         .def("setParamsExample", &PairForce::set_params_example)
         .def("setParamsTable", &PairForce::set_params_table)
+        .def("setParamsRadial", &PairForce::set_params_radial)
         .def("setRCut", &PairForce::set_r_cut)
         .def("setROn", &PairForce::set_r_on)
         .def("setSurrogate", [](PairForce& f, std::shared_ptr<MlpSurrogate> m) { f.mlp = m; })

@@ -69,6 +69,10 @@ class StepFuse(ctypes.Structure):
                 ("bussi_ring_size", c_uint)]
 
 
+class RadialParam(ctypes.Structure):
+    _fields_ = [("v", c_float * 6), ("kind", c_uint), ("aux", c_float)]
+
+
 class MlpForceArgs(ctypes.Structure):
     _fields_ = [("d_force", c_void), ("d_pos", c_void), ("N", c_uint), ("box", Box),
                 ("d_n_neigh", c_void), ("d_nlist", c_void), ("stride", c_u64), ("Nmax", c_uint),
@@ -113,6 +117,8 @@ _PROTOS = {
     "gb_sfc_scratch_bytes": (c_size, [c_uint, c_int]),
     "gb_sfc_order": (c_int, [c_void, c_uint, _P(Box), c_int, c_void, c_void, c_size, c_void]),
     "gb_gather": (c_int, [c_void, c_void, c_void, c_uint, c_uint, c_void]),
+    "gb_pair_forces_radial": (c_int, [c_void, c_void, c_void]),
+    "gb_md_pair_step_radial": (c_int, [c_void, c_void, c_void, c_void]),
     "gb_replica_scratch_bytes": (c_size, [ctypes.c_uint64]),
     "gb_replica_smem_bytes": (c_size, [ctypes.c_uint32, ctypes.c_uint32]),
     "gb_replica_ctas_per_sm": (c_int, [ctypes.c_uint32, ctypes.c_uint32]),

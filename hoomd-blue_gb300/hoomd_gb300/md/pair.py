@@ -186,3 +186,54 @@ class TableSurrogate(Pair):
     @property
     def virials(self):
         raise RuntimeError("TableSurrogate does not compute virials")
+
+
+class _Radial(Pair):
+    """The reference's other radial pair potentials, one GPU kernel family (``gb_pair_forces_radial``
+    in include/hoomd_gb300.h selects the closed form by kind). Parameter keys and modes follow
+    hoomd.md.pair."""
+
+    _kind = _hoomd_gb300.PairKind.Radial
+    _radial_kind = None
+    _keys = ()
+
+    def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
+        super().__init__(nlist, default_r_cut, default_r_on, mode)
+        self.params = TypePairDict(validator=dict_validator(self._keys))
+
+    def _set_pair_params(self, cpp, i, j, v):
+        cpp.setParamsRadial(i, j, self._radial_kind, [float(v[k]) for k in self._keys])
+
+
+def _radial(name, kind, keys, doc, modes=("none", "shift", "xplor")):
+    cls = type(name, (_Radial,), {"_radial_kind": kind, "_keys": tuple(keys),
+                                  "_accepted_modes": modes, "__doc__": doc})
+    cls.__module__ = __name__
+    return cls
+
+
+Gaussian = _radial("Gaussian", 0, ("epsilon", "sigma"),
+                   "Gaussian (hoomd/md/pair/pair.py, EvaluatorPairGauss.h): eps exp(-r^2/2 sigma^2).")
+Yukawa = _radial("Yukawa", 1, ("epsilon", "kappa"),
+                 "Yukawa (EvaluatorPairYukawa.h): eps exp(-kappa r)/r.")
+Morse = _radial("Morse", 2, ("D0", "alpha", "r0"),
+                "Morse (EvaluatorPairMorse.h): D0 [e^(-2 alpha (r-r0)) - 2 e^(-alpha (r-r0))].")
+ForceShiftedLJ = _radial("ForceShiftedLJ", 3, ("sigma", "epsilon"),
+                         "Force-shifted LJ (EvaluatorPairForceShiftedLJ.h).", ("none",))
+Mie = _radial("Mie", 4, ("epsilon", "sigma", "n", "m"), "Mie n-m (EvaluatorPairMie.h).")
+ExpandedMie = _radial("ExpandedMie", 5, ("epsilon", "sigma", "n", "m", "delta"),
+                      "Mie at r - delta (EvaluatorPairExpandedMie.h).")
+ExpandedLJ = _radial("ExpandedLJ", 6, ("sigma", "epsilon", "delta"),
+                     "LJ at r - delta (EvaluatorPairExpandedLJ.h).")
+Buckingham = _radial("Buckingham", 7, ("A", "rho", "C"),
+                     "Buckingham (EvaluatorPairBuckingham.h): A exp(-r/rho) - C/r^6.")
+LJ1208 = _radial("LJ1208", 8, ("sigma", "epsilon"), "12-8 Lennard-Jones (EvaluatorPairLJ1208.h).")
+LJ0804 = _radial("LJ0804", 9, ("sigma", "epsilon"), "8-4 Lennard-Jones (EvaluatorPairLJ0804.h).")
+LJGauss = _radial("LJGauss", 10, ("epsilon", "sigma", "r0"),
+                  "Lennard-Jones-Gauss (EvaluatorPairLJGauss.h).")
+ExpandedGaussian = _radial("ExpandedGaussian", 11, ("epsilon", "sigma", "delta"),
+                           "Gaussian at r - delta (EvaluatorPairExpandedGaussian.h).")
+OPP = _radial("OPP", 12, ("C1", "C2", "eta1", "eta2", "k", "phi"),
+              "Oscillating pair potential (EvaluatorPairOPP.h).")
+TWF = _radial("TWF", 13, ("sigma", "epsilon", "alpha"),
+              "Ten Wolde-Frenkel (EvaluatorPairTWF.h); infinite for r <= sigma.")

@@ -213,6 +213,53 @@ int gb_pair_forces_table(const gb_pair_args* args, const gb_table_param* d_param
 int gb_pair_forces_example(const gb_pair_args* args, const gb_example_param* d_params,
                            void* stream);
 
+/* The other radial evaluators of the reference, one kernel family selected by `kind` (uniform per
+ * force, so the switch does not diverge). Parameters per kind, in v[0..5], as the reference's
+ * param_type keys (hoomd/md/pair/pair.py), r in the formulas below:
+ *   GAUSS       epsilon, sigma            eps exp(-r^2 / 2 sigma^2)   (EvaluatorPairGauss.h)
+ *   YUKAWA      epsilon, kappa            eps exp(-kappa r) / r        (EvaluatorPairYukawa.h)
+ *   MORSE       D0, alpha, r0             D0 [e^{-2a(r-r0)} - 2 e^{-a(r-r0)}] (EvaluatorPairMorse.h)
+ *   FORCE_SHIFTED_LJ  sigma, epsilon      LJ(r) + (r - r_cut) F_LJ(r_cut) (EvaluatorPairForceShiftedLJ.h)
+ *   MIE         epsilon, sigma, n, m      (n/(n-m)) (n/m)^(m/(n-m)) eps [(s/r)^n - (s/r)^m] (EvaluatorPairMie.h)
+ *   EXPANDED_MIE  epsilon, sigma, n, m, delta   Mie at r - delta  (EvaluatorPairExpandedMie.h)
+ *   EXPANDED_LJ   sigma, epsilon, delta   LJ at r - delta              (EvaluatorPairExpandedLJ.h)
+ *   BUCKINGHAM  A, rho, C                 A exp(-r/rho) - C / r^6      (EvaluatorPairBuckingham.h)
+ *   LJ1208      sigma, epsilon            4 eps [(s/r)^12 - (s/r)^8]   (EvaluatorPairLJ1208.h)
+ *   LJ0804      sigma, epsilon            4 eps [(s/r)^8 - (s/r)^4]    (EvaluatorPairLJ0804.h)
+ *   LJ_GAUSS    epsilon, sigma, r0        1/r^12 - 2/r^6 - eps exp(-(r-r0)^2 / 2 sigma^2) (EvaluatorPairLJGauss.h)
+ *   EXPANDED_GAUSS  epsilon, sigma, delta eps exp(-(r-delta)^2 / 2 sigma^2) (EvaluatorPairExpandedGaussian.h)
+ *   OPP         C1, C2, eta1, eta2, k, phi  C1 r^-eta1 + C2 r^-eta2 cos(k r - phi) (EvaluatorPairOPP.h)
+ *   TWF         sigma, epsilon, alpha     4 eps/alpha^2 [s^-6 - alpha s^-3], s = (r/sigma)^2 - 1 (EvaluatorPairTWF.h)
+ * Shift mode 1 subtracts the energy at r_cut; XPLOR smoothing as for LJ. */
+typedef enum gb_radial_kind
+    {
+    GB_RADIAL_GAUSS = 0,
+    GB_RADIAL_YUKAWA = 1,
+    GB_RADIAL_MORSE = 2,
+    GB_RADIAL_FORCE_SHIFTED_LJ = 3,
+    GB_RADIAL_MIE = 4,
+    GB_RADIAL_EXPANDED_MIE = 5,
+    GB_RADIAL_EXPANDED_LJ = 6,
+    GB_RADIAL_BUCKINGHAM = 7,
+    GB_RADIAL_LJ1208 = 8,
+    GB_RADIAL_LJ0804 = 9,
+    GB_RADIAL_LJ_GAUSS = 10,
+    GB_RADIAL_EXPANDED_GAUSS = 11,
+    GB_RADIAL_OPP = 12,
+    GB_RADIAL_TWF = 13,
+    GB_RADIAL_KINDS = 14
+    } gb_radial_kind;
+
+typedef struct gb_radial_param
+    {
+    float v[6];
+    uint32_t kind;      /* gb_radial_kind, the same for every type pair of one force */
+    float aux;          /* 0 (the kernels fill it per type pair: F(r_cut) of FORCE_SHIFTED_LJ) */
+    } gb_radial_param;
+
+int gb_pair_forces_radial(const gb_pair_args* args, const gb_radial_param* d_params,
+                          void* stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Integrator halves. Replace gpu_nvt_rescale_step_one / _two
  * (hoomd/md/TwoStepConstantVolumeGPU.cu:35-89, 166-205; with scale 1 these are the NVE halves of
@@ -342,6 +389,8 @@ int gb_md_pair_step_table(const gb_pair_args* args, const gb_table_param* d_para
                           const float* d_table, const gb_step_fuse* fuse, void* stream);
 int gb_md_pair_step_example(const gb_pair_args* args, const gb_example_param* d_params,
                             const gb_step_fuse* fuse, void* stream);
+int gb_md_pair_step_radial(const gb_pair_args* args, const gb_radial_param* d_params,
+                           const gb_step_fuse* fuse, void* stream);
 
 /* ---------------------------------------------------------------------------------------------
  * Space-filling-curve sort. Replaces SFCPackTunerGPU (hoomd/SFCPackTunerGPU.cu:26-160): a

@@ -3,8 +3,9 @@ the HOOMD-blue source tree; the fixtures are committed so the GPU machine never need
 
 Outputs
 -------
-forces_and_energies_lj_table.json
-    The ``LJ`` and ``Table`` entries of the reference's Mathematica-computed fixture
+forces_and_energies_lj_table.json, forces_and_energies_radial.json
+    The ``LJ`` and ``Table`` entries (and, in the second file, those of the fourteen radial
+    potentials of ``RADIAL``) of the reference's Mathematica-computed fixture
     ``hoomd/md/pytest/forces_and_energies.json`` (force and energy of two particles at
     r = 0.75 and 1.5, r_cut = 2.5), used by the reference's ``test_force_energy_accuracy``
     (``hoomd/md/pytest/test_potential.py:952-1058``).
@@ -74,6 +75,11 @@ def table_index_safe_f32(rsq, rcutsq, rmin, width):
     return ~inside | (np.floor(vf) < width)
 
 
+# the radial potentials served by gb_pair_forces_radial
+RADIAL = ("Gaussian", "Yukawa", "Morse", "ForceShiftedLJ", "Mie", "ExpandedMie", "ExpandedLJ",
+          "Buckingham", "LJ1208", "LJ0804", "LJGauss", "ExpandedGaussian", "OPP", "TWF")
+
+
 def main():
     if not obuild.ref_available():
         raise SystemExit("reference source tree not found")
@@ -85,6 +91,9 @@ def main():
     out = {k: fe[k] for k in ("LJ", "Table")}
     out["_source"] = "hoomd/md/pytest/forces_and_energies.json (LJ, Table entries)"
     json.dump(out, open(HERE / "forces_and_energies_lj_table.json", "w"), indent=1)
+    out = {k: fe[k] for k in RADIAL}
+    out["_source"] = "hoomd/md/pytest/forces_and_energies.json (" + ", ".join(RADIAL) + ")"
+    json.dump(out, open(HERE / "forces_and_energies_radial.json", "w"), indent=1)
 
     pairs = json.load(open(REF / "hoomd/md/pytest/true_pair_list.json"))
     json.dump(pairs, open(HERE / "true_pair_list_sc7.json", "w"))
