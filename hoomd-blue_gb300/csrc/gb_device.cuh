@@ -92,6 +92,13 @@ __device__ __forceinline__ uint64_t f2mul(uint64_t a, uint64_t b)
     return r;
     }
 
+__device__ __forceinline__ uint64_t f2fma(uint64_t a, uint64_t b, uint64_t c)
+    {
+    uint64_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+    }
+
 __device__ __forceinline__ float dot3(float x, float y, float z)
     {
     return fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z));
