@@ -5,10 +5,11 @@
 
 namespace gb
 {
-// Scratch layout: [0, 256) counter word; [256, ...) 3 doubles per block of the pair kernel.
+// Scratch layout: [0, 256) counter word; [256, ...) 3 doubles per block of the pair kernel. The
+// kernel may run up to 8 lanes per particle (small systems), so room for 8 N threads.
 inline size_t step_scratch_bytes(unsigned int N)
     {
-    return 256 + 3 * sizeof(double) * (size_t)div_up(N > 0 ? N : 1, 256);
+    return 256 + 3 * sizeof(double) * (size_t)div_up(8ull * (N > 0 ? N : 1), 256);
     }
 
 inline int make_fuse_args(const gb_pair_args* a, const gb_step_fuse* f, FuseArgs& fz)

@@ -332,7 +332,10 @@ template<class P> __host__ __device__ inline size_t i4_param_bytes(unsigned int 
     return multi ? ((sizeof(P) + 2 * sizeof(float)) * ntypes * ntypes + 15) / 16 * 16 : 0;
     }
 
-template<class Eval, bool MULTI, bool ORTHO, bool FUSE, bool VIRIAL, bool XPLOR>
+// TPP > 1 (small systems): TPP consecutive lanes share one particle, lane l taking the groups of
+// four neighbours b = l, l + TPP, ... (the reference's threads-per-particle split,
+// hoomd/md/PotentialPairGPU.cuh:140-404), and the partial sums meet by shuffles.
+template<class Eval, bool MULTI, bool ORTHO, bool FUSE, bool VIRIAL, bool XPLOR, int TPP = 1>
 __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
     k_pair_i4(float4* __restrict__ d_force, float* __restrict__ d_virial, size_t pitch,
               unsigned int N, const float4* __restrict__ d_pos, gb_box box,
@@ -371,7 +374,8 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             ro0 = d_ronsq[0];
         }
 
-    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned int i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
+    const unsigned int sub = threadIdx.x % TPP;
     const bool active = i < N;
     float fx = 0.f, fy = 0.f, fz_ = 0.f, pe = 0.f;
     float vxx = 0.f, vxy = 0.f, vxz = 0.f, vyy = 0.f, vyz = 0.f, vzz = 0.f;
@@ -464,12 +468,38 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
         const unsigned int rem = nn & 3u;
         const uint4* p4 = d_nlist4 + i;
         const uint4 self = make_uint4(i, i, i, i);
+        if (TPP > 1)
+            {
+            // groups sub, sub + TPP, ...; the partial last group belongs to lane nfull % TPP
+            for (unsigned int b = sub; b < nfull; b += TPP)
+                {
+                const uint4 jc = ld_stream_u4(p4 + (uint64_t)b * stride);
+                const float4 q0 = __ldg(d_pos + jc.x);
+                const float4 q1 = __ldg(d_pos + jc.y);
+                const float4 q2 = __ldg(d_pos + jc.z);
+                const float4 q3 = __ldg(d_pos + jc.w);
+                pair(q0, true);
+                pair(q1, true);
+                pair(q2, true);
+                pair(q3, true);
+                }
+            if (rem && sub == nfull % TPP)
+                {
+                const uint4 jc = ld_stream_u4(p4 + (uint64_t)nfull * stride);
+                const float4 q0 = __ldg(d_pos + jc.x);
+                const float4 q1 = __ldg(d_pos + (rem > 1 ? jc.y : i));
+                const float4 q2 = __ldg(d_pos + (rem > 2 ? jc.z : i));
+                pair(q0, true);
+                pair(q1, rem > 1);
+                pair(q2, rem > 2);
+                }
+            }
         uint4 jA = self, jB = self;
-        if (nfull > 0)
+        if (TPP == 1 && nfull > 0)
             jA = ld_stream_u4(p4);
-        if (nfull > 1)
+        if (TPP == 1 && nfull > 1)
             jB = ld_stream_u4(p4 + stride);
-        for (unsigned int b = 0; b < nfull; b++)
+        for (unsigned int b = 0; TPP == 1 && b < nfull; b++)
             {
             const uint4 jc = jA;
             jA = jB;
@@ -484,7 +514,7 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             pair(q2, true);
             pair(q3, true);
             }
-        if (rem)
+        if (TPP == 1 && rem)
             {
             const uint4 jc = ld_stream_u4(p4 + (uint64_t)nfull * stride);
             const float4 q0 = __ldg(d_pos + jc.x);
@@ -496,8 +526,24 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             }
         pe *= 0.5f;
         }
+    if (TPP > 1)
+        {
+        fx = group_sum<TPP>(fx);
+        fy = group_sum<TPP>(fy);
+        fz_ = group_sum<TPP>(fz_);
+        pe = group_sum<TPP>(pe);
+        if (VIRIAL)
+            {
+            vxx = group_sum<TPP>(vxx);
+            vxy = group_sum<TPP>(vxy);
+            vxz = group_sum<TPP>(vxz);
+            vyy = group_sum<TPP>(vyy);
+            vyz = group_sum<TPP>(vyz);
+            vzz = group_sum<TPP>(vzz);
+            }
+        }
     double ke_d = 0.0, pe_d = 0.0, w_d = 0.0;
-    if (active)
+    if (active && sub == 0)
         {
         d_force[i] = make_float4(fx, fy, fz_, pe);
         if (VIRIAL)
@@ -535,14 +581,14 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
         fuse_finish(fz, ke_d, pe_d, w_d);
     }
 
-template<class Eval, bool MULTI, bool ORTHO, bool FUSE, bool VIRIAL, bool XPLOR>
+template<class Eval, bool MULTI, bool ORTHO, bool FUSE, bool VIRIAL, bool XPLOR, int TPP = 1>
 int launch_pair_i4_inst(const gb_pair_args& a, const typename Eval::param_type* d_params,
                         const float* ext, const FuseArgs& fz, cudaStream_t s)
     {
     const unsigned int block = 256;
-    const unsigned int grid = div_up(a.N, block);
+    const unsigned int grid = div_up((unsigned long long)a.N * TPP, block);
     const size_t smem = i4_param_bytes<typename Eval::param_type>(a.ntypes, MULTI);
-    auto kern = k_pair_i4<Eval, MULTI, ORTHO, FUSE, VIRIAL, XPLOR>;
+    auto kern = k_pair_i4<Eval, MULTI, ORTHO, FUSE, VIRIAL, XPLOR, TPP>;
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<grid, block, smem, s>>>(reinterpret_cast<float4*>(a.d_force), a.d_virial,
@@ -558,6 +604,16 @@ int dispatch_pair_i4_vx(const gb_pair_args& a, const typename Eval::param_type* 
                         const float* ext, const FuseArgs& fz, cudaStream_t s)
     {
     const bool xplor = a.shift_mode == 2;
+    // threads per particle: explicit 1, 4 or 8, or by system size (enough lanes to fill the GPU)
+    unsigned int tpp = a.threads_per_particle;
+    if (tpp == 0)
+        tpp = a.N <= 16384 ? 8u : (a.N <= 65536 ? 4u : 1u);
+    if (!xplor && !a.compute_virial && ORTHO && tpp > 1)
+        {
+        if (tpp == 8)
+            return launch_pair_i4_inst<Eval, MULTI, ORTHO, FUSE, false, false, 8>(a, d_params, ext, fz, s);
+        return launch_pair_i4_inst<Eval, MULTI, ORTHO, FUSE, false, false, 4>(a, d_params, ext, fz, s);
+        }
     if (FUSE)
         {
         // the fused step never needs the virial
@@ -643,9 +699,11 @@ int launch_pair(const gb_pair_args* a, const typename Eval::param_type* d_params
     unsigned int tpp = a->threads_per_particle;
     if (!flat)
         {
-        GB_REQUIRE(tpp <= 1, "pair force: column-major lists use one thread per particle");
         GB_REQUIRE(a->interleave <= 1 || a->interleave == 4,
                    "pair force: interleave must be 1 or 4");
+        GB_REQUIRE(a->interleave == 4 ? (tpp <= 1 || tpp == 4 || tpp == 8) : tpp <= 1,
+                   "pair force: column-major lists take 1 thread per particle (interleave 1) or "
+                   "1, 4 or 8 (interleave 4)");
         if (a->interleave == 4)
             return dispatch_pair_i4<Eval, FUSE>(*a, d_params, ext, fz, s);
         return dispatch_pair_flags<Eval, 1, false, FUSE>(*a, d_params, ext, fz, block, s);

@@ -152,7 +152,9 @@ int gb_nlist_head_list(uint64_t* d_head_list, uint64_t* d_total, const float* d_
  * Pair forces. Replaces gpu_compute_pair_forces<Evaluator> (hoomd/md/PotentialPairGPU.cuh:
  * 44-98 pair_args_t, 140-404 kernel, 579-656 driver). shift_mode: 0 none, 1 shift, 2 xplor.
  * The evaluator parameter structs below are byte-for-byte the FP32 param_type of the reference
- * evaluators. threads_per_particle 0 picks the layout's default (1 for column-major lists).
+ * evaluators. threads_per_particle: flat head lists take 1-32 (0 = 8); plain column-major lists
+ * take 1; the interleaved list takes 1, 4 or 8 lanes per particle (0 = by N: 8 up to 16,384
+ * particles, 4 up to 65,536, else 1; virials and XPLOR use 1).
  * ------------------------------------------------------------------------------------------- */
 typedef struct gb_pair_args
     {

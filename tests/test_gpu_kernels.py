@@ -140,6 +140,24 @@ def test_lj_forces_vs_fp64_oracle(layout, tpp):
     assert_close_f64(v, vo, what="virial")
 
 
+@pytest.mark.parametrize("tpp", [1, 4, 8])
+@pytest.mark.parametrize("case", ["lj4096", "binary3000"])
+def test_interleaved_threads_per_particle_vs_fp64_oracle(tpp, case):
+    """Groups of 1, 4 or 8 lanes per particle on the interleaved list (no virial, so the split
+    kernel runs), single and two types."""
+    pos4, box6, rc, rb = NLIST_CASES[case]()
+    if case == "binary3000":
+        rc = np.array([[2.5, 2.0], [2.0, 2.2]])
+        par = np.array([[1.0, 1.0], [0.8, 1.5], [0.8, 1.5], [0.88, 0.5]])
+    else:
+        par = np.array([[1.0, 1.0]])
+    nl = GpuNlist(pos4, box6, rc, rb, layout="col4")
+    f, _ = gpu_pair_forces(nl, "lj", par, rc, virial=False, shift=1, tpp=tpp)
+    fo, _ = oracle_forces_f64(pos4, box6, "lj", par, rc, shift=1)
+    assert_close_f64(f[:, :3], fo[:, :3], what="force")
+    assert_close_f64(f[:, 3], fo[:, 3], what="energy")
+
+
 @pytest.mark.parametrize("layout", ["col", "col4"])
 @pytest.mark.parametrize("shift", [0, 1, 2])
 def test_lj_binary_shift_modes_vs_fp64_oracle(shift, layout):
