@@ -373,6 +373,59 @@ void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count
     a.ntypes = pd.ntypes;
     a.d_gate = d_gate;
     check(gb_nlist_build_binned(&a, s), "gb_nlist_build_binned");
+    if (ex_pitch > 0)
+        check(gb_nlist_filter(nlist.get(), n_neigh.get(), nullptr, stride, 4, pd.N, n_ex.get(),
+                              ex_list.get(), ex_pitch, d_gate, s),
+              "gb_nlist_filter");
+    }
+
+void NeighborList::set_exclusions(const std::vector<uint32_t>& tag_pairs)
+    {
+    if (tag_pairs.size() % 2)
+        throw std::invalid_argument("exclusions are (tag, tag) pairs");
+    for (uint32_t t : tag_pairs)
+        if (t >= pdata->N)
+            throw std::invalid_argument("exclusion refers to a tag >= N");
+    ex_tags = tag_pairs;
+    ex_dirty = true;
+    }
+
+// per-index exclusion rows from the tag pairs and the current tag -> index map
+void NeighborList::refresh_exclusions()
+    {
+    ParticleData& pd = *pdata;
+    if (!ex_dirty && ex_generation == pd.sort_generation)
+        return;
+    ex_dirty = false;
+    ex_generation = pd.sort_generation;
+    if (ex_tags.empty())
+        {
+        ex_pitch = 0;
+        return;
+        }
+    const std::vector<uint32_t> rtag = pd.rtag();
+    std::vector<std::vector<uint32_t>> rows(pd.N);
+    for (size_t k = 0; k < ex_tags.size(); k += 2)
+        {
+        const uint32_t a = rtag[ex_tags[k]], b = rtag[ex_tags[k + 1]];
+        rows[a].push_back(b);
+        rows[b].push_back(a);
+        }
+    unsigned int pitch = 1;
+    for (auto& r : rows)
+        pitch = std::max<unsigned int>(pitch, (unsigned int)r.size());
+    std::vector<uint32_t> cnt(pd.N), flat((size_t)pd.N * pitch, 0u);
+    for (unsigned int i = 0; i < pd.N; i++)
+        {
+        cnt[i] = (uint32_t)rows[i].size();
+        std::copy(rows[i].begin(), rows[i].end(), flat.begin() + (size_t)i * pitch);
+        }
+    ex_pitch = pitch;
+    n_ex.resize(pd.N);
+    ex_list.resize(flat.size());
+    n_ex.upload(cnt.data(), cnt.size(), pd.stream);
+    ex_list.upload(flat.data(), flat.size(), pd.stream);
+    cuda_check(cudaStreamSynchronize(pd.stream), "exclusions");
     }
 
 bool NeighborList::grow(const DevStatus& st)
@@ -413,6 +466,7 @@ void NeighborList::build_sync()
     ParticleData& pd = *pdata;
     if (!allocated || dirty)
         allocate();
+    refresh_exclusions();
     for (int attempt = 0; attempt < 64; attempt++)
         {
         cond.zero(pd.stream);
@@ -997,7 +1051,7 @@ void Integrator::run_chunk(unsigned int k)
         cuda_check(cudaMemsetAsync(ds->cell_cond, 0, sizeof(ds->cell_cond), s), "zero cond");
         cuda_check(cudaMemsetAsync(ds->nl_cond, 0, sizeof(ds->nl_cond), s), "zero cond");
         cuda_check(cudaMemsetAsync(&ds->status, 0, sizeof(uint32_t), s), "zero status");
-        const uint64_t cell_kernels = nlist->deterministic ? 3 : 2;
+        const uint64_t cell_kernels = (nlist->deterministic ? 3 : 2) + (nlist->ex_pitch ? 1 : 0);
         if (fused && use_graph)
             {
             cuda_check(cudaGraphLaunch(graph_for(k), s), "graph launch");

@@ -197,6 +197,15 @@ class NeighborList
     bool allocated = false;
     bool dirty = true; // r_cut or capacities changed: graphs must be rebuilt
     bool capacity_fixed = false; // start from exactly Nmax_cell / Nmax (tests of the growth path)
+    // exclusions (NeighborList::addExclusion / filterNlist): unordered tag pairs, and per
+    // particle index the excluded indices (rebuilt when a sort permutes the indices)
+    void set_exclusions(const std::vector<uint32_t>& tag_pairs);
+    void refresh_exclusions();
+    std::vector<uint32_t> ex_tags;
+    unsigned int ex_pitch = 0;
+    uint64_t ex_generation = ~0ull;
+    bool ex_dirty = false;
+    DeviceArray<uint32_t> n_ex, ex_list;
     DeviceArray<float> d_r_cut, d_r_listsq, d_rcut_max, xyzf, last_pos;
     DeviceArray<uint32_t> cell_size, cell_type, adj, n_neigh, d_Nmax, cond;
     // column-major, interleaved by 4: neighbour k of particle i at ((k/4)*stride + i)*4 + k%4

@@ -114,6 +114,12 @@ PYBIND11_MODULE(_hoomd_gb300, m)
     py::class_<NeighborList, std::shared_ptr<NeighborList>>(m, "NeighborListGPUBinned")
         .def(py::init<std::shared_ptr<ParticleData>, double>())
         .def("setRCut", &NeighborList::set_r_cut)
+        .def("setExclusions",
+             [](NeighborList& n, py::array_t<uint32_t, py::array::c_style | py::array::forcecast> p) {
+                 n.set_exclusions(std::vector<uint32_t>(p.data(), p.data() + p.size()));
+                 n.dirty = true;
+             })
+        .def_property_readonly("ex_pitch", [](NeighborList& n) { return n.ex_pitch; })
         .def_property(
             "deterministic", [](NeighborList& n) { return n.deterministic; },
             [](NeighborList& n, bool v) {

@@ -623,6 +623,45 @@ void launch_nlist_layout(const gb_nlist_args& a, unsigned int ncell, cudaStream_
         launch_nlist_mi<MULTI, 1>(a, ncell, s);
     }
 
+// Stable in-place removal of excluded neighbours (one thread per particle; hoomd's
+// gpu_nlist_filter_kernel does the same per particle).
+template<int LAYOUT>
+__global__ void k_nlist_filter(unsigned int* nlist, unsigned int* n_neigh,
+                               const uint64_t* __restrict__ head, uint64_t stride, unsigned int N,
+                               const unsigned int* __restrict__ n_ex,
+                               const unsigned int* __restrict__ ex_list, unsigned int ex_pitch,
+                               const uint32_t* gate)
+    {
+    if (gate && *gate == 0)
+        return;
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N)
+        return;
+    const unsigned int ne = n_ex[i];
+    if (ne == 0)
+        return;
+    auto at = [&](unsigned int k) -> size_t {
+        if (LAYOUT == 0)
+            return (size_t)head[i] + k;
+        if (LAYOUT == 1)
+            return (size_t)k * stride + i;
+        return ((size_t)(k >> 2) * stride + i) * 4 + (k & 3u);
+    };
+    const unsigned int* ex = ex_list + (size_t)i * ex_pitch;
+    const unsigned int nn = n_neigh[i];
+    unsigned int w = 0;
+    for (unsigned int k = 0; k < nn; k++)
+        {
+        const unsigned int j = nlist[at(k)];
+        bool drop = false;
+        for (unsigned int e = 0; e < ne; e++)
+            drop = drop || ex[e] == j;
+        if (!drop)
+            nlist[at(w++)] = j;
+        }
+    n_neigh[i] = w;
+    }
+
 __global__ void k_needs_update(uint32_t* result, const float4* __restrict__ last_pos,
                                const float4* __restrict__ pos, unsigned int N, gb_box box,
                                const float* __restrict__ rcut_max, float r_buff,
@@ -790,6 +829,33 @@ extern "C"
             reinterpret_cast<const float4*>(d_pos), N, *box, d_rcut_max, r_buff, lambda_min,
             make_float3(lambda[0], lambda[1], lambda[2]), checkn);
         return check_launch("gb_nlist_needs_update");
+        }
+
+    int gb_nlist_filter(unsigned int* d_nlist, unsigned int* d_n_neigh,
+                        const uint64_t* d_head_list, uint64_t stride, uint32_t interleave,
+                        unsigned int N, const unsigned int* d_n_ex, const unsigned int* d_ex_list,
+                        unsigned int ex_pitch, const uint32_t* d_gate, void* stream)
+        {
+        GB_REQUIRE(d_nlist && d_n_neigh && d_n_ex && d_ex_list, "gb_nlist_filter: null argument");
+        GB_REQUIRE(ex_pitch > 0, "gb_nlist_filter: ex_pitch must be positive");
+        if (N == 0)
+            return GB_OK;
+        cudaStream_t s = (cudaStream_t)stream;
+        const unsigned int grid = div_up(N, 256);
+        if (d_head_list)
+            k_nlist_filter<0><<<grid, 256, 0, s>>>(d_nlist, d_n_neigh, d_head_list, stride, N,
+                                                   d_n_ex, d_ex_list, ex_pitch, d_gate);
+        else
+            {
+            GB_REQUIRE(stride >= N, "gb_nlist_filter: column-major stride < N");
+            if (interleave == 4)
+                k_nlist_filter<4><<<grid, 256, 0, s>>>(d_nlist, d_n_neigh, nullptr, stride, N,
+                                                       d_n_ex, d_ex_list, ex_pitch, d_gate);
+            else
+                k_nlist_filter<1><<<grid, 256, 0, s>>>(d_nlist, d_n_neigh, nullptr, stride, N,
+                                                       d_n_ex, d_ex_list, ex_pitch, d_gate);
+            }
+        return check_launch("gb_nlist_filter");
         }
 
     int gb_nlist_head_list(uint64_t* d_head_list, uint64_t* d_total, const float* d_pos,

@@ -119,6 +119,8 @@ _PROTOS = {
     "gb_gather": (c_int, [c_void, c_void, c_void, c_uint, c_uint, c_void]),
     "gb_pair_forces_radial": (c_int, [c_void, c_void, c_void]),
     "gb_md_pair_step_radial": (c_int, [c_void, c_void, c_void, c_void]),
+    "gb_nlist_filter": (c_int, [c_void, c_void, c_void, c_u64, ctypes.c_uint32, c_uint, c_void,
+                                c_void, c_uint, c_void, c_void]),
     "gb_replica_scratch_bytes": (c_size, [ctypes.c_uint64]),
     "gb_replica_smem_bytes": (c_size, [ctypes.c_uint32, ctypes.c_uint32]),
     "gb_replica_ctas_per_sm": (c_int, [ctypes.c_uint32, ctypes.c_uint32]),

@@ -1,8 +1,60 @@
 """Neighbour lists (hoomd/md/nlist.py:87-420). ``Cell`` builds a binned full neighbour list on the
 GPU; parity with the reference is per-particle neighbour sets, bit for bit at FP32."""
 
+import numpy as np
+
 from hoomd_gb300._native import _hoomd_gb300
 from hoomd_gb300.md.data import TypePairDict, nonnegative_real
+
+
+def excluded_pairs(topology, exclusions, N):
+    """Unordered excluded tag pairs (M, 2), sorted and unique, from the snapshot topology
+    (hoomd/md/NeighborList.cc:560-760, the exclusion kinds documented in hoomd/md/nlist.py:55-73):
+    'bond', 'constraint', 'special_pair' the groups themselves, 'angle' the first and third
+    member, 'dihedral' the first and fourth, '1-3' / '1-4' particles two / three bonds apart."""
+    out = []
+
+    def add(a, b):
+        a, b = np.asarray(a, np.int64), np.asarray(b, np.int64)
+        m = a != b
+        out.append(np.stack([np.minimum(a[m], b[m]), np.maximum(a[m], b[m])], 1))
+
+    if 'body' in exclusions:
+        pass  # no rigid bodies in this state: nothing to exclude
+    bonds = topology["bonds"].group.astype(np.int64)
+    if 'bond' in exclusions and len(bonds):
+        add(bonds[:, 0], bonds[:, 1])
+    if 'constraint' in exclusions and topology["constraints"].N:
+        g = topology["constraints"].group
+        add(g[:, 0], g[:, 1])
+    if 'special_pair' in exclusions and topology["pairs"].N:
+        g = topology["pairs"].group
+        add(g[:, 0], g[:, 1])
+    if 'angle' in exclusions and topology["angles"].N:
+        g = topology["angles"].group
+        add(g[:, 0], g[:, 2])
+    if 'dihedral' in exclusions and topology["dihedrals"].N:
+        g = topology["dihedrals"].group
+        add(g[:, 0], g[:, 3])
+    if ('1-3' in exclusions or '1-4' in exclusions) and len(bonds):
+        nbr = [[] for _ in range(N)]
+        for a, b in bonds:
+            nbr[a].append(b)
+            nbr[b].append(a)
+        for i in range(N):
+            for j in nbr[i]:
+                for k in nbr[j]:
+                    if k == i:
+                        continue
+                    if '1-3' in exclusions:
+                        add([i], [k])
+                    if '1-4' in exclusions:
+                        for m in nbr[k]:
+                            if m != j and m != i:
+                                add([i], [m])
+    if not out:
+        return np.zeros((0, 2), np.uint32)
+    return np.unique(np.concatenate(out), axis=0).astype(np.uint32)
 
 
 class NeighborList:
@@ -27,6 +79,12 @@ class NeighborList:
         self.r_cut = TypePairDict(default=float(default_r_cut), validator=nonnegative_real)
         self._cpp_obj = None
         self._simulation = None
+        self._ex_version = -1
+
+    def _apply_exclusions(self, state):
+        pairs = excluded_pairs(state._topology, self.exclusions, state.N_particles)
+        self._cpp_obj.setExclusions(pairs)
+        self._ex_version = state._topology_version
 
     def _attach(self, simulation):
         if self._cpp_obj is not None and self._simulation is simulation:
@@ -40,6 +98,7 @@ class NeighborList:
                 if j >= i:
                     self._cpp_obj.setRCut(i, j, float(self.r_cut[(a, b)]))
         self._extra_attach()
+        self._apply_exclusions(state)
         return self._cpp_obj
 
     def _extra_attach(self):

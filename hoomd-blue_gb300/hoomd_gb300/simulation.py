@@ -121,6 +121,12 @@ class Simulation:
             if sorter is not None:
                 self._cpp_integrator.setSorter(sorter.trigger.period, sorter.grid_bits)
             self._needs_prep = True
+        for f in integ.forces:
+            nl = getattr(f, "nlist", None)
+            if nl is not None and nl._cpp_obj is not None and \
+                    nl._ex_version != self._state._topology_version:
+                nl._apply_exclusions(self._state)
+                self._needs_prep = True
         if getattr(self, "_needs_prep", False):
             self._cpp_integrator.prepRun()
             self._needs_prep = False

@@ -52,13 +52,44 @@ class _Particles:
         self._alloc(self._N)
 
 
+class _Group:
+    """A topology section (hoomd.Snapshot.bonds, angles, dihedrals, constraints, pairs): N groups
+    of ``size`` particle tags with a type id (constraints carry a value instead)."""
+
+    def __init__(self, size, typed=True):
+        self._size = size
+        self._typed = typed
+        self.types = []
+        self.N = 0
+
+    @property
+    def N(self):
+        return self._N
+
+    @N.setter
+    def N(self, n):
+        self._N = int(n)
+        self.group = np.zeros((self._N, self._size), np.uint32)
+        if self._typed:
+            self.typeid = np.zeros(self._N, np.uint32)
+        else:
+            self.value = np.zeros(self._N, np.float64)
+
+
 class Snapshot:
-    """hoomd.Snapshot with the particle fields the MD step uses."""
+    """hoomd.Snapshot with the particle fields the MD step uses and the topology sections that
+    the neighbour list's exclusions read."""
 
     def __init__(self, communicator=None):
         self.communicator = communicator or Communicator()
         self.configuration = _Configuration()
         self.particles = _Particles()
+        self.bonds = _Group(2)
+        self.angles = _Group(3)
+        self.dihedrals = _Group(4)
+        self.impropers = _Group(4)
+        self.constraints = _Group(2, typed=False)
+        self.pairs = _Group(2)
 
     def validate(self):
         p = self.particles
@@ -69,3 +100,9 @@ class Snapshot:
                 raise ValueError(f"snapshot.particles.{name} must have shape {shape}")
         if N and int(np.max(p.typeid)) >= len(p.types):
             raise ValueError("typeid refers to a type not in snapshot.particles.types")
+        for name in ("bonds", "angles", "dihedrals", "impropers", "constraints", "pairs"):
+            g = getattr(self, name)
+            if np.shape(g.group) != (g.N, g._size):
+                raise ValueError(f"snapshot.{name}.group must have shape {(g.N, g._size)}")
+            if g.N and int(np.max(g.group)) >= N:
+                raise ValueError(f"snapshot.{name}.group refers to a particle tag >= N")

@@ -1,5 +1,7 @@
 """System state (hoomd/state.py), held on the GPU by the engine's ParticleData."""
 
+import copy
+
 import numpy as np
 
 from hoomd_gb300._native import _hoomd_gb300
@@ -19,6 +21,8 @@ class State:
             [float(x) for x in snapshot.configuration.box], [1, 1, 1])
         self._cpp_pdata.seed = simulation.seed & 0xFFFF
         self._cpp_pdata.timestep = simulation._initial_timestep
+        self._topology = _copy_topology(snapshot)
+        self._topology_version = 0
         self._upload(snapshot)
 
     def _upload(self, snapshot):
@@ -62,6 +66,8 @@ class State:
         s.particles.mass[:] = d["mass"]
         s.particles.typeid[:] = d["typeid"]
         s.particles.image[:] = d["image"]
+        for name, g in self._topology.items():
+            setattr(s, name, copy.deepcopy(g))
         return s
 
     def set_snapshot(self, snapshot):
@@ -72,9 +78,24 @@ class State:
         if list(snapshot.configuration.box) != list(self._cpp_pdata.getBox()):
             raise RuntimeError("set_snapshot: box changes are not supported")
         snapshot.validate()
+        topology = _copy_topology(snapshot)
+        if not _same_topology(topology, self._topology):
+            self._topology = topology
+            self._topology_version += 1
         self._upload(snapshot)
 
     def thermalize_particle_momenta(self, filter, kT):
         """Gaussian velocities at kT with zero total momentum (hoomd/state.py:759)."""
         self._cpp_pdata.thermalize(float(kT), self._simulation.timestep)
         self._simulation._state_changed(velocities_only=True)
+
+
+_SECTIONS = ("bonds", "angles", "dihedrals", "impropers", "constraints", "pairs")
+
+
+def _copy_topology(snapshot):
+    return {name: copy.deepcopy(getattr(snapshot, name)) for name in _SECTIONS}
+
+
+def _same_topology(a, b):
+    return all(a[k].N == b[k].N and np.array_equal(a[k].group, b[k].group) for k in _SECTIONS)

@@ -133,6 +133,15 @@ typedef struct gb_nlist_args
 
 int gb_nlist_build_binned(const gb_nlist_args* args, void* stream);
 
+/* Exclusions. Replaces gpu_nlist_filter (hoomd/md/NeighborListGPU.cu:140-260): removes from each
+ * particle's list the indices in its exclusion row d_ex_list[i * ex_pitch + e], e < d_n_ex[i],
+ * keeping the order of the rest, and lowers d_n_neigh[i]. Same layouts as gb_nlist_build_binned
+ * (flat with d_head_list, column-major with stride and interleave 1 or 4). d_gate as above. */
+int gb_nlist_filter(unsigned int* d_nlist, unsigned int* d_n_neigh, const uint64_t* d_head_list,
+                    uint64_t stride, uint32_t interleave, unsigned int N,
+                    const unsigned int* d_n_ex, const unsigned int* d_ex_list,
+                    unsigned int ex_pitch, const uint32_t* d_gate, void* stream);
+
 /* Rebuild check. Replaces gpu_nlist_needs_update_check_new (hoomd/md/NeighborListGPU.cu:42-83):
  * sets *d_result = checkn when any particle moved at least (r_list*lambda_min - r_cut)/2 since
  * the last build. */
