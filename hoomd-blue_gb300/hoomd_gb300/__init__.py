@@ -25,10 +25,11 @@ from hoomd_gb300.snapshot import Snapshot  # noqa: E402
 from hoomd_gb300.simulation import Simulation  # noqa: E402
 from hoomd_gb300.state import State  # noqa: E402
 from hoomd_gb300 import md  # noqa: E402
+from hoomd_gb300 import gsd, logging, write  # noqa: E402
 from hoomd_gb300.ensemble import ReplicaEnsemble  # noqa: E402
 from hoomd_gb300 import surrogate  # noqa: E402
 
 __version__ = "0.1.0"
 
-__all__ = ["Box", "ReplicaEnsemble", "Snapshot", "Simulation", "State", "device", "filter", "md",
-           "surrogate", "trigger", "tune"]
+__all__ = ["Box", "ReplicaEnsemble", "Snapshot", "Simulation", "State", "device", "filter", "gsd",
+           "logging", "md", "surrogate", "trigger", "tune", "write"]

@@ -5,6 +5,11 @@ from hoomd_gb300.filter import All
 
 
 class ThermodynamicQuantities:
+    _loggables = {q: "scalar" for q in (
+        "kinetic_energy", "translational_kinetic_energy", "potential_energy",
+        "degrees_of_freedom", "translational_degrees_of_freedom", "kinetic_temperature",
+        "volume", "pressure")}
+
     def __init__(self, filter):
         if not isinstance(filter, All):
             raise NotImplementedError("thermodynamic quantities are computed over all particles")

@@ -58,6 +58,9 @@ def excluded_pairs(topology, exclusions, N):
 
 
 class NeighborList:
+    _loggables = {"num_builds": "scalar", "dimensions": "sequence",
+                  "allocated_particles_per_cell": "scalar"}
+
     def __init__(self, buffer, exclusions, rebuild_check_delay, check_dist, mesh, default_r_cut):
         exclusions = tuple(exclusions)
         bad = [e for e in exclusions if e not in ('bond', 'angle', 'constraint', 'dihedral',

@@ -21,6 +21,8 @@ class Pair:
 
     _accepted_modes = ("none", "shift", "xplor")
     _kind = None
+    _loggables = {"energy": "scalar", "energies": "particle", "forces": "particle",
+                  "virials": "particle"}
 
     def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
         self.r_cut = TypePairDict(default=None if default_r_cut is None else float(default_r_cut),

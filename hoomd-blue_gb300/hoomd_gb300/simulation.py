@@ -38,16 +38,26 @@ class Operations:
         from hoomd_gb300.tune import ParticleSorter
         if isinstance(op, ParticleSorter):
             self.tuners.append(op)
+        elif hasattr(op, "_write"):
+            self.writers.append(op)
+            return
         else:
             self.computes.append(op)
         self._simulation._detach_all()
 
 
 class Simulation:
+    _loggables = {"timestep": "scalar", "tps": "scalar", "walltime": "scalar",
+                  "final_timestep": "scalar", "initial_timestep": "scalar"}
+    _log_namespace = ("Simulation",)
+
     def __init__(self, device, seed=None):
         self.device = device
         self._seed = 0 if seed is None else int(seed)
         self._initial_timestep = 0
+        self._timestep_set = False
+        self._run_start = 0
+        self._run_end = 0
         self._state = None
         self.operations = Operations(self)
         self._cpp_integrator = None
@@ -78,7 +88,21 @@ class Simulation:
     def timestep(self, t):
         if self._state is not None:
             raise RuntimeError("timestep can only be set before the state is created")
-        self._initial_timestep = int(t)
+        t = int(t)
+        if not 0 <= t < 2 ** 64:
+            raise ValueError("timestep must be a non-negative 64-bit integer")
+        self._initial_timestep = t
+        self._timestep_set = True
+
+    @property
+    def initial_timestep(self):
+        """The timestep at the start of the last run."""
+        return self._run_start
+
+    @property
+    def final_timestep(self):
+        """The timestep at which the last (or current) run ends."""
+        return self._run_end
 
     @property
     def tps(self):
@@ -90,9 +114,32 @@ class Simulation:
         return self._walltime
 
     def create_state_from_snapshot(self, snapshot):
+        """Create the state from a ``Snapshot`` or a ``gsd.hoomd.Frame``
+        (hoomd/simulation.py:242-290)."""
         if self._state is not None:
             raise RuntimeError("Cannot initialize more than once")
+        if not isinstance(snapshot, Snapshot):
+            snapshot = Snapshot.from_gsd_frame(snapshot)
         self._state = State(self, snapshot)
+
+    def create_state_from_gsd(self, filename, frame=-1):
+        """Create the state from frame ``frame`` of a GSD file (negative values count from the
+        end) as hoomd/simulation.py:188-240 with GSDReader (hoomd/GSDReader.cc:40-90): when the
+        timestep was not set, it becomes the frame's ``configuration/step``."""
+        if self._state is not None:
+            raise RuntimeError("Cannot initialize more than once\n")
+        from hoomd_gb300.gsd import hoomd as gh
+        with gh.open(filename, "r") as traj:
+            n = len(traj)
+            i = n - abs(int(frame)) if frame < 0 and abs(int(frame)) <= n else abs(int(frame))
+            if i >= n:
+                raise RuntimeError(f"Cannot read frame {i} {filename} only has {n} frames.")
+            fr = traj[i]
+        if fr.particles.N == 0:
+            raise RuntimeError("Cannot read a file with 0 particles.")
+        if not self._timestep_set:
+            self._initial_timestep = int(fr.configuration.step)
+        self.create_state_from_snapshot(Snapshot.from_gsd_frame(fr))
 
     def _state_changed(self, velocities_only=False):
         # positions or velocities changed outside the engine: prepare again (rebuild the
@@ -134,19 +181,47 @@ class Simulation:
             op._simulation = self
         return self._cpp_integrator
 
+    def _advance(self, cpp, steps):
+        if cpp is None:
+            self._state._cpp_pdata.timestep = self.timestep + steps
+        else:
+            cpp.run(steps)
+
     def run(self, steps, write_at_start=False):
-        """Advance the simulation by ``steps`` timesteps (hoomd/simulation.py:485-562)."""
+        """Advance the simulation by ``steps`` timesteps (hoomd/simulation.py:485-562).
+
+        Writers run after each step whose new timestep their trigger selects, and at the
+        starting timestep too with ``write_at_start`` (System::run, hoomd/System.cc:80-190);
+        the steps between two writes run as one engine call."""
         if self._state is None:
             raise RuntimeError("Cannot run before state is set.")
         steps = int(steps)
         if steps < 0:
             raise ValueError("steps must be non-negative")
         cpp = self._attach()
+        writers = list(self.operations.writers)
+        for w in writers:
+            w._attach(self)
+        start = self.timestep
+        self._run_start = start
+        self._run_end = start + steps
         t0 = time.perf_counter()
-        if steps and cpp is None:
-            self._state._cpp_pdata.timestep = self.timestep + steps
-        elif steps:
-            cpp.run(steps)
+        if write_at_start:
+            for w in writers:
+                if w.trigger(start):
+                    w._write(start)
+        t = start
+        end = start + steps
+        while t < end:
+            nxt = min([w.trigger._next(t, end) for w in writers] + [end])
+            self._advance(cpp, nxt - t)
+            t = nxt
+            fire = [w for w in writers if w.trigger(t)]
+            if fire and cpp is not None:
+                cpp.synchronize()
+            for w in fire:
+                w._write(t)
+        if steps and cpp is not None:
             cpp.synchronize()
         dt = time.perf_counter() - t0
         self._walltime += dt

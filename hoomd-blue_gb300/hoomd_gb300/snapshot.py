@@ -41,6 +41,13 @@ class _Particles:
         self.typeid = np.zeros(N, np.uint32)
         self.mass = np.ones(N, np.float64)
         self.image = np.zeros((N, 3), np.int32)
+        # carried with the particles (GSD files, snapshots) but not used by the pair step
+        self.charge = np.zeros(N, np.float64)
+        self.diameter = np.ones(N, np.float64)
+        self.body = np.full(N, -1, np.int32)
+        self.moment_inertia = np.zeros((N, 3), np.float64)
+        self.orientation = np.tile(np.array([1.0, 0.0, 0.0, 0.0]), (N, 1))
+        self.angmom = np.zeros((N, 4), np.float64)
 
     @property
     def N(self):
@@ -76,8 +83,14 @@ class _Group:
             self.value = np.zeros(self._N, np.float64)
 
 
+PARTICLE_FIELDS = (("position", 3), ("velocity", 3), ("typeid", 1), ("mass", 1), ("image", 3),
+                   ("charge", 1), ("diameter", 1), ("body", 1), ("moment_inertia", 3),
+                   ("orientation", 4), ("angmom", 4))
+TOPOLOGY_SECTIONS = ("bonds", "angles", "dihedrals", "impropers", "constraints", "pairs")
+
+
 class Snapshot:
-    """hoomd.Snapshot with the particle fields the MD step uses and the topology sections that
+    """hoomd.Snapshot: the particle fields of the hoomd schema and the topology sections that
     the neighbour list's exclusions read."""
 
     def __init__(self, communicator=None):
@@ -94,15 +107,47 @@ class Snapshot:
     def validate(self):
         p = self.particles
         N = p.N
-        for name, shape in (("position", (N, 3)), ("velocity", (N, 3)), ("typeid", (N,)),
-                            ("mass", (N,)), ("image", (N, 3))):
+        for name, m in PARTICLE_FIELDS:
+            shape = (N,) if m == 1 else (N, m)
             if np.shape(getattr(p, name)) != shape:
                 raise ValueError(f"snapshot.particles.{name} must have shape {shape}")
         if N and int(np.max(p.typeid)) >= len(p.types):
             raise ValueError("typeid refers to a type not in snapshot.particles.types")
-        for name in ("bonds", "angles", "dihedrals", "impropers", "constraints", "pairs"):
+        for name in TOPOLOGY_SECTIONS:
             g = getattr(self, name)
             if np.shape(g.group) != (g.N, g._size):
                 raise ValueError(f"snapshot.{name}.group must have shape {(g.N, g._size)}")
             if g.N and int(np.max(g.group)) >= N:
                 raise ValueError(f"snapshot.{name}.group refers to a particle tag >= N")
+
+    @classmethod
+    def from_gsd_frame(cls, gsd_snap, communicator=None):
+        """A snapshot from a ``gsd.hoomd.Frame`` (hoomd/snapshot.py:465-520): quantities the
+        frame leaves unset keep the snapshot defaults."""
+        gsd_snap.validate()
+        snap = cls(communicator)
+        c = gsd_snap.configuration
+        snap.configuration.box = [float(x) for x in c.box]
+        gp = gsd_snap.particles
+        snap.particles.N = int(gp.N)
+        if gp.types is not None:
+            snap.particles.types = list(gp.types)
+        for name, _ in PARTICLE_FIELDS:
+            v = getattr(gp, name, None)
+            if v is not None:
+                getattr(snap.particles, name)[:] = v
+        for name in TOPOLOGY_SECTIONS:
+            src = getattr(gsd_snap, name, None)
+            if src is None:
+                continue
+            dst = getattr(snap, name)
+            dst.N = int(src.N)
+            if dst._typed:
+                dst.types = list(src.types or [])
+                if src.typeid is not None:
+                    dst.typeid[:] = src.typeid
+            elif src.value is not None:
+                dst.value[:] = src.value
+            if src.group is not None:
+                dst.group[:] = src.group
+        return snap

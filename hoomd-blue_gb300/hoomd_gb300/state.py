@@ -23,6 +23,7 @@ class State:
         self._cpp_pdata.timestep = simulation._initial_timestep
         self._topology = _copy_topology(snapshot)
         self._topology_version = 0
+        self._passive = _copy_passive(snapshot)
         self._upload(snapshot)
 
     def _upload(self, snapshot):
@@ -66,6 +67,8 @@ class State:
         s.particles.mass[:] = d["mass"]
         s.particles.typeid[:] = d["typeid"]
         s.particles.image[:] = d["image"]
+        for name, v in self._passive.items():
+            getattr(s.particles, name)[:] = v
         for name, g in self._topology.items():
             setattr(s, name, copy.deepcopy(g))
         return s
@@ -82,6 +85,7 @@ class State:
         if not _same_topology(topology, self._topology):
             self._topology = topology
             self._topology_version += 1
+        self._passive = _copy_passive(snapshot)
         self._upload(snapshot)
 
     def thermalize_particle_momenta(self, filter, kT):
@@ -91,6 +95,12 @@ class State:
 
 
 _SECTIONS = ("bonds", "angles", "dihedrals", "impropers", "constraints", "pairs")
+# per-particle quantities the MD step does not change: kept on the host in tag order
+_PASSIVE = ("charge", "diameter", "body", "moment_inertia", "orientation", "angmom")
+
+
+def _copy_passive(snapshot):
+    return {name: np.array(getattr(snapshot.particles, name), copy=True) for name in _PASSIVE}
 
 
 def _copy_topology(snapshot):

@@ -15,6 +15,8 @@ Workflow::
     lj = md.pair.TableSurrogate(nlist=cell, surrogate=sur)
 """
 
+import os
+
 import numpy as np
 
 from hoomd_gb300._native import _hoomd_gb300 as _cpp
@@ -80,10 +82,13 @@ class Surrogate:
 
     def sample_pairs(self, frames, anchors=20000, seed=0):
         """Training samples from trajectory frames: ``frames`` is a list of (positions (N, 3),
-        typeid (N,), box lengths (3,)) of a cubic or orthorhombic periodic box. For ``anchors``
+        typeid (N,), box lengths (3,)) of a cubic or orthorhombic periodic box, or the name of a
+        GSD trajectory (every frame, through ``gsd_frames``). For ``anchors``
         random particles per frame, every neighbour within [r_min, r_cut) gives one sample
         (pair index, r, U, F) with the Table's values as targets."""
         from scipy.spatial import cKDTree
+        if isinstance(frames, (str, os.PathLike)):
+            frames = gsd_frames(frames)
         rng = np.random.default_rng(seed)
         P, R = [], []
         for pos, typeid, L in frames:
@@ -139,3 +144,18 @@ class Surrogate:
         sur = cls(int(d["ntypes"]), float(d["r_min"]), float(d["r_cut"]))
         sur.params = d["theta"]
         return sur
+
+
+def gsd_frames(filename, start=0, stop=None, step=1):
+    """(positions, typeid, box lengths) of frames of a ``hoomd``-schema GSD trajectory (as written
+    by hoomd.write.GSD), the input of ``Surrogate.sample_pairs``."""
+    from hoomd_gb300.gsd import hoomd as gh
+    out = []
+    with gh.open(filename, "r") as traj:
+        for fr in traj[start:stop:step]:
+            box = np.asarray(fr.configuration.box, np.float64)
+            if np.any(box[3:] != 0):
+                raise ValueError("training frames need an orthorhombic box")
+            out.append((np.asarray(fr.particles.position, np.float64),
+                        np.asarray(fr.particles.typeid, np.int64), box[:3]))
+    return out

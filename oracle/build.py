@@ -6,7 +6,10 @@
   (``hoomd/HOOMDMath.h``, ``hoomd/BoxDim.h``, ``hoomd/md/EvaluatorPairLJ.h``,
   ``hoomd/md/EvaluatorPairTable.h``, ``example_plugins/pair_plugin/EvaluatorPairExample.h``), read
   in place from the reference source tree, into ``oracle/_ref/libhoomd_ref_eval_f{32,64}.so``. It
-  runs only where that tree and pybind11/Python headers exist; elsewhere it does nothing. The rest
+  runs only where that tree and pybind11/Python headers exist; elsewhere it does nothing.
+* ``build_gsd_ref()`` compiles the reference's own GSD library ``hoomd/extern/gsd.c`` (a
+  self-contained C file, read in place) with the flat ctypes shim ``oracle/gsd_ref_shim.c`` into
+  ``oracle/_ref/libgsd_ref.so``, where the reference tree exists. The rest
   of the reference (cell list, neighbour list, pair loop, integrator) cannot be compiled in
   isolation: it needs the absent git submodules (nano-signal-slot, random123, ...) and Eigen3.
 
@@ -95,8 +98,30 @@ def build_ref(verbose=False):
     return outs
 
 
+GSD_SHIM_SRC = HERE / "gsd_ref_shim.c"
+GSD_REF_LIB = REF_DIR / "libgsd_ref.so"
+
+
+def build_gsd_ref(verbose=False):
+    """Compile hoomd/extern/gsd.c with the ctypes shim, when the reference tree is present."""
+    src = REF_ROOT / "hoomd" / "extern" / "gsd.c"
+    if not src.exists():
+        return None
+    REF_DIR.mkdir(parents=True, exist_ok=True)
+    if not _stale(GSD_REF_LIB, [GSD_SHIM_SRC]):
+        return GSD_REF_LIB
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11",
+           f"-I{REF_ROOT / 'hoomd' / 'extern'}", str(GSD_SHIM_SRC), str(src), "-o",
+           str(GSD_REF_LIB)]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    return GSD_REF_LIB
+
+
 if __name__ == "__main__":
     build_oracle(verbose=True)
     r = build_ref(verbose=True)
-    print("oracle:", ORACLE_LIB, "reference shim:", r)
+    g = build_gsd_ref(verbose=True)
+    print("oracle:", ORACLE_LIB, "reference shim:", r, "reference gsd:", g)
     sys.exit(0)
