@@ -797,8 +797,33 @@ void Integrator::set_thermostat_bussi(double kT_, double tau_)
 void Integrator::set_thermostat_none()
     {
     bussi = false;
+    langevin = false;
     prepared = false;
     drop_graphs();
+    }
+
+void Integrator::set_langevin(double kT_, const std::vector<double>& gamma_, bool tally_)
+    {
+    if (gamma_.size() != pdata->ntypes)
+        throw std::invalid_argument("Langevin: one drag coefficient per particle type");
+    bussi = false;
+    langevin = true;
+    tally = tally_;
+    langevin_kT = kT_;
+    gamma.assign(gamma_.begin(), gamma_.end());
+    d_gamma.resize(gamma.size());
+    cuda_check(cudaMemcpy(d_gamma.get(), gamma.data(), sizeof(float) * gamma.size(),
+                          cudaMemcpyHostToDevice),
+               "gamma");
+    prepared = false;
+    drop_graphs();
+    }
+
+double Integrator::reservoir_energy()
+    {
+    if (!prepared)
+        return reservoir;
+    return read_status().reservoir;
     }
 
 // Bussi draws for the next k timesteps, in parallel, ahead of a run of fused steps.
@@ -819,6 +844,9 @@ void Integrator::set_sorter(uint64_t period, int bits)
 // (hoomd/md/IntegratorTwoStep.cc:154-199): D*N - D.
 double Integrator::dof() const
     {
+    // Langevin does not conserve momentum (TwoStepLangevinBase::isMomentumConserving): D*N
+    if (langevin)
+        return double(pdata->ndim) * pdata->N;
     return double(pdata->ndim) * pdata->N - double(pdata->ndim);
     }
 
@@ -882,6 +910,7 @@ void Integrator::prepare()
     st.timestep = pd.timestep;
     st.n_builds = nlist->n_builds_host;
     st.factor = 1.0;
+    st.reservoir = reservoir;
     cuda_check(cudaMemcpyAsync(d_status.get(), &st, sizeof(st), cudaMemcpyHostToDevice, s),
                "status");
     DevStatus* ds = d_status.get();
@@ -898,10 +927,10 @@ void Integrator::prepare()
     prepared = true;
     }
 
-void Integrator::enqueue_step_fused(cudaStream_t s)
+// Arguments of step one (with the rebuild check) for the current method.
+gb_step_one_args Integrator::step_one_args(DevStatus* ds) const
     {
     ParticleData& pd = *pdata;
-    DevStatus* ds = d_status.get();
     gb_step_one_args o {};
     o.d_pos = pd.pos.get();
     o.d_vel = pd.vel.get();
@@ -916,10 +945,14 @@ void Integrator::enqueue_step_fused(cudaStream_t s)
     o.d_rcut_max = nlist->d_rcut_max.get();
     o.r_buff = nlist->r_buff;
     o.d_rebuild = &ds->rebuild;
-    check(gb_md_step_one(&o, s), "gb_md_step_one");
-    nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
-    PairForce& f = *forces[0];
-    gb_pair_args a = f.pair_args(false);
+    o.nve_order = langevin ? 1 : 0;
+    return o;
+    }
+
+// Arguments of the fused pair kernel's step two for the current method.
+gb_step_fuse Integrator::fuse_args(DevStatus* ds) const
+    {
+    ParticleData& pd = *pdata;
     gb_step_fuse fu {};
     fu.d_vel = pd.vel.get();
     fu.d_accel = pd.accel.get();
@@ -942,6 +975,29 @@ void Integrator::enqueue_step_fused(cudaStream_t s)
         fu.d_bussi_ring = d_bussi_ring.get();
         fu.bussi_ring_size = BUSSI_RING;
         }
+    if (langevin)
+        {
+        fu.langevin = 1;
+        fu.d_tag = pd.tag.get();
+        fu.d_pos = pd.pos.get();
+        fu.d_gamma = d_gamma.get();
+        fu.langevin_kT = (float)langevin_kT;
+        fu.ndim = pd.ndim;
+        fu.d_reservoir = tally ? &ds->reservoir : nullptr;
+        }
+    return fu;
+    }
+
+void Integrator::enqueue_step_fused(cudaStream_t s)
+    {
+    ParticleData& pd = *pdata;
+    DevStatus* ds = d_status.get();
+    const gb_step_one_args o = step_one_args(ds);
+    check(gb_md_step_one(&o, s), "gb_md_step_one");
+    nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
+    PairForce& f = *forces[0];
+    gb_pair_args a = f.pair_args(false);
+    const gb_step_fuse fu = fuse_args(ds);
     check(f.launch_fused(a, fu, s), "fused pair step");
     }
 
@@ -949,20 +1005,7 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
     {
     ParticleData& pd = *pdata;
     DevStatus* ds = d_status.get();
-    gb_step_one_args o {};
-    o.d_pos = pd.pos.get();
-    o.d_vel = pd.vel.get();
-    o.d_accel = pd.accel.get();
-    o.d_image = pd.image.get();
-    o.N = pd.N;
-    o.box = pd.box;
-    o.dt = (float)dt;
-    o.scale = 1.0f;
-    o.d_scale = bussi ? &ds->factor : nullptr;
-    o.d_last_pos = nlist->last_pos.get();
-    o.d_rcut_max = nlist->d_rcut_max.get();
-    o.r_buff = nlist->r_buff;
-    o.d_rebuild = &ds->rebuild;
+    const gb_step_one_args o = step_one_args(ds);
     check(gb_md_step_one(&o, s), "gb_md_step_one");
     nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
     for (auto& f : forces)
@@ -977,11 +1020,23 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
               "gb_sum_net_force");
         net = net_force.get();
         }
-    check(gb_cv_step_two(pd.vel.get(), pd.accel.get(), net, pd.N, (float)dt, 1.0f, nullptr, s),
-          "gb_cv_step_two");
-    check(gb_thermo_reduce(pd.vel.get(), net, nullptr, 0, pd.N, d_thermo_scratch.get(),
-                           ds->thermo, s),
-          "thermo");
+    if (langevin)
+        {
+        check(gb_langevin_step_two(pd.vel.get(), pd.accel.get(), net, pd.pos.get(), pd.tag.get(),
+                                   d_gamma.get(), pd.N, (float)dt, (float)langevin_kT, pd.ndim,
+                                   pd.seed, &ds->timestep, d_step_scratch.get(), ds->thermo,
+                                   tally ? &ds->reservoir : nullptr, s),
+              "gb_langevin_step_two");
+        }
+    else
+        {
+        check(gb_cv_step_two(pd.vel.get(), pd.accel.get(), net, pd.N, (float)dt, 1.0f, nullptr,
+                             s),
+              "gb_cv_step_two");
+        check(gb_thermo_reduce(pd.vel.get(), net, nullptr, 0, pd.N, d_thermo_scratch.get(),
+                               ds->thermo, s),
+              "thermo");
+        }
     if (bussi)
         check(gb_bussi_factor(&ds->thermo[0], dof(), dt, tau, kT, step + 1, pd.seed, 0u,
                               &ds->factor, s),
@@ -1073,7 +1128,7 @@ void Integrator::run_chunk(unsigned int k)
                 enqueue_step_general(s, pd.timestep + i);
             launch_count += (uint64_t)k
                             * (1 + cell_kernels + 1 + forces.size() + (forces.size() > 1 ? 1 : 0)
-                               + 2 + (bussi ? 1 : 0));
+                               + (langevin ? 1 : 2) + (bussi ? 1 : 0));
             }
         DevStatus st = read_status();
         if (st.cell_cond[1])
@@ -1095,6 +1150,7 @@ void Integrator::run_chunk(unsigned int k)
             }
         if (st.status & 1u)
             throw std::runtime_error("Bussi thermostat requires non-zero initial momenta.");
+        reservoir = st.reservoir;
         pd.timestep += k;
         steps_run += k;
         if (!fused)
@@ -1209,20 +1265,7 @@ std::vector<double> Integrator::time_phases(unsigned int reps)
     DevStatus* ds = d_status.get();
     for (unsigned int r = 0; r < reps; r++)
         {
-        gb_step_one_args o {};
-        o.d_pos = pd.pos.get();
-        o.d_vel = pd.vel.get();
-        o.d_accel = pd.accel.get();
-        o.d_image = pd.image.get();
-        o.N = pd.N;
-        o.box = pd.box;
-        o.dt = (float)dt;
-        o.scale = 1.0f;
-        o.d_scale = bussi ? &ds->factor : nullptr;
-        o.d_last_pos = nlist->last_pos.get();
-        o.d_rcut_max = nlist->d_rcut_max.get();
-        o.r_buff = nlist->r_buff;
-        o.d_rebuild = &ds->rebuild;
+        const gb_step_one_args o = step_one_args(ds);
         cuda_check(cudaEventRecord(ev[0], s), "record");
         check(gb_md_step_one(&o, s), "gb_md_step_one");
         cuda_check(cudaEventRecord(ev[1], s), "record");
@@ -1241,27 +1284,9 @@ std::vector<double> Integrator::time_phases(unsigned int reps)
         cudaEventElapsedTime(&t23, ev[2], ev[3]);
         PairForce& f = *forces[0];
         gb_pair_args a = f.pair_args(false);
-        gb_step_fuse fu {};
-        fu.d_vel = pd.vel.get();
-        fu.d_accel = pd.accel.get();
-        fu.dt = (float)dt;
-        fu.d_scratch = d_step_scratch.get();
-        fu.d_thermo = ds->thermo;
-        fu.bussi = bussi ? 1 : 0;
-        fu.dof = dof();
-        fu.tau = tau;
-        fu.kT = kT;
-        fu.seed = pd.seed;
-        fu.d_timestep = &ds->timestep;
-        fu.d_factor = &ds->factor;
-        fu.d_status = &ds->status;
-        fu.d_rebuild_reset = &ds->rebuild;
+        const gb_step_fuse fu = fuse_args(ds);
         if (bussi)
-            {
             enqueue_bussi_draws(*this, ds, d_bussi_ring.get(), BUSSI_RING, 1, s);
-            fu.d_bussi_ring = d_bussi_ring.get();
-            fu.bussi_ring_size = BUSSI_RING;
-            }
         cuda_check(cudaEventRecord(ev[0], s), "record");
         if (f.kind == PairKind::MLP)
             {

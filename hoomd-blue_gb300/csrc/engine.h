@@ -131,6 +131,7 @@ struct DevStatus
     uint64_t n_builds;
     double factor;         // Bussi rescale factor for the next step one
     double thermo[3];      // KE, PE, W after the last step
+    double reservoir;      // Langevin reservoir energy (tally_reservoir_energy)
     uint32_t nl_cond[64];  // per-type neighbours needed on overflow
     };
 
@@ -268,6 +269,9 @@ class Integrator
     void add_force(std::shared_ptr<PairForce> f);
     void set_thermostat_bussi(double kT, double tau);
     void set_thermostat_none();
+    // TwoStepLangevin (translational part): per-type drag coefficients, constant kT
+    void set_langevin(double kT, const std::vector<double>& gamma, bool tally);
+    double reservoir_energy();
     void set_sorter(uint64_t period, int grid_bits);
     void set_chunk(unsigned int steps)
         {
@@ -285,6 +289,10 @@ class Integrator
     double dt;
     bool bussi = false;
     double kT = 1.0, tau = 0.0;
+    bool langevin = false, tally = false;
+    double langevin_kT = 1.0;
+    std::vector<float> gamma;
+    double reservoir = 0.0; // host copy, carried across prepare()
     uint64_t sort_period = 0;
     int sort_bits = 8;
     unsigned int chunk = 50;
@@ -306,6 +314,8 @@ class Integrator
 
     private:
     void sort_particles();
+    gb_step_one_args step_one_args(DevStatus* ds) const;
+    gb_step_fuse fuse_args(DevStatus* ds) const;
     void enqueue_step_fused(cudaStream_t s);
     void enqueue_step_general(cudaStream_t s, uint64_t step);
     void run_chunk(unsigned int k);
@@ -318,7 +328,7 @@ class Integrator
     DeviceArray<char> d_step_scratch, d_thermo_scratch;
     static constexpr unsigned int BUSSI_RING = 1024; // >= the longest chunk
     DeviceArray<double> d_bussi_ring;                // (normal, 2*gamma) per timestep % RING
-    DeviceArray<float> net_force;
+    DeviceArray<float> net_force, d_gamma;
     DeviceArray<float> ck_pos, ck_vel, ck_accel;
     DeviceArray<int32_t> ck_image;
     DeviceArray<DevStatus> ck_status;

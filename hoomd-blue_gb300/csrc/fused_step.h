@@ -42,6 +42,20 @@ inline int make_fuse_args(const gb_pair_args* a, const gb_step_fuse* f, FuseArgs
     GB_REQUIRE(!f->d_bussi_ring || f->bussi_ring_size > 0, "fused step: empty Bussi ring");
     fz.d_ring = reinterpret_cast<const double2*>(f->d_bussi_ring);
     fz.ring_size = f->bussi_ring_size;
+    fz.langevin = f->langevin;
+    if (f->langevin)
+        {
+        GB_REQUIRE(!f->bussi && !f->d_scale2, "fused step: Langevin excludes rescaling");
+        GB_REQUIRE(f->d_tag && f->d_pos && f->d_gamma && f->d_timestep,
+                   "fused step: Langevin needs tags, positions, drag coefficients and the "
+                   "timestep");
+        }
+    fz.tag = f->d_tag;
+    fz.pos = reinterpret_cast<const float4*>(f->d_pos);
+    fz.gamma = f->d_gamma;
+    fz.lkT = f->langevin_kT;
+    fz.ndim = f->ndim ? f->ndim : 3u;
+    fz.d_reservoir = f->d_reservoir;
     return GB_OK;
     }
 } // namespace gb

@@ -22,7 +22,7 @@ struct StepOneCheck
     uint32_t* rebuild;
     };
 
-template<bool CHECK>
+template<bool CHECK, bool NVE>
 __global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
                            const float* __restrict__ accel, int* __restrict__ image,
                            unsigned int N, gb_box box, float dt, float scale,
@@ -32,21 +32,35 @@ __global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
     bool moved = false;
     if (j < N)
         {
-        const float s = d_scale ? (float)*d_scale : scale;
+        const float s = (!NVE && d_scale) ? (float)*d_scale : scale;
         float4 v = vel[j];
         float4 p = pos[j];
         const float ax = accel[3 * (size_t)j], ay = accel[3 * (size_t)j + 1],
                     az = accel[3 * (size_t)j + 2];
-        // v = v + (1/2) a dt ; v *= s ; x += dt v   (TwoStepConstantVolume.cc:37-55)
-        v.x = fadd(v.x, fmul(fmul(0.5f, ax), dt));
-        v.y = fadd(v.y, fmul(fmul(0.5f, ay), dt));
-        v.z = fadd(v.z, fmul(fmul(0.5f, az), dt));
-        v.x = fmul(v.x, s);
-        v.y = fmul(v.y, s);
-        v.z = fmul(v.z, s);
-        p.x = fadd(p.x, fmul(dt, v.x));
-        p.y = fadd(p.y, fmul(dt, v.y));
-        p.z = fadd(p.z, fmul(dt, v.z));
+        if (NVE)
+            {
+            // x += v dt + (1/2) a dt^2 ; v += (1/2) a dt   (TwoStepNVEGPU.cu:68-98,
+            // TwoStepLangevin.cc:57-81)
+            p.x = fadd(p.x, fadd(fmul(v.x, dt), fmul(fmul(fmul(0.5f, ax), dt), dt)));
+            p.y = fadd(p.y, fadd(fmul(v.y, dt), fmul(fmul(fmul(0.5f, ay), dt), dt)));
+            p.z = fadd(p.z, fadd(fmul(v.z, dt), fmul(fmul(fmul(0.5f, az), dt), dt)));
+            v.x = fadd(v.x, fmul(fmul(0.5f, ax), dt));
+            v.y = fadd(v.y, fmul(fmul(0.5f, ay), dt));
+            v.z = fadd(v.z, fmul(fmul(0.5f, az), dt));
+            }
+        else
+            {
+            // v = v + (1/2) a dt ; v *= s ; x += dt v   (TwoStepConstantVolume.cc:37-55)
+            v.x = fadd(v.x, fmul(fmul(0.5f, ax), dt));
+            v.y = fadd(v.y, fmul(fmul(0.5f, ay), dt));
+            v.z = fadd(v.z, fmul(fmul(0.5f, az), dt));
+            v.x = fmul(v.x, s);
+            v.y = fmul(v.y, s);
+            v.z = fmul(v.z, s);
+            p.x = fadd(p.x, fmul(dt, v.x));
+            p.y = fadd(p.y, fmul(dt, v.y));
+            p.z = fadd(p.z, fmul(dt, v.z));
+            }
         int ix = 0, iy = 0, iz = 0;
         wrap(box, p.x, p.y, p.z, ix, iy, iz);
         if (ix | iy | iz)
@@ -246,6 +260,19 @@ __global__ void k_thermalize_shift(float4* __restrict__ vel, unsigned int N, uns
         v.z = v.z - cz / v.w;
     vel[j] = v;
     }
+// Langevin step two from the net force, with the step's FP64 sums (last block).
+__global__ void k_langevin_two(FuseArgs fz, const float4* __restrict__ net, unsigned int N)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double ke = 0.0, pe = 0.0, w = 0.0;
+    if (j < N)
+        {
+        const float4 f = net[j];
+        fuse_step_two(fz, j, f.x, f.y, f.z, f.w, ke, pe, w);
+        }
+    fuse_finish(fz, ke, pe, w);
+    }
+
 struct ForcePtrs
     {
     const float4* f[8];
@@ -284,7 +311,7 @@ extern "C"
         if (N == 0)
             return GB_OK;
         StepOneCheck none {nullptr, nullptr, 0.0f, nullptr};
-        k_step_one<false><<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
+        k_step_one<false, false><<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
             reinterpret_cast<float4*>(d_pos), reinterpret_cast<float4*>(d_vel), d_accel, d_image,
             N, *box, dt, scale, d_scale, none);
         return check_launch("gb_cv_step_one");
@@ -302,14 +329,12 @@ extern "C"
         StepOneCheck chk {reinterpret_cast<const float4*>(a->d_last_pos), a->d_rcut_max,
                           a->r_buff, a->d_rebuild};
         cudaStream_t s = (cudaStream_t)stream;
-        if (a->d_last_pos)
-            k_step_one<true><<<div_up(a->N, 256), 256, 0, s>>>(
-                reinterpret_cast<float4*>(a->d_pos), reinterpret_cast<float4*>(a->d_vel),
-                a->d_accel, a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk);
-        else
-            k_step_one<false><<<div_up(a->N, 256), 256, 0, s>>>(
-                reinterpret_cast<float4*>(a->d_pos), reinterpret_cast<float4*>(a->d_vel),
-                a->d_accel, a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk);
+        auto kern = a->d_last_pos ? (a->nve_order ? k_step_one<true, true> : k_step_one<true, false>)
+                                  : (a->nve_order ? k_step_one<false, true>
+                                                  : k_step_one<false, false>);
+        kern<<<div_up(a->N, 256), 256, 0, s>>>(
+            reinterpret_cast<float4*>(a->d_pos), reinterpret_cast<float4*>(a->d_vel), a->d_accel,
+            a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk);
         return check_launch("gb_md_step_one");
         }
 
@@ -323,6 +348,37 @@ extern "C"
             reinterpret_cast<float4*>(d_vel), d_accel, reinterpret_cast<const float4*>(d_net_force),
             N, dt, scale, d_scale);
         return check_launch("gb_cv_step_two");
+        }
+
+    int gb_langevin_step_two(float* d_vel, float* d_accel, const float* d_net_force,
+                             const float* d_pos, const uint32_t* d_tag, const float* d_gamma,
+                             unsigned int N, float dt, float kT, uint32_t ndim, uint16_t seed,
+                             uint64_t* d_timestep, void* d_scratch, double* d_thermo,
+                             double* d_reservoir, void* stream)
+        {
+        GB_REQUIRE(d_timestep && d_scratch && d_thermo, "gb_langevin_step_two: null argument");
+        GB_REQUIRE(N == 0 || (d_vel && d_accel && d_net_force && d_pos && d_tag && d_gamma),
+                   "gb_langevin_step_two: null particle array");
+        FuseArgs fz {};
+        fz.vel = reinterpret_cast<float4*>(d_vel);
+        fz.accel = d_accel;
+        fz.dt = dt;
+        fz.dt_d = (double)dt;
+        fz.counter = reinterpret_cast<unsigned int*>(d_scratch);
+        fz.partials = reinterpret_cast<double*>(reinterpret_cast<char*>(d_scratch) + 256);
+        fz.out = d_thermo;
+        fz.seed = seed;
+        fz.d_timestep = d_timestep;
+        fz.langevin = 1;
+        fz.tag = d_tag;
+        fz.pos = reinterpret_cast<const float4*>(d_pos);
+        fz.gamma = d_gamma;
+        fz.lkT = kT;
+        fz.ndim = ndim ? ndim : 3u;
+        fz.d_reservoir = d_reservoir;
+        k_langevin_two<<<div_up(N > 0 ? N : 1, 256), 256, 0, (cudaStream_t)stream>>>(
+            fz, reinterpret_cast<const float4*>(d_net_force), N);
+        return check_launch("gb_langevin_step_two");
         }
 
     int gb_sum_net_force(float* d_net, const float* const* h_force_ptrs, unsigned int n_forces,

@@ -210,6 +210,8 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("addForce", &Integrator::add_force)
         .def("setBussi", &Integrator::set_thermostat_bussi)
         .def("setNoThermostat", &Integrator::set_thermostat_none)
+        .def("setLangevin", &Integrator::set_langevin)
+        .def_property_readonly("reservoir_energy", &Integrator::reservoir_energy)
         .def("setSorter", &Integrator::set_sorter)
         .def("setChunk", &Integrator::set_chunk)
         .def_readwrite("use_graph", &Integrator::use_graph)

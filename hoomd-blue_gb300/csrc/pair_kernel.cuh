@@ -45,6 +45,13 @@ struct FuseArgs
     uint32_t* d_rebuild_reset;
     const double2* d_ring;  // optional pre-drawn Bussi draws, indexed by timestep % ring_size
     unsigned int ring_size;
+    int langevin;           // Langevin step two instead of the rescaled one
+    const uint32_t* tag;    // [N] tags (Langevin random-number counters)
+    const float4* pos;      // [N] positions, type in w
+    const float* gamma;     // [ntypes] drag coefficients
+    float lkT;
+    unsigned int ndim;
+    double* d_reservoir;    // optional Langevin reservoir energy
     };
 
 template<int TPP> __device__ __forceinline__ double block_sum_d(double v, double* s_red)
@@ -63,6 +70,61 @@ template<int TPP> __device__ __forceinline__ double block_sum_d(double v, double
         }
     __syncthreads();
     return r; // valid in thread 0
+    }
+
+// Step two of the integrator for particle gi from its net force (fx, fy, fz_), and the
+// particle's FP64 terms of the step's sums: 2 KE, PE, and for Langevin F_bd . v.
+__device__ __forceinline__ void fuse_step_two(const FuseArgs& fz, unsigned int gi, float fx,
+                                              float fy, float fz_, float pe, double& ke_d,
+                                              double& pe_d, double& w_d)
+    {
+    float4 v = fz.vel[gi];
+    const float minv = __frcp_rn(v.w);
+    float ax, ay, az;
+    if (fz.langevin)
+        {
+        // hoomd/md/TwoStepLangevin.cc:248-292: F_bd = r * sqrt(6 gamma kT / dt) - gamma v with
+        // r uniform in [-1, 1] (three draws, Seed(25, timestep, seed), Counter(tag)),
+        // a = (F + F_bd) / m, v += (a / 2) dt
+        const unsigned int type = __float_as_uint(__ldg(fz.pos + gi).w);
+        const float gamma = __ldg(fz.gamma + type);
+        const float coeff
+            = __fsqrt_rn(__fdiv_rn(__fmul_rn(__fmul_rn(6.0f, gamma), fz.lkT), fz.dt));
+        Philox rng(25, *fz.d_timestep, fz.seed, __ldg(fz.tag + gi));
+        const float rx = uniform_m11_f(rng);
+        const float ry = uniform_m11_f(rng);
+        const float rz = uniform_m11_f(rng);
+        const float bx = __fsub_rn(__fmul_rn(rx, coeff), __fmul_rn(gamma, v.x));
+        const float by = __fsub_rn(__fmul_rn(ry, coeff), __fmul_rn(gamma, v.y));
+        const float bz
+            = fz.ndim < 3 ? 0.0f : __fsub_rn(__fmul_rn(rz, coeff), __fmul_rn(gamma, v.z));
+        ax = __fmul_rn(__fadd_rn(fx, bx), minv);
+        ay = __fmul_rn(__fadd_rn(fy, by), minv);
+        az = __fmul_rn(__fadd_rn(fz_, bz), minv);
+        v.x = __fadd_rn(v.x, __fmul_rn(__fmul_rn(0.5f, ax), fz.dt));
+        v.y = __fadd_rn(v.y, __fmul_rn(__fmul_rn(0.5f, ay), fz.dt));
+        v.z = __fadd_rn(v.z, __fmul_rn(__fmul_rn(0.5f, az), fz.dt));
+        w_d = (double)bx * (double)v.x + (double)by * (double)v.y + (double)bz * (double)v.z;
+        }
+    else
+        {
+        // a = F/m, v = v*s + dt/2 * a (TwoStepConstantVolume.cc:213-261 order)
+        ax = __fmul_rn(fx, minv);
+        ay = __fmul_rn(fy, minv);
+        az = __fmul_rn(fz_, minv);
+        const float s2 = fz.d_scale2 ? (float)*fz.d_scale2 : 1.0f;
+        const float hdt = __fmul_rn(0.5f, fz.dt);
+        v.x = __fadd_rn(__fmul_rn(v.x, s2), __fmul_rn(hdt, ax));
+        v.y = __fadd_rn(__fmul_rn(v.y, s2), __fmul_rn(hdt, ay));
+        v.z = __fadd_rn(__fmul_rn(v.z, s2), __fmul_rn(hdt, az));
+        }
+    fz.vel[gi] = v;
+    fz.accel[3 * (size_t)gi + 0] = ax;
+    fz.accel[3 * (size_t)gi + 1] = ay;
+    fz.accel[3 * (size_t)gi + 2] = az;
+    ke_d = (double)v.w
+           * ((double)v.x * (double)v.x + (double)v.y * (double)v.y + (double)v.z * (double)v.z);
+    pe_d = (double)pe;
     }
 
 __device__ inline void fuse_finish(const FuseArgs& fz, double ke, double pe, double w)
@@ -101,7 +163,10 @@ __device__ inline void fuse_finish(const FuseArgs& fz, double ke, double pe, dou
         const double K = 0.5 * a;
         fz.out[0] = K;
         fz.out[1] = b;
-        fz.out[2] = c / 3.0;
+        fz.out[2] = fz.langevin ? 0.0 : c / 3.0;
+        // the Langevin tally: c = sum of F_bd . v (hoomd/md/TwoStepLangevin.cc:396-412)
+        if (fz.langevin && fz.d_reservoir)
+            *fz.d_reservoir -= c * fz.dt_d;
         if (fz.bussi)
             {
             const uint64_t next = *fz.d_timestep + 1;
@@ -291,26 +356,7 @@ __global__ void __launch_bounds__(256)
             w_d = (double)vxx + (double)vyy + (double)vzz;
             }
         if (FUSE)
-            {
-            // step two: a = F/m, v = v*s + dt/2 * a (TwoStepConstantVolume.cc:213-261 order)
-            float4 v = fz.vel[gi];
-            const float minv = __frcp_rn(v.w);
-            const float ax = __fmul_rn(fx, minv), ay = __fmul_rn(fy, minv),
-                        az = __fmul_rn(fz_, minv);
-            const float s2 = fz.d_scale2 ? (float)*fz.d_scale2 : 1.0f;
-            const float hdt = __fmul_rn(0.5f, fz.dt);
-            v.x = __fadd_rn(__fmul_rn(v.x, s2), __fmul_rn(hdt, ax));
-            v.y = __fadd_rn(__fmul_rn(v.y, s2), __fmul_rn(hdt, ay));
-            v.z = __fadd_rn(__fmul_rn(v.z, s2), __fmul_rn(hdt, az));
-            fz.vel[gi] = v;
-            fz.accel[3 * (size_t)gi + 0] = ax;
-            fz.accel[3 * (size_t)gi + 1] = ay;
-            fz.accel[3 * (size_t)gi + 2] = az;
-            ke_d = (double)v.w
-                   * ((double)v.x * (double)v.x + (double)v.y * (double)v.y
-                      + (double)v.z * (double)v.z);
-            pe_d = (double)pe;
-            }
+            fuse_step_two(fz, gi, fx, fy, fz_, pe, ke_d, pe_d, w_d);
         }
     if (FUSE)
         fuse_finish(fz, ke_d, pe_d, w_d);
@@ -557,25 +603,7 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             w_d = (double)vxx + (double)vyy + (double)vzz;
             }
         if (FUSE)
-            {
-            float4 v = fz.vel[i];
-            const float minv = __frcp_rn(v.w);
-            const float ax = __fmul_rn(fx, minv), ay = __fmul_rn(fy, minv),
-                        az = __fmul_rn(fz_, minv);
-            const float s2 = fz.d_scale2 ? (float)*fz.d_scale2 : 1.0f;
-            const float hdt = __fmul_rn(0.5f, fz.dt);
-            v.x = __fadd_rn(__fmul_rn(v.x, s2), __fmul_rn(hdt, ax));
-            v.y = __fadd_rn(__fmul_rn(v.y, s2), __fmul_rn(hdt, ay));
-            v.z = __fadd_rn(__fmul_rn(v.z, s2), __fmul_rn(hdt, az));
-            fz.vel[i] = v;
-            fz.accel[3 * (size_t)i + 0] = ax;
-            fz.accel[3 * (size_t)i + 1] = ay;
-            fz.accel[3 * (size_t)i + 2] = az;
-            ke_d = (double)v.w
-                   * ((double)v.x * (double)v.x + (double)v.y * (double)v.y
-                      + (double)v.z * (double)v.z);
-            pe_d = (double)pe;
-            }
+            fuse_step_two(fz, i, fx, fy, fz_, pe, ke_d, pe_d, w_d);
         }
     if (FUSE)
         fuse_finish(fz, ke_d, pe_d, w_d);

@@ -91,6 +91,14 @@ template<class R> __host__ __device__ inline R uneg11(uint64_t in)
     return R(int64_t(in)) * factor + R(0.5) * factor;
     }
 
+// UniformDistribution<float>(-1, 1) (hoomd/RandomNumbers.h:317-341): a + width * u01(draw), one
+// generator draw per value. The products by powers of two are exact, so contraction into a fused
+// multiply-add cannot change the result.
+__host__ __device__ inline float uniform_m11_f(Philox& rng)
+    {
+    return -1.0f + 2.0f * u01<float>(rng.u64());
+    }
+
 // Box-Muller, one value per draw (hoomd/RandomNumbers.h:346-372).
 __device__ inline double normal_d(Philox& rng)
     {

@@ -57,7 +57,7 @@ class StepOneArgs(ctypes.Structure):
     _fields_ = [("d_pos", c_void), ("d_vel", c_void), ("d_accel", c_void), ("d_image", c_void),
                 ("N", c_uint), ("box", Box), ("dt", c_float), ("scale", c_float),
                 ("d_scale", c_void), ("d_last_pos", c_void), ("d_rcut_max", c_void),
-                ("r_buff", c_float), ("d_rebuild", c_void)]
+                ("r_buff", c_float), ("d_rebuild", c_void), ("nve_order", c_int)]
 
 
 class StepFuse(ctypes.Structure):
@@ -66,7 +66,9 @@ class StepFuse(ctypes.Structure):
                 ("tau", c_double), ("kT", c_double), ("seed", c_uint), ("instance_id", c_uint),
                 ("d_timestep", c_void), ("d_factor", c_void), ("d_status", c_void),
                 ("d_rebuild_reset", c_void), ("d_bussi_ring", c_void),
-                ("bussi_ring_size", c_uint)]
+                ("bussi_ring_size", c_uint), ("langevin", c_int), ("d_tag", c_void),
+                ("d_pos", c_void), ("d_gamma", c_void), ("langevin_kT", c_float),
+                ("ndim", ctypes.c_uint32), ("d_reservoir", c_void)]
 
 
 class RadialParam(ctypes.Structure):
@@ -109,6 +111,9 @@ _PROTOS = {
     "gb_thermalize": (c_int, [c_void, c_void, c_uint, c_double, c_u64, ctypes.c_uint16, c_uint,
                               c_void, c_void]),
     "gb_md_step_one": (c_int, [_P(StepOneArgs), c_void]),
+    "gb_langevin_step_two": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_uint,
+                                     c_float, c_float, ctypes.c_uint32, ctypes.c_uint16, c_void,
+                                     c_void, c_void, c_void, c_void]),
     "gb_md_step_scratch_bytes": (c_size, [c_uint]),
     "gb_md_pair_step_lj": (c_int, [_P(PairArgs), c_void, _P(StepFuse), c_void]),
     "gb_md_pair_step_table": (c_int, [_P(PairArgs), c_void, c_void, _P(StepFuse), c_void]),

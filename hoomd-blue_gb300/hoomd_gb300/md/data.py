@@ -89,3 +89,45 @@ def nonnegative_real(v):
     if v < 0:
         raise ValueError("value must be non-negative")
     return v
+
+
+class TypeDict:
+    """Mapping particle type -> value (a TypeParameter with len_keys=1); a list key sets each
+    type in it."""
+
+    def __init__(self, default=None, validator=None):
+        self._d = {}
+        self.default = default
+        self._validator = validator
+        self._on_change = None
+
+    @staticmethod
+    def _keys(key):
+        return [key] if isinstance(key, str) else list(key)
+
+    def __setitem__(self, key, value):
+        if self._validator is not None:
+            value = self._validator(value)
+        for k in self._keys(key):
+            self._d[k] = value
+        if self._on_change is not None:
+            self._on_change(key)
+
+    def __getitem__(self, key):
+        ks = self._keys(key)
+        if len(ks) != 1 or not isinstance(key, str):
+            return {k: self[k] for k in ks}
+        if key in self._d:
+            return self._d[key]
+        if self.default is not None:
+            return self.default
+        raise KeyError(f"{key} has not been set")
+
+    def __contains__(self, key):
+        return all(k in self._d for k in self._keys(key))
+
+    def keys(self):
+        return self._d.keys()
+
+    def to_base(self):
+        return dict(self._d)

@@ -1,6 +1,6 @@
 """The MD integrator (hoomd/md/integrate.py:128-296): velocity Verlet two-step integration with
-one ConstantVolume method over all particles and any number of pair forces sharing one
-neighbour list."""
+one method (ConstantVolume or Langevin) over all particles and any number of pair forces sharing
+one neighbour list."""
 
 from hoomd_gb300._native import _hoomd_gb300
 
@@ -33,8 +33,8 @@ class Integrator:
 
     def _attach(self, simulation):
         if len(self.methods) != 1:
-            raise NotImplementedError("exactly one integration method (ConstantVolume) is "
-                                      "supported")
+            raise NotImplementedError("exactly one integration method (ConstantVolume or "
+                                      "Langevin) is supported")
         if not self.forces:
             raise RuntimeError("the integrator needs at least one force")
         nl = self.forces[0].nlist
@@ -46,7 +46,7 @@ class Integrator:
         integ = _hoomd_gb300.IntegratorTwoStep(simulation.state._cpp_pdata, cpp_nl, self._dt)
         for f in self.forces:
             integ.addForce(f._attach(simulation, cpp_nl))
-        self.methods[0]._attach(integ)
+        self.methods[0]._attach(integ, simulation.state)
         self._cpp_obj = integ
         return integ
 

@@ -1,12 +1,13 @@
-"""Integration methods (hoomd/md/methods/methods.py:85-176): ConstantVolume, which is NVE without a
-thermostat and NVT with one."""
+"""Integration methods (hoomd/md/methods/methods.py): ConstantVolume (NVE without a thermostat, NVT
+with one) and Langevin, each over the group of all particles."""
 
 from hoomd_gb300.filter import All
+from hoomd_gb300.md.data import TypeDict, nonnegative_real
 from hoomd_gb300.md.methods import thermostats  # noqa: F401
 
 
 class Method:
-    pass
+    _loggables = {}
 
 
 class ConstantVolume(Method):
@@ -33,7 +34,7 @@ class ConstantVolume(Method):
         else:
             self._thermostat._apply(integ)
 
-    def _attach(self, integ):
+    def _attach(self, integ, state=None):
         self._cpp_integ = integ
         self._apply(integ)
 
@@ -43,3 +44,74 @@ class NVE(ConstantVolume):
 
     def __init__(self, filter):
         super().__init__(filter, thermostat=None)
+
+
+def _gamma_r(v):
+    v = tuple(float(x) for x in v)
+    if len(v) != 3 or min(v) < 0:
+        raise ValueError("gamma_r is three non-negative numbers")
+    return v
+
+
+class Langevin(Method):
+    """Langevin dynamics (hoomd/md/methods/methods.py:637-833, hoomd/md/TwoStepLangevin.cc).
+
+    Translational degrees of freedom only: drag ``gamma[type]`` and a uniform random force of
+    variance 2 kT gamma / dt per direction, velocity-Verlet halves in the reference's order. The
+    random numbers follow the reference's streams (Philox, Seed(25, timestep, seed), Counter(tag)),
+    so a trajectory is a function of the seed and the initial state. ``kT`` is a constant.
+    ``gamma_r`` is accepted for the rotational degrees of freedom, which this path does not
+    integrate. ``reservoir_energy`` is tallied with ``tally_reservoir_energy=True``.
+    """
+
+    _loggables = {"reservoir_energy": "scalar"}
+
+    def __init__(self, filter, kT, tally_reservoir_energy=False, default_gamma=1.0,
+                 default_gamma_r=(1.0, 1.0, 1.0)):
+        if not isinstance(filter, All):
+            raise NotImplementedError("Langevin integrates the group of all particles")
+        self.filter = filter
+        self._kT = float(kT)
+        self._tally = bool(tally_reservoir_energy)
+        self.gamma = TypeDict(default=float(default_gamma), validator=nonnegative_real)
+        self.gamma_r = TypeDict(default=_gamma_r(default_gamma_r), validator=_gamma_r)
+        self.gamma._on_change = self.gamma_r._on_change = lambda key: self._reapply()
+        self._cpp_integ = None
+        self._types = None
+
+    @property
+    def kT(self):
+        return self._kT
+
+    @kT.setter
+    def kT(self, v):
+        self._kT = float(v)
+        self._reapply()
+
+    @property
+    def tally_reservoir_energy(self):
+        return self._tally
+
+    @tally_reservoir_energy.setter
+    def tally_reservoir_energy(self, v):
+        self._tally = bool(v)
+        self._reapply()
+
+    @property
+    def reservoir_energy(self):
+        if self._cpp_integ is None:
+            raise RuntimeError("reservoir_energy is available after the simulation runs")
+        return self._cpp_integ.reservoir_energy
+
+    def _reapply(self):
+        if self._cpp_integ is not None:
+            self._apply(self._cpp_integ)
+
+    def _apply(self, integ):
+        gam = [float(self.gamma[t]) for t in self._types]
+        integ.setLangevin(self._kT, gam, self._tally)
+
+    def _attach(self, integ, state=None):
+        self._types = list(state.particle_types)
+        self._cpp_integ = integ
+        self._apply(integ)

@@ -353,6 +353,10 @@ typedef struct gb_step_one_args
     const float* d_rcut_max;    /* [ntypes] */
     float r_buff;
     uint32_t* d_rebuild;        /* set to 1 when any particle moved >= (r_buff)/2 */
+    /* 0: TwoStepConstantVolume order (v += a dt/2, v *= s, x += v dt); 1: TwoStepNVE order
+       (x += v dt + a dt^2/2, then v += a dt/2; hoomd/md/TwoStepNVEGPU.cu:68-98), which the
+       Langevin method uses (hoomd/md/TwoStepLangevin.cc:57-81); scale is ignored */
+    int nve_order;
     } gb_step_one_args;
 
 int gb_md_step_one(const gb_step_one_args* args, void* stream);
@@ -378,7 +382,28 @@ typedef struct gb_step_fuse
                                    gb_bussi_draws, at index timestep % bussi_ring_size; NULL =
                                    draw in the kernel's last block */
     uint32_t bussi_ring_size;
+    /* Langevin step two (hoomd/md/TwoStepLangevin.cc:206-290) instead of the rescaled one:
+       drag -gamma v plus a uniform random force of amplitude sqrt(6 gamma kT / dt), drawn from
+       Philox with Seed(25, timestep, seed), Counter(tag); excludes bussi and d_scale2 */
+    int langevin;
+    const uint32_t* d_tag;      /* [N] particle tag of each index */
+    const float* d_pos;         /* float4[N] positions (type in w) */
+    const float* d_gamma;       /* [ntypes] drag coefficients */
+    float langevin_kT;
+    uint32_t ndim;              /* 2: no random or drag force along z */
+    double* d_reservoir;        /* optional: reservoir energy, reduced by dt * sum(F_bd . v) */
     } gb_step_fuse;
+
+/* Langevin step two on its own (the unfused path: several forces, the virial, the MLP
+ * surrogate): a = (F_net + F_bd) / m, v += a dt/2 for all N particles at timestep *d_timestep
+ * (incremented by one when the step is done), then the FP64 sums into d_thermo (KE, PE, 0) and,
+ * when d_reservoir is given, *d_reservoir -= dt * sum(F_bd . v).
+ * d_scratch: gb_md_step_scratch_bytes(N), zeroed once before first use. */
+int gb_langevin_step_two(float* d_vel, float* d_accel, const float* d_net_force,
+                         const float* d_pos, const uint32_t* d_tag, const float* d_gamma,
+                         unsigned int N, float dt, float kT, uint32_t ndim, uint16_t seed,
+                         uint64_t* d_timestep, void* d_scratch, double* d_thermo,
+                         double* d_reservoir, void* stream);
 
 /* Pre-draws the random numbers of the Bussi factor (hoomd/md/Thermostat.h:416-446) for timesteps
  * *d_timestep + 1 ... *d_timestep + count, one thread per timestep, into

@@ -997,6 +997,75 @@ void thermalize(unsigned int N, R* vel, const unsigned int* tags, R kT, uint64_t
     }
 
 // ------------------------------------------------------------------------------------------------
+// Langevin dynamics, translational part. Step one in the TwoStepNVE order
+// (hoomd/md/TwoStepLangevin.cc:57-81): x += v dt + (1/2) a dt^2, wrap, v += (1/2) a dt.
+// Step two (hoomd/md/TwoStepLangevin.cc:206-292): three UniformDistribution<R>(-1, 1) draws from
+// Seed(25, timestep, seed), Counter(tag); F_bd = r sqrt(6 gamma T / dt) - gamma v (z term zero in
+// 2D); a = (F + F_bd) / m; v += (1/2) a dt; the reservoir tally sums F_bd . v in R
+// (:290-292, :396-412). Returns that sum.
+// ------------------------------------------------------------------------------------------------
+template<class R>
+void nve_step_one(unsigned int N, R* pos, R* vel, const R* accel, int* image, const Box<R>& box,
+                  R dt, int nthreads = 1)
+    {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(std::max(nthreads, 1))
+#endif
+    for (unsigned int j = 0; j < N; j++)
+        {
+        R dx = vel[4 * j] * dt + R(1.0 / 2.0) * accel[3 * j] * dt * dt;
+        R dy = vel[4 * j + 1] * dt + R(1.0 / 2.0) * accel[3 * j + 1] * dt * dt;
+        R dz = vel[4 * j + 2] * dt + R(1.0 / 2.0) * accel[3 * j + 2] * dt * dt;
+        R px = pos[4 * j] + dx, py = pos[4 * j + 1] + dy, pz = pos[4 * j + 2] + dz;
+        box.wrap(px, py, pz, image[3 * j], image[3 * j + 1], image[3 * j + 2]);
+        pos[4 * j] = px;
+        pos[4 * j + 1] = py;
+        pos[4 * j + 2] = pz;
+        vel[4 * j] += R(1.0 / 2.0) * accel[3 * j] * dt;
+        vel[4 * j + 1] += R(1.0 / 2.0) * accel[3 * j + 1] * dt;
+        vel[4 * j + 2] += R(1.0 / 2.0) * accel[3 * j + 2] * dt;
+        }
+    }
+
+template<class R> static inline R uniform_m11(RNG& rng)
+    {
+    // hoomd/RandomNumbers.h:317-341: a + (b - a) * u01(draw)
+    return R(-1) + R(2) * u01<R>(rng.u64());
+    }
+
+template<class R>
+double langevin_step_two(unsigned int N, R* vel, R* accel, const R* pos, const unsigned int* tags,
+                         const R* net_force, const R* gamma_t, R T, R dt, uint16_t seed,
+                         uint64_t timestep, int ndim)
+    {
+    R bd_energy_transfer = 0;
+    for (unsigned int j = 0; j < N; j++)
+        {
+        RNG rng(25, timestep, seed, tags[j]);
+        R rx = uniform_m11<R>(rng);
+        R ry = uniform_m11<R>(rng);
+        R rz = uniform_m11<R>(rng);
+        R gamma = gamma_t[as_uint(pos[4 * j + 3])];
+        R coeff = std::sqrt(R(6.0) * gamma * T / dt);
+        R bd_fx = rx * coeff - gamma * vel[4 * j];
+        R bd_fy = ry * coeff - gamma * vel[4 * j + 1];
+        R bd_fz = rz * coeff - gamma * vel[4 * j + 2];
+        if (ndim < 3)
+            bd_fz = R(0.0);
+        R minv = R(1.0) / vel[4 * j + 3];
+        accel[3 * j] = (net_force[4 * j] + bd_fx) * minv;
+        accel[3 * j + 1] = (net_force[4 * j + 1] + bd_fy) * minv;
+        accel[3 * j + 2] = (net_force[4 * j + 2] + bd_fz) * minv;
+        vel[4 * j] += R(1.0 / 2.0) * accel[3 * j] * dt;
+        vel[4 * j + 1] += R(1.0 / 2.0) * accel[3 * j + 1] * dt;
+        vel[4 * j + 2] += R(1.0 / 2.0) * accel[3 * j + 2] * dt;
+        bd_energy_transfer
+            += bd_fx * vel[4 * j] + bd_fy * vel[4 * j + 1] + bd_fz * vel[4 * j + 2];
+        }
+    return double(bd_energy_transfer);
+    }
+
+// ------------------------------------------------------------------------------------------------
 // Whole-step runner: hoomd/md/IntegratorTwoStep.cc:51-139 (update), :226-298 (prepRun),
 // hoomd/md/NeighborList.cc:363-435 (compute), :452-529 (updateRList), :1220-1289 (distanceCheck),
 // :1325-1418 (needsUpdating, rebuild_check_delay = 1, check_dist = true), :1544-1617 (head list,
@@ -1034,6 +1103,10 @@ template<class R> struct Sim
     uint64_t n_builds = 0;
     // integrator
     R dt = 0;
+    bool langevin = false;
+    std::vector<R> gamma;
+    R langevin_T = 0;
+    double reservoir = 0;
     bool bussi = false;
     double kT = 0, tau = 0;
     uint16_t seed = 0;
@@ -1234,11 +1307,24 @@ template<class R> struct Sim
     double dof() const
         {
         // IntegratorTwoStep::getTranslationalDOF: D*N - D for one momentum-conserving method on all
-        return double(ndim) * N - double(ndim);
+        // particles; D*N for Langevin (TwoStepLangevinBase::isMomentumConserving)
+        return langevin ? double(ndim) * N : double(ndim) * N - double(ndim);
         }
 
     bool step()
         {
+        if (langevin)
+            {
+            nve_step_one(N, pos.data(), vel.data(), accel.data(), image.data(), box, dt, nthreads);
+            if (!compute_forces())
+                return false;
+            const double e = langevin_step_two(N, vel.data(), accel.data(), pos.data(),
+                                               tags.data(), force.data(), gamma.data(),
+                                               langevin_T, dt, seed, timestep, ndim);
+            reservoir -= e * double(dt);
+            timestep++;
+            return true;
+            }
         R s = R(1.0);
         if (bussi)
             {
@@ -1515,6 +1601,39 @@ using namespace orc;
         s->Nmax.assign(ntypes, 4);                                                                 \
         s->update_rlist();                                                                         \
         return s;                                                                                  \
+        }                                                                                          \
+    ORC_EXPORT void orc_sim_set_langevin_##SUF(void* h, double kT, const double* gamma)            \
+        {                                                                                          \
+        auto* s = (Sim<R>*)h;                                                                      \
+        s->langevin = true;                                                                        \
+        s->bussi = false;                                                                          \
+        s->langevin_T = R(kT);                                                                     \
+        s->gamma.assign(s->ntypes, R(0));                                                          \
+        for (unsigned int t = 0; t < s->ntypes; t++)                                               \
+            s->gamma[t] = R(gamma[t]);                                                             \
+        }                                                                                          \
+    ORC_EXPORT double orc_sim_reservoir_##SUF(void* h)                                             \
+        {                                                                                          \
+        return ((Sim<R>*)h)->reservoir;                                                            \
+        }                                                                                          \
+    ORC_EXPORT void orc_nve_step_one_##SUF(unsigned int N, R* pos, R* vel, const R* accel,         \
+                                           int* image, const double* b6, const int* per,           \
+                                           double dt)                                              \
+        {                                                                                          \
+        Box<R> box;                                                                                \
+        box.set(b6, per);                                                                          \
+        nve_step_one<R>(N, pos, vel, accel, image, box, R(dt));                                    \
+        }                                                                                          \
+    ORC_EXPORT double orc_langevin_step_two_##SUF(                                                 \
+        unsigned int N, R* vel, R* accel, const R* pos, const unsigned int* tags,                  \
+        const R* net_force, const double* gamma, unsigned int ntypes, double kT, double dt,        \
+        unsigned int seed, uint64_t timestep, int ndim)                                            \
+        {                                                                                          \
+        std::vector<R> g(ntypes);                                                                  \
+        for (unsigned int t = 0; t < ntypes; t++)                                                  \
+            g[t] = R(gamma[t]);                                                                    \
+        return langevin_step_two<R>(N, vel, accel, pos, tags, net_force, g.data(), R(kT), R(dt),   \
+                                    uint16_t(seed), timestep, ndim);                               \
         }                                                                                          \
     ORC_EXPORT int orc_sim_run_##SUF(void* h, uint64_t nsteps)                                     \
         {                                                                                          \

@@ -36,6 +36,8 @@ def lib():
         _lib.orc_bussi_factor.restype = ctypes.c_double
         for suf in ("f32", "f64"):
             getattr(_lib, f"orc_kinetic_energy_{suf}").restype = ctypes.c_double
+            getattr(_lib, f"orc_langevin_step_two_{suf}").restype = ctypes.c_double
+            getattr(_lib, f"orc_sim_reservoir_{suf}").restype = ctypes.c_double
             getattr(_lib, f"orc_sim_create_{suf}").restype = ctypes.c_void_p
             getattr(_lib, f"orc_sim_error_{suf}").restype = ctypes.c_char_p
             for name in ("run", "get", "stats", "destroy", "error"):
@@ -303,6 +305,37 @@ def cv_step_two(vel4, net_force4, dt, s=1.0, prec=32):
     return vel4, accel3
 
 
+def nve_step_one(pos4, vel4, accel3, image3, box, dt, prec=32, periodic=(1, 1, 1)):
+    """TwoStepNVE / Langevin step one (x += v dt + a dt^2 / 2, then v += a dt / 2)."""
+    R = rdtype(prec)
+    pos4 = np.ascontiguousarray(pos4, R).copy()
+    vel4 = np.ascontiguousarray(vel4, R).copy()
+    accel3 = np.ascontiguousarray(accel3, R)
+    image3 = np.ascontiguousarray(image3, np.int32).copy()
+    b, p = box6(box), periodic3(periodic)
+    getattr(lib(), f"orc_nve_step_one_{suf(prec)}")(len(pos4), ptr(pos4), ptr(vel4), ptr(accel3),
+                                                    ptr(image3), ptr(b), ptr(p),
+                                                    ctypes.c_double(dt))
+    return pos4, vel4, image3
+
+
+def langevin_step_two(vel4, pos4, tags, net_force4, gamma, kT, dt, seed, timestep, ndim=3,
+                      prec=32):
+    """Langevin step two; returns (vel4, accel3, sum of F_bd . v)."""
+    R = rdtype(prec)
+    vel4 = np.ascontiguousarray(vel4, R).copy()
+    pos4 = np.ascontiguousarray(pos4, R)
+    accel3 = np.zeros((len(vel4), 3), R)
+    tags = np.ascontiguousarray(tags, np.uint32)
+    f = np.ascontiguousarray(net_force4, R)
+    g = np.ascontiguousarray(gamma, np.float64)
+    e = getattr(lib(), f"orc_langevin_step_two_{suf(prec)}")(
+        len(vel4), ptr(vel4), ptr(accel3), ptr(pos4), ptr(tags), ptr(f), ptr(g),
+        ctypes.c_uint32(len(g)), ctypes.c_double(kT), ctypes.c_double(dt), ctypes.c_uint32(seed),
+        ctypes.c_uint64(timestep), ctypes.c_int(ndim))
+    return vel4, accel3, e
+
+
 def kinetic_energy(vel4, prec=32):
     vel4 = np.ascontiguousarray(vel4, rdtype(prec))
     return getattr(lib(), f"orc_kinetic_energy_{suf(prec)}")(len(vel4), ptr(vel4))
@@ -363,7 +396,7 @@ class Sim:
 
     def __init__(self, pos4, vel4, image3, tags, box, r_cut, r_buff, dt, kind="lj", params=None,
                  tdata=None, shift_mode=0, full=False, bussi=False, kT=1.0, tau=0.0, seed=0,
-                 timestep=0, ndim=3, prec=32, nthreads=1, periodic=(1, 1, 1)):
+                 timestep=0, ndim=3, prec=32, nthreads=1, periodic=(1, 1, 1), langevin=None):
         R = rdtype(prec)
         self.prec = prec
         self.N = len(pos4)
@@ -389,6 +422,15 @@ class Sim:
             ctypes.c_int(int(bussi)), d(kT), d(tau), ctypes.c_uint32(seed),
             ctypes.c_uint64(timestep), ctypes.c_int(nthreads))
         self.h = ctypes.c_void_p(self.h)
+        if langevin is not None:
+            # langevin = per-type drag coefficients; kT is the bath temperature
+            g = np.ascontiguousarray(langevin, np.float64)
+            self._keep.append(g)
+            getattr(L, f"orc_sim_set_langevin_{self._s}")(self.h, d(kT), ptr(g))
+
+    @property
+    def reservoir_energy(self):
+        return getattr(lib(), f"orc_sim_reservoir_{self._s}")(self.h)
 
     def run(self, nsteps):
         rc = getattr(lib(), f"orc_sim_run_{self._s}")(self.h, ctypes.c_uint64(nsteps))

@@ -92,6 +92,7 @@ def test_logged_thermodynamics(tmp_path):
     path = str(tmp_path / "log.gsd")
     snap = workloads.lj_fluid_sc(8, density=0.8, jitter=0.05, seed=4)
     sim, lj = lj_sim(snap)
+    sim.state.thermalize_particle_momenta(hoomd.filter.All(), 1.2)
     thermo = md.compute.ThermodynamicQuantities(hoomd.filter.All())
     sim.operations.computes.append(thermo)
     logger = hoomd.logging.Logger(categories=["scalar"])
