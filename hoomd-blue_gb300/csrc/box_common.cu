@@ -31,6 +31,18 @@ int num_sms()
 
 extern "C"
     {
+    unsigned int gb_abi_struct_sizes(size_t* out, unsigned int n)
+        {
+        const size_t sizes[10] = {sizeof(gb_box),           sizeof(gb_cell_list_args),
+                                  sizeof(gb_nlist_args),    sizeof(gb_pair_args),
+                                  sizeof(gb_radial_param),  sizeof(gb_step_one_args),
+                                  sizeof(gb_step_fuse),     sizeof(gb_mlp_force_args),
+                                  sizeof(gb_replica),       sizeof(gb_replica_batch)};
+        for (unsigned int k = 0; k < n && k < 10 && out; k++)
+            out[k] = sizes[k];
+        return 10;
+        }
+
     const char* gb_last_error(void)
         {
         return gb::g_last_error.c_str();

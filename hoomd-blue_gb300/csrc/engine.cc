@@ -788,6 +788,7 @@ void Integrator::add_force(std::shared_ptr<PairForce> f)
 void Integrator::set_thermostat_bussi(double kT_, double tau_)
     {
     bussi = true;
+    berendsen = mttk = langevin = false;
     kT = kT_;
     tau = tau_;
     prepared = false;
@@ -797,6 +798,7 @@ void Integrator::set_thermostat_bussi(double kT_, double tau_)
 void Integrator::set_thermostat_none()
     {
     bussi = false;
+    berendsen = mttk = false;
     langevin = false;
     prepared = false;
     drop_graphs();
@@ -807,6 +809,7 @@ void Integrator::set_langevin(double kT_, const std::vector<double>& gamma_, boo
     if (gamma_.size() != pdata->ntypes)
         throw std::invalid_argument("Langevin: one drag coefficient per particle type");
     bussi = false;
+    berendsen = mttk = false;
     langevin = true;
     tally = tally_;
     langevin_kT = kT_;
@@ -817,6 +820,76 @@ void Integrator::set_langevin(double kT_, const std::vector<double>& gamma_, boo
                "gamma");
     prepared = false;
     drop_graphs();
+    }
+
+void Integrator::set_thermostat_berendsen(double kT_, double tau_)
+    {
+    if (!(tau_ > 0.0))
+        throw std::invalid_argument("Berendsen: tau must be positive");
+    berendsen = true;
+    bussi = mttk = langevin = false;
+    kT = kT_;
+    tau = tau_;
+    prepared = false;
+    drop_graphs();
+    }
+
+void Integrator::set_thermostat_mttk(double kT_, double tau_)
+    {
+    if (!(tau_ > 0.0))
+        throw std::invalid_argument("MTTK: tau must be positive");
+    mttk = true;
+    bussi = berendsen = langevin = false;
+    kT = kT_;
+    tau = tau_;
+    prepared = false;
+    drop_graphs();
+    }
+
+std::vector<double> Integrator::mttk_state()
+    {
+    if (prepared)
+        {
+        DevStatus st = read_status();
+        mttk_host[0] = st.mttk[0];
+        mttk_host[1] = st.mttk[1];
+        }
+    return {mttk_host[0], mttk_host[1]};
+    }
+
+void Integrator::set_mttk_state(double xi, double eta)
+    {
+    mttk_host[0] = xi;
+    mttk_host[1] = eta;
+    if (prepared)
+        {
+        double v[2] = {xi, eta};
+        cuda_check(cudaMemcpyAsync(d_status.get()->mttk, v, sizeof(v), cudaMemcpyHostToDevice,
+                                   pdata->stream),
+                   "mttk state");
+        cuda_check(cudaStreamSynchronize(pdata->stream), "mttk state");
+        }
+    }
+
+void Integrator::thermalize_mttk(uint64_t timestep)
+    {
+    // xi ~ Normal(sqrt(1 / (dof tau^2))), Seed(28, timestep, seed), Counter(first tag = 0)
+    DeviceArray<double> out;
+    out.resize(1);
+    const double sigma = std::sqrt(1.0 / (dof() * tau * tau));
+    check(gb_normal_draw(28, timestep, pdata->seed, 0u, sigma, out.get(), pdata->stream),
+          "gb_normal_draw");
+    double xi = 0.0;
+    out.download(&xi, 1, pdata->stream);
+    cuda_check(cudaStreamSynchronize(pdata->stream), "thermalize");
+    const std::vector<double> cur = mttk_state();
+    set_mttk_state(xi, cur[1]);
+    }
+
+double Integrator::mttk_energy()
+    {
+    const std::vector<double> st = mttk_state();
+    return dof() * kT * (st[0] * st[0] * tau * tau / 2.0 + st[1]);
     }
 
 double Integrator::reservoir_energy()
@@ -911,6 +984,9 @@ void Integrator::prepare()
     st.n_builds = nlist->n_builds_host;
     st.factor = 1.0;
     st.reservoir = reservoir;
+    st.mttk[0] = mttk_host[0];
+    st.mttk[1] = mttk_host[1];
+    st.mttk_scale2 = 1.0;
     cuda_check(cudaMemcpyAsync(d_status.get(), &st, sizeof(st), cudaMemcpyHostToDevice, s),
                "status");
     DevStatus* ds = d_status.get();
@@ -921,9 +997,15 @@ void Integrator::prepare()
         check(gb_bussi_factor(&ds->thermo[0], dof(), dt, tau, kT, pd.timestep, pd.seed, 0u,
                               &ds->factor, s),
               "bussi");
+    if (berendsen)
+        check(gb_berendsen_factor(&ds->thermo[0], dof(), dt, tau, kT, &ds->factor, &ds->status,
+                                  s),
+              "berendsen");
     DevStatus back = read_status();
     if (bussi && dof() != 0 && back.thermo[0] == 0.0)
         throw std::runtime_error("Bussi thermostat requires non-zero initial momenta.");
+    if (berendsen && (back.status & 2u))
+        throw std::runtime_error("Berendsen thermostat requires non-zero initial temperatures");
     prepared = true;
     }
 
@@ -940,12 +1022,21 @@ gb_step_one_args Integrator::step_one_args(DevStatus* ds) const
     o.box = pd.box;
     o.dt = (float)dt;
     o.scale = 1.0f;
-    o.d_scale = bussi ? &ds->factor : nullptr;
+    o.d_scale = (bussi || berendsen) ? &ds->factor : nullptr;
     o.d_last_pos = nlist->last_pos.get();
     o.d_rcut_max = nlist->d_rcut_max.get();
     o.r_buff = nlist->r_buff;
     o.d_rebuild = &ds->rebuild;
     o.nve_order = langevin ? 1 : 0;
+    if (mttk)
+        {
+        o.d_mttk_state = ds->mttk;
+        o.d_mttk_scale2 = &ds->mttk_scale2;
+        o.mttk_dof = dof();
+        o.mttk_kT = kT;
+        o.mttk_tau = tau;
+        o.d_mttk_scratch = d_thermo_scratch.get();
+        }
     return o;
     }
 
@@ -957,7 +1048,8 @@ gb_step_fuse Integrator::fuse_args(DevStatus* ds) const
     fu.d_vel = pd.vel.get();
     fu.d_accel = pd.accel.get();
     fu.dt = (float)dt;
-    fu.d_scale2 = nullptr;
+    fu.d_scale2 = mttk ? &ds->mttk_scale2 : nullptr;
+    fu.berendsen = berendsen ? 1 : 0;
     fu.d_scratch = d_step_scratch.get();
     fu.d_thermo = ds->thermo;
     fu.bussi = bussi ? 1 : 0;
@@ -1030,8 +1122,8 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
         }
     else
         {
-        check(gb_cv_step_two(pd.vel.get(), pd.accel.get(), net, pd.N, (float)dt, 1.0f, nullptr,
-                             s),
+        check(gb_cv_step_two(pd.vel.get(), pd.accel.get(), net, pd.N, (float)dt, 1.0f,
+                             mttk ? &ds->mttk_scale2 : nullptr, s),
               "gb_cv_step_two");
         check(gb_thermo_reduce(pd.vel.get(), net, nullptr, 0, pd.N, d_thermo_scratch.get(),
                                ds->thermo, s),
@@ -1041,6 +1133,10 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
         check(gb_bussi_factor(&ds->thermo[0], dof(), dt, tau, kT, step + 1, pd.seed, 0u,
                               &ds->factor, s),
               "bussi");
+    if (berendsen)
+        check(gb_berendsen_factor(&ds->thermo[0], dof(), dt, tau, kT, &ds->factor, &ds->status,
+                                  s),
+              "berendsen");
     cuda_check(cudaMemsetAsync(&ds->rebuild, 0, sizeof(uint32_t), s), "reset rebuild");
     }
 
@@ -1128,7 +1224,7 @@ void Integrator::run_chunk(unsigned int k)
                 enqueue_step_general(s, pd.timestep + i);
             launch_count += (uint64_t)k
                             * (1 + cell_kernels + 1 + forces.size() + (forces.size() > 1 ? 1 : 0)
-                               + (langevin ? 1 : 2) + (bussi ? 1 : 0));
+                               + (langevin ? 1 : 2) + ((bussi || berendsen) ? 1 : 0));
             }
         DevStatus st = read_status();
         if (st.cell_cond[1])
@@ -1150,7 +1246,11 @@ void Integrator::run_chunk(unsigned int k)
             }
         if (st.status & 1u)
             throw std::runtime_error("Bussi thermostat requires non-zero initial momenta.");
+        if (st.status & 2u)
+            throw std::runtime_error("Berendsen thermostat requires non-zero initial temperatures");
         reservoir = st.reservoir;
+        mttk_host[0] = st.mttk[0];
+        mttk_host[1] = st.mttk[1];
         pd.timestep += k;
         steps_run += k;
         if (!fused)

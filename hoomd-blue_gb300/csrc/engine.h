@@ -125,13 +125,15 @@ struct DevStatus
     {
     uint32_t cell_cond[3]; // needed Nmax, NaN index+1, out-of-box index+1
     uint32_t rebuild;      // rebuild gate for the current step
-    uint32_t status;       // bit 0: Bussi with zero kinetic energy
+    uint32_t status;       // bit 0: Bussi, bit 1: Berendsen with zero kinetic energy
     uint32_t pad[3];
     uint64_t timestep;
     uint64_t n_builds;
     double factor;         // Bussi rescale factor for the next step one
     double thermo[3];      // KE, PE, W after the last step
     double reservoir;      // Langevin reservoir energy (tally_reservoir_energy)
+    double mttk[2];        // MTTK thermostat xi, eta
+    double mttk_scale2;    // MTTK step-two factor of the current step
     uint32_t nl_cond[64];  // per-type neighbours needed on overflow
     };
 
@@ -272,6 +274,13 @@ class Integrator
     // TwoStepLangevin (translational part): per-type drag coefficients, constant kT
     void set_langevin(double kT, const std::vector<double>& gamma, bool tally);
     double reservoir_energy();
+    // ConstantVolume thermostats: Berendsen and MTTK (Nose-Hoover), hoomd/md/Thermostat.h
+    void set_thermostat_berendsen(double kT, double tau);
+    void set_thermostat_mttk(double kT, double tau);
+    std::vector<double> mttk_state();               // xi, eta
+    void set_mttk_state(double xi, double eta);
+    void thermalize_mttk(uint64_t timestep);         // MTTKThermostat::thermalizeThermostat
+    double mttk_energy();                            // MTTKThermostat::getThermostatEnergy
     void set_sorter(uint64_t period, int grid_bits);
     void set_chunk(unsigned int steps)
         {
@@ -290,6 +299,8 @@ class Integrator
     bool bussi = false;
     double kT = 1.0, tau = 0.0;
     bool langevin = false, tally = false;
+    bool berendsen = false, mttk = false;
+    double mttk_host[2] = {0.0, 0.0}; // xi, eta carried across prepare()
     double langevin_kT = 1.0;
     std::vector<float> gamma;
     double reservoir = 0.0; // host copy, carried across prepare()

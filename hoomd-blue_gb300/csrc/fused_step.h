@@ -56,6 +56,11 @@ inline int make_fuse_args(const gb_pair_args* a, const gb_step_fuse* f, FuseArgs
     fz.lkT = f->langevin_kT;
     fz.ndim = f->ndim ? f->ndim : 3u;
     fz.d_reservoir = f->d_reservoir;
+    fz.berendsen = f->berendsen;
+    GB_REQUIRE(!f->berendsen || (!f->bussi && !f->langevin && f->d_factor && f->d_status
+                                 && f->tau > 0.0),
+               "fused step: Berendsen needs the factor and status buffers and tau > 0, and "
+               "excludes Bussi and Langevin");
     return GB_OK;
     }
 } // namespace gb

@@ -14,105 +14,6 @@ namespace gb
 {
 namespace
 {
-struct StepOneCheck
-    {
-    const float4* last_pos;
-    const float* rcut_max;
-    float r_buff;
-    uint32_t* rebuild;
-    };
-
-template<bool CHECK, bool NVE>
-__global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
-                           const float* __restrict__ accel, int* __restrict__ image,
-                           unsigned int N, gb_box box, float dt, float scale,
-                           const double* __restrict__ d_scale, StepOneCheck chk)
-    {
-    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
-    bool moved = false;
-    if (j < N)
-        {
-        const float s = (!NVE && d_scale) ? (float)*d_scale : scale;
-        float4 v = vel[j];
-        float4 p = pos[j];
-        const float ax = accel[3 * (size_t)j], ay = accel[3 * (size_t)j + 1],
-                    az = accel[3 * (size_t)j + 2];
-        if (NVE)
-            {
-            // x += v dt + (1/2) a dt^2 ; v += (1/2) a dt   (TwoStepNVEGPU.cu:68-98,
-            // TwoStepLangevin.cc:57-81)
-            p.x = fadd(p.x, fadd(fmul(v.x, dt), fmul(fmul(fmul(0.5f, ax), dt), dt)));
-            p.y = fadd(p.y, fadd(fmul(v.y, dt), fmul(fmul(fmul(0.5f, ay), dt), dt)));
-            p.z = fadd(p.z, fadd(fmul(v.z, dt), fmul(fmul(fmul(0.5f, az), dt), dt)));
-            v.x = fadd(v.x, fmul(fmul(0.5f, ax), dt));
-            v.y = fadd(v.y, fmul(fmul(0.5f, ay), dt));
-            v.z = fadd(v.z, fmul(fmul(0.5f, az), dt));
-            }
-        else
-            {
-            // v = v + (1/2) a dt ; v *= s ; x += dt v   (TwoStepConstantVolume.cc:37-55)
-            v.x = fadd(v.x, fmul(fmul(0.5f, ax), dt));
-            v.y = fadd(v.y, fmul(fmul(0.5f, ay), dt));
-            v.z = fadd(v.z, fmul(fmul(0.5f, az), dt));
-            v.x = fmul(v.x, s);
-            v.y = fmul(v.y, s);
-            v.z = fmul(v.z, s);
-            p.x = fadd(p.x, fmul(dt, v.x));
-            p.y = fadd(p.y, fmul(dt, v.y));
-            p.z = fadd(p.z, fmul(dt, v.z));
-            }
-        int ix = 0, iy = 0, iz = 0;
-        wrap(box, p.x, p.y, p.z, ix, iy, iz);
-        if (ix | iy | iz)
-            {
-            image[3 * (size_t)j] += ix;
-            image[3 * (size_t)j + 1] += iy;
-            image[3 * (size_t)j + 2] += iz;
-            }
-        vel[j] = v;
-        pos[j] = p;
-        if (CHECK)
-            {
-            // hoomd/md/NeighborListGPU.cu:42-83 with lambda = 1 (fixed box)
-            const float4 lp = chk.last_pos[j];
-            float dx = fsub(p.x, lp.x), dy = fsub(p.y, lp.y), dz = fsub(p.z, lp.z);
-            min_image(box, dx, dy, dz);
-            const float rmin = chk.rcut_max[__float_as_uint(p.w)];
-            const float rmax = fadd(rmin, chk.r_buff);
-            const float delta_max = fmul(fsub(rmax, rmin), 0.5f);
-            const float maxsq = (delta_max > 0.0f) ? fmul(delta_max, delta_max) : 0.0f;
-            moved = dot3(dx, dy, dz) >= maxsq;
-            }
-        }
-    if (CHECK && __any_sync(0xffffffffu, moved) && (threadIdx.x % 32) == 0)
-        *chk.rebuild = 1u;
-    }
-
-__global__ void k_step_two(float4* __restrict__ vel, float* __restrict__ accel,
-                           const float4* __restrict__ net_force, unsigned int N, float dt,
-                           float scale, const double* __restrict__ d_scale)
-    {
-    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= N)
-        return;
-    const float s = d_scale ? (float)*d_scale : scale;
-    float4 v = vel[j];
-    const float4 f = net_force[j];
-    const float minv = __frcp_rn(v.w);
-    const float ax = fmul(f.x, minv), ay = fmul(f.y, minv), az = fmul(f.z, minv);
-    v.x = fmul(v.x, s);
-    v.y = fmul(v.y, s);
-    v.z = fmul(v.z, s);
-    const float hdt = fmul(0.5f, dt);
-    v.x = fadd(v.x, fmul(hdt, ax));
-    v.y = fadd(v.y, fmul(hdt, ay));
-    v.z = fadd(v.z, fmul(hdt, az));
-    vel[j] = v;
-    accel[3 * (size_t)j] = ax;
-    accel[3 * (size_t)j + 1] = ay;
-    accel[3 * (size_t)j + 2] = az;
-    }
-
 // Block sum of three doubles; result valid in thread 0.
 __device__ inline void block_sum3(double& a, double& b, double& c)
     {
@@ -173,6 +74,143 @@ __device__ inline bool reduce3_last(double& a, double& b, double& c, unsigned in
     return true;
     }
 
+struct StepOneCheck
+    {
+    const float4* last_pos;
+    const float* rcut_max;
+    float r_buff;
+    uint32_t* rebuild;
+    };
+
+// MTTK thermostat state and the reduction scratch of step one.
+struct MttkStep
+    {
+    double* state;  // xi, eta
+    double* scale2; // exp(-xi dt / 2) for step two
+    double dof, kT, tau, dt;
+    unsigned int* counter;
+    double* partials;
+    };
+
+template<bool CHECK, bool NVE, bool MTTK>
+__global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
+                           const float* __restrict__ accel, int* __restrict__ image,
+                           unsigned int N, gb_box box, float dt, float scale,
+                           const double* __restrict__ d_scale, StepOneCheck chk, MttkStep mk)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    bool moved = false;
+    __shared__ float s_mttk;
+    if (MTTK)
+        {
+        // exp(-xi dt / 2) of the current xi (hoomd/md/Thermostat.h:148-153), once per block
+        if (threadIdx.x == 0)
+            s_mttk = (float)exp(-(1.0 / 2.0) * mk.state[0] * mk.dt);
+        __syncthreads();
+        }
+    double ke = 0.0;
+    if (j < N)
+        {
+        const float s = MTTK ? s_mttk : ((!NVE && d_scale) ? (float)*d_scale : scale);
+        float4 v = vel[j];
+        float4 p = pos[j];
+        const float ax = accel[3 * (size_t)j], ay = accel[3 * (size_t)j + 1],
+                    az = accel[3 * (size_t)j + 2];
+        if (NVE)
+            {
+            // x += v dt + (1/2) a dt^2 ; v += (1/2) a dt   (TwoStepNVEGPU.cu:68-98,
+            // TwoStepLangevin.cc:57-81)
+            p.x = fadd(p.x, fadd(fmul(v.x, dt), fmul(fmul(fmul(0.5f, ax), dt), dt)));
+            p.y = fadd(p.y, fadd(fmul(v.y, dt), fmul(fmul(fmul(0.5f, ay), dt), dt)));
+            p.z = fadd(p.z, fadd(fmul(v.z, dt), fmul(fmul(fmul(0.5f, az), dt), dt)));
+            v.x = fadd(v.x, fmul(fmul(0.5f, ax), dt));
+            v.y = fadd(v.y, fmul(fmul(0.5f, ay), dt));
+            v.z = fadd(v.z, fmul(fmul(0.5f, az), dt));
+            }
+        else
+            {
+            // v = v + (1/2) a dt ; v *= s ; x += dt v   (TwoStepConstantVolume.cc:37-55)
+            v.x = fadd(v.x, fmul(fmul(0.5f, ax), dt));
+            v.y = fadd(v.y, fmul(fmul(0.5f, ay), dt));
+            v.z = fadd(v.z, fmul(fmul(0.5f, az), dt));
+            v.x = fmul(v.x, s);
+            v.y = fmul(v.y, s);
+            v.z = fmul(v.z, s);
+            p.x = fadd(p.x, fmul(dt, v.x));
+            p.y = fadd(p.y, fmul(dt, v.y));
+            p.z = fadd(p.z, fmul(dt, v.z));
+            }
+        int ix = 0, iy = 0, iz = 0;
+        wrap(box, p.x, p.y, p.z, ix, iy, iz);
+        if (ix | iy | iz)
+            {
+            image[3 * (size_t)j] += ix;
+            image[3 * (size_t)j + 1] += iy;
+            image[3 * (size_t)j + 2] += iz;
+            }
+        vel[j] = v;
+        pos[j] = p;
+        if (MTTK)
+            ke = (double)v.w
+                 * ((double)v.x * (double)v.x + (double)v.y * (double)v.y
+                    + (double)v.z * (double)v.z);
+        if (CHECK)
+            {
+            // hoomd/md/NeighborListGPU.cu:42-83 with lambda = 1 (fixed box)
+            const float4 lp = chk.last_pos[j];
+            float dx = fsub(p.x, lp.x), dy = fsub(p.y, lp.y), dz = fsub(p.z, lp.z);
+            min_image(box, dx, dy, dz);
+            const float rmin = chk.rcut_max[__float_as_uint(p.w)];
+            const float rmax = fadd(rmin, chk.r_buff);
+            const float delta_max = fmul(fsub(rmax, rmin), 0.5f);
+            const float maxsq = (delta_max > 0.0f) ? fmul(delta_max, delta_max) : 0.0f;
+            moved = dot3(dx, dy, dz) >= maxsq;
+            }
+        }
+    if (CHECK && __any_sync(0xffffffffu, moved) && (threadIdx.x % 32) == 0)
+        *chk.rebuild = 1u;
+    if (MTTK)
+        {
+        // advanceThermostat (hoomd/md/Thermostat.h:162-177) on the half-step kinetic energy
+        double b = 0.0, c = 0.0;
+        if (reduce3_last(ke, b, c, mk.counter, mk.partials) && threadIdx.x == 0)
+            {
+            const double T_cur = 2.0 * (0.5 * ke) / mk.dof;
+            const double drive = (1.0 / 2.0) * mk.dt / mk.tau / mk.tau * (T_cur / mk.kT - 1.0);
+            const double xi_prime = mk.state[0] + drive;
+            const double xi = xi_prime + drive;
+            mk.state[0] = xi;
+            mk.state[1] += xi_prime * mk.dt;
+            *mk.scale2 = exp(-(1.0 / 2.0) * xi * mk.dt);
+            }
+        }
+    }
+
+__global__ void k_step_two(float4* __restrict__ vel, float* __restrict__ accel,
+                           const float4* __restrict__ net_force, unsigned int N, float dt,
+                           float scale, const double* __restrict__ d_scale)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N)
+        return;
+    const float s = d_scale ? (float)*d_scale : scale;
+    float4 v = vel[j];
+    const float4 f = net_force[j];
+    const float minv = __frcp_rn(v.w);
+    const float ax = fmul(f.x, minv), ay = fmul(f.y, minv), az = fmul(f.z, minv);
+    v.x = fmul(v.x, s);
+    v.y = fmul(v.y, s);
+    v.z = fmul(v.z, s);
+    const float hdt = fmul(0.5f, dt);
+    v.x = fadd(v.x, fmul(hdt, ax));
+    v.y = fadd(v.y, fmul(hdt, ay));
+    v.z = fadd(v.z, fmul(hdt, az));
+    vel[j] = v;
+    accel[3 * (size_t)j] = ax;
+    accel[3 * (size_t)j + 1] = ay;
+    accel[3 * (size_t)j + 2] = az;
+    }
+
 __global__ void k_thermo(const float4* __restrict__ vel, const float4* __restrict__ force,
                          const float* __restrict__ virial, size_t pitch, unsigned int N,
                          unsigned int* counter, double* partials, double* out)
@@ -213,6 +251,31 @@ __global__ void k_bussi(const double* d_ke, double dof, double dt, double tau, d
     {
     if (threadIdx.x == 0 && blockIdx.x == 0)
         *d_factor = bussi_factor_d(*d_ke, dof, dt, tau, kT, timestep, seed, instance_id);
+    }
+
+__global__ void k_berendsen(const double* d_ke, double dof, double dt, double tau, double kT,
+                            double* d_factor, uint32_t* d_status)
+    {
+    if (threadIdx.x != 0 || blockIdx.x != 0)
+        return;
+    const double K = *d_ke;
+    if (dof != 0.0 && K <= 0.0)
+        {
+        atomicOr(d_status, 2u);
+        *d_factor = 1.0;
+        return;
+        }
+    *d_factor = berendsen_factor_d(K, dof, dt, tau, kT);
+    }
+
+__global__ void k_normal_draw(uint8_t id, uint64_t timestep, uint16_t seed, uint32_t counter,
+                              double sigma, double* out)
+    {
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        {
+        Philox rng(id, timestep, seed, counter);
+        *out = normal_d(rng) * sigma + 0.0;
+        }
     }
 
 // hoomd/ParticleGroup.cc:719-746: velocities from NormalDistribution<float>(sqrt(kT/m)) with
@@ -311,9 +374,9 @@ extern "C"
         if (N == 0)
             return GB_OK;
         StepOneCheck none {nullptr, nullptr, 0.0f, nullptr};
-        k_step_one<false, false><<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
+        k_step_one<false, false, false><<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
             reinterpret_cast<float4*>(d_pos), reinterpret_cast<float4*>(d_vel), d_accel, d_image,
-            N, *box, dt, scale, d_scale, none);
+            N, *box, dt, scale, d_scale, none, MttkStep {});
         return check_launch("gb_cv_step_one");
         }
 
@@ -329,12 +392,33 @@ extern "C"
         StepOneCheck chk {reinterpret_cast<const float4*>(a->d_last_pos), a->d_rcut_max,
                           a->r_buff, a->d_rebuild};
         cudaStream_t s = (cudaStream_t)stream;
-        auto kern = a->d_last_pos ? (a->nve_order ? k_step_one<true, true> : k_step_one<true, false>)
-                                  : (a->nve_order ? k_step_one<false, true>
-                                                  : k_step_one<false, false>);
+        const bool mttk = a->d_mttk_state != nullptr;
+        GB_REQUIRE(!mttk || (a->d_mttk_scale2 && a->d_mttk_scratch && !a->nve_order),
+                   "gb_md_step_one: MTTK needs the step-two factor, scratch and the "
+                   "ConstantVolume order");
+        MttkStep mk {};
+        if (mttk)
+            {
+            mk.state = a->d_mttk_state;
+            mk.scale2 = a->d_mttk_scale2;
+            mk.dof = a->mttk_dof;
+            mk.kT = a->mttk_kT;
+            mk.tau = a->mttk_tau;
+            mk.dt = (double)a->dt;
+            mk.counter = reinterpret_cast<unsigned int*>(a->d_mttk_scratch);
+            mk.partials
+                = reinterpret_cast<double*>(reinterpret_cast<char*>(a->d_mttk_scratch) + 256);
+            }
+        auto kern = a->d_last_pos
+                        ? (mttk ? k_step_one<true, false, true>
+                                : (a->nve_order ? k_step_one<true, true, false>
+                                                : k_step_one<true, false, false>))
+                        : (mttk ? k_step_one<false, false, true>
+                                : (a->nve_order ? k_step_one<false, true, false>
+                                                : k_step_one<false, false, false>));
         kern<<<div_up(a->N, 256), 256, 0, s>>>(
             reinterpret_cast<float4*>(a->d_pos), reinterpret_cast<float4*>(a->d_vel), a->d_accel,
-            a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk);
+            a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk, mk);
         return check_launch("gb_md_step_one");
         }
 
@@ -444,6 +528,25 @@ extern "C"
             d_timestep, count, dof, seed, instance_id, reinterpret_cast<double2*>(d_ring),
             ring_size);
         return check_launch("gb_bussi_draws");
+        }
+
+    int gb_berendsen_factor(const double* d_ke, double dof, double dt, double tau, double kT,
+                            double* d_factor, uint32_t* d_status, void* stream)
+        {
+        GB_REQUIRE(d_ke && d_factor && d_status, "gb_berendsen_factor: null argument");
+        GB_REQUIRE(tau > 0.0, "gb_berendsen_factor: tau must be positive");
+        k_berendsen<<<1, 32, 0, (cudaStream_t)stream>>>(d_ke, dof, dt, tau, kT, d_factor,
+                                                        d_status);
+        return check_launch("gb_berendsen_factor");
+        }
+
+    int gb_normal_draw(uint8_t id, uint64_t timestep, uint16_t seed, uint32_t counter,
+                       double sigma, double* d_out, void* stream)
+        {
+        GB_REQUIRE(d_out, "gb_normal_draw: null argument");
+        k_normal_draw<<<1, 32, 0, (cudaStream_t)stream>>>(id, timestep, seed, counter, sigma,
+                                                          d_out);
+        return check_launch("gb_normal_draw");
         }
 
     int gb_thermalize(float* d_vel, const uint32_t* d_tag, unsigned int N, double kT,

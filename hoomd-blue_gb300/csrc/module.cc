@@ -211,6 +211,12 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setBussi", &Integrator::set_thermostat_bussi)
         .def("setNoThermostat", &Integrator::set_thermostat_none)
         .def("setLangevin", &Integrator::set_langevin)
+        .def("setBerendsen", &Integrator::set_thermostat_berendsen)
+        .def("setMTTK", &Integrator::set_thermostat_mttk)
+        .def("getMTTKState", &Integrator::mttk_state)
+        .def("setMTTKState", &Integrator::set_mttk_state)
+        .def("thermalizeMTTK", &Integrator::thermalize_mttk)
+        .def("mttkEnergy", &Integrator::mttk_energy)
         .def_property_readonly("reservoir_energy", &Integrator::reservoir_energy)
         .def("setSorter", &Integrator::set_sorter)
         .def("setChunk", &Integrator::set_chunk)

@@ -52,6 +52,7 @@ struct FuseArgs
     float lkT;
     unsigned int ndim;
     double* d_reservoir;    // optional Langevin reservoir energy
+    int berendsen;          // draw-free Berendsen factor for the next step one into d_factor
     };
 
 template<int TPP> __device__ __forceinline__ double block_sum_d(double v, double* s_red)
@@ -167,6 +168,16 @@ __device__ inline void fuse_finish(const FuseArgs& fz, double ke, double pe, dou
         // the Langevin tally: c = sum of F_bd . v (hoomd/md/TwoStepLangevin.cc:396-412)
         if (fz.langevin && fz.d_reservoir)
             *fz.d_reservoir -= c * fz.dt_d;
+        if (fz.berendsen)
+            {
+            if (fz.dof != 0.0 && K <= 0.0)
+                {
+                atomicOr(fz.d_status, 2u);
+                *fz.d_factor = 1.0;
+                }
+            else
+                *fz.d_factor = berendsen_factor_d(K, fz.dof, fz.dt_d, fz.tau, fz.kT);
+            }
         if (fz.bussi)
             {
             const uint64_t next = *fz.d_timestep + 1;

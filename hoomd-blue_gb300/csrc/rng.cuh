@@ -195,4 +195,12 @@ __device__ inline double bussi_factor_d(double K, double dof, double dt, double 
                                    bussi_draws_d(dof, timestep, seed, instance_id));
     }
 
+// BerendsenThermostat::getRescalingFactorsOne (hoomd/md/Thermostat.h:469-489), translational:
+// sqrt(1 + dt / tau (kT / T - 1)) with T = 2 K / dof.
+__device__ inline double berendsen_factor_d(double K, double dof, double dt, double tau, double kT)
+    {
+    const double T_cur = 2.0 * K / dof;
+    return sqrt(1.0 + dt / tau * (kT / T_cur - 1.0));
+    }
+
 } // namespace gb

@@ -57,7 +57,9 @@ class StepOneArgs(ctypes.Structure):
     _fields_ = [("d_pos", c_void), ("d_vel", c_void), ("d_accel", c_void), ("d_image", c_void),
                 ("N", c_uint), ("box", Box), ("dt", c_float), ("scale", c_float),
                 ("d_scale", c_void), ("d_last_pos", c_void), ("d_rcut_max", c_void),
-                ("r_buff", c_float), ("d_rebuild", c_void), ("nve_order", c_int)]
+                ("r_buff", c_float), ("d_rebuild", c_void), ("nve_order", c_int),
+                ("d_mttk_state", c_void), ("d_mttk_scale2", c_void), ("mttk_dof", c_double),
+                ("mttk_kT", c_double), ("mttk_tau", c_double), ("d_mttk_scratch", c_void)]
 
 
 class StepFuse(ctypes.Structure):
@@ -68,7 +70,7 @@ class StepFuse(ctypes.Structure):
                 ("d_rebuild_reset", c_void), ("d_bussi_ring", c_void),
                 ("bussi_ring_size", c_uint), ("langevin", c_int), ("d_tag", c_void),
                 ("d_pos", c_void), ("d_gamma", c_void), ("langevin_kT", c_float),
-                ("ndim", ctypes.c_uint32), ("d_reservoir", c_void)]
+                ("ndim", ctypes.c_uint32), ("d_reservoir", c_void), ("berendsen", c_int)]
 
 
 class RadialParam(ctypes.Structure):
@@ -111,6 +113,11 @@ _PROTOS = {
     "gb_thermalize": (c_int, [c_void, c_void, c_uint, c_double, c_u64, ctypes.c_uint16, c_uint,
                               c_void, c_void]),
     "gb_md_step_one": (c_int, [_P(StepOneArgs), c_void]),
+    "gb_abi_struct_sizes": (c_uint, [_P(c_size), c_uint]),
+    "gb_berendsen_factor": (c_int, [c_void, c_double, c_double, c_double, c_double, c_void, c_void,
+                                    c_void]),
+    "gb_normal_draw": (c_int, [ctypes.c_uint8, c_u64, ctypes.c_uint16, ctypes.c_uint32, c_double,
+                               c_void, c_void]),
     "gb_langevin_step_two": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_uint,
                                      c_float, c_float, ctypes.c_uint32, ctypes.c_uint16, c_void,
                                      c_void, c_void, c_void, c_void]),
@@ -157,8 +164,22 @@ def load():
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        check_struct_sizes(lib)
         _lib = lib
     return _lib
+
+
+def check_struct_sizes(lib):
+    """Refuse a library whose argument structs differ in size from the mirrors here: a struct
+    passed short would have the library read fields past its end."""
+    mirrors = [Box, CellListArgs, NlistArgs, PairArgs, RadialParam, StepOneArgs, StepFuse,
+               MlpForceArgs]
+    sizes = (c_size * 10)()
+    lib.gb_abi_struct_sizes(sizes, 10)
+    bad = [(m.__name__, ctypes.sizeof(m), sizes[k]) for k, m in enumerate(mirrors)
+           if ctypes.sizeof(m) != sizes[k]]
+    if bad:
+        raise RuntimeError(f"C-ABI struct mirrors differ from the library: {bad}")
 
 
 def declared_functions(header=HEADER):

@@ -36,6 +36,8 @@ class ConstantVolume(Method):
 
     def _attach(self, integ, state=None):
         self._cpp_integ = integ
+        if self._thermostat is not None and state is not None:
+            self._thermostat._simulation = state._simulation
         self._apply(integ)
 
 

@@ -51,6 +51,12 @@ typedef struct gb_box
     } gb_box;
 
 /* BoxDim(Lx, Ly, Lz) + setTiltFactors + setPeriodic (hoomd/BoxDim.h:103-180), host only. */
+/* sizeof of the argument structs, in this order: gb_box, gb_cell_list_args, gb_nlist_args,
+ * gb_pair_args, gb_radial_param, gb_step_one_args, gb_step_fuse, gb_mlp_force_args, gb_replica,
+ * gb_replica_batch. Writes min(n, 10) values and returns 10, so a binding can check its own
+ * mirror of each struct before it passes one. */
+unsigned int gb_abi_struct_sizes(size_t* out, unsigned int n);
+
 int gb_box_make(const double L[3], double xy, double xz, double yz, const int periodic[3],
                 gb_box* out);
 
@@ -357,6 +363,15 @@ typedef struct gb_step_one_args
        (x += v dt + a dt^2/2, then v += a dt/2; hoomd/md/TwoStepNVEGPU.cu:68-98), which the
        Langevin method uses (hoomd/md/TwoStepLangevin.cc:57-81); scale is ignored */
     int nve_order;
+    /* MTTK (Nose-Hoover) thermostat, hoomd/md/Thermostat.h:119-212 with the call order of
+       hoomd/md/TwoStepConstantVolume.cc:7-80, 205-210: when d_mttk_state is given, step one scales
+       the half-step velocities by exp(-xi dt/2) (not by scale / d_scale), reduces their kinetic
+       energy in FP64, advances (xi, eta) with T = 2 KE / mttk_dof against mttk_kT, and writes
+       exp(-xi dt/2) of the advanced xi to *d_mttk_scale2 for step two */
+    double* d_mttk_state;       /* [2]: xi, eta */
+    double* d_mttk_scale2;
+    double mttk_dof, mttk_kT, mttk_tau;
+    void* d_mttk_scratch;       /* gb_thermo_scratch_bytes(N), zeroed once before first use */
     } gb_step_one_args;
 
 int gb_md_step_one(const gb_step_one_args* args, void* stream);
@@ -392,7 +407,21 @@ typedef struct gb_step_fuse
     float langevin_kT;
     uint32_t ndim;              /* 2: no random or drag force along z */
     double* d_reservoir;        /* optional: reservoir energy, reduced by dt * sum(F_bd . v) */
+    /* Berendsen thermostat (hoomd/md/Thermostat.h:450-490): write the next step one's factor
+       sqrt(1 + dt/tau (kT / T - 1)), T = 2 KE / dof, into d_factor; bit 1 of d_status when the
+       kinetic energy is zero. Excludes bussi and langevin */
+    int berendsen;
     } gb_step_fuse;
+
+/* The Berendsen factor from a kinetic energy on the device (the first step of a run). */
+int gb_berendsen_factor(const double* d_ke, double dof, double dt, double tau, double kT,
+                        double* d_factor, uint32_t* d_status, void* stream);
+
+/* One NormalDistribution<double>(sigma) draw (hoomd/RandomNumbers.h:346-372) from Philox with
+ * Seed(id, timestep, seed), Counter(counter), into *d_out: the MTTK thermostat's
+ * thermalize_dof (hoomd/md/Thermostat.h:273-300, id 28). */
+int gb_normal_draw(uint8_t id, uint64_t timestep, uint16_t seed, uint32_t counter, double sigma,
+                   double* d_out, void* stream);
 
 /* Langevin step two on its own (the unfused path: several forces, the virial, the MLP
  * surrogate): a = (F_net + F_bd) / m, v += a dt/2 for all N particles at timestep *d_timestep

@@ -1104,6 +1104,8 @@ template<class R> struct Sim
     // integrator
     R dt = 0;
     bool langevin = false;
+    int thermostat = 0; // 0: none or Bussi (bussi flag), 2: Berendsen, 3: MTTK
+    double xi = 0, eta = 0;
     std::vector<R> gamma;
     R langevin_T = 0;
     double reservoir = 0;
@@ -1322,6 +1324,45 @@ template<class R> struct Sim
                                                tags.data(), force.data(), gamma.data(),
                                                langevin_T, dt, seed, timestep, ndim);
             reservoir -= e * double(dt);
+            timestep++;
+            return true;
+            }
+        if (thermostat == 2)
+            {
+            // BerendsenThermostat::getRescalingFactorsOne (hoomd/md/Thermostat.h:469-489)
+            double K = kinetic_energy(N, vel.data());
+            if (K == 0.0)
+                {
+                error = "Berendsen thermostat requires non-zero initial temperatures";
+                return false;
+                }
+            double T_cur = 2.0 * K / dof();
+            R s = R(std::sqrt(1.0 + double(dt) / tau * (kT / T_cur - 1.0)));
+            cv_step_one(N, pos.data(), vel.data(), accel.data(), image.data(), box, dt, s,
+                        nthreads);
+            if (!compute_forces())
+                return false;
+            cv_step_two(N, vel.data(), accel.data(), force.data(), dt, R(1.0), nthreads);
+            timestep++;
+            return true;
+            }
+        if (thermostat == 3)
+            {
+            // MTTKThermostat (hoomd/md/Thermostat.h:148-177) in TwoStepConstantVolume's order:
+            // scale, advance (xi, eta) on the half-step temperature, forces, scale
+            const double ddt = double(dt);
+            R s1 = R(std::exp(-(1.0 / 2.0) * xi * ddt));
+            cv_step_one(N, pos.data(), vel.data(), accel.data(), image.data(), box, dt, s1,
+                        nthreads);
+            double T_cur = 2.0 * kinetic_energy(N, vel.data()) / dof();
+            double drive = (1.0 / 2.0) * ddt / tau / tau * (T_cur / kT - 1.0);
+            double xi_prime = xi + drive;
+            xi = xi_prime + drive;
+            eta += xi_prime * ddt;
+            if (!compute_forces())
+                return false;
+            R s2 = R(std::exp(-(1.0 / 2.0) * xi * ddt));
+            cv_step_two(N, vel.data(), accel.data(), force.data(), dt, s2, nthreads);
             timestep++;
             return true;
             }
@@ -1611,6 +1652,22 @@ using namespace orc;
         s->gamma.assign(s->ntypes, R(0));                                                          \
         for (unsigned int t = 0; t < s->ntypes; t++)                                               \
             s->gamma[t] = R(gamma[t]);                                                             \
+        }                                                                                          \
+    ORC_EXPORT void orc_sim_set_thermostat_##SUF(void* h, int kind, double kT, double tau,          \
+                                                 double xi, double eta)                            \
+        {                                                                                          \
+        auto* s = (Sim<R>*)h;                                                                      \
+        s->thermostat = kind;                                                                      \
+        s->bussi = kind == 1;                                                                      \
+        s->kT = kT;                                                                                \
+        s->tau = tau;                                                                              \
+        s->xi = xi;                                                                                \
+        s->eta = eta;                                                                              \
+        }                                                                                          \
+    ORC_EXPORT void orc_sim_mttk_##SUF(void* h, double* out2)                                      \
+        {                                                                                          \
+        out2[0] = ((Sim<R>*)h)->xi;                                                                \
+        out2[1] = ((Sim<R>*)h)->eta;                                                               \
         }                                                                                          \
     ORC_EXPORT double orc_sim_reservoir_##SUF(void* h)                                             \
         {                                                                                          \

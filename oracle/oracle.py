@@ -396,7 +396,8 @@ class Sim:
 
     def __init__(self, pos4, vel4, image3, tags, box, r_cut, r_buff, dt, kind="lj", params=None,
                  tdata=None, shift_mode=0, full=False, bussi=False, kT=1.0, tau=0.0, seed=0,
-                 timestep=0, ndim=3, prec=32, nthreads=1, periodic=(1, 1, 1), langevin=None):
+                 timestep=0, ndim=3, prec=32, nthreads=1, periodic=(1, 1, 1), langevin=None,
+                 thermostat=None, mttk_state=(0.0, 0.0)):
         R = rdtype(prec)
         self.prec = prec
         self.N = len(pos4)
@@ -422,11 +423,23 @@ class Sim:
             ctypes.c_int(int(bussi)), d(kT), d(tau), ctypes.c_uint32(seed),
             ctypes.c_uint64(timestep), ctypes.c_int(nthreads))
         self.h = ctypes.c_void_p(self.h)
+        if thermostat is not None:
+            # "berendsen" or "mttk" with kT and tau (ConstantVolume thermostats)
+            kind = {"bussi": 1, "berendsen": 2, "mttk": 3}[thermostat]
+            getattr(L, f"orc_sim_set_thermostat_{self._s}")(self.h, ctypes.c_int(kind), d(kT),
+                                                             d(tau), d(mttk_state[0]),
+                                                             d(mttk_state[1]))
         if langevin is not None:
             # langevin = per-type drag coefficients; kT is the bath temperature
             g = np.ascontiguousarray(langevin, np.float64)
             self._keep.append(g)
             getattr(L, f"orc_sim_set_langevin_{self._s}")(self.h, d(kT), ptr(g))
+
+    @property
+    def mttk_state(self):
+        out = np.zeros(2, np.float64)
+        getattr(lib(), f"orc_sim_mttk_{self._s}")(self.h, ptr(out))
+        return tuple(out)
 
     @property
     def reservoir_energy(self):
