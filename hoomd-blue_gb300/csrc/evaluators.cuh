@@ -176,6 +176,9 @@ struct EvalRadial
             eval(p, sqrtf(rcutsq), V, F);
             p.aux = F;
             }
+        else if (p.kind == GB_RADIAL_DPD_CONSERVATIVE || p.kind == GB_RADIAL_FOURIER
+                 || p.kind == GB_RADIAL_REACTION_FIELD)
+            p.aux = sqrtf(rcutsq); // r_cut enters the functional form
         }
     float rsq, rcutsq;
     param_type p;
@@ -301,6 +304,102 @@ struct EvalRadial
                 const float c = cosf(arg), s = sinf(arg);
                 V = a + b * c;
                 F = (v[2] * a + v[3] * b * c) / r + v[4] * b * s;
+                break;
+                }
+            case GB_RADIAL_DPD_CONSERVATIVE:
+                {
+                const float rc = p.aux;
+                V = v[0] * (rc - r) - 0.5f * v[0] / rc * (rc * rc - r * r);
+                F = v[0] * (1.0f - r / rc);
+                break;
+                }
+            case GB_RADIAL_DLVO:
+                {
+                const float kappa = v[0], Z = v[1], A = v[2], a1 = v[3], a2 = v[4];
+                if (kappa == 0.0f)
+                    {
+                    V = F = 0.0f;
+                    break;
+                    }
+                const float radsum = a1 + a2, radsub = a1 - a2, radprod = a1 * a2;
+                const float radsumsq = a1 * a1 + a2 * a2, radsubsq = a1 * a1 - a2 * a2;
+                const float r2 = r * r;
+                const float rmdsqs = r2 - radsum * radsum, rmdsqm = r2 - radsub * radsub;
+                const float rep = kappa * radprod / radsum * Z * expf(-kappa * (r - radsum));
+                const float t1 = r2 * r2 + radsubsq * radsubsq - 2.0f * r2 * radsumsq;
+                const float atr_divr = -32.0f * A / 3.0f * radprod * radprod * radprod / (t1 * t1);
+                F = rep + atr_divr * r;
+                V = rep / kappa - radprod / rmdsqs * A / 3.0f - radprod / rmdsqm * A / 3.0f
+                    - logf(rmdsqs / rmdsqm) * A / 6.0f;
+                break;
+                }
+            case GB_RADIAL_FOURIER:
+                {
+                const float rc = p.aux;
+                const float k = 3.14159265358979f / rc;
+                const float x = r * k;
+                const float ir = 1.0f / r, ir2 = ir * ir, ir3 = ir * ir2;
+                const float ir12 = ir3 * ir3 * ir3 * ir3;
+                // the n = 1 coefficients follow from V(r_c) = 0 and V'(r_c) = 0
+                float a1s = 0.0f, b1s = 0.0f;
+                for (int n = 2; n < 5; n++)
+                    {
+                    const float sgn = (n & 1) ? -1.0f : 1.0f;
+                    a1s += sgn * v[n - 2];
+                    b1s += (float)n * sgn * v[n + 1];
+                    }
+                float s, c;
+                sincosf(x, &s, &c);
+                float four = a1s * c + b1s * s;
+                float dfour = a1s * s - b1s * c; // -(d/dx) of the n = 1 terms
+                for (int n = 2; n < 5; n++)
+                    {
+                    sincosf((float)n * x, &s, &c);
+                    four += v[n - 2] * c + v[n + 1] * s;
+                    dfour += (float)n * (v[n - 2] * s - v[n + 1] * c);
+                    }
+                V = ir12 + ir2 * four;
+                F = 12.0f * ir12 * ir + ir2 * k * dfour + 2.0f * ir3 * four;
+                break;
+                }
+            case GB_RADIAL_MOLIERE:
+            case GB_RADIAL_ZBL:
+                {
+                const float Zsq = v[0] * v[1], aF = v[2];
+                if (Zsq == 0.0f || aF == 0.0f)
+                    {
+                    V = F = 0.0f;
+                    break;
+                    }
+                const float x = r / aF;
+                float e = 0.0f, de = 0.0f;
+                if (p.kind == GB_RADIAL_MOLIERE)
+                    {
+                    const float e1 = 0.35f * expf(-0.3f * x), e2 = 0.55f * expf(-1.2f * x),
+                                e3 = 0.1f * expf(-6.0f * x);
+                    e = e1 + e2 + e3;
+                    de = 0.3f * e1 + 1.2f * e2 + 6.0f * e3;
+                    }
+                else
+                    {
+                    const float e1 = 0.1818f * expf(-3.2f * x), e2 = 0.5099f * expf(-0.9423f * x),
+                                e3 = 0.2802f * expf(-0.4029f * x),
+                                e4 = 0.02817f * expf(-0.2016f * x);
+                    e = e1 + e2 + e3 + e4;
+                    de = 3.2f * e1 + 0.9423f * e2 + 0.4029f * e3 + 0.2016f * e4;
+                    }
+                V = Zsq / r * e;
+                F = Zsq / (r * r) * e + Zsq / r * de / aF;
+                break;
+                }
+            case GB_RADIAL_REACTION_FIELD:
+                {
+                const float eps = v[0], epsrf = v[1], rc = p.aux;
+                const float rc3inv = 1.0f / (rc * rc * rc);
+                const float eps_fac = epsrf == 0.0f ? 0.5f * rc3inv
+                                                    : (epsrf - 1.0f) / (2.0f * epsrf + 1.0f) * rc3inv;
+                V = eps * (1.0f / r + eps_fac * r * r);
+                F = eps * (1.0f / (r * r) - 2.0f * eps_fac * r);
                 break;
                 }
             default: // GB_RADIAL_TWF

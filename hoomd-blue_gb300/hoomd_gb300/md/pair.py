@@ -239,3 +239,51 @@ OPP = _radial("OPP", 12, ("C1", "C2", "eta1", "eta2", "k", "phi"),
               "Oscillating pair potential (EvaluatorPairOPP.h).")
 TWF = _radial("TWF", 13, ("sigma", "epsilon", "alpha"),
               "Ten Wolde-Frenkel (EvaluatorPairTWF.h); infinite for r <= sigma.")
+DPDConservative = _radial("DPDConservative", 14, ("A",),
+                          "Conservative DPD force (EvaluatorPairDPDThermoDPD.h): "
+                          "A (r_c - r) - A (r_c^2 - r^2) / (2 r_c).", ("none",))
+DLVO = _radial("DLVO", 15, ("kappa", "Z", "A", "a1", "a2"),
+               "DLVO colloid force (EvaluatorPairDLVO.h): screened repulsion and sphere-sphere "
+               "van der Waals attraction of radii a1, a2.", ("none", "shift"))
+Moliere = _radial("Moliere", 17, ("qi", "qj", "aF"),
+                  "Moliere screened Coulomb (EvaluatorPairMoliere.h).")
+ZBL = _radial("ZBL", 18, ("qi", "qj", "aF"),
+              "Ziegler-Biersack-Littmark screened Coulomb (EvaluatorPairZBL.h).", ("none",))
+
+
+class Fourier(_Radial):
+    """Fourier pair force (EvaluatorPairFourier.h): 1/r^12 + sum over n = 1..4 of
+    [a_n cos(n pi r / r_c) + b_n sin(n pi r / r_c)] / r^2, with ``a`` and ``b`` the three
+    coefficients of n = 2, 3, 4 (those of n = 1 make the force and energy vanish at r_c)."""
+
+    _radial_kind = 16
+    _accepted_modes = ("none", "xplor")
+
+    def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
+        super().__init__(nlist, default_r_cut, default_r_on, mode)
+        self.params = TypePairDict(validator=dict_validator(("a", "b"), arrays=("a", "b")))
+
+    def _set_pair_params(self, cpp, i, j, v):
+        a, b = np.asarray(v["a"], np.float64), np.asarray(v["b"], np.float64)
+        if a.shape != (3,) or b.shape != (3,):
+            raise ValueError("Fourier: a and b are three coefficients each")
+        cpp.setParamsRadial(i, j, self._radial_kind, [float(x) for x in (*a, *b)])
+
+
+class ReactionField(_Radial):
+    """Reaction-field electrostatics (EvaluatorPairReactionField.h) with unit charges
+    (``use_charge=False``): eps [1/r + (eps_rf - 1)/(2 eps_rf + 1) r^2 / r_c^3]; eps_rf = 0
+    stands for an infinite dielectric."""
+
+    _radial_kind = 19
+
+    def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
+        super().__init__(nlist, default_r_cut, default_r_on, mode)
+        self.params = TypePairDict(validator=dict_validator(("epsilon", "eps_rf"),
+                                                            optional={"use_charge": False}))
+
+    def _set_pair_params(self, cpp, i, j, v):
+        if v.get("use_charge"):
+            raise NotImplementedError("ReactionField with use_charge=True needs per-particle "
+                                      "charges, which this pair path does not carry")
+        cpp.setParamsRadial(i, j, self._radial_kind, [float(v["epsilon"]), float(v["eps_rf"])])

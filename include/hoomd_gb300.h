@@ -247,7 +247,15 @@ int gb_pair_forces_example(const gb_pair_args* args, const gb_example_param* d_p
  *   EXPANDED_GAUSS  epsilon, sigma, delta eps exp(-(r-delta)^2 / 2 sigma^2) (EvaluatorPairExpandedGaussian.h)
  *   OPP         C1, C2, eta1, eta2, k, phi  C1 r^-eta1 + C2 r^-eta2 cos(k r - phi) (EvaluatorPairOPP.h)
  *   TWF         sigma, epsilon, alpha     4 eps/alpha^2 [s^-6 - alpha s^-3], s = (r/sigma)^2 - 1 (EvaluatorPairTWF.h)
- * Shift mode 1 subtracts the energy at r_cut; XPLOR smoothing as for LJ. */
+ *   DPD_CONSERVATIVE  A                   A (r_c - r) - A (r_c^2 - r^2) / (2 r_c)  (EvaluatorPairDPDThermoDPD.h:190-208)
+ *   DLVO        kappa, Z, A, a1, a2       screened repulsion + sphere-sphere van der Waals (EvaluatorPairDLVO.h:120-169)
+ *   FOURIER     a1, a2, a3, b1, b2, b3    1/r^12 + sum_n [a_n cos(n pi r / r_c) + b_n sin(n pi r / r_c)] / r^2 (EvaluatorPairFourier.h:135-180)
+ *   MOLIERE     qi, qj, aF                qi qj / r (0.35 e^{-0.3 r/aF} + 0.55 e^{-1.2 r/aF} + 0.1 e^{-6 r/aF}) (EvaluatorPairMoliere.h:112-148)
+ *   ZBL         qi, qj, aF                the four-exponential ZBL screening (EvaluatorPairZBL.h:95-123)
+ *   REACTION_FIELD  epsilon, eps_rf       eps [1/r + (eps_rf - 1) / (2 eps_rf + 1) r^2 / r_c^3], charges 1 (EvaluatorPairReactionField.h:122-151)
+ * Shift mode 1 subtracts the energy at r_cut; XPLOR smoothing as for LJ. DLVO, MOLIERE, ZBL and
+ * REACTION_FIELD give zero force where the reference's evaluators return false (kappa, qi qj,
+ * aF or epsilon zero). */
 typedef enum gb_radial_kind
     {
     GB_RADIAL_GAUSS = 0,
@@ -264,14 +272,21 @@ typedef enum gb_radial_kind
     GB_RADIAL_EXPANDED_GAUSS = 11,
     GB_RADIAL_OPP = 12,
     GB_RADIAL_TWF = 13,
-    GB_RADIAL_KINDS = 14
+    GB_RADIAL_DPD_CONSERVATIVE = 14,
+    GB_RADIAL_DLVO = 15,
+    GB_RADIAL_FOURIER = 16,
+    GB_RADIAL_MOLIERE = 17,
+    GB_RADIAL_ZBL = 18,
+    GB_RADIAL_REACTION_FIELD = 19,
+    GB_RADIAL_KINDS = 20
     } gb_radial_kind;
 
 typedef struct gb_radial_param
     {
     float v[6];
     uint32_t kind;      /* gb_radial_kind, the same for every type pair of one force */
-    float aux;          /* 0 (the kernels fill it per type pair: F(r_cut) of FORCE_SHIFTED_LJ) */
+    float aux;          /* 0 (the kernels fill it per type pair: F(r_cut) of FORCE_SHIFTED_LJ,
+                           the Mie prefactor, or r_cut) */
     } gb_radial_param;
 
 int gb_pair_forces_radial(const gb_pair_args* args, const gb_radial_param* d_params,
