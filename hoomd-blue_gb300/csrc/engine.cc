@@ -372,6 +372,7 @@ void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count
     a.d_r_listsq = d_r_listsq.get();
     a.ntypes = pd.ntypes;
     a.d_gate = d_gate;
+    a.nlist_capacity = nlist.size();
     check(gb_nlist_build_binned(&a, s), "gb_nlist_build_binned");
     if (ex_pitch > 0)
         check(gb_nlist_filter(nlist.get(), n_neigh.get(), nullptr, stride, 4, pd.N, n_ex.get(),

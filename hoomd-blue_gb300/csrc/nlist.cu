@@ -14,6 +14,7 @@
 // column-major layout nlist[k * stride + i] (coalesced across particles in SFC order) or the
 // reference's flat head-list layout.
 #include <cstdint>
+#include <type_traits>
 
 #include "gb_device.cuh"
 #include "gb_host.h"
@@ -548,6 +549,237 @@ __global__ void __launch_bounds__(TILE_WARPS_MAX * 32)
         }
     }
 
+// Lane-per-particle tiled build (same cases as k_nlist_tile): one warp per cell, lane l holds own
+// particle ob + l in registers. The nine cells of each stencil plane are staged in shared memory
+// as structure-of-arrays (x, y, z, index[, type]), every cell starting at an even slot, so two
+// consecutive candidates load as one 8-byte packed pair. Every lane tests its own particle
+// against the staged candidates two at a time in packed FP32 pairs (each half rounds as the
+// scalar minImage sequence, so the decisions are bit-identical) and writes its hits straight into
+// its own row; a cell's exact image shift is applied only when the stencil wraps there (it is
+// zero otherwise, and x - 0 is exact). Hits come in the order (plane, cell, slot) of the
+// warp-cooperative kernel above, so the lists are the same.
+constexpr int LANE_WARPS = 4;
+
+__host__ __device__ inline unsigned int lane_cap(unsigned int Nmax_cell)
+    {
+    return 9u * (Nmax_cell + 1u) + 1u & ~1u; // even-rounded cells, even total
+    }
+
+template<bool MULTI, int LAYOUT, bool ORTHO>
+__global__ void __launch_bounds__(LANE_WARPS * 32)
+    k_nlist_lane(unsigned int* __restrict__ nlist, unsigned int* __restrict__ n_neigh,
+                 float4* __restrict__ last_pos, unsigned int* __restrict__ cond, uint64_t stride,
+                 const unsigned int* __restrict__ Nmax_t,
+                 const unsigned int* __restrict__ cell_size, const float4* __restrict__ xyzf,
+                 const unsigned int* __restrict__ cell_type, uint3 dim, unsigned int ncell,
+                 unsigned int Nmax_cell, gb_box box, const float* __restrict__ r_cut,
+                 const float* __restrict__ r_listsq, unsigned int ntypes, const uint32_t* gate)
+    {
+    if (gate && *gate == 0)
+        return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wpb = blockDim.x / 32;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    float* s_tab = reinterpret_cast<float*>(smem);
+    const size_t tab_bytes = MULTI ? ((2 * sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
+    if (MULTI)
+        {
+        for (unsigned int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x)
+            {
+            s_tab[t] = r_cut[t];
+            s_tab[ntypes * ntypes + t] = r_listsq[t];
+            }
+        __syncthreads();
+        }
+    const unsigned int cap = lane_cap(Nmax_cell);
+    const size_t per_warp = ((size_t)cap * 4u * (MULTI ? 5u : 4u) + 15) / 16 * 16;
+    unsigned char* base = smem + tab_bytes + (size_t)warp * per_warp;
+    float* s_x = reinterpret_cast<float*>(base);
+    float* s_y = s_x + cap;
+    float* s_z = s_y + cap;
+    unsigned int* s_j = reinterpret_cast<unsigned int*>(s_z + cap);
+    unsigned int* s_t = s_j + cap;
+
+    const unsigned int cell = blockIdx.x * wpb + warp;
+    if (cell >= ncell)
+        return;
+    const int ci = cell % dim.x, cj = (cell / dim.x) % dim.y, ck = cell / (dim.x * dim.y);
+    const unsigned int csize = min(cell_size[cell], Nmax_cell);
+    if (csize == 0)
+        return;
+    const size_t row4 = (size_t)stride * 4u;
+
+    for (unsigned int ob = 0; ob < csize; ob += 32)
+        {
+        const bool active = ob + lane < csize;
+        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+        unsigned int ti = 0;
+        if (active)
+            {
+            pi = __ldg(xyzf + (size_t)cell * Nmax_cell + ob + lane);
+            if (MULTI)
+                ti = __ldg(cell_type + (size_t)cell * Nmax_cell + ob + lane);
+            }
+        const unsigned int i = __float_as_uint(pi.w);
+        const unsigned int nmax_i = active ? __ldg(Nmax_t + (MULTI ? ti : 0u)) : 0u;
+        // next free slot of this particle's row (interleaved by four: four consecutive slots, then
+        // a jump of one row of groups)
+        // (word offsets fit 32 bits: a list of 2^32 words would be 16 GB)
+        unsigned int wo = LAYOUT == 4 ? i * 4u : i;
+        const unsigned int jump = LAYOUT == 4 ? (unsigned int)row4 - 3u : (unsigned int)stride;
+        unsigned int cnt = 0;
+        auto put = [&](bool hit, unsigned int j) {
+            if (hit && cnt < nmax_i)
+                nlist[wo] = j;
+            if (hit)
+                {
+                cnt++;
+                if (LAYOUT == 4)
+                    wo += (cnt & 3u) ? 1u : jump;
+                else
+                    wo += jump;
+                }
+        };
+        // r_list^2 of the pair, or -1 (never met) for an inactive lane or a pair without r_cut
+        const float rl_single = (!MULTI && active && __ldg(r_cut) > 0.0f) ? __ldg(r_listsq) : -1.0f;
+        auto rlim = [&](unsigned int slot) -> float {
+            if (MULTI)
+                {
+                const unsigned int tp = ti * ntypes + s_t[slot];
+                return (active && s_tab[tp] > 0.0f) ? s_tab[ntypes * ntypes + tp] : -1.0f;
+                }
+            return rl_single;
+        };
+        const uint64_t px2 = f2pack(pi.x, pi.x), py2 = f2pack(pi.y, pi.y), pz2 = f2pack(pi.z, pi.z);
+
+        for (int pz = -1; pz <= 1; pz++)
+            {
+            unsigned int q_cell = 0, q_n = 0;
+            if (lane < 9)
+                {
+                const int ox = lane % 3 - 1, oy = lane / 3 - 1;
+                q_cell = (wrap_cell(ck + pz, dim.z) * dim.y + wrap_cell(cj + oy, dim.y)) * dim.x
+                         + wrap_cell(ci + ox, dim.x);
+                q_n = min(__ldg(cell_size + q_cell), Nmax_cell);
+                }
+            const unsigned int q_pad = (q_n + 1u) & ~1u;
+            unsigned int incl = q_pad;
+#pragma unroll
+            for (int o = 1; o < 16; o <<= 1)
+                {
+                const unsigned int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                    incl += y;
+                }
+            const unsigned int q_off = incl - q_pad;
+            for (int q = 0; q < 9; q++)
+                {
+                const unsigned int qc = __shfl_sync(0xffffffffu, q_cell, q);
+                const unsigned int qn = __shfl_sync(0xffffffffu, q_n, q);
+                const unsigned int qo = __shfl_sync(0xffffffffu, q_off, q);
+                for (unsigned int t = lane; t < qn; t += 32)
+                    {
+                    const float4 c = __ldg(xyzf + (size_t)qc * Nmax_cell + t);
+                    s_x[qo + t] = c.x;
+                    s_y[qo + t] = c.y;
+                    s_z[qo + t] = c.z;
+                    s_j[qo + t] = __float_as_uint(c.w);
+                    if (MULTI)
+                        s_t[qo + t] = __ldg(cell_type + (size_t)qc * Nmax_cell + t);
+                    }
+                }
+            __syncwarp();
+            for (int q = 0; q < 9; q++)
+                {
+                const unsigned int qn = __shfl_sync(0xffffffffu, q_n, q);
+                const unsigned int qo = __shfl_sync(0xffffffffu, q_off, q);
+                const int ox = q % 3 - 1, oy = q / 3 - 1;
+                // minImage's image for this cell: +1 past the high face, -1 past the low face
+                const float ix = (ci + ox >= (int)dim.x) ? 1.f : (ci + ox < 0 ? -1.f : 0.f);
+                const float iy = (cj + oy >= (int)dim.y) ? 1.f : (cj + oy < 0 ? -1.f : 0.f);
+                const float iz = (ck + pz >= (int)dim.z) ? 1.f : (ck + pz < 0 ? -1.f : 0.f);
+                const bool wrapped = ix != 0.f || iy != 0.f || iz != 0.f;
+                const float sz = fmul(box.L[2], iz), sy = fmul(box.L[1], iy), sx = fmul(box.L[0], ix);
+                const float syz = ORTHO ? 0.f : fmul(fmul(box.L[2], box.yz), iz);
+                const float sxz = ORTHO ? 0.f : fmul(fmul(box.L[2], box.xz), iz);
+                const float sxy = ORTHO ? 0.f : fmul(fmul(box.L[1], box.xy), iy);
+                // the own particle itself can only be met in the centre cell
+                auto scan = [&](auto centre_tag) {
+                constexpr bool centre = decltype(centre_tag)::value;
+                unsigned int t = 0;
+                if (ORTHO)
+                    {
+                    const uint64_t sx2 = f2pack(sx, sx), sy2 = f2pack(sy, sy), sz2 = f2pack(sz, sz);
+                    for (; t + 1 < qn; t += 2)
+                        {
+                        const unsigned int slot = qo + t;
+                        const uint64_t cx = *reinterpret_cast<const uint64_t*>(s_x + slot);
+                        const uint64_t cy = *reinterpret_cast<const uint64_t*>(s_y + slot);
+                        const uint64_t cz = *reinterpret_cast<const uint64_t*>(s_z + slot);
+                        uint64_t dx = f2sub(px2, cx), dy = f2sub(py2, cy), dz = f2sub(pz2, cz);
+                        if (wrapped)
+                            {
+                            dz = f2sub(dz, sz2);
+                            dy = f2sub(dy, sy2);
+                            dx = f2sub(dx, sx2);
+                            }
+                        const uint64_t r2
+                            = f2add(f2add(f2mul(dx, dx), f2mul(dy, dy)), f2mul(dz, dz));
+                        float rsq0, rsq1;
+                        f2unpack(r2, rsq0, rsq1);
+                        const uint2 jj = *reinterpret_cast<const uint2*>(s_j + slot);
+                        put(rsq0 <= rlim(slot) && (!centre || jj.x != i), jj.x);
+                        put(rsq1 <= rlim(slot + 1) && (!centre || jj.y != i), jj.y);
+                        }
+                    }
+                for (; t < qn; t++)
+                    {
+                    const unsigned int slot = qo + t;
+                    const unsigned int j = s_j[slot];
+                    float dx = fsub(pi.x, s_x[slot]), dy = fsub(pi.y, s_y[slot]),
+                          dz = fsub(pi.z, s_z[slot]);
+                    if (wrapped)
+                        {
+                        dz = fsub(dz, sz);
+                        if (!ORTHO)
+                            {
+                            dy = fsub(dy, syz); // tilt terms; exactly zero in an orthorhombic box
+                            dx = fsub(dx, sxz);
+                            }
+                        dy = fsub(dy, sy);
+                        if (!ORTHO)
+                            dx = fsub(dx, sxy);
+                        dx = fsub(dx, sx);
+                        }
+                    const float rsq = dot3(dx, dy, dz);
+                    put(rsq <= rlim(slot) && (!centre || j != i), j);
+                    }
+                };
+                if (pz == 0 && q == 4)
+                    scan(std::true_type {});
+                else
+                    scan(std::false_type {});
+                }
+            __syncwarp();
+            }
+        if (active)
+            {
+            n_neigh[i] = min(cnt, nmax_i);
+            if (cnt > nmax_i)
+                atomicMax(&cond[MULTI ? ti : 0u], cnt);
+            if (last_pos)
+                last_pos[i] = make_float4(pi.x, pi.y, pi.z, 0.0f);
+            }
+        }
+    }
+
+size_t lane_smem_bytes(unsigned int Nmax_cell, unsigned int ntypes, bool multi, int wpb)
+    {
+    const size_t tab = multi ? ((2 * sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
+    const size_t per_warp = ((size_t)lane_cap(Nmax_cell) * 4u * (multi ? 5u : 4u) + 15) / 16 * 16;
+    return tab + (size_t)wpb * per_warp;
+    }
+
 size_t tile_smem_bytes(unsigned int Nmax_cell, unsigned int ntypes, bool multi, int wpb)
     {
     const size_t tab = multi ? ((2 * sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
@@ -559,6 +791,24 @@ template<bool MULTI, int LAYOUT>
 bool launch_nlist_tile(const gb_nlist_args& a, unsigned int ncell, cudaStream_t s)
     {
     const bool ortho = a.box.xy == 0.0f && a.box.xz == 0.0f && a.box.yz == 0.0f;
+    if (a.nlist_capacity != 0 && a.nlist_capacity <= 0xffffffffull)
+        {
+        int wpb = LANE_WARPS;
+        size_t smem = lane_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, wpb);
+        while (smem > 96 * 1024 && wpb > 1)
+            smem = lane_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, --wpb);
+        if (smem > 200 * 1024)
+            return false;
+        auto kern = ortho ? k_nlist_lane<MULTI, LAYOUT, true> : k_nlist_lane<MULTI, LAYOUT, false>;
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<div_up(ncell, wpb), wpb * 32, smem, s>>>(
+            a.d_nlist, a.d_n_neigh, reinterpret_cast<float4*>(a.d_last_pos), a.d_conditions,
+            a.stride, a.d_Nmax, a.d_cell_size, reinterpret_cast<const float4*>(a.d_xyzf),
+            a.d_cell_type, make_uint3(a.dim[0], a.dim[1], a.dim[2]), ncell, a.Nmax_cell, a.box,
+            a.d_r_cut, a.d_r_listsq, a.ntypes, a.d_gate);
+        return true;
+        }
     int wpb = TILE_WARPS_MAX;
     size_t smem = tile_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, wpb);
     while (smem > 96 * 1024 && wpb > 1)

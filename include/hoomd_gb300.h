@@ -135,6 +135,10 @@ typedef struct gb_nlist_args
     const float* d_r_listsq;          /* [ntypes^2] (r_cut + r_buff)^2, 0 where r_cut <= 0 */
     unsigned int ntypes;
     const uint32_t* d_gate;           /* optional no-op gate, as for the cell list */
+    uint64_t nlist_capacity;          /* words allocated at d_nlist, or 0 when unknown; below 2^32
+                                         the tiled build addresses slots with 32-bit offsets
+                                         (one lane per particle), else it uses the warp-per-cell
+                                         form */
     } gb_nlist_args;
 
 int gb_nlist_build_binned(const gb_nlist_args* args, void* stream);

@@ -46,7 +46,12 @@ class GpuNlist:
     """Cell list + neighbour list through the C ABI, with the reference's overflow retries."""
 
     def __init__(self, pos4, box6, r_cut, r_buff, layout="col", deterministic=False, ndim=3):
+        """layout: "col", "col4" (column-major, interleaved by 4), "flat" (head list); a trailing
+        "w" ("colw", "col4w") withholds the list capacity, which selects the warp-per-cell form
+        of the tiled build instead of the lane-per-particle one."""
         L = abi.load()
+        self.warp_build = layout.endswith("w")
+        layout = layout[:-1] if self.warp_build else layout
         self.N = N = len(pos4)
         self.box = abi.make_box(box6[:3], box6[3:6])
         self.pos = dev(np.asarray(pos4, np.float32))
@@ -109,7 +114,8 @@ class GpuNlist:
                               d_xyzf=p(self.xyzf), d_cell_type=p(self.cell_type),
                               d_cell_adj=p(self.adj), dim=(ctypes.c_uint32 * 3)(*self.dim),
                               Nmax_cell=self.Nmax_cell, adj_width=self.adj_w, box=self.box,
-                              d_r_cut=p(self.d_rc), d_r_listsq=p(self.d_rl), ntypes=nt)
+                              d_r_cut=p(self.d_rc), d_r_listsq=p(self.d_rl), ntypes=nt,
+                              nlist_capacity=0 if self.warp_build else self.nlist.numel())
             abi.check(L.gb_nlist_build_binned(ctypes.byref(a), stream()), "nlist")
             cond = host(self.ncond)
             over = cond > Nmax
