@@ -148,6 +148,17 @@ void ParticleData::set_particles(const double* p, const double* v, const double*
     cuda_check(cudaStreamSynchronize(stream), "set_particles");
     }
 
+void ParticleData::set_charges(const double* q)
+    {
+    const std::vector<uint32_t> r = rtag();
+    std::vector<float> h(N);
+    for (unsigned int t = 0; t < N; t++)
+        h[r[t]] = (float)q[t];
+    charge.resize(N);
+    charge.upload(h.data(), h.size(), stream);
+    cuda_check(cudaStreamSynchronize(stream), "set_charges");
+    }
+
 std::vector<uint32_t> ParticleData::rtag()
     {
     std::vector<uint32_t> t(N), r(N);
@@ -699,6 +710,12 @@ gb_pair_args PairForce::pair_args(bool with_virial)
     a.ntypes = ntypes;
     a.shift_mode = (unsigned int)shift_mode;
     a.compute_virial = with_virial ? 1 : 0;
+    if (uses_charge)
+        {
+        if (pd.charge.size() != pd.N)
+            throw std::runtime_error("pair force needs particle charges, which are not set");
+        a.d_charge = pd.charge.get();
+        }
     return a;
     }
 
@@ -1293,6 +1310,8 @@ void Integrator::sort_particles()
     apply(pd.accel.get(), 12);
     apply(pd.image.get(), 12);
     apply(pd.tag.get(), 4);
+    if (pd.charge.size() == pd.N)
+        apply(pd.charge.get(), 4);
     for (auto& f : forces)
         {
         apply(f->force.get(), 16);

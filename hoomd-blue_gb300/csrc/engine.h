@@ -148,6 +148,9 @@ class ParticleData
     void get_particles(double* pos, double* vel, double* mass, uint32_t* typeid_,
                        int32_t* image);
     std::vector<uint32_t> rtag(); // tag -> index
+    // per-particle charges in tag order (kept in index order on the device, sorted with the
+    // particles); read by the pair forces that need them
+    void set_charges(const double* q);
     void thermalize(double kT, uint64_t timestep);
 
     unsigned int N, ntypes, ndim;
@@ -158,7 +161,7 @@ class ParticleData
     uint64_t timestep = 0;
     bool accel_set = false;
     cudaStream_t stream = nullptr;
-    DeviceArray<float> pos, vel, accel, alt;
+    DeviceArray<float> pos, vel, accel, alt, charge;
     DeviceArray<int32_t> image;
     DeviceArray<uint32_t> tag;
     DeviceArray<char> scratch;
@@ -248,6 +251,7 @@ class PairForce
     std::shared_ptr<NeighborList> nlist;
     PairKind kind;
     int shift_mode = 0;
+    bool uses_charge = false; // the evaluator scales pairs by q_i q_j (d_charge in the args)
     unsigned int ntypes;
     std::vector<float> r_cut, r_on;
     std::vector<gb_lj_param> lj;

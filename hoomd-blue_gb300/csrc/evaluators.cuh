@@ -39,7 +39,7 @@ struct EvalLJ
           lj2(p.epsilon_x_4 * p.sigma_6)
         {
         }
-    static constexpr bool needsCharge()
+    __host__ __device__ static constexpr bool needsCharge()
         {
         return false;
         }
@@ -90,7 +90,7 @@ struct EvalTable
         {
         inv_dr = __uint_as_float(p.reserved);
         }
-    static constexpr bool needsCharge()
+    __host__ __device__ static constexpr bool needsCharge()
         {
         return false;
         }
@@ -125,7 +125,7 @@ struct EvalExample
         : rsq(rsq_), rcutsq(rcutsq_), k(p.k), sigma(p.sigma)
         {
         }
-    static constexpr bool needsCharge()
+    __host__ __device__ static constexpr bool needsCharge()
         {
         return false;
         }
@@ -158,7 +158,10 @@ struct EvalExample
 // non-divergent branch per pair and the whole family shares one set of kernel instantiations.
 // Each kind writes V(r) and F(r) = -dV/dr from its closed form; shift mode subtracts V(r_cut).
 // The closed forms are one out-of-line function, so every kernel variant shares its code.
-struct EvalRadial
+// Q = true multiplies every pair's force and energy by q_i q_j (Ewald, ReactionField with
+// use_charge): the closed forms below are written for unit charges, and all of them are linear
+// in q_i q_j.
+template<bool Q> struct EvalRadialT
     {
     using param_type = gb_radial_param;
     // derived per type pair: the Mie prefactor, or F(r_cut) of the force-shifted LJ
@@ -182,16 +185,21 @@ struct EvalRadial
         }
     float rsq, rcutsq;
     param_type p;
-    __device__ __forceinline__ EvalRadial(float rsq_, float rcutsq_, const param_type& p_,
-                                          const float*)
+    float qiqj = 1.0f;
+    __device__ __forceinline__ EvalRadialT(float rsq_, float rcutsq_, const param_type& p_,
+                                           const float*)
         : rsq(rsq_), rcutsq(rcutsq_), p(p_)
         {
         }
-    static constexpr bool needsCharge()
+    __host__ __device__ static constexpr bool needsCharge()
         {
-        return false;
+        return Q;
         }
-    __device__ __forceinline__ void setCharge(float, float) { }
+    __device__ __forceinline__ void setCharge(float qi, float qj)
+        {
+        if (Q)
+            qiqj = qi * qj;
+        }
 
     // (s/x)^n - style LJ of exponents (n, m) with prefactor c: V and F at distance x = r - delta
     __device__ __forceinline__ static void lj_nm(float c, float sigma, float x, int n, int m,
@@ -392,6 +400,22 @@ struct EvalRadial
                 F = Zsq / (r * r) * e + Zsq / r * de / aF;
                 break;
                 }
+            case GB_RADIAL_EWALD:
+                {
+                // real-space Ewald sum with a Gaussian-smeared screening alpha
+                // (EvaluatorPairEwald.h:121-148), unit charges
+                const float kappa = v[0], alpha = v[1];
+                const float a1 = kappa * r + alpha / (2.0f * kappa);
+                const float a2 = kappa * r - alpha / (2.0f * kappa);
+                const float e1 = expf(alpha * r), e2 = expf(-alpha * r);
+                const float c1 = erfcf(a1), c2 = erfcf(a2);
+                const float val = 0.5f * (c1 * e1 + c2 * e2) / r;
+                V = val;
+                F = (val + e2 * 2.0f * kappa * expf(-a2 * a2) * 0.564189583547756f
+                     + alpha * 0.5f * e2 * c2 - alpha * 0.5f * e1 * c1)
+                    / r;
+                break;
+                }
             case GB_RADIAL_REACTION_FIELD:
                 {
                 const float eps = v[0], epsrf = v[1], rc = p.aux;
@@ -433,8 +457,15 @@ struct EvalRadial
             }
         force_divr = F / r;
         pair_eng = V;
+        if (Q)
+            {
+            force_divr *= qiqj;
+            pair_eng *= qiqj;
+            }
         return true;
         }
     };
+using EvalRadial = EvalRadialT<false>;
+using EvalRadialQ = EvalRadialT<true>;
 
 } // namespace gb

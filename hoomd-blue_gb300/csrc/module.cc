@@ -81,6 +81,12 @@ PYBIND11_MODULE(_hoomd_gb300, m)
                  pd.set_particles(pos.data(), vel.data(), mass.data(), typeid_.data(),
                                   image.data());
              })
+        .def("setCharges",
+             [](ParticleData& pd, py::array_t<double, py::array::c_style | py::array::forcecast> q) {
+                 if ((size_t)q.size() != pd.N)
+                     throw std::invalid_argument("charge array size does not match N");
+                 pd.set_charges(q.data());
+             })
         .def("getParticles",
              [](ParticleData& pd) {
                  const size_t N = pd.N;
@@ -184,6 +190,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setParamsExample", &PairForce::set_params_example)
         .def("setParamsTable", &PairForce::set_params_table)
         .def("setParamsRadial", &PairForce::set_params_radial)
+        .def_readwrite("useCharge", &PairForce::uses_charge)
         .def("setRCut", &PairForce::set_r_cut)
         .def("setROn", &PairForce::set_r_on)
         .def("setSurrogate", [](PairForce& f, std::shared_ptr<MlpSurrogate> m) { f.mlp = m; })

@@ -211,8 +211,8 @@ __global__ void __launch_bounds__(256)
            const uint64_t* __restrict__ d_head_list, uint64_t stride,
            const typename Eval::param_type* __restrict__ d_params,
            const float* __restrict__ d_rcutsq, const float* __restrict__ d_ronsq,
-           unsigned int ntypes, const float* __restrict__ ext, int SHIFT, bool VIRIAL,
-           bool ORTHO, FuseArgs fz)
+           unsigned int ntypes, const float* __restrict__ ext,
+           const float* __restrict__ d_charge, int SHIFT, bool VIRIAL, bool ORTHO, FuseArgs fz)
     {
     using P = typename Eval::param_type;
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -285,6 +285,8 @@ __global__ void __launch_bounds__(256)
             bool energy_shift = (SHIFT == 1) || (SHIFT == 2 && ronsq > rcutsq);
             float force_divr = 0.0f, pair_eng = 0.0f;
             Eval eval(rsq, rcutsq, *param, ext);
+            if (Eval::needsCharge())
+                eval.setCharge(__ldg(d_charge + gi), __ldg(d_charge + j));
             eval.evalForceAndEnergy(force_divr, pair_eng, energy_shift);
             if (SHIFT == 2)
                 {
@@ -399,7 +401,8 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
               const unsigned int* __restrict__ d_n_neigh, const uint4* __restrict__ d_nlist4,
               uint64_t stride, const typename Eval::param_type* __restrict__ d_params,
               const float* __restrict__ d_rcutsq, const float* __restrict__ d_ronsq,
-              unsigned int ntypes, const float* __restrict__ ext, bool SHIFT1, FuseArgs fz)
+              unsigned int ntypes, const float* __restrict__ ext,
+              const float* __restrict__ d_charge, bool SHIFT1, FuseArgs fz)
     {
     using P = typename Eval::param_type;
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -446,7 +449,8 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
         const float Lx = box.L[0], Ly = box.L[1], Lz = box.L[2];
         const float Lix = box.Linv[0], Liy = box.Linv[1], Liz = box.Linv[2];
         const float Lzxz = box.L[2] * box.xz, Lzyz = box.L[2] * box.yz, Lyxy = box.L[1] * box.xy;
-        auto pair = [&](const float4 pj, bool valid) {
+        const float qi = Eval::needsCharge() ? __ldg(d_charge + i) : 0.0f;
+        auto pair = [&](const float4 pj, unsigned int j, bool valid) {
             float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             if (ORTHO)
                 {
@@ -485,6 +489,8 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             const bool energy_shift = XPLOR ? (ronsq > rcutsq) : SHIFT1;
             float force_divr = 0.0f, pair_eng = 0.0f;
             Eval eval(rsq, rcutsq, *param, ext);
+            if (Eval::needsCharge())
+                eval.setCharge(qi, __ldg(d_charge + j));
             eval.evalForceAndEnergy(force_divr, pair_eng, energy_shift);
             if (XPLOR && rsq >= ronsq && rsq < rcutsq)
                 {
@@ -535,10 +541,10 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
                 const float4 q1 = __ldg(d_pos + jc.y);
                 const float4 q2 = __ldg(d_pos + jc.z);
                 const float4 q3 = __ldg(d_pos + jc.w);
-                pair(q0, true);
-                pair(q1, true);
-                pair(q2, true);
-                pair(q3, true);
+                pair(q0, jc.x, true);
+                pair(q1, jc.y, true);
+                pair(q2, jc.z, true);
+                pair(q3, jc.w, true);
                 }
             if (rem && sub == nfull % TPP)
                 {
@@ -546,9 +552,9 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
                 const float4 q0 = __ldg(d_pos + jc.x);
                 const float4 q1 = __ldg(d_pos + (rem > 1 ? jc.y : i));
                 const float4 q2 = __ldg(d_pos + (rem > 2 ? jc.z : i));
-                pair(q0, true);
-                pair(q1, rem > 1);
-                pair(q2, rem > 2);
+                pair(q0, jc.x, true);
+                pair(q1, rem > 1 ? jc.y : i, rem > 1);
+                pair(q2, rem > 2 ? jc.z : i, rem > 2);
                 }
             }
         uint4 jA = self, jB = self;
@@ -566,10 +572,10 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             const float4 q1 = __ldg(d_pos + jc.y);
             const float4 q2 = __ldg(d_pos + jc.z);
             const float4 q3 = __ldg(d_pos + jc.w);
-            pair(q0, true);
-            pair(q1, true);
-            pair(q2, true);
-            pair(q3, true);
+            pair(q0, jc.x, true);
+            pair(q1, jc.y, true);
+            pair(q2, jc.z, true);
+            pair(q3, jc.w, true);
             }
         if (TPP == 1 && rem)
             {
@@ -577,9 +583,9 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             const float4 q0 = __ldg(d_pos + jc.x);
             const float4 q1 = __ldg(d_pos + (rem > 1 ? jc.y : i));
             const float4 q2 = __ldg(d_pos + (rem > 2 ? jc.z : i));
-            pair(q0, true);
-            pair(q1, rem > 1);
-            pair(q2, rem > 2);
+            pair(q0, jc.x, true);
+            pair(q1, rem > 1 ? jc.y : i, rem > 1);
+            pair(q2, rem > 2 ? jc.z : i, rem > 2);
             }
         pe *= 0.5f;
         }
@@ -634,7 +640,7 @@ int launch_pair_i4_inst(const gb_pair_args& a, const typename Eval::param_type* 
                                    a.virial_pitch, a.N, reinterpret_cast<const float4*>(a.d_pos),
                                    a.box, a.d_n_neigh, reinterpret_cast<const uint4*>(a.d_nlist),
                                    a.stride, d_params, a.d_rcutsq, a.d_ronsq, a.ntypes, ext,
-                                   a.shift_mode == 1, fz);
+                                   a.d_charge, a.shift_mode == 1, fz);
     return check_launch("pair force kernel (interleaved list)");
     }
 
@@ -701,7 +707,7 @@ int launch_pair_inst(const gb_pair_args& a, const typename Eval::param_type* d_p
     kern<<<grid, block, smem, s>>>(reinterpret_cast<float4*>(a.d_force), a.d_virial,
                                    a.virial_pitch, a.N, reinterpret_cast<const float4*>(a.d_pos),
                                    a.box, a.d_n_neigh, a.d_nlist, a.d_head_list, a.stride,
-                                   d_params, a.d_rcutsq, a.d_ronsq, a.ntypes, ext,
+                                   d_params, a.d_rcutsq, a.d_ronsq, a.ntypes, ext, a.d_charge,
                                    (int)a.shift_mode, a.compute_virial != 0, ortho, fz);
     return check_launch("pair force kernel");
     }
@@ -730,6 +736,7 @@ int launch_pair(const gb_pair_args* a, const typename Eval::param_type* d_params
     GB_REQUIRE(a->shift_mode != 2 || a->d_ronsq, "pair force: xplor needs r_on^2");
     GB_REQUIRE(a->ntypes >= 1 && a->ntypes <= 64, "pair force: 1 <= ntypes <= 64");
     GB_REQUIRE(a->d_head_list || a->stride >= a->N, "pair force: column-major stride < N");
+    GB_REQUIRE(!Eval::needsCharge() || a->d_charge, "pair force: this evaluator needs charges");
     if (a->N == 0)
         return GB_OK;
     unsigned int block = a->block_size ? a->block_size : 256;

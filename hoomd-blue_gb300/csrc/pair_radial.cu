@@ -1,8 +1,15 @@
 // Pair-force entry points for the radial evaluator family (EvalRadial): the reference builds one
 // PotentialPairGPU instantiation per evaluator (hoomd/md/CMakeLists.txt:505-550); here the
-// fourteen closed forms share one instantiation set, selected per force by gb_radial_param.kind.
+// closed forms share one instantiation set, selected per force by gb_radial_param.kind. With
+// per-particle charges (args->d_charge) the charged instantiation set of pair_radial_q.cu runs.
 #include "fused_step.h"
 #include "pair_kernel.cuh"
+
+namespace gb
+{
+int radial_charged(const gb_pair_args* args, const gb_radial_param* d_params, const FuseArgs& fz,
+                   bool fused, cudaStream_t s);
+}
 
 using namespace gb;
 
@@ -12,6 +19,8 @@ extern "C"
                               void* stream)
         {
         FuseArgs none {};
+        if (args && args->d_charge)
+            return radial_charged(args, d_params, none, false, (cudaStream_t)stream);
         return launch_pair<EvalRadial, false>(args, d_params, nullptr, none,
                                               (cudaStream_t)stream);
         }
@@ -23,6 +32,8 @@ extern "C"
         int rc = make_fuse_args(args, fuse, fz);
         if (rc != GB_OK)
             return rc;
+        if (args->d_charge)
+            return radial_charged(args, d_params, fz, true, (cudaStream_t)stream);
         return launch_pair<EvalRadial, true>(args, d_params, nullptr, fz, (cudaStream_t)stream);
         }
     }

@@ -56,6 +56,7 @@ class Pair:
         self._cpp_obj = _hoomd_gb300.PotentialPairGPU(state._cpp_pdata, cpp_nlist, self._kind)
         self._cpp_obj.mode = _MODES[self._mode]
         types = state.particle_types
+        self._cpp_obj.useCharge = bool(self._needs_charge(types))
         for i, a in enumerate(types):
             for j, b in enumerate(types):
                 if j < i:
@@ -75,6 +76,10 @@ class Pair:
 
     def _detach(self):
         self._cpp_obj = None
+
+    def _needs_charge(self, types):
+        """True when every pair is scaled by q_i q_j (the reference's needsCharge())."""
+        return False
 
     def _require_run(self):
         if self._cpp_obj is None or self._simulation is None:
@@ -271,9 +276,10 @@ class Fourier(_Radial):
 
 
 class ReactionField(_Radial):
-    """Reaction-field electrostatics (EvaluatorPairReactionField.h) with unit charges
-    (``use_charge=False``): eps [1/r + (eps_rf - 1)/(2 eps_rf + 1) r^2 / r_c^3]; eps_rf = 0
-    stands for an infinite dielectric."""
+    """Reaction-field electrostatics (EvaluatorPairReactionField.h):
+    eps [1/r + (eps_rf - 1)/(2 eps_rf + 1) r^2 / r_c^3], times q_i q_j with ``use_charge=True``;
+    eps_rf = 0 stands for an infinite dielectric. ``use_charge`` must be the same for every type
+    pair (one kernel instantiation scales all pairs or none)."""
 
     _radial_kind = 19
 
@@ -283,7 +289,28 @@ class ReactionField(_Radial):
                                                             optional={"use_charge": False}))
 
     def _set_pair_params(self, cpp, i, j, v):
-        if v.get("use_charge"):
-            raise NotImplementedError("ReactionField with use_charge=True needs per-particle "
-                                      "charges, which this pair path does not carry")
         cpp.setParamsRadial(i, j, self._radial_kind, [float(v["epsilon"]), float(v["eps_rf"])])
+
+    def _needs_charge(self, types):
+        flags = {bool(self.params[(a, b)].get("use_charge")) for a in types for b in types}
+        if len(flags) > 1:
+            raise NotImplementedError("ReactionField: use_charge must be the same for every "
+                                      "type pair")
+        return flags.pop()
+
+
+class Ewald(_Radial):
+    """Real-space part of the Ewald sum (EvaluatorPairEwald.h): q_i q_j [erfc(kappa r +
+    alpha / 2 kappa) e^{alpha r} + erfc(kappa r - alpha / 2 kappa) e^{-alpha r}] / 2r; alpha = 0
+    is the plain erfc(kappa r) / r. Reads the particle charges."""
+
+    _radial_kind = 20
+    _keys = ("kappa", "alpha")
+    _accepted_modes = ("none",)
+
+    def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
+        super().__init__(nlist, default_r_cut, default_r_on, mode)
+        self.params = TypePairDict(validator=dict_validator(("kappa",), optional={"alpha": 0.0}))
+
+    def _needs_charge(self, types):
+        return True

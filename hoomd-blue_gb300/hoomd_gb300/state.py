@@ -34,6 +34,7 @@ class State:
             np.ascontiguousarray(p.mass, np.float64),
             np.ascontiguousarray(p.typeid, np.uint32),
             np.ascontiguousarray(p.image, np.int32))
+        self._cpp_pdata.setCharges(np.ascontiguousarray(p.charge, np.float64))
         self._simulation._state_changed()
 
     @property

@@ -256,7 +256,11 @@ int gb_pair_forces_example(const gb_pair_args* args, const gb_example_param* d_p
  *   FOURIER     a1, a2, a3, b1, b2, b3    1/r^12 + sum_n [a_n cos(n pi r / r_c) + b_n sin(n pi r / r_c)] / r^2 (EvaluatorPairFourier.h:135-180)
  *   MOLIERE     qi, qj, aF                qi qj / r (0.35 e^{-0.3 r/aF} + 0.55 e^{-1.2 r/aF} + 0.1 e^{-6 r/aF}) (EvaluatorPairMoliere.h:112-148)
  *   ZBL         qi, qj, aF                the four-exponential ZBL screening (EvaluatorPairZBL.h:95-123)
- *   REACTION_FIELD  epsilon, eps_rf       eps [1/r + (eps_rf - 1) / (2 eps_rf + 1) r^2 / r_c^3], charges 1 (EvaluatorPairReactionField.h:122-151)
+ *   REACTION_FIELD  epsilon, eps_rf       eps [1/r + (eps_rf - 1) / (2 eps_rf + 1) r^2 / r_c^3] (EvaluatorPairReactionField.h:122-151)
+ *   EWALD       kappa, alpha              real-space Ewald term, erfc screening (EvaluatorPairEwald.h:121-148)
+ * The forms are for unit charges; when args->d_charge is given, every pair's force and energy
+ * is multiplied by q_i q_j (the reference's needsCharge evaluators: Ewald always,
+ * ReactionField with use_charge).
  * Shift mode 1 subtracts the energy at r_cut; XPLOR smoothing as for LJ. DLVO, MOLIERE, ZBL and
  * REACTION_FIELD give zero force where the reference's evaluators return false (kappa, qi qj,
  * aF or epsilon zero). */
@@ -282,7 +286,8 @@ typedef enum gb_radial_kind
     GB_RADIAL_MOLIERE = 17,
     GB_RADIAL_ZBL = 18,
     GB_RADIAL_REACTION_FIELD = 19,
-    GB_RADIAL_KINDS = 20
+    GB_RADIAL_EWALD = 20,
+    GB_RADIAL_KINDS = 21
     } gb_radial_kind;
 
 typedef struct gb_radial_param

@@ -78,7 +78,7 @@ def table_index_safe_f32(rsq, rcutsq, rmin, width):
 # the radial potentials served by gb_pair_forces_radial
 RADIAL = ("Gaussian", "Yukawa", "Morse", "ForceShiftedLJ", "Mie", "ExpandedMie", "ExpandedLJ",
           "Buckingham", "LJ1208", "LJ0804", "LJGauss", "ExpandedGaussian", "OPP", "TWF",
-          "DPDConservative", "DLVO", "Fourier", "Moliere", "ZBL", "ReactionField")
+          "DPDConservative", "DLVO", "Fourier", "Moliere", "ZBL", "ReactionField", "Ewald")
 
 
 def main():

@@ -20,12 +20,13 @@ GOLD = json.load(open(pathlib.Path(__file__).resolve().parent / "golden"
 NAMES = [k for k in GOLD if not k.startswith("_")]
 
 
-def two_particles(d, L=20.0):
+def two_particles(d, L=20.0, charge=0.0):
     s = hoomd.Snapshot()
     s.configuration.box = [L, L, L, 0, 0, 0]
     s.particles.N = 2
     s.particles.types = ["A"]
     s.particles.position[:] = [[0, 0, 0.1], [0, 0, d + 0.1]]
+    s.particles.charge[:] = charge
     return s
 
 
@@ -42,7 +43,8 @@ def test_force_energy_accuracy(name):
     for i, params in enumerate(ent["params"]):
         f = potential(name, params)
         sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=1)
-        sim.create_state_from_snapshot(two_particles(0.75))
+        # unit charges for Ewald, as the reference's harness sets them
+        sim.create_state_from_snapshot(two_particles(0.75, charge=1.0 if name == "Ewald" else 0.0))
         sim.operations.integrator = md.Integrator(
             dt=0.005, forces=[f], methods=[md.methods.ConstantVolume(hoomd.filter.All())])
         sim.run(0)
@@ -126,6 +128,11 @@ def closed_form(name, p):
         return lambda r: Z / r * (0.1818 * np.exp(-3.2 * r / aF) + 0.5099 * np.exp(-0.9423 * r / aF)
                                   + 0.2802 * np.exp(-0.4029 * r / aF)
                                   + 0.02817 * np.exp(-0.2016 * r / aF))
+    if name == "Ewald":
+        from scipy.special import erfc
+        k, a = p["kappa"], p.get("alpha", 0.0)
+        return lambda r: 0.5 * (erfc(k * r + a / (2 * k)) * np.exp(a * r)
+                                + erfc(k * r - a / (2 * k)) * np.exp(-a * r)) / r
     if name == "ReactionField":
         rc, erf = 2.5, p["eps_rf"]
         fac = (0.5 if erf == 0 else (erf - 1) / (2 * erf + 1)) / rc ** 3
@@ -143,8 +150,12 @@ def test_many_particle_forces_vs_fp64(name, mode):
     the unfused kernel; per-particle forces and the total energy against an FP64 brute force."""
     if mode == "shift" and "shift" not in getattr(md.pair, name)._accepted_modes:
         pytest.skip(f"{name} does not accept mode 'shift'")
-    p = GOLD[name]["params"][1 if len(GOLD[name]["params"]) > 1 else 0]
+    p = dict(GOLD[name]["params"][1 if len(GOLD[name]["params"]) > 1 else 0])
     snap = workloads.lj_fluid_sc(8, density=0.7, jitter=0.05, seed=4)
+    charged = name == "Ewald"
+    if charged:
+        snap.particles.charge[:] = np.random.default_rng(5).choice([-1.0, 0.5, 1.0],
+                                                                  snap.particles.N)
     f = potential(name, p, mode=mode)
     sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=1)
     sim.create_state_from_snapshot(snap)
@@ -152,6 +163,7 @@ def test_many_particle_forces_vs_fp64(name, mode):
         dt=0.005, forces=[f], methods=[md.methods.ConstantVolume(hoomd.filter.All())])
     sim.run(0)
     pos = np.asarray(sim.state.get_snapshot().particles.position, np.float32).astype(np.float64)
+    q = np.asarray(snap.particles.charge, np.float32).astype(np.float64) if charged else None
     L = snap.configuration.box[0]
     V = closed_form(name, p)
     N = len(pos)
@@ -166,9 +178,10 @@ def test_many_particle_forces_vs_fp64(name, mode):
         r = np.sqrt((d * d).sum(1))
         m = (r < rc) & (r > 0)
         rr = r[m]
-        F = -(V(rr + h) - V(rr - h)) / (2 * h)
+        qq = q[i] * q[m] if charged else 1.0
+        F = -(V(rr + h) - V(rr - h)) / (2 * h) * qq
         Fo[i] = ((F / rr)[:, None] * d[m]).sum(0)
-        Eo += 0.5 * (V(rr) - vshift).sum()
+        Eo += 0.5 * ((V(rr) - vshift) * qq).sum()
     Fg = f.forces
     scale = np.abs(Fo).max()
     assert np.all(np.abs(Fg - Fo) <= 1e-4 * np.abs(Fo) + 1e-5 * scale), name
@@ -191,3 +204,48 @@ def test_fused_nve_with_morse_conserves_energy():
     sim.run(1000)
     e1 = thermo.kinetic_energy + thermo.potential_energy
     assert abs(e1 - e0) / snap.particles.N < 1e-3
+
+
+def test_reaction_field_with_charges_and_sort():
+    """ReactionField with use_charge=True scales each pair by q_i q_j; the charges follow the
+    particles through the Hilbert sort (a sorted run equals an unsorted one)."""
+    snap = workloads.lj_fluid_sc(10, density=0.8, jitter=0.05, seed=8)
+    rng = np.random.default_rng(3)
+    snap.particles.charge[:] = rng.choice([-1.0, 1.0], snap.particles.N)
+    p = dict(epsilon=0.3, eps_rf=2.0, use_charge=True)
+    out = []
+    for sorter in (None, 5):
+        sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=2)
+        sim.create_state_from_snapshot(snap)
+        sim.state.thermalize_particle_momenta(hoomd.filter.All(), 1.0)
+        f = md.pair.ReactionField(nlist=md.nlist.Cell(buffer=0.4), default_r_cut=2.5)
+        f.params[("A", "A")] = p
+        lj = md.pair.LJ(nlist=f.nlist, default_r_cut=2.5)
+        lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+        sim.operations.integrator = md.Integrator(
+            dt=0.004, forces=[lj, f], methods=[md.methods.ConstantVolume(hoomd.filter.All())])
+        if sorter:
+            sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=sorter))
+        sim.run(0)
+        if sorter is None:
+            pos = np.asarray(sim.state.get_snapshot().particles.position, np.float32)
+            pos = pos.astype(np.float64)
+            L = snap.configuration.box[0]
+            V = closed_form("ReactionField", p)
+            q = snap.particles.charge
+            E = 0.0
+            for i in range(len(pos)):
+                d = pos[i] - pos
+                d -= L * np.rint(d / L)
+                r = np.sqrt((d * d).sum(1))
+                m = (r < 2.5) & (r > 0)
+                E += 0.5 * (V(r[m]) * q[i] * q[m]).sum()
+            assert math.isclose(f.energy, E, rel_tol=1e-4, abs_tol=1e-4)
+        sim.run(20)
+        out.append(sim.state.get_snapshot())
+    a, b = out
+    box = np.array(snap.configuration.box[:3])
+    ua = a.particles.position + a.particles.image * box
+    ub = b.particles.position + b.particles.image * box
+    assert np.abs(ua - ub).max() < 1e-3
+    assert np.array_equal(a.particles.charge, b.particles.charge)
