@@ -541,11 +541,31 @@ PairForce::PairForce(std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborL
     lj.assign(np, gb_lj_param {0.0f, 0.0f});
     ex.assign(np, gb_example_param {0.0f, 0.0f});
     rad.assign(np, gb_radial_param {});
+    dpd.assign(np, gb_dpd_param {});
     t_rmin.assign(np, 0.0);
     t_U.assign(np, std::vector<double>(1, 0.0));
     t_F.assign(np, std::vector<double>(1, 0.0));
     force.resize(4 * (size_t)std::max(1u, pdata->N));
     force.zero(pdata->stream);
+    }
+
+// EvaluatorPairDPDThermoDPD / DPDThermoLJ parameters (hoomd/md/EvaluatorPairDPDThermoLJ.h:60-90)
+void PairForce::set_params_dpd(unsigned int i, unsigned int j, bool lj, double a_or_eps,
+                               double sigma, double gamma)
+    {
+    gb_dpd_param p {};
+    if (lj)
+        {
+        const double s6 = sigma * sigma * sigma * sigma * sigma * sigma;
+        p.lj1 = (float)(4.0 * a_or_eps * s6 * s6);
+        p.lj2 = (float)(4.0 * a_or_eps * s6);
+        }
+    else
+        p.a = (float)a_or_eps;
+    p.gamma = (float)gamma;
+    dpd_lj = lj;
+    dpd[i * ntypes + j] = dpd[j * ntypes + i] = p;
+    params_dirty = true;
     }
 
 // EvaluatorPairLJ::param_type(sigma, epsilon) at FP32 (hoomd/md/EvaluatorPairLJ.h:125-142)
@@ -637,6 +657,13 @@ void PairForce::upload()
         {
         d_params.resize(np * sizeof(gb_radial_param));
         cuda_check(cudaMemcpyAsync(d_params.get(), rad.data(), np * sizeof(gb_radial_param),
+                                   cudaMemcpyHostToDevice, s),
+                   "params");
+        }
+    else if (kind == PairKind::DPD)
+        {
+        d_params.resize(np * sizeof(gb_dpd_param));
+        cuda_check(cudaMemcpyAsync(d_params.get(), dpd.data(), np * sizeof(gb_dpd_param),
                                    cudaMemcpyHostToDevice, s),
                    "params");
         }
@@ -761,6 +788,10 @@ void PairForce::compute(cudaStream_t s, bool with_virial)
         rc = gb_pair_forces_example(&a, (const gb_example_param*)d_params.get(), s);
     else if (kind == PairKind::Radial)
         rc = gb_pair_forces_radial(&a, (const gb_radial_param*)d_params.get(), s);
+    else if (kind == PairKind::DPD)
+        rc = gb_pair_forces_dpd(&a, (const gb_dpd_param*)d_params.get(), pdata->vel.get(),
+                                pdata->tag.get(), dpd_lj ? 1 : 0, force_timestep, pdata->seed,
+                                force_dt, (float)dpd_kT, s);
     else
         rc = gb_pair_forces_table(&a, (const gb_table_param*)d_params.get(), d_table.get(), s);
     check(rc, "pair force");
@@ -775,6 +806,8 @@ int PairForce::launch_fused(const gb_pair_args& a, const gb_step_fuse& f, cudaSt
         return gb_md_pair_step_example(&a, (const gb_example_param*)d_params.get(), &f, s);
     if (kind == PairKind::Radial)
         return gb_md_pair_step_radial(&a, (const gb_radial_param*)d_params.get(), &f, s);
+    if (kind == PairKind::DPD || kind == PairKind::MLP)
+        throw std::logic_error("this pair force has no fused step");
     return gb_md_pair_step_table(&a, (const gb_table_param*)d_params.get(), d_table.get(), &f, s);
     }
 
@@ -973,7 +1006,11 @@ void Integrator::prepare()
     nlist->build_sync();
     drop_graphs();
     for (auto& f : forces)
+        {
+        f->force_timestep = pd.timestep;
+        f->force_dt = (float)dt;
         f->compute(s, compute_virial);
+        }
     const float* net = forces[0]->force.get();
     if (forces.size() > 1)
         {
@@ -1119,7 +1156,12 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
     check(gb_md_step_one(&o, s), "gb_md_step_one");
     nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
     for (auto& f : forces)
+        {
+        // IntegratorTwoStep::update computes the net force for timestep + 1
+        f->force_timestep = step + 1;
+        f->force_dt = (float)dt;
         f->compute(s, compute_virial);
+        }
     const float* net = forces[0]->force.get();
     if (forces.size() > 1)
         {
@@ -1212,7 +1254,8 @@ void Integrator::run_chunk(unsigned int k)
     {
     ParticleData& pd = *pdata;
     cudaStream_t s = pd.stream;
-    const bool fused = forces.size() == 1 && !compute_virial && forces[0]->kind != PairKind::MLP;
+    const bool fused = forces.size() == 1 && !compute_virial && forces[0]->kind != PairKind::MLP
+                       && forces[0]->kind != PairKind::DPD;
     for (int attempt = 0; attempt < 16; attempt++)
         {
         checkpoint();
@@ -1408,7 +1451,7 @@ std::vector<double> Integrator::time_phases(unsigned int reps)
         if (bussi)
             enqueue_bussi_draws(*this, ds, d_bussi_ring.get(), BUSSI_RING, 1, s);
         cuda_check(cudaEventRecord(ev[0], s), "record");
-        if (f.kind == PairKind::MLP)
+        if (f.kind == PairKind::MLP || f.kind == PairKind::DPD)
             {
             // unfused: forces, step two, thermo and the Bussi factor as enqueue_step_general
             f.compute(s, false);

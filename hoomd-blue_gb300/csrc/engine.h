@@ -224,7 +224,8 @@ enum class PairKind
     Table = 1,
     Example = 2,
     MLP = 3, // radial MLP surrogate of Table (unfused path: pair list + tensor-core tiles)
-    Radial = 4 // the other radial evaluators (gb_radial_param.kind)
+    Radial = 4, // the other radial evaluators (gb_radial_param.kind)
+    DPD = 5  // DPD thermostat pair forces (unfused: they read the velocities step two writes)
     };
 
 class MlpSurrogate;
@@ -238,6 +239,9 @@ class PairForce
     void set_params_example(unsigned int i, unsigned int j, double k, double sigma);
     void set_params_radial(unsigned int i, unsigned int j, unsigned int kind,
                            const std::vector<double>& v);
+    // DPD (lj = false: A) or DPDLJ (lj = true: epsilon, sigma), drag gamma
+    void set_params_dpd(unsigned int i, unsigned int j, bool lj, double a_or_eps, double sigma,
+                        double gamma);
     void set_params_table(unsigned int i, unsigned int j, double r_min,
                           const std::vector<double>& U, const std::vector<double>& F);
     void set_r_cut(unsigned int i, unsigned int j, double r);
@@ -257,6 +261,11 @@ class PairForce
     std::vector<gb_lj_param> lj;
     std::vector<gb_example_param> ex;
     std::vector<gb_radial_param> rad;
+    std::vector<gb_dpd_param> dpd;
+    bool dpd_lj = false;
+    double dpd_kT = 1.0;
+    uint64_t force_timestep = 0; // timestep of the force evaluation (DPD random numbers)
+    float force_dt = 0.0f;       // integrator time step (DPD random force amplitude)
     std::vector<double> t_rmin;
     std::vector<std::vector<double>> t_U, t_F;
     bool params_dirty = true;

@@ -182,7 +182,8 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .value("Table", PairKind::Table)
         .value("Example", PairKind::Example)
         .value("MLP", PairKind::MLP)
-        .value("Radial", PairKind::Radial);
+        .value("Radial", PairKind::Radial)
+        .value("DPD", PairKind::DPD);
 
     py::class_<PairForce, std::shared_ptr<PairForce>>(m, "PotentialPairGPU")
         .def(py::init<std::shared_ptr<ParticleData>, std::shared_ptr<NeighborList>, PairKind>())
@@ -190,6 +191,8 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setParamsExample", &PairForce::set_params_example)
         .def("setParamsTable", &PairForce::set_params_table)
         .def("setParamsRadial", &PairForce::set_params_radial)
+        .def("setParamsDPD", &PairForce::set_params_dpd)
+        .def_readwrite("dpdKT", &PairForce::dpd_kT)
         .def_readwrite("useCharge", &PairForce::uses_charge)
         .def("setRCut", &PairForce::set_r_cut)
         .def("setROn", &PairForce::set_r_on)

@@ -314,3 +314,59 @@ class Ewald(_Radial):
 
     def _needs_charge(self, types):
         return True
+
+
+class _DPDBase(Pair):
+    """DPD thermostat pair forces (hoomd/md/pair/pair.py DPD, DPDLJ; PotentialPairDPDThermo):
+    a conservative force plus the drag and random forces of the DPD thermostat at ``kT``, whose
+    random numbers come from both particles' tags and the timestep. They read the velocities, so
+    the integrator runs them on its unfused path."""
+
+    _kind = _hoomd_gb300.PairKind.DPD
+    _lj = False
+
+    def __init__(self, nlist, kT, default_r_cut=None, mode='none'):
+        super().__init__(nlist, default_r_cut, 0.0, mode)
+        self._kT = float(kT)
+
+    @property
+    def kT(self):
+        return self._kT
+
+    @kT.setter
+    def kT(self, v):
+        self._kT = float(v)
+        if self._cpp_obj is not None:
+            self._cpp_obj.dpdKT = self._kT
+
+    def _attach(self, simulation, cpp_nlist):
+        obj = super()._attach(simulation, cpp_nlist)
+        obj.dpdKT = self._kT
+        return obj
+
+
+class DPD(_DPDBase):
+    """DPD (EvaluatorPairDPDThermoDPD.h): conservative force A (1 - r/r_c), drag
+    -gamma w^2 (r . v) / r and random force sqrt(6 gamma kT / dt) w alpha, w = 1 - r/r_c."""
+
+    _accepted_modes = ("none",)
+
+    def __init__(self, nlist, kT, default_r_cut=None):
+        super().__init__(nlist, kT, default_r_cut, 'none')
+        self.params = TypePairDict(validator=dict_validator(("A", "gamma")))
+
+    def _set_pair_params(self, cpp, i, j, v):
+        cpp.setParamsDPD(i, j, False, float(v["A"]), 0.0, float(v["gamma"]))
+
+
+class DPDLJ(_DPDBase):
+    """DPD thermostat with a Lennard-Jones conservative force (EvaluatorPairDPDThermoLJ.h)."""
+
+    _accepted_modes = ("none", "shift")
+
+    def __init__(self, nlist, kT, default_r_cut=None, mode='none'):
+        super().__init__(nlist, kT, default_r_cut, mode)
+        self.params = TypePairDict(validator=dict_validator(("epsilon", "sigma", "gamma")))
+
+    def _set_pair_params(self, cpp, i, j, v):
+        cpp.setParamsDPD(i, j, True, float(v["epsilon"]), float(v["sigma"]), float(v["gamma"]))

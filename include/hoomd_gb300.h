@@ -301,6 +301,28 @@ typedef struct gb_radial_param
 int gb_pair_forces_radial(const gb_pair_args* args, const gb_radial_param* d_params,
                           void* stream);
 
+/* DPD thermostat pair forces (EvaluatorPairDPDThermoDPD.h:190-272, EvaluatorPairDPDThermoLJ.h:
+ * 216-276, PotentialPairDPDThermo.h:160-240): a conservative part (DPD: A (1 - r/r_c); DPDLJ:
+ * the LJ force with lj1 = 4 eps sigma^12, lj2 = 4 eps sigma^6), a drag
+ * -gamma w(r)^2 (r_ij . v_ij) / r with w = 1 - r/r_c, and a random force
+ * sqrt(6 gamma kT / dt) w(r) alpha with alpha uniform in [-1, 1] drawn from Philox with
+ * Seed(22, timestep, seed), Counter(min(tag_i, tag_j), max(tag_i, tag_j)), so both particles of a
+ * pair draw the same number. Energies and the virial use the conservative part only.
+ * Column-major list interleaved by 4 (args->interleave == 4). d_vel: float4[N] velocities (mass in
+ * w); d_tag: [N] tags. lj = 0: DPD (param a), lj = 1: DPDLJ (lj1, lj2; shift_mode 1 subtracts the
+ * LJ energy at r_cut). */
+typedef struct gb_dpd_param
+    {
+    float a;     /* DPD conservative amplitude A */
+    float lj1;   /* DPDLJ: 4 eps sigma^12 */
+    float lj2;   /* DPDLJ: 4 eps sigma^6 */
+    float gamma; /* drag coefficient */
+    } gb_dpd_param;
+
+int gb_pair_forces_dpd(const gb_pair_args* args, const gb_dpd_param* d_params,
+                       const float* d_vel, const uint32_t* d_tag, int lj, uint64_t timestep,
+                       uint16_t seed, float dt, float kT, void* stream);
+
 /* ---------------------------------------------------------------------------------------------
  * Integrator halves. Replace gpu_nvt_rescale_step_one / _two
  * (hoomd/md/TwoStepConstantVolumeGPU.cu:35-89, 166-205; with scale 1 these are the NVE halves of
