@@ -851,6 +851,7 @@ void Integrator::set_thermostat_none()
     bussi = false;
     berendsen = mttk = false;
     langevin = false;
+    brownian = false;
     prepared = false;
     drop_graphs();
     }
@@ -861,6 +862,7 @@ void Integrator::set_langevin(double kT_, const std::vector<double>& gamma_, boo
         throw std::invalid_argument("Langevin: one drag coefficient per particle type");
     bussi = false;
     berendsen = mttk = false;
+    brownian = false;
     langevin = true;
     tally = tally_;
     langevin_kT = kT_;
@@ -943,6 +945,32 @@ double Integrator::mttk_energy()
     return dof() * kT * (st[0] * st[0] * tau * tau / 2.0 + st[1]);
     }
 
+void Integrator::set_brownian(double kT_, const std::vector<double>& gamma_, bool noiseless)
+    {
+    if (gamma_.size() != pdata->ntypes)
+        throw std::invalid_argument("Brownian: one drag coefficient per particle type");
+    for (double g : gamma_)
+        if (!(g > 0.0))
+            throw std::invalid_argument("Brownian: drag coefficients must be positive");
+    bussi = berendsen = mttk = langevin = false;
+    brownian = true;
+    bd_noiseless = noiseless;
+    bd_kT = kT_;
+    gamma.assign(gamma_.begin(), gamma_.end());
+    d_gamma.resize(gamma.size());
+    cuda_check(cudaMemcpy(d_gamma.get(), gamma.data(), sizeof(float) * gamma.size(),
+                          cudaMemcpyHostToDevice),
+               "gamma");
+    prepared = false;
+    drop_graphs();
+    }
+
+void Integrator::set_max_displacement(double d)
+    {
+    max_disp = d > 0.0 ? d : 0.0;
+    drop_graphs();
+    }
+
 double Integrator::reservoir_energy()
     {
     if (!prepared)
@@ -968,8 +996,9 @@ void Integrator::set_sorter(uint64_t period, int bits)
 // (hoomd/md/IntegratorTwoStep.cc:154-199): D*N - D.
 double Integrator::dof() const
     {
-    // Langevin does not conserve momentum (TwoStepLangevinBase::isMomentumConserving): D*N
-    if (langevin)
+    // Langevin and Brownian dynamics do not conserve momentum
+    // (TwoStepLangevinBase::isMomentumConserving): D*N
+    if (langevin || brownian)
         return double(pdata->ndim) * pdata->N;
     return double(pdata->ndim) * pdata->N - double(pdata->ndim);
     }
@@ -1083,6 +1112,20 @@ gb_step_one_args Integrator::step_one_args(DevStatus* ds) const
     o.r_buff = nlist->r_buff;
     o.d_rebuild = &ds->rebuild;
     o.nve_order = langevin ? 1 : 0;
+    o.max_displacement = (float)max_disp;
+    if (brownian)
+        {
+        o.brownian = 1;
+        o.d_scale = nullptr;
+        o.d_bd_force = forces.size() > 1 ? net_force.get() : forces[0]->force.get();
+        o.d_tag = pd.tag.get();
+        o.d_gamma = d_gamma.get();
+        o.bd_kT = (float)bd_kT;
+        o.ndim = pd.ndim;
+        o.seed = pd.seed;
+        o.d_timestep = &ds->timestep;
+        o.noiseless = bd_noiseless ? 1 : 0;
+        }
     if (mttk)
         {
         o.d_mttk_state = ds->mttk;
@@ -1105,6 +1148,7 @@ gb_step_fuse Integrator::fuse_args(DevStatus* ds) const
     fu.dt = (float)dt;
     fu.d_scale2 = mttk ? &ds->mttk_scale2 : nullptr;
     fu.berendsen = berendsen ? 1 : 0;
+    fu.brownian = brownian ? 1 : 0;
     fu.d_scratch = d_step_scratch.get();
     fu.d_thermo = ds->thermo;
     fu.bussi = bussi ? 1 : 0;
@@ -1152,7 +1196,13 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
     {
     ParticleData& pd = *pdata;
     DevStatus* ds = d_status.get();
-    const gb_step_one_args o = step_one_args(ds);
+    gb_step_one_args o = step_one_args(ds);
+    if (brownian)
+        {
+        // the device step counter advances only on the fused path; here the host knows it
+        o.d_timestep = nullptr;
+        o.timestep = step;
+        }
     check(gb_md_step_one(&o, s), "gb_md_step_one");
     nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
     for (auto& f : forces)
@@ -1179,6 +1229,13 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
                                    pd.seed, &ds->timestep, d_step_scratch.get(), ds->thermo,
                                    tally ? &ds->reservoir : nullptr, s),
               "gb_langevin_step_two");
+        }
+    else if (brownian)
+        {
+        // TwoStepBD has no second half; the sums only
+        check(gb_thermo_reduce(pd.vel.get(), net, nullptr, 0, pd.N, d_thermo_scratch.get(),
+                               ds->thermo, s),
+              "thermo");
         }
     else
         {
@@ -1285,7 +1342,7 @@ void Integrator::run_chunk(unsigned int k)
                 enqueue_step_general(s, pd.timestep + i);
             launch_count += (uint64_t)k
                             * (1 + cell_kernels + 1 + forces.size() + (forces.size() > 1 ? 1 : 0)
-                               + (langevin ? 1 : 2) + ((bussi || berendsen) ? 1 : 0));
+                               + (langevin || brownian ? 1 : 2) + ((bussi || berendsen) ? 1 : 0));
             }
         DevStatus st = read_status();
         if (st.cell_cond[1])
@@ -1360,6 +1417,9 @@ void Integrator::sort_particles()
         apply(f->force.get(), 16);
         f->virial_valid = false;
         }
+    // Brownian step one reads the summed force of the last step
+    if (net_force.size() == 4 * (size_t)pd.N)
+        apply(net_force.get(), 16);
     // the old scratch counter words may have been overwritten: re-zero the thermo scratch
     pd.scratch.zero(s);
     pd.sort_generation++;

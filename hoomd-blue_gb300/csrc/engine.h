@@ -294,6 +294,10 @@ class Integrator
     void set_mttk_state(double xi, double eta);
     void thermalize_mttk(uint64_t timestep);         // MTTKThermostat::thermalizeThermostat
     double mttk_energy();                            // MTTKThermostat::getThermostatEnergy
+    // TwoStepBD (Brownian; noiseless = OverdampedViscous), translational part
+    void set_brownian(double kT, const std::vector<double>& gamma, bool noiseless);
+    // DisplacementCapped: limit of |v| dt in the ConstantVolume step one (0 = none)
+    void set_max_displacement(double d);
     void set_sorter(uint64_t period, int grid_bits);
     void set_chunk(unsigned int steps)
         {
@@ -313,6 +317,9 @@ class Integrator
     double kT = 1.0, tau = 0.0;
     bool langevin = false, tally = false;
     bool berendsen = false, mttk = false;
+    bool brownian = false, bd_noiseless = false;
+    double bd_kT = 1.0;
+    double max_disp = 0.0;
     double mttk_host[2] = {0.0, 0.0}; // xi, eta carried across prepare()
     double langevin_kT = 1.0;
     std::vector<float> gamma;

@@ -57,6 +57,9 @@ inline int make_fuse_args(const gb_pair_args* a, const gb_step_fuse* f, FuseArgs
     fz.ndim = f->ndim ? f->ndim : 3u;
     fz.d_reservoir = f->d_reservoir;
     fz.berendsen = f->berendsen;
+    fz.brownian = f->brownian;
+    GB_REQUIRE(!f->brownian || (!f->bussi && !f->langevin && !f->berendsen && !f->d_scale2),
+               "fused step: Brownian dynamics excludes the velocity-Verlet methods");
     GB_REQUIRE(!f->berendsen || (!f->bussi && !f->langevin && f->d_factor && f->d_status
                                  && f->tau > 0.0),
                "fused step: Berendsen needs the factor and status buffers and tau > 0, and "

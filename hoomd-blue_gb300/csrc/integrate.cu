@@ -82,6 +82,21 @@ struct StepOneCheck
     uint32_t* rebuild;
     };
 
+// Brownian dynamics (TwoStepBD) and the DisplacementCapped limit of step one.
+struct StepOneExtra
+    {
+    float max_disp;           // > 0: cap |v| dt at this length (ConstantVolume order only)
+    const float4* force;      // BD: net force
+    const uint32_t* tag;      // BD: tags (random-number counters)
+    const float* gamma;       // BD: drag per type
+    float kT;
+    unsigned int ndim;
+    uint16_t seed;
+    const uint64_t* d_timestep; // BD: current step on the device, or NULL to use timestep
+    uint64_t timestep;
+    int noiseless;            // OverdampedViscous: no random force, v = F / gamma
+    };
+
 // MTTK thermostat state and the reduction scratch of step one.
 struct MttkStep
     {
@@ -92,11 +107,12 @@ struct MttkStep
     double* partials;
     };
 
-template<bool CHECK, bool NVE, bool MTTK>
+template<bool CHECK, bool NVE, bool MTTK, bool BD>
 __global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
                            const float* __restrict__ accel, int* __restrict__ image,
                            unsigned int N, gb_box box, float dt, float scale,
-                           const double* __restrict__ d_scale, StepOneCheck chk, MttkStep mk)
+                           const double* __restrict__ d_scale, StepOneCheck chk, MttkStep mk,
+                           StepOneExtra ex)
     {
     const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool moved = false;
@@ -114,9 +130,44 @@ __global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
         const float s = MTTK ? s_mttk : ((!NVE && d_scale) ? (float)*d_scale : scale);
         float4 v = vel[j];
         float4 p = pos[j];
-        const float ax = accel[3 * (size_t)j], ay = accel[3 * (size_t)j + 1],
-                    az = accel[3 * (size_t)j + 2];
-        if (NVE)
+        const float ax = BD ? 0.0f : accel[3 * (size_t)j], ay = BD ? 0.0f : accel[3 * (size_t)j + 1],
+                    az = BD ? 0.0f : accel[3 * (size_t)j + 2];
+        if (BD)
+            {
+            // TwoStepBD::integrateStepOne (hoomd/md/TwoStepBD.cc:90-151): three uniform draws
+            // from Seed(24, timestep, seed), Counter(tag); x += (F + F_r) dt / gamma with
+            // F_r = r sqrt(6 gamma kT / dt); then new velocities from the same stream
+            // (NormalDistribution(sqrt(kT / m))), or F / gamma without noise
+            const uint64_t ts = ex.d_timestep ? *ex.d_timestep : ex.timestep;
+            Philox rng(24, ts, ex.seed, ex.tag[j]);
+            const float rx = uniform_m11_f(rng);
+            const float ry = uniform_m11_f(rng);
+            const float rz = uniform_m11_f(rng);
+            const float gamma = ex.gamma[__float_as_uint(p.w)];
+            float coeff = __fsqrt_rn(__fdiv_rn(fmul(fmul(6.0f, gamma), ex.kT), dt));
+            if (ex.noiseless)
+                coeff = 0.0f;
+            const float frx = fmul(rx, coeff), fry = fmul(ry, coeff);
+            const float frz = ex.ndim < 3 ? 0.0f : fmul(rz, coeff);
+            const float4 f = ex.force[j];
+            p.x = fadd(p.x, __fdiv_rn(fmul(fadd(f.x, frx), dt), gamma));
+            p.y = fadd(p.y, __fdiv_rn(fmul(fadd(f.y, fry), dt), gamma));
+            p.z = fadd(p.z, __fdiv_rn(fmul(fadd(f.z, frz), dt), gamma));
+            if (ex.noiseless)
+                {
+                v.x = __fdiv_rn(f.x, gamma);
+                v.y = __fdiv_rn(f.y, gamma);
+                v.z = ex.ndim > 2 ? __fdiv_rn(f.z, gamma) : 0.0f;
+                }
+            else
+                {
+                const float sigma = __fsqrt_rn(__fdiv_rn(ex.kT, v.w));
+                v.x = normal_f(rng) * sigma + 0.0f;
+                v.y = normal_f(rng) * sigma + 0.0f;
+                v.z = ex.ndim > 2 ? normal_f(rng) * sigma + 0.0f : 0.0f;
+                }
+            }
+        else if (NVE)
             {
             // x += v dt + (1/2) a dt^2 ; v += (1/2) a dt   (TwoStepNVEGPU.cu:68-98,
             // TwoStepLangevin.cc:57-81)
@@ -136,6 +187,21 @@ __global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
             v.x = fmul(v.x, s);
             v.y = fmul(v.y, s);
             v.z = fmul(v.z, s);
+            if (ex.max_disp > 0.0f)
+                {
+                // DisplacementCapped: |v| dt at most the limit, the documented behaviour of
+                // hoomd/md/methods/methods.py:583-598. (The reference's CPU path,
+                // TwoStepConstantVolume.cc:44-52, divides by dt once more and its GPU path,
+                // TwoStepConstantVolumeGPU.cu:69-74, multiplies by dt instead; neither caps the
+                // step at the limit.) With len = |v| dt, v / len * limit has length limit / dt.
+                const float len = fmul(__fsqrt_rn(dot3(v.x, v.y, v.z)), dt);
+                if (len > ex.max_disp)
+                    {
+                    v.x = fmul(__fdiv_rn(v.x, len), ex.max_disp);
+                    v.y = fmul(__fdiv_rn(v.y, len), ex.max_disp);
+                    v.z = fmul(__fdiv_rn(v.z, len), ex.max_disp);
+                    }
+                }
             p.x = fadd(p.x, fmul(dt, v.x));
             p.y = fadd(p.y, fmul(dt, v.y));
             p.z = fadd(p.z, fmul(dt, v.z));
@@ -374,9 +440,9 @@ extern "C"
         if (N == 0)
             return GB_OK;
         StepOneCheck none {nullptr, nullptr, 0.0f, nullptr};
-        k_step_one<false, false, false><<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
+        k_step_one<false, false, false, false><<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
             reinterpret_cast<float4*>(d_pos), reinterpret_cast<float4*>(d_vel), d_accel, d_image,
-            N, *box, dt, scale, d_scale, none, MttkStep {});
+            N, *box, dt, scale, d_scale, none, MttkStep {}, StepOneExtra {});
         return check_launch("gb_cv_step_one");
         }
 
@@ -409,16 +475,37 @@ extern "C"
             mk.partials
                 = reinterpret_cast<double*>(reinterpret_cast<char*>(a->d_mttk_scratch) + 256);
             }
-        auto kern = a->d_last_pos
-                        ? (mttk ? k_step_one<true, false, true>
-                                : (a->nve_order ? k_step_one<true, true, false>
-                                                : k_step_one<true, false, false>))
-                        : (mttk ? k_step_one<false, false, true>
-                                : (a->nve_order ? k_step_one<false, true, false>
-                                                : k_step_one<false, false, false>));
+        const bool bd = a->brownian != 0;
+        GB_REQUIRE(!bd || (a->d_bd_force && a->d_tag && a->d_gamma && !mttk && !a->nve_order),
+                   "gb_md_step_one: Brownian dynamics needs the net force, tags and drag "
+                   "coefficients, and excludes the other methods");
+        StepOneExtra ex {};
+        ex.max_disp = (!a->nve_order && !bd) ? a->max_displacement : 0.0f;
+        ex.force = reinterpret_cast<const float4*>(a->d_bd_force);
+        ex.tag = a->d_tag;
+        ex.gamma = a->d_gamma;
+        ex.kT = a->bd_kT;
+        ex.ndim = a->ndim ? a->ndim : 3u;
+        ex.seed = (uint16_t)a->seed;
+        ex.d_timestep = a->d_timestep;
+        ex.timestep = a->timestep;
+        ex.noiseless = a->noiseless;
+        using K = void (*)(float4*, float4*, const float*, int*, unsigned int, gb_box, float,
+                           float, const double*, StepOneCheck, MttkStep, StepOneExtra);
+        K kern;
+        if (a->d_last_pos)
+            kern = bd ? k_step_one<true, false, false, true>
+                      : (mttk ? k_step_one<true, false, true, false>
+                              : (a->nve_order ? k_step_one<true, true, false, false>
+                                              : k_step_one<true, false, false, false>));
+        else
+            kern = bd ? k_step_one<false, false, false, true>
+                      : (mttk ? k_step_one<false, false, true, false>
+                              : (a->nve_order ? k_step_one<false, true, false, false>
+                                              : k_step_one<false, false, false, false>));
         kern<<<div_up(a->N, 256), 256, 0, s>>>(
             reinterpret_cast<float4*>(a->d_pos), reinterpret_cast<float4*>(a->d_vel), a->d_accel,
-            a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk, mk);
+            a->d_image, a->N, a->box, a->dt, a->scale, a->d_scale, chk, mk, ex);
         return check_launch("gb_md_step_one");
         }
 

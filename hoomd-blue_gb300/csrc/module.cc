@@ -221,6 +221,8 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setBussi", &Integrator::set_thermostat_bussi)
         .def("setNoThermostat", &Integrator::set_thermostat_none)
         .def("setLangevin", &Integrator::set_langevin)
+        .def("setBrownian", &Integrator::set_brownian)
+        .def("setMaxDisplacement", &Integrator::set_max_displacement)
         .def("setBerendsen", &Integrator::set_thermostat_berendsen)
         .def("setMTTK", &Integrator::set_thermostat_mttk)
         .def("getMTTKState", &Integrator::mttk_state)

@@ -53,6 +53,7 @@ struct FuseArgs
     unsigned int ndim;
     double* d_reservoir;    // optional Langevin reservoir energy
     int berendsen;          // draw-free Berendsen factor for the next step one into d_factor
+    int brownian;           // no second half (Brownian dynamics): sums only
     };
 
 template<int TPP> __device__ __forceinline__ double block_sum_d(double v, double* s_red)
@@ -80,6 +81,14 @@ __device__ __forceinline__ void fuse_step_two(const FuseArgs& fz, unsigned int g
                                               double& pe_d, double& w_d)
     {
     float4 v = fz.vel[gi];
+    if (fz.brownian)
+        {
+        ke_d = (double)v.w
+               * ((double)v.x * (double)v.x + (double)v.y * (double)v.y
+                  + (double)v.z * (double)v.z);
+        pe_d = (double)pe;
+        return;
+        }
     const float minv = __frcp_rn(v.w);
     float ax, ay, az;
     if (fz.langevin)

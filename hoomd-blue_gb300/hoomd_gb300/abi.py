@@ -59,7 +59,11 @@ class StepOneArgs(ctypes.Structure):
                 ("d_scale", c_void), ("d_last_pos", c_void), ("d_rcut_max", c_void),
                 ("r_buff", c_float), ("d_rebuild", c_void), ("nve_order", c_int),
                 ("d_mttk_state", c_void), ("d_mttk_scale2", c_void), ("mttk_dof", c_double),
-                ("mttk_kT", c_double), ("mttk_tau", c_double), ("d_mttk_scratch", c_void)]
+                ("mttk_kT", c_double), ("mttk_tau", c_double), ("d_mttk_scratch", c_void),
+                ("max_displacement", c_float), ("brownian", c_int), ("d_bd_force", c_void),
+                ("d_tag", c_void), ("d_gamma", c_void), ("bd_kT", c_float),
+                ("ndim", ctypes.c_uint32), ("seed", ctypes.c_uint32), ("d_timestep", c_void),
+                ("timestep", c_u64), ("noiseless", c_int)]
 
 
 class StepFuse(ctypes.Structure):
@@ -70,7 +74,8 @@ class StepFuse(ctypes.Structure):
                 ("d_rebuild_reset", c_void), ("d_bussi_ring", c_void),
                 ("bussi_ring_size", c_uint), ("langevin", c_int), ("d_tag", c_void),
                 ("d_pos", c_void), ("d_gamma", c_void), ("langevin_kT", c_float),
-                ("ndim", ctypes.c_uint32), ("d_reservoir", c_void), ("berendsen", c_int)]
+                ("ndim", ctypes.c_uint32), ("d_reservoir", c_void), ("berendsen", c_int),
+                ("brownian", c_int)]
 
 
 class RadialParam(ctypes.Structure):

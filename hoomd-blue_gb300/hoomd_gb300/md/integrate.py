@@ -33,8 +33,7 @@ class Integrator:
 
     def _attach(self, simulation):
         if len(self.methods) != 1:
-            raise NotImplementedError("exactly one integration method (ConstantVolume or "
-                                      "Langevin) is supported")
+            raise NotImplementedError("exactly one integration method is supported")
         if not self.forces:
             raise RuntimeError("the integrator needs at least one force")
         nl = self.forces[0].nlist

@@ -1,5 +1,6 @@
 """Integration methods (hoomd/md/methods/methods.py): ConstantVolume (NVE without a thermostat, NVT
-with one) and Langevin, each over the group of all particles."""
+with one), DisplacementCapped, Langevin, Brownian and OverdampedViscous, each over the group of
+all particles."""
 
 from hoomd_gb300.filter import All
 from hoomd_gb300.md.data import TypeDict, nonnegative_real
@@ -117,3 +118,81 @@ class Langevin(Method):
         self._types = list(state.particle_types)
         self._cpp_integ = integ
         self._apply(integ)
+
+
+class DisplacementCapped(ConstantVolume):
+    """ConstantVolume without a thermostat whose step one caps each particle's displacement at
+    ``maximum_displacement`` (hoomd/md/methods/methods.py:583-635, TwoStepConstantVolume.cc:44-52);
+    a constant here."""
+
+    def __init__(self, filter, maximum_displacement):
+        super().__init__(filter, thermostat=None)
+        self._max = float(maximum_displacement)
+
+    @property
+    def maximum_displacement(self):
+        return self._max
+
+    @maximum_displacement.setter
+    def maximum_displacement(self, v):
+        self._max = float(v)
+        if self._cpp_integ is not None:
+            self._cpp_integ.setMaxDisplacement(self._max)
+
+    def _apply(self, integ):
+        super()._apply(integ)
+        integ.setMaxDisplacement(self._max)
+
+
+class Brownian(Method):
+    """Brownian dynamics (hoomd/md/methods/methods.py:835-1023, hoomd/md/TwoStepBD.cc): each step
+    x += (F + F_r) dt / gamma with a uniform random force of variance 2 kT gamma / dt per
+    direction, and velocities drawn from the Maxwell-Boltzmann distribution at kT (they carry
+    no dynamics). The random numbers follow the reference's stream (Seed(24, timestep, seed),
+    Counter(tag)). Translational degrees of freedom only; ``kT`` is a constant."""
+
+    _noiseless = False
+
+    def __init__(self, filter, kT, default_gamma=1.0, default_gamma_r=(1.0, 1.0, 1.0)):
+        if not isinstance(filter, All):
+            raise NotImplementedError(f"{type(self).__name__} integrates the group of all "
+                                      "particles")
+        self.filter = filter
+        self._kT = float(kT)
+        self.gamma = TypeDict(default=float(default_gamma), validator=nonnegative_real)
+        self.gamma_r = TypeDict(default=_gamma_r(default_gamma_r), validator=_gamma_r)
+        self.gamma._on_change = self.gamma_r._on_change = lambda key: self._reapply()
+        self._cpp_integ = None
+        self._types = None
+
+    @property
+    def kT(self):
+        return self._kT
+
+    @kT.setter
+    def kT(self, v):
+        self._kT = float(v)
+        self._reapply()
+
+    def _reapply(self):
+        if self._cpp_integ is not None:
+            self._apply(self._cpp_integ)
+
+    def _apply(self, integ):
+        integ.setBrownian(self._kT, [float(self.gamma[t]) for t in self._types],
+                          self._noiseless)
+
+    def _attach(self, integ, state=None):
+        self._types = list(state.particle_types)
+        self._cpp_integ = integ
+        self._apply(integ)
+
+
+class OverdampedViscous(Brownian):
+    """Overdamped viscous dynamics (hoomd/md/methods/methods.py:1025-1160): Brownian dynamics
+    without the random force, x += F dt / gamma and v = F / gamma."""
+
+    _noiseless = True
+
+    def __init__(self, filter, default_gamma=1.0, default_gamma_r=(1.0, 1.0, 1.0)):
+        super().__init__(filter, 0.0, default_gamma, default_gamma_r)

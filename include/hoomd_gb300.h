@@ -418,6 +418,24 @@ typedef struct gb_step_one_args
     double* d_mttk_scale2;
     double mttk_dof, mttk_kT, mttk_tau;
     void* d_mttk_scratch;       /* gb_thermo_scratch_bytes(N), zeroed once before first use */
+    /* DisplacementCapped (hoomd/md/TwoStepConstantVolume.cc:44-52): when > 0 (ConstantVolume
+       order), velocities with |v| dt above this length are scaled down to it */
+    float max_displacement;
+    /* Brownian dynamics, TwoStepBD::integrateStepOne (hoomd/md/TwoStepBD.cc:47-151), instead of
+       the velocity-Verlet half: x += (F + F_r) dt / gamma, F_r uniform of amplitude
+       sqrt(6 gamma kT / dt) from Philox Seed(24, timestep, seed), Counter(tag); velocities drawn
+       from NormalDistribution(sqrt(kT / m)) of the same stream, or set to F / gamma when
+       noiseless (OverdampedViscous). Excludes nve_order and MTTK; scale is ignored. */
+    int brownian;
+    const float* d_bd_force;    /* float4[N] net force at the current positions */
+    const uint32_t* d_tag;      /* [N] */
+    const float* d_gamma;       /* [ntypes] */
+    float bd_kT;
+    uint32_t ndim;              /* 2: no random force or velocity along z */
+    uint32_t seed;              /* low 16 bits */
+    const uint64_t* d_timestep; /* current step on the device; NULL = use timestep */
+    uint64_t timestep;
+    int noiseless;
     } gb_step_one_args;
 
 int gb_md_step_one(const gb_step_one_args* args, void* stream);
@@ -457,6 +475,9 @@ typedef struct gb_step_fuse
        sqrt(1 + dt/tau (kT / T - 1)), T = 2 KE / dof, into d_factor; bit 1 of d_status when the
        kinetic energy is zero. Excludes bussi and langevin */
     int berendsen;
+    /* Brownian dynamics has no second half: the epilogue writes the forces and the sums (KE of
+       the velocities step one drew, PE) and leaves the velocities as they are */
+    int brownian;
     } gb_step_fuse;
 
 /* The Berendsen factor from a kinetic energy on the device (the first step of a run). */

@@ -740,7 +740,7 @@ void pair_forces(unsigned int N,
 // ------------------------------------------------------------------------------------------------
 template<class R>
 void cv_step_one(unsigned int N, R* pos, R* vel, const R* accel, int* image, const Box<R>& box,
-                 R dt, R s, int nthreads = 1)
+                 R dt, R s, int nthreads = 1, R limit = R(0))
     {
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static) num_threads(std::max(nthreads, 1))
@@ -755,6 +755,19 @@ void cv_step_one(unsigned int N, R* pos, R* vel, const R* accel, int* image, con
         vx *= s;
         vy *= s;
         vz *= s;
+        if (limit > R(0))
+            {
+            // DisplacementCapped (hoomd/md/TwoStepConstantVolume.cc:44-52) with the step capped at
+            // the limit as hoomd/md/methods/methods.py:583-598 documents: the reference's
+            // expression divides by dt once more, which caps the step at limit / dt instead
+            R len = std::sqrt(vx * vx + vy * vy + vz * vz) * dt;
+            if (len > limit)
+                {
+                vx = vx / len * limit;
+                vy = vy / len * limit;
+                vz = vz / len * limit;
+                }
+            }
         px += dt * vx;
         py += dt * vy;
         pz += dt * vz;
@@ -1063,6 +1076,53 @@ double langevin_step_two(unsigned int N, R* vel, R* accel, const R* pos, const u
             += bd_fx * vel[4 * j] + bd_fy * vel[4 * j + 1] + bd_fz * vel[4 * j + 2];
         }
     return double(bd_energy_transfer);
+    }
+
+// ------------------------------------------------------------------------------------------------
+// Brownian dynamics, TwoStepBD::integrateStepOne (hoomd/md/TwoStepBD.cc:47-151), translational
+// part: three UniformDistribution<R>(-1, 1) draws from Seed(24, timestep, seed), Counter(tag);
+// x += (F + F_r) dt / gamma, F_r = r sqrt(6 gamma T / dt) (z zero in 2D); wrap; velocities from
+// NormalDistribution<R>(sqrt(T / m)) of the same stream, or F / gamma when noiseless.
+// ------------------------------------------------------------------------------------------------
+template<class R>
+void bd_step_one(unsigned int N, R* pos, R* vel, const R* force, int* image,
+                 const unsigned int* tags, const R* gamma_t, const Box<R>& box, R T, R dt,
+                 uint16_t seed, uint64_t timestep, int ndim, bool noiseless)
+    {
+    for (unsigned int j = 0; j < N; j++)
+        {
+        RNG rng(24, timestep, seed, tags[j]);
+        R rx = uniform_m11<R>(rng);
+        R ry = uniform_m11<R>(rng);
+        R rz = uniform_m11<R>(rng);
+        R gamma = gamma_t[as_uint(pos[4 * j + 3])];
+        R coeff = std::sqrt(R(3.0) * R(2.0) * gamma * T / dt);
+        if (noiseless)
+            coeff = R(0.0);
+        R frx = rx * coeff, fry = ry * coeff, frz = rz * coeff;
+        if (ndim < 3)
+            frz = R(0.0);
+        R px = pos[4 * j] + (force[4 * j] + frx) * dt / gamma;
+        R py = pos[4 * j + 1] + (force[4 * j + 1] + fry) * dt / gamma;
+        R pz = pos[4 * j + 2] + (force[4 * j + 2] + frz) * dt / gamma;
+        box.wrap(px, py, pz, image[3 * j], image[3 * j + 1], image[3 * j + 2]);
+        pos[4 * j] = px;
+        pos[4 * j + 1] = py;
+        pos[4 * j + 2] = pz;
+        if (noiseless)
+            {
+            vel[4 * j] = force[4 * j] / gamma;
+            vel[4 * j + 1] = force[4 * j + 1] / gamma;
+            vel[4 * j + 2] = ndim > 2 ? force[4 * j + 2] / gamma : R(0);
+            }
+        else
+            {
+            R sigma = std::sqrt(T / vel[4 * j + 3]);
+            vel[4 * j] = normal<R>(rng, sigma);
+            vel[4 * j + 1] = normal<R>(rng, sigma);
+            vel[4 * j + 2] = ndim > 2 ? normal<R>(rng, sigma) : R(0);
+            }
+        }
     }
 
 // ------------------------------------------------------------------------------------------------
@@ -1672,6 +1732,29 @@ using namespace orc;
     ORC_EXPORT double orc_sim_reservoir_##SUF(void* h)                                             \
         {                                                                                          \
         return ((Sim<R>*)h)->reservoir;                                                            \
+        }                                                                                          \
+    ORC_EXPORT void orc_cv_step_one_capped_##SUF(unsigned int N, R* pos, R* vel, const R* accel,   \
+                                                 int* image, const double* b6, const int* per,     \
+                                                 double dt, double s, double limit)                \
+        {                                                                                          \
+        Box<R> box;                                                                                \
+        box.set(b6, per);                                                                          \
+        cv_step_one<R>(N, pos, vel, accel, image, box, R(dt), R(s), 1, R(limit));                  \
+        }                                                                                          \
+    ORC_EXPORT void orc_bd_step_one_##SUF(unsigned int N, R* pos, R* vel, const R* force,          \
+                                          int* image, const unsigned int* tags,                    \
+                                          const double* gamma, unsigned int ntypes,                \
+                                          const double* b6, const int* per, double kT, double dt,  \
+                                          unsigned int seed, uint64_t timestep, int ndim,          \
+                                          int noiseless)                                           \
+        {                                                                                          \
+        Box<R> box;                                                                                \
+        box.set(b6, per);                                                                          \
+        std::vector<R> g(ntypes);                                                                  \
+        for (unsigned int t = 0; t < ntypes; t++)                                                  \
+            g[t] = R(gamma[t]);                                                                    \
+        bd_step_one<R>(N, pos, vel, force, image, tags, g.data(), box, R(kT), R(dt),               \
+                       uint16_t(seed), timestep, ndim, noiseless != 0);                            \
         }                                                                                          \
     ORC_EXPORT void orc_nve_step_one_##SUF(unsigned int N, R* pos, R* vel, const R* accel,         \
                                            int* image, const double* b6, const int* per,           \

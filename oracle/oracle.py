@@ -319,6 +319,41 @@ def nve_step_one(pos4, vel4, accel3, image3, box, dt, prec=32, periodic=(1, 1, 1
     return pos4, vel4, image3
 
 
+def cv_step_one_capped(pos4, vel4, accel3, image3, box, dt, s, limit, prec=32,
+                       periodic=(1, 1, 1)):
+    """ConstantVolume step one with the DisplacementCapped limit."""
+    R = rdtype(prec)
+    pos4 = np.ascontiguousarray(pos4, R).copy()
+    vel4 = np.ascontiguousarray(vel4, R).copy()
+    accel3 = np.ascontiguousarray(accel3, R)
+    image3 = np.ascontiguousarray(image3, np.int32).copy()
+    b, p = box6(box), periodic3(periodic)
+    d = ctypes.c_double
+    getattr(lib(), f"orc_cv_step_one_capped_{suf(prec)}")(
+        len(pos4), ptr(pos4), ptr(vel4), ptr(accel3), ptr(image3), ptr(b), ptr(p), d(dt), d(s),
+        d(limit))
+    return pos4, vel4, image3
+
+
+def bd_step_one(pos4, vel4, force4, image3, tags, gamma, box, kT, dt, seed, timestep, ndim=3,
+                noiseless=False, prec=32, periodic=(1, 1, 1)):
+    """Brownian (or overdamped, noiseless) step one; returns (pos4, vel4, image3)."""
+    R = rdtype(prec)
+    pos4 = np.ascontiguousarray(pos4, R).copy()
+    vel4 = np.ascontiguousarray(vel4, R).copy()
+    f = np.ascontiguousarray(force4, R)
+    image3 = np.ascontiguousarray(image3, np.int32).copy()
+    tags = np.ascontiguousarray(tags, np.uint32)
+    g = np.ascontiguousarray(gamma, np.float64)
+    b, p = box6(box), periodic3(periodic)
+    getattr(lib(), f"orc_bd_step_one_{suf(prec)}")(
+        len(pos4), ptr(pos4), ptr(vel4), ptr(f), ptr(image3), ptr(tags), ptr(g),
+        ctypes.c_uint32(len(g)), ptr(b), ptr(p), ctypes.c_double(kT), ctypes.c_double(dt),
+        ctypes.c_uint32(seed), ctypes.c_uint64(timestep), ctypes.c_int(ndim),
+        ctypes.c_int(int(noiseless)))
+    return pos4, vel4, image3
+
+
 def langevin_step_two(vel4, pos4, tags, net_force4, gamma, kT, dt, seed, timestep, ndim=3,
                       prec=32):
     """Langevin step two; returns (vel4, accel3, sum of F_bd . v)."""
