@@ -159,6 +159,13 @@ void ParticleData::set_charges(const double* q)
     cuda_check(cudaStreamSynchronize(stream), "set_charges");
     }
 
+void ParticleData::set_box(const double* b6)
+    {
+    for (int d = 0; d < 6; d++)
+        box6[d] = b6[d];
+    check(gb_box_make(box6, box6[3], box6[4], box6[5], periodic, &box), "gb_box_make");
+    }
+
 std::vector<uint32_t> ParticleData::rtag()
     {
     std::vector<uint32_t> t(N), r(N);
@@ -1444,6 +1451,11 @@ void Integrator::run(uint64_t nsteps)
             f->upload();
             drop_graphs();
             }
+    if (npt)
+        {
+        run_npt(nsteps);
+        return;
+        }
     uint64_t done = 0;
     while (done < nsteps)
         {

@@ -148,6 +148,7 @@ class ParticleData
     void get_particles(double* pos, double* vel, double* mass, uint32_t* typeid_,
                        int32_t* image);
     std::vector<uint32_t> rtag(); // tag -> index
+    void set_box(const double* b6); // [Lx, Ly, Lz, xy, xz, yz]
     // per-particle charges in tag order (kept in index order on the device, sorted with the
     // particles); read by the pair forces that need them
     void set_charges(const double* q);
@@ -298,6 +299,16 @@ class Integrator
     void set_brownian(double kT, const std::vector<double>& gamma, bool noiseless);
     // DisplacementCapped: limit of |v| dt in the ConstantVolume step one (0 = none)
     void set_max_displacement(double d);
+    // ConstantPressure (TwoStepConstantPressure, MTK barostat), translational part; thermostat
+    // none or MTTK. S = (xx, yy, zz, yz, xz, xy); couple 0 none, 1 xy, 2 xz, 3 yz, 4 xyz;
+    // flags = box_dof (x, y, z, xy, xz, yz)
+    void set_npt(const std::vector<double>& S, double tauS, int couple,
+                 const std::vector<int>& box_dof, double gamma);
+    std::vector<double> barostat_dof();             // (nu_xx, nu_xy, nu_xz, nu_yy, nu_yz, nu_zz)
+    void set_barostat_dof(const std::vector<double>& nu);
+    double barostat_energy();
+    // FP64 sums over all forces: kinetic tensor (6), virial tensor (6), potential energy
+    std::vector<double> thermo_tensor();
     void set_sorter(uint64_t period, int grid_bits);
     void set_chunk(unsigned int steps)
         {
@@ -320,6 +331,13 @@ class Integrator
     bool brownian = false, bd_noiseless = false;
     double bd_kT = 1.0;
     double max_disp = 0.0;
+    bool npt = false;
+    double npt_S[6] = {0, 0, 0, 0, 0, 0}, npt_tauS = 1.0, npt_gamma = 0.0;
+    int npt_couple = 4;
+    unsigned int npt_flags = 7;
+    double nu[6] = {0, 0, 0, 0, 0, 0}; // xx, xy, xz, yy, yz, zz
+    double mat_v[6], mat_r[6], mat_ri[6];
+    std::vector<double> npt_tensor;     // thermo_tensor() at the last full step
     double mttk_host[2] = {0.0, 0.0}; // xi, eta carried across prepare()
     double langevin_kT = 1.0;
     std::vector<float> gamma;
@@ -350,6 +368,10 @@ class Integrator
     void enqueue_step_fused(cudaStream_t s);
     void enqueue_step_general(cudaStream_t s, uint64_t step);
     void run_chunk(unsigned int k);
+    void run_npt(uint64_t nsteps);
+    void npt_advance_barostat(uint64_t timestep);
+    void npt_update_propagator();
+    double npt_temperature() const;
     void checkpoint();
     void restore();
     cudaGraphExec_t graph_for(unsigned int k);

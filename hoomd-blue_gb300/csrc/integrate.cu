@@ -277,6 +277,143 @@ __global__ void k_step_two(float4* __restrict__ vel, float* __restrict__ accel,
     accel[3 * (size_t)j + 2] = az;
     }
 
+// ConstantPressure halves (TwoStepConstantPressure.cc:206-330, 587-640): upper-triangular
+// propagators m = (xx, xy, xz, yy, yz, zz) applied as the reference writes them.
+struct Tri
+    {
+    float m[6];
+    };
+
+__device__ __forceinline__ void tri_apply(const Tri& t, float& x, float& y, float& z)
+    {
+    const float nx = fadd(fadd(fmul(t.m[0], x), fmul(t.m[1], y)), fmul(t.m[2], z));
+    const float ny = fadd(fmul(t.m[3], y), fmul(t.m[4], z));
+    const float nz = fmul(t.m[5], z);
+    x = nx;
+    y = ny;
+    z = nz;
+    }
+
+__global__ void k_npt_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
+                               const float* __restrict__ accel, int* __restrict__ image,
+                               unsigned int N, gb_box box, float dt, float s, Tri mv, Tri mr,
+                               Tri mri)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N)
+        return;
+    float4 v = vel[j];
+    float4 p = pos[j];
+    const float hdt = __fdiv_rn(dt, 2.0f);
+    // v += dt/2 a ; v = M_v v ; v *= s ; r = M_r r ; r += M_r,int v
+    v.x = fadd(v.x, fmul(hdt, accel[3 * (size_t)j]));
+    v.y = fadd(v.y, fmul(hdt, accel[3 * (size_t)j + 1]));
+    v.z = fadd(v.z, fmul(hdt, accel[3 * (size_t)j + 2]));
+    tri_apply(mv, v.x, v.y, v.z);
+    v.x = fmul(v.x, s);
+    v.y = fmul(v.y, s);
+    v.z = fmul(v.z, s);
+    tri_apply(mr, p.x, p.y, p.z);
+    float ix = v.x, iy = v.y, iz = v.z;
+    tri_apply(mri, ix, iy, iz);
+    p.x = fadd(p.x, ix);
+    p.y = fadd(p.y, iy);
+    p.z = fadd(p.z, iz);
+    int wx = 0, wy = 0, wz = 0;
+    wrap(box, p.x, p.y, p.z, wx, wy, wz);
+    if (wx | wy | wz)
+        {
+        image[3 * (size_t)j] += wx;
+        image[3 * (size_t)j + 1] += wy;
+        image[3 * (size_t)j + 2] += wz;
+        }
+    vel[j] = v;
+    pos[j] = p;
+    }
+
+__global__ void k_npt_step_two(float4* __restrict__ vel, float* __restrict__ accel,
+                               const float4* __restrict__ net, unsigned int N, float dt, float s,
+                               Tri mv)
+    {
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N)
+        return;
+    float4 v = vel[j];
+    const float4 f = net[j];
+    const float minv = __frcp_rn(v.w);
+    const float ax = fmul(f.x, minv), ay = fmul(f.y, minv), az = fmul(f.z, minv);
+    v.x = fmul(v.x, s);
+    v.y = fmul(v.y, s);
+    v.z = fmul(v.z, s);
+    tri_apply(mv, v.x, v.y, v.z);
+    const float hdt = __fdiv_rn(dt, 2.0f);
+    v.x = fadd(v.x, fmul(hdt, ax));
+    v.y = fadd(v.y, fmul(hdt, ay));
+    v.z = fadd(v.z, fmul(hdt, az));
+    vel[j] = v;
+    accel[3 * (size_t)j] = ax;
+    accel[3 * (size_t)j + 1] = ay;
+    accel[3 * (size_t)j + 2] = az;
+    }
+
+// Kinetic and virial tensors in FP64: per block 13 partial sums (sum m v_a v_b, sum W_ab, PE),
+// then one block adds the partials in a fixed order.
+constexpr int TENSOR_TERMS = 13;
+
+__global__ void k_tensor_partials(const float4* __restrict__ vel, const float4* __restrict__ force,
+                                  const float* __restrict__ virial, size_t pitch, unsigned int N,
+                                  double* __restrict__ partials)
+    {
+    __shared__ double s[TENSOR_TERMS][256 / 32];
+    const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double t[TENSOR_TERMS];
+    for (int k = 0; k < TENSOR_TERMS; k++)
+        t[k] = 0.0;
+    if (j < N)
+        {
+        const float4 v = vel[j];
+        const double m = v.w, vx = v.x, vy = v.y, vz = v.z;
+        t[0] = m * vx * vx;
+        t[1] = m * vx * vy;
+        t[2] = m * vx * vz;
+        t[3] = m * vy * vy;
+        t[4] = m * vy * vz;
+        t[5] = m * vz * vz;
+        if (virial)
+            for (int k = 0; k < 6; k++)
+                t[6 + k] = (double)virial[k * pitch + j];
+        if (force)
+            t[12] = (double)force[j].w;
+        }
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+    for (int k = 0; k < TENSOR_TERMS; k++)
+        {
+        double x = warp_sum(t[k]);
+        if (lane == 0)
+            s[k][warp] = x;
+        }
+    __syncthreads();
+    if (threadIdx.x < TENSOR_TERMS)
+        {
+        double x = 0.0;
+        for (int w = 0; w < (int)(blockDim.x / 32); w++)
+            x += s[threadIdx.x][w];
+        partials[(size_t)blockIdx.x * TENSOR_TERMS + threadIdx.x] = x;
+        }
+    }
+
+__global__ void k_tensor_final(const double* __restrict__ partials, unsigned int nblocks,
+                               double* __restrict__ out)
+    {
+    if (threadIdx.x < TENSOR_TERMS)
+        {
+        double x = 0.0;
+        for (unsigned int b = 0; b < nblocks; b++)
+            x += partials[(size_t)b * TENSOR_TERMS + threadIdx.x];
+        out[threadIdx.x] = x;
+        }
+    }
+
 __global__ void k_thermo(const float4* __restrict__ vel, const float4* __restrict__ force,
                          const float* __restrict__ virial, size_t pitch, unsigned int N,
                          unsigned int* counter, double* partials, double* out)
@@ -550,6 +687,67 @@ extern "C"
         k_langevin_two<<<div_up(N > 0 ? N : 1, 256), 256, 0, (cudaStream_t)stream>>>(
             fz, reinterpret_cast<const float4*>(d_net_force), N);
         return check_launch("gb_langevin_step_two");
+        }
+
+    int gb_npt_step_one(float* d_pos, float* d_vel, const float* d_accel, int* d_image,
+                        unsigned int N, const gb_box* new_box, float dt, float scale,
+                        const float* mat_exp_v, const float* mat_exp_r,
+                        const float* mat_exp_r_int, void* stream)
+        {
+        GB_REQUIRE(new_box && mat_exp_v && mat_exp_r && mat_exp_r_int,
+                   "gb_npt_step_one: null argument");
+        GB_REQUIRE(N == 0 || (d_pos && d_vel && d_accel && d_image),
+                   "gb_npt_step_one: null particle array");
+        if (N == 0)
+            return GB_OK;
+        Tri mv, mr, mri;
+        for (int k = 0; k < 6; k++)
+            {
+            mv.m[k] = mat_exp_v[k];
+            mr.m[k] = mat_exp_r[k];
+            mri.m[k] = mat_exp_r_int[k];
+            }
+        k_npt_step_one<<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
+            reinterpret_cast<float4*>(d_pos), reinterpret_cast<float4*>(d_vel), d_accel, d_image,
+            N, *new_box, dt, scale, mv, mr, mri);
+        return check_launch("gb_npt_step_one");
+        }
+
+    int gb_npt_step_two(float* d_vel, float* d_accel, const float* d_net_force, unsigned int N,
+                        float dt, float scale, const float* mat_exp_v, void* stream)
+        {
+        GB_REQUIRE(mat_exp_v, "gb_npt_step_two: null argument");
+        GB_REQUIRE(N == 0 || (d_vel && d_accel && d_net_force),
+                   "gb_npt_step_two: null particle array");
+        if (N == 0)
+            return GB_OK;
+        Tri mv;
+        for (int k = 0; k < 6; k++)
+            mv.m[k] = mat_exp_v[k];
+        k_npt_step_two<<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
+            reinterpret_cast<float4*>(d_vel), d_accel, reinterpret_cast<const float4*>(d_net_force),
+            N, dt, scale, mv);
+        return check_launch("gb_npt_step_two");
+        }
+
+    size_t gb_thermo_tensor_scratch_bytes(unsigned int N)
+        {
+        return sizeof(double) * TENSOR_TERMS * (size_t)div_up(N > 0 ? N : 1, 256);
+        }
+
+    int gb_thermo_tensor(const float* d_vel, const float* d_force, const float* d_virial,
+                         size_t virial_pitch, unsigned int N, void* d_scratch, double* d_out,
+                         void* stream)
+        {
+        GB_REQUIRE(d_vel && d_scratch && d_out, "gb_thermo_tensor: null argument");
+        GB_REQUIRE(!d_virial || virial_pitch >= N, "gb_thermo_tensor: virial pitch < N");
+        const unsigned int nb = div_up(N > 0 ? N : 1, 256);
+        cudaStream_t s = (cudaStream_t)stream;
+        k_tensor_partials<<<nb, 256, 0, s>>>(reinterpret_cast<const float4*>(d_vel),
+                                             reinterpret_cast<const float4*>(d_force), d_virial,
+                                             virial_pitch, N, reinterpret_cast<double*>(d_scratch));
+        k_tensor_final<<<1, 32, 0, s>>>(reinterpret_cast<const double*>(d_scratch), nb, d_out);
+        return check_launch("gb_thermo_tensor");
         }
 
     int gb_sum_net_force(float* d_net, const float* const* h_force_ptrs, unsigned int n_forces,

@@ -223,6 +223,11 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setLangevin", &Integrator::set_langevin)
         .def("setBrownian", &Integrator::set_brownian)
         .def("setMaxDisplacement", &Integrator::set_max_displacement)
+        .def("setNPT", &Integrator::set_npt)
+        .def("getBarostatDOF", &Integrator::barostat_dof)
+        .def("setBarostatDOF", &Integrator::set_barostat_dof)
+        .def("barostatEnergy", &Integrator::barostat_energy)
+        .def("thermoTensor", &Integrator::thermo_tensor)
         .def("setBerendsen", &Integrator::set_thermostat_berendsen)
         .def("setMTTK", &Integrator::set_thermostat_mttk)
         .def("getMTTKState", &Integrator::mttk_state)

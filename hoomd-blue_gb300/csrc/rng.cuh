@@ -6,6 +6,11 @@
 
 #include <cstdint>
 
+#ifndef __CUDACC__
+// host compilers: the generator and the uniform conversions are plain host code
+#include <cuda_runtime.h>
+#endif
+
 namespace gb
 {
 
@@ -99,6 +104,7 @@ __host__ __device__ inline float uniform_m11_f(Philox& rng)
     return -1.0f + 2.0f * u01<float>(rng.u64());
     }
 
+#ifdef __CUDACC__
 // Box-Muller, one value per draw (hoomd/RandomNumbers.h:346-372).
 __device__ inline double normal_d(Philox& rng)
     {
@@ -202,5 +208,7 @@ __device__ inline double berendsen_factor_d(double K, double dof, double dt, dou
     const double T_cur = 2.0 * K / dof;
     return sqrt(1.0 + dt / tau * (kT / T_cur - 1.0));
     }
+
+#endif // __CUDACC__
 
 } // namespace gb

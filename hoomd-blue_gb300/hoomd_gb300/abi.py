@@ -119,6 +119,12 @@ _PROTOS = {
                               c_void, c_void]),
     "gb_md_step_one": (c_int, [_P(StepOneArgs), c_void]),
     "gb_abi_struct_sizes": (c_uint, [_P(c_size), c_uint]),
+    "gb_npt_step_one": (c_int, [c_void, c_void, c_void, c_void, c_uint, _P(Box), c_float, c_float,
+                                c_void, c_void, c_void, c_void]),
+    "gb_npt_step_two": (c_int, [c_void, c_void, c_void, c_uint, c_float, c_float, c_void,
+                                c_void]),
+    "gb_thermo_tensor_scratch_bytes": (c_size, [c_uint]),
+    "gb_thermo_tensor": (c_int, [c_void, c_void, c_void, c_size, c_uint, c_void, c_void, c_void]),
     "gb_berendsen_factor": (c_int, [c_void, c_double, c_double, c_double, c_double, c_void, c_void,
                                     c_void]),
     "gb_normal_draw": (c_int, [ctypes.c_uint8, c_u64, ctypes.c_uint16, ctypes.c_uint32, c_double,

@@ -1,5 +1,6 @@
 """Integration methods (hoomd/md/methods/methods.py): ConstantVolume (NVE without a thermostat, NVT
-with one), DisplacementCapped, Langevin, Brownian and OverdampedViscous, each over the group of
+with one), ConstantPressure, DisplacementCapped, Langevin, Brownian and OverdampedViscous, each over
+the group of
 all particles."""
 
 from hoomd_gb300.filter import All
@@ -196,3 +197,89 @@ class OverdampedViscous(Brownian):
 
     def __init__(self, filter, default_gamma=1.0, default_gamma_r=(1.0, 1.0, 1.0)):
         super().__init__(filter, 0.0, default_gamma, default_gamma_r)
+
+
+_COUPLE = {"none": 0, "xy": 1, "xz": 2, "yz": 3, "xyz": 4}
+
+
+class ConstantPressure(Method):
+    """Constant pressure (hoomd/md/methods/methods.py:177-580, TwoStepConstantPressure.cc): the
+    MTK barostat with box degrees of freedom ``box_dof`` = (x, y, z, xy, xz, yz), couplings
+    ``couple`` ("xyz", "xy", "xz", "yz", "none"), time constant ``tauS`` and Langevin damping
+    ``gamma`` of the barostat, with the MTTK thermostat or none. ``S`` is the target stress: one
+    number (hydrostatic pressure) or six (xx, yy, zz, yz, xz, xy), constants here. Translational
+    degrees of freedom only; ``rescale_all`` has no effect (the group is all particles)."""
+
+    _loggables = {"barostat_energy": "scalar"}
+
+    def __init__(self, filter, S, tauS, couple, thermostat=None,
+                 box_dof=(True, True, True, False, False, False), rescale_all=False, gamma=0.0):
+        if not isinstance(filter, All):
+            raise NotImplementedError("ConstantPressure integrates the group of all particles")
+        if thermostat is not None and not isinstance(thermostat, thermostats.MTTK):
+            raise NotImplementedError("ConstantPressure runs with the MTTK thermostat or none")
+        if couple not in _COUPLE:
+            raise ValueError(f"couple must be one of {tuple(_COUPLE)}")
+        self.filter = filter
+        self.S = S
+        self.tauS = float(tauS)
+        self.couple = couple
+        self.thermostat = thermostat
+        self.box_dof = [bool(x) for x in box_dof]
+        if len(self.box_dof) != 6:
+            raise ValueError("box_dof has six entries")
+        self.rescale_all = bool(rescale_all)
+        self.gamma = float(gamma)
+        self._barostat_dof = (0.0,) * 6
+        self._cpp_integ = None
+
+    @staticmethod
+    def _stress(S):
+        try:
+            v = [float(x) for x in S]
+        except TypeError:
+            v = [float(S)] * 3 + [0.0] * 3
+        if len(v) != 6:
+            raise ValueError("S is one number or six")
+        return v
+
+    @property
+    def barostat_dof(self):
+        if self._cpp_integ is None:
+            return self._barostat_dof
+        return tuple(self._cpp_integ.getBarostatDOF())
+
+    @barostat_dof.setter
+    def barostat_dof(self, v):
+        v = tuple(float(x) for x in v)
+        if len(v) != 6:
+            raise ValueError("barostat_dof has six entries")
+        self._barostat_dof = v
+        if self._cpp_integ is not None:
+            self._cpp_integ.setBarostatDOF(list(v))
+
+    @property
+    def barostat_energy(self):
+        if self._cpp_integ is None:
+            raise RuntimeError("barostat_energy is available after the simulation runs")
+        return self._cpp_integ.barostatEnergy()
+
+    def thermalize_barostat_dof(self):
+        raise NotImplementedError("thermalize_barostat_dof is not available on this path")
+
+    def _apply(self, integ):
+        if self.thermostat is None:
+            integ.setNoThermostat()
+        else:
+            self.thermostat._apply(integ)
+        integ.setNPT(self._stress(self.S), self.tauS, _COUPLE[self.couple],
+                     [int(x) for x in self.box_dof], self.gamma)
+        integ.setBarostatDOF(list(self._barostat_dof))
+
+    def _attach(self, integ, state=None):
+        if self._cpp_integ is not None and self._cpp_integ is not integ:
+            self._barostat_dof = tuple(self._cpp_integ.getBarostatDOF())
+        self._cpp_integ = integ
+        if self.thermostat is not None and state is not None:
+            self.thermostat._simulation = state._simulation
+        self._apply(integ)

@@ -509,6 +509,27 @@ int gb_langevin_step_two(float* d_vel, float* d_accel, const float* d_net_force,
 int gb_bussi_draws(const uint64_t* d_timestep, unsigned int count, double dof, uint16_t seed,
                    uint32_t instance_id, double* d_ring, unsigned int ring_size, void* stream);
 
+/* ConstantPressure halves (hoomd/md/TwoStepConstantPressure.cc:206-330, 587-640), translational
+ * part. The propagators are upper-triangular 3x3 matrices given as (xx, xy, xz, yy, yz, zz).
+ * Step one: v += dt/2 a; v = M_v v; v *= scale; r = M_r r; r += M_r,int v; wrap into new_box
+ * (the box already scaled by M_r). Step two: a = F/m; v *= scale; v = M_v v; v += dt/2 a. */
+int gb_npt_step_one(float* d_pos, float* d_vel, const float* d_accel, int* d_image,
+                    unsigned int N, const gb_box* new_box, float dt, float scale,
+                    const float* mat_exp_v, const float* mat_exp_r, const float* mat_exp_r_int,
+                    void* stream);
+int gb_npt_step_two(float* d_vel, float* d_accel, const float* d_net_force, unsigned int N,
+                    float dt, float scale, const float* mat_exp_v, void* stream);
+
+/* Kinetic and virial tensors for the pressure tensor (ComputeThermo::computeProperties,
+ * hoomd/md/ComputeThermo.cc:76-290), summed in FP64 in a fixed order: d_out[0..5] =
+ * sum m v_a v_b (xx, xy, xz, yy, yz, zz), d_out[6..11] = sum of the per-particle virial
+ * (6 x virial_pitch, may be NULL), d_out[12] = sum of the force array's energies (may be NULL).
+ * d_scratch: gb_thermo_tensor_scratch_bytes(N). */
+size_t gb_thermo_tensor_scratch_bytes(unsigned int N);
+int gb_thermo_tensor(const float* d_vel, const float* d_force, const float* d_virial,
+                     size_t virial_pitch, unsigned int N, void* d_scratch, double* d_out,
+                     void* stream);
+
 /* Net force (hoomd/Integrator.cu:68-170 gpu_integrator_sum_net_force): d_net[i] = sum over the
  * n_forces force arrays (float4; energy in w), n_forces <= 8. */
 int gb_sum_net_force(float* d_net, const float* const* h_force_ptrs, unsigned int n_forces,

@@ -1126,6 +1126,73 @@ void bd_step_one(unsigned int N, R* pos, R* vel, const R* force, int* image,
     }
 
 // ------------------------------------------------------------------------------------------------
+// ConstantPressure halves, translational part (hoomd/md/TwoStepConstantPressure.cc:262-300 and
+// :600-625): upper-triangular propagators (xx, xy, xz, yy, yz, zz) in R.
+// ------------------------------------------------------------------------------------------------
+template<class R> static inline void tri_apply(const R* m, R& x, R& y, R& z)
+    {
+    R nx = m[0] * x + m[1] * y + m[2] * z;
+    R ny = m[3] * y + m[4] * z;
+    R nz = m[5] * z;
+    x = nx;
+    y = ny;
+    z = nz;
+    }
+
+template<class R>
+void npt_step_one(unsigned int N, R* pos, R* vel, const R* accel, int* image,
+                  const Box<R>& new_box, R dt, R s, const R* mv, const R* mr, const R* mri)
+    {
+    for (unsigned int j = 0; j < N; j++)
+        {
+        R vx = vel[4 * j], vy = vel[4 * j + 1], vz = vel[4 * j + 2];
+        R px = pos[4 * j], py = pos[4 * j + 1], pz = pos[4 * j + 2];
+        vx += dt / R(2.0) * accel[3 * j];
+        vy += dt / R(2.0) * accel[3 * j + 1];
+        vz += dt / R(2.0) * accel[3 * j + 2];
+        tri_apply(mv, vx, vy, vz);
+        vx *= s;
+        vy *= s;
+        vz *= s;
+        tri_apply(mr, px, py, pz);
+        R ix = vx, iy = vy, iz = vz;
+        tri_apply(mri, ix, iy, iz);
+        px += ix;
+        py += iy;
+        pz += iz;
+        new_box.wrap(px, py, pz, image[3 * j], image[3 * j + 1], image[3 * j + 2]);
+        pos[4 * j] = px;
+        pos[4 * j + 1] = py;
+        pos[4 * j + 2] = pz;
+        vel[4 * j] = vx;
+        vel[4 * j + 1] = vy;
+        vel[4 * j + 2] = vz;
+        }
+    }
+
+template<class R>
+void npt_step_two(unsigned int N, R* vel, R* accel, const R* net_force, R dt, R s, const R* mv)
+    {
+    for (unsigned int j = 0; j < N; j++)
+        {
+        R minv = R(1.0) / vel[4 * j + 3];
+        R ax = net_force[4 * j] * minv, ay = net_force[4 * j + 1] * minv,
+          az = net_force[4 * j + 2] * minv;
+        R vx = vel[4 * j] * s, vy = vel[4 * j + 1] * s, vz = vel[4 * j + 2] * s;
+        tri_apply(mv, vx, vy, vz);
+        vx += dt / R(2.0) * ax;
+        vy += dt / R(2.0) * ay;
+        vz += dt / R(2.0) * az;
+        vel[4 * j] = vx;
+        vel[4 * j + 1] = vy;
+        vel[4 * j + 2] = vz;
+        accel[3 * j] = ax;
+        accel[3 * j + 1] = ay;
+        accel[3 * j + 2] = az;
+        }
+    }
+
+// ------------------------------------------------------------------------------------------------
 // Whole-step runner: hoomd/md/IntegratorTwoStep.cc:51-139 (update), :226-298 (prepRun),
 // hoomd/md/NeighborList.cc:363-435 (compute), :452-529 (updateRList), :1220-1289 (distanceCheck),
 // :1325-1418 (needsUpdating, rebuild_check_delay = 1, check_dist = true), :1544-1617 (head list,
@@ -1755,6 +1822,30 @@ using namespace orc;
             g[t] = R(gamma[t]);                                                                    \
         bd_step_one<R>(N, pos, vel, force, image, tags, g.data(), box, R(kT), R(dt),               \
                        uint16_t(seed), timestep, ndim, noiseless != 0);                            \
+        }                                                                                          \
+    ORC_EXPORT void orc_npt_step_one_##SUF(unsigned int N, R* pos, R* vel, const R* accel,         \
+                                           int* image, const double* b6, const int* per, double dt, \
+                                           double s, const float* mv, const float* mr,             \
+                                           const float* mri)                                       \
+        {                                                                                          \
+        Box<R> box;                                                                                \
+        box.set(b6, per);                                                                          \
+        R a[6], b[6], c[6];                                                                        \
+        for (int k = 0; k < 6; k++)                                                                \
+            {                                                                                      \
+            a[k] = R(mv[k]);                                                                       \
+            b[k] = R(mr[k]);                                                                       \
+            c[k] = R(mri[k]);                                                                      \
+            }                                                                                      \
+        npt_step_one<R>(N, pos, vel, accel, image, box, R(dt), R(s), a, b, c);                     \
+        }                                                                                          \
+    ORC_EXPORT void orc_npt_step_two_##SUF(unsigned int N, R* vel, R* accel, const R* net_force,   \
+                                           double dt, double s, const float* mv)                   \
+        {                                                                                          \
+        R a[6];                                                                                    \
+        for (int k = 0; k < 6; k++)                                                                \
+            a[k] = R(mv[k]);                                                                       \
+        npt_step_two<R>(N, vel, accel, net_force, R(dt), R(s), a);                                 \
         }                                                                                          \
     ORC_EXPORT void orc_nve_step_one_##SUF(unsigned int N, R* pos, R* vel, const R* accel,         \
                                            int* image, const double* b6, const int* per,           \

@@ -335,6 +335,34 @@ def cv_step_one_capped(pos4, vel4, accel3, image3, box, dt, s, limit, prec=32,
     return pos4, vel4, image3
 
 
+def npt_step_one(pos4, vel4, accel3, image3, new_box, dt, s, mv, mr, mri, prec=32,
+                 periodic=(1, 1, 1)):
+    """ConstantPressure step one with float32 propagators (xx, xy, xz, yy, yz, zz)."""
+    R = rdtype(prec)
+    pos4 = np.ascontiguousarray(pos4, R).copy()
+    vel4 = np.ascontiguousarray(vel4, R).copy()
+    accel3 = np.ascontiguousarray(accel3, R)
+    image3 = np.ascontiguousarray(image3, np.int32).copy()
+    m = [np.ascontiguousarray(x, np.float32) for x in (mv, mr, mri)]
+    b, p = box6(new_box), periodic3(periodic)
+    getattr(lib(), f"orc_npt_step_one_{suf(prec)}")(
+        len(pos4), ptr(pos4), ptr(vel4), ptr(accel3), ptr(image3), ptr(b), ptr(p),
+        ctypes.c_double(dt), ctypes.c_double(s), ptr(m[0]), ptr(m[1]), ptr(m[2]))
+    return pos4, vel4, image3
+
+
+def npt_step_two(vel4, net_force4, dt, s, mv, prec=32):
+    R = rdtype(prec)
+    vel4 = np.ascontiguousarray(vel4, R).copy()
+    accel3 = np.zeros((len(vel4), 3), R)
+    f = np.ascontiguousarray(net_force4, R)
+    m = np.ascontiguousarray(mv, np.float32)
+    getattr(lib(), f"orc_npt_step_two_{suf(prec)}")(len(vel4), ptr(vel4), ptr(accel3), ptr(f),
+                                                    ctypes.c_double(dt), ctypes.c_double(s),
+                                                    ptr(m))
+    return vel4, accel3
+
+
 def bd_step_one(pos4, vel4, force4, image3, tags, gamma, box, kT, dt, seed, timestep, ndim=3,
                 noiseless=False, prec=32, periodic=(1, 1, 1)):
     """Brownian (or overdamped, noiseless) step one; returns (pos4, vel4, image3)."""
