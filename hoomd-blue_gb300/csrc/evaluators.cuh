@@ -9,7 +9,7 @@
 // the parameters (derived constants, e.g. the Table's 1/dr).
 //
 // A plugin evaluator is added by writing a struct with this interface and instantiating
-// gb::launch_pair<Evaluator>() from pair_kernel.cuh.
+// gb::launch_pair<Evaluator>() from pair_kernel.cuh; pair_example.cu is a complete example.
 #pragma once
 
 #include "gb_device.cuh"

@@ -15,7 +15,9 @@
 // draws the Bussi factor for the next step on the device (no host synchronisation per step).
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "evaluators.cuh"
 #include "gb_device.cuh"
@@ -419,6 +421,9 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
     const unsigned int np = ntypes * ntypes;
     float* s_rcutsq = reinterpret_cast<float*>(s_raw + sizeof(P) * np);
     float* s_ronsq = s_rcutsq + np;
+    // largest r_cut^2 of any type pair (non-negative floats order as their bit patterns)
+    __shared__ unsigned int s_rcmax[8];
+    unsigned int rcmax_bits = 0;
     if (MULTI)
         {
         for (unsigned int t = threadIdx.x; t < np; t += blockDim.x)
@@ -427,10 +432,16 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             Eval::prepare_param(pt, d_rcutsq[t]);
             s_params[t] = pt;
             s_rcutsq[t] = d_rcutsq[t];
+            rcmax_bits = max(rcmax_bits, __float_as_uint(fmaxf(d_rcutsq[t], 0.0f)));
             if (XPLOR)
                 s_ronsq[t] = d_ronsq[t];
             }
+        rcmax_bits = __reduce_max_sync(0xffffffffu, rcmax_bits);
+        if (threadIdx.x % 32 == 0)
+            s_rcmax[threadIdx.x / 32] = rcmax_bits;
         __syncthreads();
+        for (unsigned int w = 0; w < blockDim.x / 32; w++)
+            rcmax_bits = max(rcmax_bits, s_rcmax[w]);
         }
     P p0;
     float rc0 = 0.0f, ro0 = 0.0f;
@@ -441,17 +452,39 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
         Eval::prepare_param(p0, rc0);
         if (XPLOR)
             ro0 = d_ronsq[0];
+        rcmax_bits = __float_as_uint(fmaxf(rc0, 0.0f));
         }
+    // Wrap-free warps. A particle at least r_cut (plus a margin) from every face of an
+    // orthorhombic box has all its partners within r_cut at their stored positions without an
+    // image shift, so minimum image changes no pair inside r_cut; a pair that it would shift
+    // lies beyond r_cut either way (the raw separation then exceeds L - r_cut >= r_cut) and
+    // contributes zero. Warps whose particles all qualify skip the image arithmetic.
+    const float rcmax = sqrtf(__uint_as_float(rcmax_bits)) * 1.001f + 1e-6f;
+    const float hx = 0.5f * box.L[0] - rcmax, hy = 0.5f * box.L[1] - rcmax,
+                hz = 0.5f * box.L[2] - rcmax;
 
-    const unsigned int i = (blockIdx.x * blockDim.x + threadIdx.x) / TPP;
     const unsigned int sub = threadIdx.x % TPP;
+    // Resident grid: each warp walks chunks of 32 threads, warp w of the grid taking chunks
+    // w, w + W, ... (W = warps in the grid), so a block meets its FP64 reduction barrier once,
+    // after several chunks, instead of after one chunk whose slowest warp holds the rest.
+    double ke_d = 0.0, pe_d = 0.0, w_d = 0.0;
+    const uint64_t grid_threads = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+         t0 < (uint64_t)N * TPP; t0 += grid_threads)
+    {
+    const unsigned int i = (unsigned int)((t0 + (threadIdx.x & 31u)) / TPP);
     const bool active = i < N;
     float fx = 0.f, fy = 0.f, fz_ = 0.f, pe = 0.f;
     float vxx = 0.f, vxy = 0.f, vxz = 0.f, vyy = 0.f, vyz = 0.f, vzz = 0.f;
+    const float4 pi = active ? __ldg(d_pos + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool wrap_free
+        = ORTHO
+          && __all_sync(0xffffffffu, !active
+                                         || (fabsf(pi.x) < hx && fabsf(pi.y) < hy
+                                             && fabsf(pi.z) < hz));
     if (active)
         {
         const unsigned int nn = d_n_neigh[i];
-        const float4 pi = __ldg(d_pos + i);
         const unsigned int ti = __float_as_uint(pi.w);
         // minimum image with fused multiply-adds (forces are held to a tolerance; only the
         // neighbour-list build needs minImage's exact roundings); every direction periodic
@@ -459,13 +492,16 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
         const float Lix = box.Linv[0], Liy = box.Linv[1], Liz = box.Linv[2];
         const float Lzxz = box.L[2] * box.xz, Lzyz = box.L[2] * box.yz, Lyxy = box.L[1] * box.xy;
         const float qi = Eval::needsCharge() ? __ldg(d_charge + i) : 0.0f;
-        auto pair = [&](const float4 pj, unsigned int j, bool valid) {
+        auto pair = [&](auto wrap, const float4 pj, unsigned int j, bool valid) {
             float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             if (ORTHO)
                 {
-                dx -= Lx * rintf(dx * Lix);
-                dy -= Ly * rintf(dy * Liy);
-                dz -= Lz * rintf(dz * Liz);
+                if (decltype(wrap)::value)
+                    {
+                    dx -= Lx * rintf(dx * Lix);
+                    dy -= Ly * rintf(dy * Liy);
+                    dz -= Lz * rintf(dz * Liz);
+                    }
                 }
             else
                 {
@@ -539,63 +575,69 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
         const unsigned int nfull = nn >> 2;
         const unsigned int rem = nn & 3u;
         const uint4* p4 = d_nlist4 + i;
-        const uint4 self = make_uint4(i, i, i, i);
-        if (TPP > 1)
-            {
-            // groups sub, sub + TPP, ...; the partial last group belongs to lane nfull % TPP
-            for (unsigned int b = sub; b < nfull; b += TPP)
+        auto walk = [&](auto wrap) {
+            const uint4 self = make_uint4(i, i, i, i);
+            if (TPP > 1)
                 {
-                const uint4 jc = ld_stream_u4(p4 + (uint64_t)b * stride);
+                // groups sub, sub + TPP, ...; the partial last group belongs to lane nfull % TPP
+                for (unsigned int b = sub; b < nfull; b += TPP)
+                    {
+                    const uint4 jc = ld_stream_u4(p4 + (uint64_t)b * stride);
+                    const float4 q0 = __ldg(d_pos + jc.x);
+                    const float4 q1 = __ldg(d_pos + jc.y);
+                    const float4 q2 = __ldg(d_pos + jc.z);
+                    const float4 q3 = __ldg(d_pos + jc.w);
+                    pair(wrap, q0, jc.x, true);
+                    pair(wrap, q1, jc.y, true);
+                    pair(wrap, q2, jc.z, true);
+                    pair(wrap, q3, jc.w, true);
+                    }
+                if (rem && sub == nfull % TPP)
+                    {
+                    const uint4 jc = ld_stream_u4(p4 + (uint64_t)nfull * stride);
+                    const float4 q0 = __ldg(d_pos + jc.x);
+                    const float4 q1 = __ldg(d_pos + (rem > 1 ? jc.y : i));
+                    const float4 q2 = __ldg(d_pos + (rem > 2 ? jc.z : i));
+                    pair(wrap, q0, jc.x, true);
+                    pair(wrap, q1, rem > 1 ? jc.y : i, rem > 1);
+                    pair(wrap, q2, rem > 2 ? jc.z : i, rem > 2);
+                    }
+                }
+            uint4 jA = self, jB = self;
+            if (TPP == 1 && nfull > 0)
+                jA = ld_stream_u4(p4);
+            if (TPP == 1 && nfull > 1)
+                jB = ld_stream_u4(p4 + stride);
+            for (unsigned int b = 0; TPP == 1 && b < nfull; b++)
+                {
+                const uint4 jc = jA;
+                jA = jB;
+                if (b + 2 < nfull)
+                    jB = ld_stream_u4(p4 + (uint64_t)(b + 2) * stride);
                 const float4 q0 = __ldg(d_pos + jc.x);
                 const float4 q1 = __ldg(d_pos + jc.y);
                 const float4 q2 = __ldg(d_pos + jc.z);
                 const float4 q3 = __ldg(d_pos + jc.w);
-                pair(q0, jc.x, true);
-                pair(q1, jc.y, true);
-                pair(q2, jc.z, true);
-                pair(q3, jc.w, true);
+                pair(wrap, q0, jc.x, true);
+                pair(wrap, q1, jc.y, true);
+                pair(wrap, q2, jc.z, true);
+                pair(wrap, q3, jc.w, true);
                 }
-            if (rem && sub == nfull % TPP)
+            if (TPP == 1 && rem)
                 {
                 const uint4 jc = ld_stream_u4(p4 + (uint64_t)nfull * stride);
                 const float4 q0 = __ldg(d_pos + jc.x);
                 const float4 q1 = __ldg(d_pos + (rem > 1 ? jc.y : i));
                 const float4 q2 = __ldg(d_pos + (rem > 2 ? jc.z : i));
-                pair(q0, jc.x, true);
-                pair(q1, rem > 1 ? jc.y : i, rem > 1);
-                pair(q2, rem > 2 ? jc.z : i, rem > 2);
+                pair(wrap, q0, jc.x, true);
+                pair(wrap, q1, rem > 1 ? jc.y : i, rem > 1);
+                pair(wrap, q2, rem > 2 ? jc.z : i, rem > 2);
                 }
-            }
-        uint4 jA = self, jB = self;
-        if (TPP == 1 && nfull > 0)
-            jA = ld_stream_u4(p4);
-        if (TPP == 1 && nfull > 1)
-            jB = ld_stream_u4(p4 + stride);
-        for (unsigned int b = 0; TPP == 1 && b < nfull; b++)
-            {
-            const uint4 jc = jA;
-            jA = jB;
-            if (b + 2 < nfull)
-                jB = ld_stream_u4(p4 + (uint64_t)(b + 2) * stride);
-            const float4 q0 = __ldg(d_pos + jc.x);
-            const float4 q1 = __ldg(d_pos + jc.y);
-            const float4 q2 = __ldg(d_pos + jc.z);
-            const float4 q3 = __ldg(d_pos + jc.w);
-            pair(q0, jc.x, true);
-            pair(q1, jc.y, true);
-            pair(q2, jc.z, true);
-            pair(q3, jc.w, true);
-            }
-        if (TPP == 1 && rem)
-            {
-            const uint4 jc = ld_stream_u4(p4 + (uint64_t)nfull * stride);
-            const float4 q0 = __ldg(d_pos + jc.x);
-            const float4 q1 = __ldg(d_pos + (rem > 1 ? jc.y : i));
-            const float4 q2 = __ldg(d_pos + (rem > 2 ? jc.z : i));
-            pair(q0, jc.x, true);
-            pair(q1, rem > 1 ? jc.y : i, rem > 1);
-            pair(q2, rem > 2 ? jc.z : i, rem > 2);
-            }
+        };
+        if (wrap_free)
+            walk(std::false_type {});
+        else
+            walk(std::true_type {});
         pe *= 0.5f;
         }
     if (TPP > 1)
@@ -614,10 +656,10 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             vzz = group_sum<TPP>(vzz);
             }
         }
-    double ke_d = 0.0, pe_d = 0.0, w_d = 0.0;
     if (active && sub == 0)
         {
         d_force[i] = make_float4(fx, fy, fz_, pe);
+        double ke_i = 0.0, pe_i = 0.0, w_i = 0.0;
         if (VIRIAL)
             {
             d_virial[0 * pitch + i] = vxx;
@@ -626,25 +668,59 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
             d_virial[3 * pitch + i] = vyy;
             d_virial[4 * pitch + i] = vyz;
             d_virial[5 * pitch + i] = vzz;
-            w_d = (double)vxx + (double)vyy + (double)vzz;
+            w_i = (double)vxx + (double)vyy + (double)vzz;
             }
         if (FUSE)
-            fuse_step_two(fz, i, fx, fy, fz_, pe, ke_d, pe_d, w_d);
+            {
+            fuse_step_two(fz, i, fx, fy, fz_, pe, ke_i, pe_i, w_i);
+            ke_d += ke_i;
+            pe_d += pe_i;
+            w_d += w_i;
+            }
         }
+    }
     if (FUSE)
         fuse_finish(fz, ke_d, pe_d, w_d);
     }
+
+// Blocks of one kernel resident on the current GPU at once (SM count x blocks per SM), cached
+// per kernel, dynamic shared memory size and device.
+struct ResidentGrid
+    {
+    int dev = -1;
+    size_t smem = ~size_t(0);
+    unsigned int n = 0;
+    unsigned int blocks(const void* kern, unsigned int block, size_t smem_bytes)
+        {
+        int d = 0;
+        cudaGetDevice(&d);
+        if (d != dev || smem_bytes != smem)
+            {
+            int sms = 0, per_sm = 0;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)block, smem_bytes);
+            n = (unsigned int)std::max(1, sms * std::max(1, per_sm));
+            dev = d;
+            smem = smem_bytes;
+            }
+        return n;
+        }
+    };
 
 template<class Eval, bool MULTI, bool ORTHO, bool FUSE, bool VIRIAL, bool XPLOR, int TPP = 1>
 int launch_pair_i4_inst(const gb_pair_args& a, const typename Eval::param_type* d_params,
                         const float* ext, const FuseArgs& fz, cudaStream_t s)
     {
     const unsigned int block = 256;
-    const unsigned int grid = div_up((unsigned long long)a.N * TPP, block);
     const size_t smem = i4_param_bytes<typename Eval::param_type>(a.ntypes, MULTI);
     auto kern = k_pair_i4<Eval, MULTI, ORTHO, FUSE, VIRIAL, XPLOR, TPP>;
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // no more blocks than fit on the GPU at once (the kernel loops over the rest)
+    static thread_local ResidentGrid cache;
+    const unsigned int grid = std::min<unsigned long long>(
+        div_up((unsigned long long)a.N * TPP, block),
+        cache.blocks(reinterpret_cast<const void*>(kern), block, smem));
     kern<<<grid, block, smem, s>>>(reinterpret_cast<float4*>(a.d_force), a.d_virial,
                                    a.virial_pitch, a.N, reinterpret_cast<const float4*>(a.d_pos),
                                    a.box, a.d_n_neigh, reinterpret_cast<const uint4*>(a.d_nlist),
