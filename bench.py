@@ -688,6 +688,49 @@ def run_reference(args):
         flush=True)
 
 
+def run_drift(args):
+    """NVE energy drift of the 1M-particle LJ fluid: the Bussi equilibration of the workload
+    (1000 steps at kT 1.5), then ``--drift-steps`` ConstantVolume steps with no thermostat, the
+    total energy KE + PE (FP64 reductions) sampled every 500 steps. Prints one JSON line with the
+    least-squares slope per particle per unit time and the largest excursion per particle."""
+    import numpy as np
+    import torch
+    import hoomd_gb300 as hoomd
+    from hoomd_gb300 import md
+
+    wl = workloads_registry(args.fcc_m)["lj_fcc_1m"]
+    torch.cuda.set_device(0)
+    snap = wl.make_snap(1)
+    N = snap.particles.N
+    sim, force, cell, method = make_sim(wl, snap, seed=1)
+    force.mode = args.drift_mode
+    thermo = md.compute.ThermodynamicQuantities(hoomd.filter.All())
+    sim.operations.computes.append(thermo)
+    sim.run(1000)
+    method.thermostat = None
+    sim._needs_prep = True
+    sim.run(0)
+    every = 500
+    t, e = [], []
+    for k in range(args.drift_steps // every + 1):
+        if k:
+            sim.run(every)
+        t.append(k * every * wl.config["dt"])
+        e.append(thermo.kinetic_energy + thermo.potential_energy)
+    t, e = np.array(t), np.array(e)
+    slope = np.polyfit(t, e, 1)[0]
+    print(json.dumps({
+        "metric": "NVE total-energy drift", "workload": wl.config["workload"], "N": N,
+        "pair_mode": args.drift_mode,
+        "steps": args.drift_steps, "dt": wl.config["dt"], "sample_every": every,
+        "E0_per_particle": e[0] / N, "drift_per_particle_per_tau": slope / N,
+        "max_excursion_per_particle": float(np.abs(e - e[0]).max() / N),
+        "relative_change": float((e[-1] - e[0]) / abs(e[0])),
+        "kinetic_temperature_end": thermo.kinetic_temperature,
+        "precision": "fp32 positions/forces, fp64 reductions",
+        "energies": [float(x) for x in e]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
@@ -711,10 +754,17 @@ def main():
     ap.add_argument("--fcc-m", type=int, default=64,
                     help="FCC cells per side of lj_fcc_1m (64 = the 1,048,576-particle workload; "
                          "smaller values are for profiling captures only)")
+    ap.add_argument("--nve-drift", action="store_true",
+                    help="measure the NVE energy drift of lj_fcc_1m instead of the throughput")
+    ap.add_argument("--drift-steps", type=int, default=10000)
+    ap.add_argument("--drift-mode", default="none", choices=["none", "shift"],
+                    help="LJ energy mode of the drift run (none = the workload's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.nve_drift:
+        run_drift(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "replicas_256":
         run_replicas(args)

@@ -1585,10 +1585,18 @@ std::vector<double> Integrator::thermo(bool with_virial)
         out.download(h, 3, s);
         cuda_check(cudaStreamSynchronize(s), "thermo");
         ke = h[0];
-        pe += h[1];
-        w += h[2];
+        // tail corrections: energy, and the same term on each diagonal of the virial (W is the
+        // trace over 3)
+        pe += h[1] + f.tail_energy / f.box_volume();
+        w += h[2] + f.tail_virial / f.box_volume();
         }
     return {ke, pe, w};
+    }
+
+double PairForce::box_volume() const
+    {
+    const double* b = pdata->box6;
+    return pdata->ndim == 2 ? b[0] * b[1] : b[0] * b[1] * b[2];
     }
 
 } // namespace gbe

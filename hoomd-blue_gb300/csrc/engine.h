@@ -257,6 +257,10 @@ class PairForce
     PairKind kind;
     int shift_mode = 0;
     bool uses_charge = false; // the evaluator scales pairs by q_i q_j (d_charge in the args)
+    // Isotropic long-range tail correction (PotentialPair::computeTailCorrection): the energy and
+    // each diagonal virial term it adds are these coefficients over the box volume
+    double tail_energy = 0.0, tail_virial = 0.0;
+    double box_volume() const;
     unsigned int ntypes;
     std::vector<float> r_cut, r_on;
     std::vector<gb_lj_param> lj;

@@ -194,6 +194,13 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setParamsDPD", &PairForce::set_params_dpd)
         .def_readwrite("dpdKT", &PairForce::dpd_kT)
         .def_readwrite("useCharge", &PairForce::uses_charge)
+        .def("setTailCorrection",
+             [](PairForce& f, double energy, double virial) {
+                 f.tail_energy = energy;
+                 f.tail_virial = virial;
+             })
+        .def("tailEnergy", [](PairForce& f) { return f.tail_energy / f.box_volume(); })
+        .def("tailVirial", [](PairForce& f) { return f.tail_virial / f.box_volume(); })
         .def("setRCut", &PairForce::set_r_cut)
         .def("setROn", &PairForce::set_r_on)
         .def("setSurrogate", [](PairForce& f, std::shared_ptr<MlpSurrogate> m) { f.mlp = m; })

@@ -133,6 +133,11 @@ std::vector<double> Integrator::thermo_tensor()
         cuda_check(cudaStreamSynchronize(s), "thermo tensor");
         for (int t = 0; t < 13; t++)
             total[t] += (t < 6 && k > 0) ? 0.0 : h[t];
+        const double V = f.box_volume();
+        total[6] += f.tail_virial / V;
+        total[9] += f.tail_virial / V;
+        total[11] += f.tail_virial / V;
+        total[12] += f.tail_energy / V;
         }
     return total;
     }

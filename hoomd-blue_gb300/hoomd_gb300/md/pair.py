@@ -46,6 +46,32 @@ class Pair:
         self._mode = m
         if self._cpp_obj is not None:
             self._cpp_obj.mode = _MODES[m]
+            self._update_tail()
+
+    def _tail_coefficients(self, state):
+        """(energy, virial) tail-correction coefficients: the energy and each diagonal virial
+        term are these over the volume. Forces without a tail correction have none."""
+        return 0.0, 0.0
+
+    def _update_tail(self):
+        """Recompute the tail-correction coefficients from the attached state."""
+        if self._cpp_obj is None:
+            return
+        e, w = self._tail_coefficients(self._simulation.state)
+        self._cpp_obj.setTailCorrection(float(e), float(w))
+
+    @property
+    def additional_energy(self):
+        """Energy not attributed to particles (the tail correction; hoomd/md/force.py:97)."""
+        self._require_run()
+        return self._cpp_obj.tailEnergy()
+
+    @property
+    def additional_virial(self):
+        """Virial not attributed to particles, (xx, xy, xz, yy, yz, zz)."""
+        self._require_run()
+        w = self._cpp_obj.tailVirial()
+        return [w, 0.0, 0.0, w, 0.0, w]
 
     def _set_pair_params(self, cpp, i, j, value):
         raise NotImplementedError
@@ -72,6 +98,7 @@ class Pair:
                     raise RuntimeError(f"{type(self).__name__}: r_cut[({a!r}, {b!r})] is not set")
                 self._cpp_obj.setRCut(i, j, float(rc))
                 self._cpp_obj.setROn(i, j, float(self.r_on[(a, b)]))
+        self._update_tail()
         return self._cpp_obj
 
     def _detach(self):
@@ -106,8 +133,9 @@ class Pair:
 
     @property
     def energy(self):
-        """Total energy of this force (summed in double)."""
-        return float(np.sum(self.energies, dtype=np.float64))
+        """Total energy of this force: the additional energy plus the per-particle energies
+        summed in double (ForceCompute::calcEnergySum)."""
+        return self.additional_energy + float(np.sum(self.energies, dtype=np.float64))
 
 
 class LJ(Pair):
@@ -118,13 +146,50 @@ class LJ(Pair):
     def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none',
                  tail_correction=False):
         super().__init__(nlist, default_r_cut, default_r_on, mode)
-        if tail_correction:
-            raise NotImplementedError("tail_correction is not implemented")
-        self.tail_correction = False
+        self._tail_correction = bool(tail_correction)
         self.params = TypePairDict(validator=dict_validator(("epsilon", "sigma")))
+
+    @property
+    def tail_correction(self):
+        """Whether the isotropic integrated long-range tail correction is applied."""
+        return self._tail_correction
+
+    @tail_correction.setter
+    def tail_correction(self, value):
+        self._tail_correction = bool(value)
+        self._update_tail()
 
     def _set_pair_params(self, cpp, i, j, v):
         cpp.setParamsLJ(i, j, v["sigma"], v["epsilon"])
+
+    def _tail_coefficients(self, state):
+        """PotentialPair::computeTailCorrection (hoomd/md/PotentialPair.h:255-341) with the LJ
+        integrals of EvaluatorPairLJ::evalEnergyLRCIntegral / evalPressureLRCIntegral
+        (hoomd/md/EvaluatorPairLJ.h:213-248). Over the volume V: energy
+        sum_ij 2 pi N_i (N_j / V) I_E, pressure sum_ij (4/6) pi (N_i / V)(N_j / V) I_P, and each
+        diagonal virial term D V dP / 3."""
+        if not self._tail_correction:
+            return 0.0, 0.0
+        if self._mode != "none":
+            raise RuntimeError(
+                'Pair potential shift mode must be "none" to apply tail corrections.')
+        types, counts, dimensions = state.particle_types, state._type_counts(), state.dimensions
+        e = w = 0.0
+        for i, a in enumerate(types):
+            for j, b in enumerate(types):
+                rc = float(self.r_cut[(a, b)])
+                if rc == 0.0:
+                    continue
+                p = self.params[(a, b)]
+                lj1 = 4.0 * p["epsilon"] * p["sigma"] ** 12
+                lj2 = 4.0 * p["epsilon"] * p["sigma"] ** 6
+                rc3inv = 1.0 / (rc * rc) ** 1.5
+                rc9inv = rc3inv ** 3
+                i_e = lj1 / 9.0 * rc9inv - lj2 / 3.0 * rc3inv
+                i_p = lj1 * 4.0 / 3.0 * rc9inv - lj2 * 2.0 * rc3inv
+                e += 2.0 * np.pi * counts[i] * counts[j] * i_e
+                w += dimensions / 3.0 * (4.0 / 6.0) * np.pi * counts[i] * counts[j] * i_p
+        return e, w
 
 
 class Table(Pair):

@@ -63,6 +63,9 @@ class Simulation:
         self._cpp_integrator = None
         self._walltime = 0.0
         self._tps = 0.0
+        # hoomd/simulation.py always_compute_pressure: kept for scripts that set it; the virial
+        # is computed whenever a pressure is asked for, so it changes nothing here
+        self.always_compute_pressure = False
 
     @property
     def seed(self):
@@ -175,6 +178,9 @@ class Simulation:
                 nl._apply_exclusions(self._state)
                 self._needs_prep = True
         if getattr(self, "_needs_prep", False):
+            for f in integ.forces:
+                if getattr(f, "_cpp_obj", None) is not None and hasattr(f, "_update_tail"):
+                    f._update_tail()
             self._cpp_integrator.prepRun()
             self._needs_prep = False
         for op in self.operations.computes:

@@ -24,6 +24,7 @@ class State:
         self._topology = _copy_topology(snapshot)
         self._topology_version = 0
         self._passive = _copy_passive(snapshot)
+        self._counts = None
         self._upload(snapshot)
 
     def _upload(self, snapshot):
@@ -35,7 +36,15 @@ class State:
             np.ascontiguousarray(p.typeid, np.uint32),
             np.ascontiguousarray(p.image, np.int32))
         self._cpp_pdata.setCharges(np.ascontiguousarray(p.charge, np.float64))
+        self._counts = None
         self._simulation._state_changed()
+
+    def _type_counts(self):
+        """Number of particles of each type."""
+        if self._counts is None:
+            tid = np.asarray(self._cpp_pdata.getParticles()["typeid"], np.int64)
+            self._counts = np.bincount(tid, minlength=len(self._types))
+        return self._counts
 
     @property
     def N_particles(self):
