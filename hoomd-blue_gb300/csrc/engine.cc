@@ -1593,6 +1593,25 @@ std::vector<double> Integrator::thermo(bool with_virial)
     return {ke, pe, w};
     }
 
+double PairForce::energy_sum()
+    {
+    ParticleData& pd = *pdata;
+    const size_t need = gb_thermo_scratch_bytes(pd.N);
+    if (d_esum_scratch.size() != need)
+        {
+        d_esum_scratch.resize(need);
+        d_esum_scratch.zero(pd.stream); // the reduction's counter word starts at zero
+        }
+    d_esum.resize(3);
+    check(gb_thermo_reduce(pd.vel.get(), force.get(), nullptr, pd.N, pd.N, d_esum_scratch.get(),
+                           d_esum.get(), pd.stream),
+          "energy sum");
+    double h[3];
+    d_esum.download(h, 3, pd.stream);
+    cuda_check(cudaStreamSynchronize(pd.stream), "energy sum");
+    return h[1];
+    }
+
 double PairForce::box_volume() const
     {
     const double* b = pdata->box6;

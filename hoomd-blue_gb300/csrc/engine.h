@@ -275,8 +275,11 @@ class PairForce
     std::vector<std::vector<double>> t_U, t_F;
     bool params_dirty = true;
     std::shared_ptr<MlpSurrogate> mlp;
-    DeviceArray<char> d_params, mlp_scratch;
+    DeviceArray<char> d_params, mlp_scratch, d_esum_scratch;
     DeviceArray<float> d_rcutsq, d_ronsq, d_table, force, virial;
+    DeviceArray<double> d_esum;
+    // sum of the per-particle energies of the last computed forces (FP64, on the device)
+    double energy_sum();
     bool virial_valid = false;
     };
 

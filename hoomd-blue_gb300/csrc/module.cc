@@ -220,6 +220,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
              })
         .def("getForces", [](PairForce& f) { return force_by_tag(f, 0); })
         .def("getEnergies", [](PairForce& f) { return force_by_tag(f, 1); })
+        .def("energySum", &PairForce::energy_sum)
         .def("getVirials", [](PairForce& f) { return force_by_tag(f, 2); });
 
     py::class_<Integrator, std::shared_ptr<Integrator>>(m, "IntegratorTwoStep")

@@ -134,8 +134,9 @@ class Pair:
     @property
     def energy(self):
         """Total energy of this force: the additional energy plus the per-particle energies
-        summed in double (ForceCompute::calcEnergySum)."""
-        return self.additional_energy + float(np.sum(self.energies, dtype=np.float64))
+        summed in FP64 on the device (ForceCompute::calcEnergySum)."""
+        self._require_run()
+        return self.additional_energy + self._cpp_obj.energySum()
 
 
 class LJ(Pair):

@@ -42,12 +42,20 @@ class _Particles:
         self.mass = np.ones(N, np.float64)
         self.image = np.zeros((N, 3), np.int32)
         # carried with the particles (GSD files, snapshots) but not used by the pair step
-        self.charge = np.zeros(N, np.float64)
-        self.diameter = np.ones(N, np.float64)
-        self.body = np.full(N, -1, np.int32)
-        self.moment_inertia = np.zeros((N, 3), np.float64)
-        self.orientation = np.tile(np.array([1.0, 0.0, 0.0, 0.0]), (N, 1))
-        self.angmom = np.zeros((N, 4), np.float64)
+        for name in PASSIVE_DEFAULTS:
+            setattr(self, name, passive_default(name, N))
+
+    def _adopt(self, N, arrays):
+        """Take ``arrays`` (name -> array of the right shape, owned by this snapshot from now
+        on) as the particle data of N particles; fields not given get their defaults."""
+        self._N = int(N)
+        for name, m in PARTICLE_FIELDS:
+            a = arrays.get(name)
+            if a is None:
+                a = passive_default(name, self._N) if name in PASSIVE_DEFAULTS else None
+            if a is None:
+                raise ValueError(f"_adopt: {name} is required")
+            setattr(self, name, a)
 
     @property
     def N(self):
@@ -81,6 +89,35 @@ class _Group:
             self.typeid = np.zeros(self._N, np.uint32)
         else:
             self.value = np.zeros(self._N, np.float64)
+
+
+# per-particle quantities the MD step carries but does not change, with their default values
+PASSIVE_DEFAULTS = {"charge": (1, np.float64, 0.0), "diameter": (1, np.float64, 1.0),
+                    "body": (1, np.int32, -1), "moment_inertia": (3, np.float64, 0.0),
+                    "orientation": (4, np.float64, (1.0, 0.0, 0.0, 0.0)),
+                    "angmom": (4, np.float64, 0.0)}
+
+
+def passive_default(name, N):
+    """A fresh array of N default values of the passive field ``name``."""
+    m, dt, v = PASSIVE_DEFAULTS[name]
+    shape = (N,) if m == 1 else (N, m)
+    if np.ndim(v) == 0 and v == 0:
+        return np.zeros(shape, dt)
+    a = np.empty(shape, dt)
+    a[...] = v
+    return a
+
+
+def is_passive_default(name, a):
+    """True when every entry of ``a`` holds the default of the passive field ``name``."""
+    m, dt, v = PASSIVE_DEFAULTS[name]
+    a = np.asarray(a)
+    if a.size == 0:
+        return True
+    if np.ndim(v) == 0:
+        return not np.any(a != v) if v != 0 else not np.any(a)
+    return not np.any(a[:, 0] != v[0]) and not np.any(a[:, 1:])
 
 
 PARTICLE_FIELDS = (("position", 3), ("velocity", 3), ("typeid", 1), ("mass", 1), ("image", 3),

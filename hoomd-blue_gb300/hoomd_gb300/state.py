@@ -6,7 +6,7 @@ import numpy as np
 
 from hoomd_gb300._native import _hoomd_gb300
 from hoomd_gb300.box import Box
-from hoomd_gb300.snapshot import Snapshot
+from hoomd_gb300.snapshot import Snapshot, is_passive_default
 
 
 class State:
@@ -70,15 +70,13 @@ class State:
         d = self._cpp_pdata.getParticles()
         s = Snapshot()
         s.configuration.box = self._cpp_pdata.getBox()
-        s.particles.N = self.N_particles
         s.particles.types = self.particle_types
-        s.particles.position[:] = d["position"]
-        s.particles.velocity[:] = d["velocity"]
-        s.particles.mass[:] = d["mass"]
-        s.particles.typeid[:] = d["typeid"]
-        s.particles.image[:] = d["image"]
+        # the engine's fresh tag-ordered arrays become the snapshot's; passive fields are copied
+        # where they differ from their defaults and created at their defaults otherwise
+        arrays = {k: d[k] for k in ("position", "velocity", "mass", "typeid", "image")}
         for name, v in self._passive.items():
-            getattr(s.particles, name)[:] = v
+            arrays[name] = v.copy()
+        s.particles._adopt(self.N_particles, arrays)
         for name, g in self._topology.items():
             setattr(s, name, copy.deepcopy(g))
         return s
@@ -110,7 +108,13 @@ _PASSIVE = ("charge", "diameter", "body", "moment_inertia", "orientation", "angm
 
 
 def _copy_passive(snapshot):
-    return {name: np.array(getattr(snapshot.particles, name), copy=True) for name in _PASSIVE}
+    """Host copies of the passive fields that differ from their defaults."""
+    out = {}
+    for name in _PASSIVE:
+        a = getattr(snapshot.particles, name)
+        if not is_passive_default(name, a):
+            out[name] = np.array(a, copy=True)
+    return out
 
 
 def _copy_topology(snapshot):
