@@ -271,6 +271,7 @@ void NeighborList::allocate()
     {
     ParticleData& pd = *pdata;
     const unsigned int nt = pd.ntypes;
+    alloc_generation++;
     update_rlist();
     float rmax = 0.0f;
     for (float v : rcut_max)
@@ -415,6 +416,9 @@ void NeighborList::refresh_exclusions()
     ParticleData& pd = *pdata;
     if (!ex_dirty && ex_generation == pd.sort_generation)
         return;
+    // new exclusions (not a re-sort of the same ones) may change the row pitch and the buffers
+    if (ex_dirty)
+        alloc_generation++;
     ex_dirty = false;
     ex_generation = pd.sort_generation;
     if (ex_tags.empty())
@@ -1266,6 +1270,13 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
 
 cudaGraphExec_t Integrator::graph_for(unsigned int k)
     {
+    // a neighbour list regrown or reallocated outside run_chunk (a forced build, a build for a
+    // query) moved the buffers the captured graphs address
+    if (nlist->alloc_generation != graph_nlist_generation)
+        {
+        drop_graphs();
+        graph_nlist_generation = nlist->alloc_generation;
+        }
     auto it = graphs.find(k);
     if (it != graphs.end())
         return it->second;

@@ -211,6 +211,9 @@ class NeighborList
     std::vector<uint32_t> ex_tags;
     unsigned int ex_pitch = 0;
     uint64_t ex_generation = ~0ull;
+    // incremented whenever allocate() replaces the device buffers (captured graphs hold their
+    // addresses, so graphs captured under an older generation must not be replayed)
+    uint64_t alloc_generation = 0;
     bool ex_dirty = false;
     DeviceArray<uint32_t> n_ex, ex_list;
     DeviceArray<float> d_r_cut, d_r_listsq, d_rcut_max, xyzf, last_pos;
@@ -394,6 +397,7 @@ class Integrator
     DeviceArray<DevStatus> ck_status;
     std::map<unsigned int, cudaGraphExec_t> graphs;
     uint64_t graph_sort_generation = ~0ull;
+    uint64_t graph_nlist_generation = ~0ull; // NeighborList::alloc_generation of the graphs
     };
 
 } // namespace gbe

@@ -177,13 +177,17 @@ __global__ void __launch_bounds__(NL_WARPS * 32)
         return;
     __shared__ float4 s_cand[NL_WARPS][32];
     __shared__ unsigned int s_ctype[NL_WARPS][32];
-    extern __shared__ float s_tab[]; // [2 * ntypes^2] r_cut then r_listsq (MULTI only)
+    // [2 * ntypes^2] r_cut then r_listsq (MULTI only), stored transposed: entry (a, b) at
+    // b * ntypes + a, so the lanes of a warp (own particles of any type) testing one candidate
+    // read consecutive words, free of bank conflicts
+    extern __shared__ float s_tab[];
     if (MULTI)
         {
         for (unsigned int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x)
             {
-            s_tab[t] = r_cut[t];
-            s_tab[ntypes * ntypes + t] = r_listsq[t];
+            const unsigned int tt = (t % ntypes) * ntypes + t / ntypes;
+            s_tab[tt] = r_cut[t];
+            s_tab[ntypes * ntypes + tt] = r_listsq[t];
             }
         __syncthreads();
         }
@@ -280,7 +284,7 @@ __global__ void __launch_bounds__(NL_WARPS * 32)
                         float rc, rl;
                         if (MULTI)
                             {
-                            const unsigned int tp = ti * ntypes + s_ctype[warp][t];
+                            const unsigned int tp = s_ctype[warp][t] * ntypes + ti;
                             rc = s_tab[tp];
                             rl = s_tab[ntypes * ntypes + tp];
                             }
@@ -580,15 +584,15 @@ __global__ void __launch_bounds__(LANE_WARPS * 32)
     extern __shared__ __align__(16) unsigned char smem[];
     const int wpb = blockDim.x / 32;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    // r_list^2 per type pair, -1 where r_cut is off (MULTI only), stored transposed: entry
+    // (a, b) at b * ntypes + a, so the lanes (own particles of any type) testing one candidate
+    // read consecutive words, free of bank conflicts
     float* s_tab = reinterpret_cast<float*>(smem);
     const size_t tab_bytes = MULTI ? ((2 * sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
     if (MULTI)
         {
         for (unsigned int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x)
-            {
-            s_tab[t] = r_cut[t];
-            s_tab[ntypes * ntypes + t] = r_listsq[t];
-            }
+            s_tab[(t % ntypes) * ntypes + t / ntypes] = r_cut[t] > 0.0f ? r_listsq[t] : -1.0f;
         __syncthreads();
         }
     const unsigned int cap = lane_cap(Nmax_cell);
@@ -644,10 +648,7 @@ __global__ void __launch_bounds__(LANE_WARPS * 32)
         const float rl_single = (!MULTI && active && __ldg(r_cut) > 0.0f) ? __ldg(r_listsq) : -1.0f;
         auto rlim = [&](unsigned int slot) -> float {
             if (MULTI)
-                {
-                const unsigned int tp = ti * ntypes + s_t[slot];
-                return (active && s_tab[tp] > 0.0f) ? s_tab[ntypes * ntypes + tp] : -1.0f;
-                }
+                return active ? s_tab[s_t[slot] * ntypes + ti] : -1.0f;
             return rl_single;
         };
         const uint64_t px2 = f2pack(pi.x, pi.x), py2 = f2pack(pi.y, pi.y), pz2 = f2pack(pi.z, pi.z);
