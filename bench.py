@@ -303,6 +303,7 @@ def run_gb300(args):
     phases = integ.timePhases(20)  # [step one, rebuild, fused pair step] ms
     launches0 = integ.launch_count
     builds0 = cell.num_builds
+    rollbacks0 = integ.n_rollbacks
 
     clocks = ClockSampler(local) if rank == 0 else None
     barrier(world)
@@ -318,6 +319,7 @@ def run_gb300(args):
     ms_max = max_over_ranks(ms, world)
     launches = integ.launch_count - launches0
     builds = cell.num_builds - builds0
+    rollbacks = integ.n_rollbacks - rollbacks0
     tps = args.steps / (ms_max / 1e3)
 
     # end to end through the public API: host snapshot in (H2D), K steps, snapshot and
@@ -357,6 +359,7 @@ def run_gb300(args):
             "data": "synthetic (seeded lattice, jittered, thermalised)",
             "config": dict(wl.config, parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
             "pair_evals_per_s": sum_n * tps * world, "nlist_builds": builds,
+            "nlist_rollbacks": rollbacks,
             "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk}
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:

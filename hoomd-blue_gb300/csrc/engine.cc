@@ -459,13 +459,22 @@ bool NeighborList::grow(const DevStatus& st)
         Nmax_cell = st.cell_cond[0] + std::max(4u, st.cell_cond[0] / 8);
         grew = true;
         }
+    std::vector<bool> over(pdata->ntypes, false);
+    bool nl_grew = false;
     for (unsigned int t = 0; t < pdata->ntypes; t++)
         if (st.nl_cond[t] > Nmax[t])
             {
             unsigned int want = st.nl_cond[t] + std::max(8u, st.nl_cond[t] / 8);
             Nmax[t] = (want + 3) & ~3u;
-            grew = true;
+            over[t] = true;
+            grew = nl_grew = true;
             }
+    // the types share one density: when one type's row overflows, the others are near their
+    // capacity too, so give every type an eighth more at once instead of one rollback each
+    if (nl_grew)
+        for (unsigned int t = 0; t < pdata->ntypes; t++)
+            if (!over[t])
+                Nmax[t] = (Nmax[t] + std::max(8u, Nmax[t] / 8) + 3) & ~3u;
     if (grew)
         {
         allocated = false;
