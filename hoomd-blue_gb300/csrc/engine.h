@@ -370,6 +370,15 @@ class Integrator
         return (uintptr_t)pdata->stream;
         }
     double sum_n_neigh();
+    // captured step graphs and the neighbour-list buffer generation they were captured under
+    size_t graph_count() const
+        {
+        return graphs.size();
+        }
+    uint64_t graph_generation() const
+        {
+        return graph_nlist_generation;
+        }
 
     private:
     void sort_particles();

@@ -166,6 +166,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
                  return out;
              })
         .def("buildNow", &NeighborList::build_sync)
+        .def_readonly("alloc_generation", &NeighborList::alloc_generation)
         .def("setStartCapacity",
              [](NeighborList& n, unsigned int cell, std::vector<uint32_t> per_type) {
                  if (per_type.size() != n.pdata->ntypes)
@@ -248,6 +249,8 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def_readwrite("use_graph", &Integrator::use_graph)
         .def_readwrite("compute_virial", &Integrator::compute_virial)
         .def_readonly("n_rollbacks", &Integrator::n_rollbacks)
+        .def("graphCount", &Integrator::graph_count)
+        .def("graphGeneration", &Integrator::graph_generation)
         .def_readonly("steps_run", &Integrator::steps_run)
         .def_readonly("launch_count", &Integrator::launch_count)
         .def("timePhases", &Integrator::time_phases)

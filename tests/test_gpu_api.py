@@ -224,6 +224,31 @@ def test_overflow_rolls_back_and_matches():
     assert np.abs(a.particles.position - b.particles.position).max() < 5e-2
 
 
+def test_graphs_follow_list_reallocation():
+    """A neighbour list rebuilt with larger buffers outside a run (here: new capacities and a
+    build on request) moves the buffers the captured step graphs address; the next run must
+    capture new graphs and give the same trajectory as a run without the extra build."""
+    snap = workloads.lj_fluid_sc(12)
+    res = []
+    for rebuild in (False, True):
+        sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.5)
+        sim.run(60)
+        integ = sim._cpp_integrator
+        assert integ.graphCount() >= 1
+        if rebuild:
+            gen = cell._cpp_obj.alloc_generation
+            cell._cpp_obj.setStartCapacity(int(cell._cpp_obj.getNmax()) + 16,
+                                           [int(n) + 64 for n in cell._cpp_obj.getNmaxPerType()])
+            cell._cpp_obj.buildNow()
+            assert cell._cpp_obj.alloc_generation > gen
+        sim.run(60)
+        assert integ.graphGeneration() == cell._cpp_obj.alloc_generation
+        res.append(sim.state.get_snapshot())
+    box = np.array(snap.configuration.box[:3])
+    ua, ub = [s.particles.position + s.particles.image * box for s in res]
+    assert np.abs(ua - ub).max() < 1e-3
+
+
 def test_nan_position_raises_with_tag():
     snap = workloads.lj_fluid_sc(8)
     snap.particles.position[17] = [np.nan, 0, 0]
