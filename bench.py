@@ -237,7 +237,8 @@ def make_sim(wl, snap, seed=1):
                                        md.methods.thermostats.Bussi(kT=c["kT"]))
     sim.operations.integrator = md.Integrator(dt=c["dt"], forces=[force], methods=[method])
     if c.get("sort_period"):
-        sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=c["sort_period"]))
+        sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=c["sort_period"],
+                                                               grid=c.get("sort_grid")))
     return sim, force, cell, method
 
 
@@ -287,6 +288,8 @@ def run_gb300(args):
     import torch
 
     wl = workloads_registry(args.fcc_m)[args.workload]
+    if args.sort_grid:
+        wl.config["sort_grid"] = args.sort_grid
     rank, world, local = dist_init()
     torch.cuda.set_device(local)
     snap = wl.make_snap(1 + rank)
@@ -757,6 +760,8 @@ def main():
     ap.add_argument("--fcc-m", type=int, default=64,
                     help="FCC cells per side of lj_fcc_1m (64 = the 1,048,576-particle workload; "
                          "smaller values are for profiling captures only)")
+    ap.add_argument("--sort-grid", type=int, default=0,
+                    help="ParticleSorter grid (bins per box side); 0 = the sorter's default, 256")
     ap.add_argument("--nve-drift", action="store_true",
                     help="measure the NVE energy drift of lj_fcc_1m instead of the throughput")
     ap.add_argument("--drift-steps", type=int, default=10000)
