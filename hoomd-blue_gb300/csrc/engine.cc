@@ -236,6 +236,20 @@ void NeighborList::add_consumer(const std::vector<float>* m)
     dirty = true;
     }
 
+void NeighborList::ensure_consumer(const std::vector<float>* m)
+    {
+    if (std::find(consumers.begin(), consumers.end(), m) == consumers.end())
+        add_consumer(m);
+    }
+
+void NeighborList::remove_consumer(const std::vector<float>* m)
+    {
+    const auto n = consumers.size();
+    consumers.erase(std::remove(consumers.begin(), consumers.end(), m), consumers.end());
+    if (consumers.size() != n)
+        dirty = true;
+    }
+
 void NeighborList::clear_consumers()
     {
     consumers.clear();
@@ -567,6 +581,21 @@ PairForce::PairForce(std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborL
     t_F.assign(np, std::vector<double>(1, 0.0));
     force.resize(4 * (size_t)std::max(1u, pdata->N));
     force.zero(pdata->stream);
+    }
+
+PairForce::~PairForce()
+    {
+    // the list keeps a pointer to this force's r_cut matrix while it is a consumer
+    if (nlist)
+        nlist->remove_consumer(&r_cut);
+    }
+
+void PairForce::compute_standalone(bool with_virial)
+    {
+    nlist->ensure_consumer(&r_cut);
+    nlist->build_sync();
+    compute(pdata->stream, with_virial);
+    cuda_check(cudaStreamSynchronize(pdata->stream), "compute");
     }
 
 // EvaluatorPairDPDThermoDPD / DPDThermoLJ parameters (hoomd/md/EvaluatorPairDPDThermoLJ.h:60-90)

@@ -175,6 +175,9 @@ class NeighborList
     NeighborList(std::shared_ptr<ParticleData> pdata, double r_buff);
     void set_r_cut(unsigned int i, unsigned int j, double r); // the nlist's own r_cut matrix
     void add_consumer(const std::vector<float>* rcut_matrix);
+    // add unless already present; remove every entry of one matrix (its owner is going away)
+    void ensure_consumer(const std::vector<float>* rcut_matrix);
+    void remove_consumer(const std::vector<float>* rcut_matrix);
     void clear_consumers();
     void update_rlist();        // NeighborList::updateRList
     void allocate();            // cell grid, adjacency, capacities
@@ -239,6 +242,12 @@ class PairForce
     public:
     PairForce(std::shared_ptr<ParticleData> pdata, std::shared_ptr<NeighborList> nlist,
               PairKind kind);
+    ~PairForce();
+    PairForce(const PairForce&) = delete;
+    PairForce& operator=(const PairForce&) = delete;
+    // forces at the current positions outside an integrator (a force used as a compute): makes
+    // this force's r_cut part of its list's r_list, builds the list and computes
+    void compute_standalone(bool with_virial);
     void set_params_lj(unsigned int i, unsigned int j, double sigma, double epsilon);
     void set_params_example(unsigned int i, unsigned int j, double k, double sigma);
     void set_params_radial(unsigned int i, unsigned int j, unsigned int kind,

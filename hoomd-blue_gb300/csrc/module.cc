@@ -213,12 +213,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
                 f.shift_mode = v;
                 f.params_dirty = true;
             })
-        .def("compute",
-             [](PairForce& f, bool virial) {
-                 f.nlist->build_sync();
-                 f.compute(f.pdata->stream, virial);
-                 cuda_check(cudaStreamSynchronize(f.pdata->stream), "compute");
-             })
+        .def("compute", &PairForce::compute_standalone)
         .def("getForces", [](PairForce& f) { return force_by_tag(f, 0); })
         .def("getEnergies", [](PairForce& f) { return force_by_tag(f, 1); })
         .def("energySum", &PairForce::energy_sum)

@@ -78,6 +78,7 @@ class Pair:
 
     def _attach(self, simulation, cpp_nlist):
         self._simulation = simulation
+        self._standalone = False
         state = simulation.state
         self._cpp_obj = _hoomd_gb300.PotentialPairGPU(state._cpp_pdata, cpp_nlist, self._kind)
         self._cpp_obj.mode = _MODES[self._mode]
@@ -108,10 +109,13 @@ class Pair:
         """True when every pair is scaled by q_i q_j (the reference's needsCharge())."""
         return False
 
-    def _require_run(self):
+    def _require_run(self, virial=False):
         if self._cpp_obj is None or self._simulation is None:
             raise RuntimeError("forces are available after Simulation.run")
         self._simulation._attach()
+        if getattr(self, "_standalone", False):
+            # a compute, not held by an integrator: evaluate at the current positions
+            self._cpp_obj.compute(bool(virial))
 
     @property
     def forces(self):
@@ -128,7 +132,7 @@ class Pair:
     @property
     def virials(self):
         """(N, 6) per-particle virials (xx, xy, xz, yy, yz, zz) in tag order."""
-        self._require_run()
+        self._require_run(virial=True)
         return self._cpp_obj.getVirials()
 
     @property
@@ -244,6 +248,7 @@ class TableSurrogate(Pair):
 
     def _attach(self, simulation, cpp_nlist):
         self._simulation = simulation
+        self._standalone = False
         state = simulation.state
         ntypes = len(state.particle_types)
         if ntypes != self.surrogate.ntypes:

@@ -164,6 +164,7 @@ class Simulation:
             for op in self.operations.computes:
                 if isinstance(op, NeighborList):
                     op._attach(self).buildNow()
+            self._attach_compute_forces()
             return None
         if self._cpp_integrator is None:
             self._cpp_integrator = integ._attach(self)
@@ -185,7 +186,17 @@ class Simulation:
             self._needs_prep = False
         for op in self.operations.computes:
             op._simulation = self
+        self._attach_compute_forces()
         return self._cpp_integrator
+
+    def _attach_compute_forces(self):
+        """Pair forces in ``operations.computes`` that no integrator holds are evaluated on
+        their own at the current positions when read (hoomd's forces are computes too)."""
+        from hoomd_gb300.md.pair import Pair
+        for op in self.operations.computes:
+            if isinstance(op, Pair) and op._cpp_obj is None:
+                op._attach(self, op.nlist._attach(self))
+                op._standalone = True
 
     def _advance(self, cpp, steps):
         if cpp is None:

@@ -249,6 +249,63 @@ def test_graphs_follow_list_reallocation():
     assert np.abs(ua - ub).max() < 1e-3
 
 
+def test_adding_to_operations():
+    """hoomd/md/pytest/test_potential.py:1296-1305: a force added to the operations (no
+    integrator) is a compute evaluated at the current positions."""
+    sim = make_sim(two_particle_snapshot(d=0.5))
+    lj = md.pair.LJ(nlist=md.nlist.Cell(0.4))
+    lj.r_cut.default = 2.5
+    lj.params.default = {"epsilon": 1.0, "sigma": 1.0}
+    sim.operations += lj
+    sim.run(0)
+    assert lj.energy != 0
+    e = 4 * (0.5 ** -12 - 0.5 ** -6)
+    assert lj.energy == pytest.approx(e, rel=1e-5)
+    f = lj.forces
+    fmag = 24 * (2 * 0.5 ** -13 - 0.5 ** -7)
+    assert f[1, 0] == pytest.approx(fmag, rel=1e-5) and f[0, 0] == pytest.approx(-fmag, rel=1e-5)
+    assert lj.virials.shape == (2, 6)
+
+
+@pytest.mark.parametrize("name,params", [
+    ("LJ", dict(epsilon=1.5, sigma=1.1)),
+    ("Gaussian", dict(epsilon=1.0, sigma=0.8)),
+    ("Yukawa", dict(epsilon=2.0, kappa=1.5)),
+    ("Morse", dict(D0=1.0, alpha=2.0, r0=1.1)),
+    ("Mie", dict(epsilon=1.0, sigma=1.0, n=12, m=6))])
+def test_shift(name, params):
+    """hoomd/md/pytest/test_potential.py:1349-1390: two forces used as computes, one shifted,
+    at r just inside r_cut: the shifted energy is much closer to zero."""
+    r_cut = 2.0
+    pots = []
+    for mode in ("none", "shift"):
+        p = getattr(md.pair, name)(nlist=md.nlist.Cell(buffer=0.4), default_r_cut=r_cut)
+        p.params[("A", "A")] = params
+        p.mode = mode
+        pots.append(p)
+    sim = make_sim(two_particle_snapshot(d=r_cut - 1e-3))
+    sim.operations.computes.extend(pots)
+    sim.run(0)
+    V, V_shifted = pots[0].energy, pots[1].energy
+    assert V != 0
+    assert V_shifted == pytest.approx(0, abs=max(abs(V) / 1e2, 1e-8))
+
+
+def test_force_in_integrator_and_computes():
+    """A force held by the integrator and listed as a compute is evaluated once, by the
+    integrator; a second, compute-only copy with the same parameters agrees with it."""
+    snap = workloads.lj_fluid_sc(8)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0)
+    sim.operations.computes.append(lj)
+    other = md.pair.LJ(nlist=md.nlist.Cell(buffer=0.4), default_r_cut=2.5)
+    other.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+    sim.operations.computes.append(other)
+    sim.run(20)
+    assert not getattr(lj, "_standalone", False) and other._standalone
+    assert np.allclose(other.forces, lj.forces, rtol=1e-4, atol=1e-4)
+    assert other.energy == pytest.approx(lj.energy, rel=1e-5)
+
+
 def test_nan_position_raises_with_tag():
     snap = workloads.lj_fluid_sc(8)
     snap.particles.position[17] = [np.nan, 0, 0]
