@@ -22,7 +22,8 @@ class Pair:
     _accepted_modes = ("none", "shift", "xplor")
     _kind = None
     _loggables = {"energy": "scalar", "energies": "particle", "forces": "particle",
-                  "virials": "particle"}
+                  "torques": "particle", "virials": "particle", "additional_energy": "scalar",
+                  "additional_virial": "sequence"}
 
     def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
         self.r_cut = TypePairDict(default=None if default_r_cut is None else float(default_r_cut),
@@ -122,6 +123,12 @@ class Pair:
         """(N, 3) forces in tag order."""
         self._require_run()
         return self._cpp_obj.getForces()
+
+    @property
+    def torques(self):
+        """(N, 3) torques: zero for these isotropic pair forces."""
+        self._require_run()
+        return np.zeros((self._simulation.state.N_particles, 3))
 
     @property
     def energies(self):

@@ -265,6 +265,14 @@ def test_adding_to_operations():
     fmag = 24 * (2 * 0.5 ** -13 - 0.5 ** -7)
     assert f[1, 0] == pytest.approx(fmag, rel=1e-5) and f[0, 0] == pytest.approx(-fmag, rel=1e-5)
     assert lj.virials.shape == (2, 6)
+    assert np.array_equal(lj.torques, np.zeros((2, 3)))
+    assert lj.additional_energy == 0.0 and lj.additional_virial == [0.0] * 6
+    logger = hoomd.logging.Logger(categories=["scalar", "sequence"])
+    logger.add(lj, quantities=["energy", "additional_energy", "additional_virial"])
+    logged = logger.log()["md"]["pair"]["LJ"]
+    assert logged["energy"] == (pytest.approx(e, rel=1e-5), "scalar")
+    assert logged["additional_energy"] == (0.0, "scalar")
+    assert logged["additional_virial"] == ([0.0] * 6, "sequence")
 
 
 @pytest.mark.parametrize("name,params", [
