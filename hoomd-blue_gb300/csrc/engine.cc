@@ -847,6 +847,55 @@ void PairForce::compute(cudaStream_t s, bool with_virial)
     virial_valid = with_virial;
     }
 
+double PairForce::energy_between_sets(const std::vector<uint32_t>& tags1,
+                                      const std::vector<uint32_t>& tags2)
+    {
+    if (kind == PairKind::MLP || kind == PairKind::DPD)
+        throw std::runtime_error("compute_energy is not available for this pair force");
+    ParticleData& pd = *pdata;
+    cudaStream_t s = pd.stream;
+    upload();
+    nlist->ensure_consumer(&r_cut);
+    nlist->build_sync();
+    const std::vector<uint32_t> rt = pd.rtag();
+    std::vector<uint8_t> set(pd.N, 0);
+    for (int which = 1; which <= 2; which++)
+        for (uint32_t t : (which == 1 ? tags1 : tags2))
+            {
+            if (t >= pd.N)
+                throw std::invalid_argument("compute_energy: tag out of range");
+            set[rt[t]] = (uint8_t)which;
+            }
+    DeviceArray<uint8_t> d_set;
+    d_set.resize(std::max(1u, pd.N));
+    d_set.upload(set.data(), pd.N, s);
+    const unsigned int nb = gb_pair_energy_sets_blocks(pd.N);
+    DeviceArray<double> parts;
+    parts.resize(nb);
+    gb_pair_args a = pair_args(false);
+    int rc;
+    if (kind == PairKind::LJ)
+        rc = gb_pair_energy_sets_lj(&a, (const gb_lj_param*)d_params.get(), d_set.get(),
+                                    parts.get(), s);
+    else if (kind == PairKind::Example)
+        rc = gb_pair_energy_sets_example(&a, (const gb_example_param*)d_params.get(), d_set.get(),
+                                         parts.get(), s);
+    else if (kind == PairKind::Radial)
+        rc = gb_pair_energy_sets_radial(&a, (const gb_radial_param*)d_params.get(), d_set.get(),
+                                        parts.get(), s);
+    else
+        rc = gb_pair_energy_sets_table(&a, (const gb_table_param*)d_params.get(), d_table.get(),
+                                       d_set.get(), parts.get(), s);
+    check(rc, "energy between sets");
+    std::vector<double> h(nb);
+    parts.download(h.data(), nb, s);
+    cuda_check(cudaStreamSynchronize(s), "energy between sets");
+    double u = 0.0;
+    for (double v : h)
+        u += v;
+    return u;
+    }
+
 int PairForce::launch_fused(const gb_pair_args& a, const gb_step_fuse& f, cudaStream_t s)
     {
     if (kind == PairKind::LJ)

@@ -248,6 +248,10 @@ class PairForce
     // forces at the current positions outside an integrator (a force used as a compute): makes
     // this force's r_cut part of its list's r_list, builds the list and computes
     void compute_standalone(bool with_virial);
+    // PotentialPair::computeEnergyBetweenSets: sum of V_ij over i in tags1, j in tags2, on the
+    // device from a freshly built list
+    double energy_between_sets(const std::vector<uint32_t>& tags1,
+                               const std::vector<uint32_t>& tags2);
     void set_params_lj(unsigned int i, unsigned int j, double sigma, double epsilon);
     void set_params_example(unsigned int i, unsigned int j, double k, double sigma);
     void set_params_radial(unsigned int i, unsigned int j, unsigned int kind,

@@ -214,6 +214,22 @@ PYBIND11_MODULE(_hoomd_gb300, m)
                 f.params_dirty = true;
             })
         .def("compute", &PairForce::compute_standalone)
+        .def("computeEnergyBetweenSets",
+             [](PairForce& f, py::array_t<int64_t, py::array::c_style | py::array::forcecast> a,
+                py::array_t<int64_t, py::array::c_style | py::array::forcecast> b) {
+                 auto conv = [](const py::array_t<int64_t, py::array::c_style
+                                                               | py::array::forcecast>& x) {
+                     std::vector<uint32_t> v((size_t)x.size());
+                     for (size_t k = 0; k < v.size(); k++)
+                         {
+                         if (x.data()[k] < 0)
+                             throw std::invalid_argument("compute_energy: negative tag");
+                         v[k] = (uint32_t)x.data()[k];
+                         }
+                     return v;
+                 };
+                 return f.energy_between_sets(conv(a), conv(b));
+             })
         .def("getForces", [](PairForce& f) { return force_by_tag(f, 0); })
         .def("getEnergies", [](PairForce& f) { return force_by_tag(f, 1); })
         .def("energySum", &PairForce::energy_sum)

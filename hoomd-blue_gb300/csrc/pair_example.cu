@@ -21,4 +21,11 @@ extern "C"
             return rc;
         return launch_pair<EvalExample, true>(args, d_params, nullptr, fz, (cudaStream_t)stream);
         }
+
+    int gb_pair_energy_sets_example(const gb_pair_args* args, const gb_example_param* d_params,
+                                  const uint8_t* d_set, double* d_partials, void* stream)
+        {
+        return launch_energy_sets<EvalExample>(args, d_params, nullptr, d_set, d_partials,
+                                        (cudaStream_t)stream);
+        }
     }

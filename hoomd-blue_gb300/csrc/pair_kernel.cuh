@@ -861,3 +861,103 @@ int launch_pair(const gb_pair_args* a, const typename Eval::param_type* d_params
     }
 
 } // namespace gb
+
+namespace gb
+{
+// PotentialPair::computeEnergyBetweenSets (hoomd/md/PotentialPair.h, exported as
+// computeEnergyBetweenSets; hoomd/md/pair/pair.py compute_energy): U = sum over i in set 1 and
+// j in set 2 of V_ij(r), with the force's shift / XPLOR mode. d_set[i] is 1 or 2 for the two
+// sets (0 otherwise); every unordered pair appears once, from its set-1 particle's row of the
+// full list. Each block writes its partial sum to d_partials[blockIdx.x]; the caller adds them in
+// order.
+template<class Eval, bool MULTI, bool XPLOR>
+__global__ void __launch_bounds__(256)
+    k_energy_sets(unsigned int N, const float4* __restrict__ d_pos, gb_box box,
+                  const unsigned int* __restrict__ d_n_neigh, const unsigned int* __restrict__ d_nlist,
+                  const uint64_t* __restrict__ d_head_list, uint64_t stride, unsigned int interleave,
+                  const typename Eval::param_type* __restrict__ d_params,
+                  const float* __restrict__ d_rcutsq, const float* __restrict__ d_ronsq,
+                  unsigned int ntypes, const float* __restrict__ ext,
+                  const float* __restrict__ d_charge, bool SHIFT1,
+                  const uint8_t* __restrict__ d_set, double* __restrict__ d_partials)
+    {
+    using P = typename Eval::param_type;
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double u = 0.0;
+    if (i < N && d_set[i] == 1)
+        {
+        const float4 pi = d_pos[i];
+        const unsigned int ti = __float_as_uint(pi.w);
+        const unsigned int nn = d_n_neigh[i];
+        const float qi = Eval::needsCharge() ? d_charge[i] : 0.0f;
+        for (unsigned int k = 0; k < nn; k++)
+            {
+            size_t w;
+            if (d_head_list)
+                w = d_head_list[i] + k;
+            else if (interleave == 4)
+                w = (((size_t)(k >> 2) * stride + i) << 2) + (k & 3u);
+            else
+                w = (size_t)k * stride + i;
+            const unsigned int j = d_nlist[w];
+            if (d_set[j] != 2)
+                continue;
+            const float4 pj = d_pos[j];
+            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            min_image(box, dx, dy, dz);
+            const float rsq = dx * dx + dy * dy + dz * dz;
+            const unsigned int tp = MULTI ? ti * ntypes + __float_as_uint(pj.w) : 0u;
+            P param = d_params[tp];
+            const float rcutsq = d_rcutsq[tp];
+            Eval::prepare_param(param, rcutsq);
+            const float ronsq = XPLOR ? d_ronsq[tp] : 0.0f;
+            float force_divr = 0.0f, pair_eng = 0.0f;
+            Eval eval(rsq, rcutsq, param, ext);
+            if (Eval::needsCharge())
+                eval.setCharge(qi, d_charge[j]);
+            eval.evalForceAndEnergy(force_divr, pair_eng, XPLOR ? (ronsq > rcutsq) : SHIFT1);
+            if (XPLOR && rsq >= ronsq && rsq < rcutsq)
+                {
+                // the XPLOR smoothing of the energy (hoomd/md/PotentialPair.h:711-737)
+                const float d = rcutsq - ronsq;
+                const float m = rsq - rcutsq;
+                pair_eng *= m * m * (rcutsq + 2.0f * rsq - 3.0f * ronsq) / (d * d * d);
+                }
+            u += (double)pair_eng;
+            }
+        }
+    __shared__ double s_red[32];
+    u = block_sum_d<1>(u, s_red);
+    if (threadIdx.x == 0)
+        d_partials[blockIdx.x] = u;
+    }
+
+inline unsigned int energy_sets_blocks(unsigned int N)
+    {
+    return div_up(N > 0 ? N : 1u, 256u);
+    }
+
+template<class Eval>
+int launch_energy_sets(const gb_pair_args* a, const typename Eval::param_type* d_params,
+                       const float* ext, const uint8_t* d_set, double* d_partials,
+                       cudaStream_t s)
+    {
+    GB_REQUIRE(a && d_set && d_partials, "energy between sets: null argument");
+    GB_REQUIRE(a->d_pos && a->d_n_neigh && a->d_nlist && a->d_rcutsq && d_params,
+               "energy between sets: null device pointer");
+    GB_REQUIRE(a->shift_mode <= 2 && (a->shift_mode != 2 || a->d_ronsq),
+               "energy between sets: shift_mode 0, 1 or 2 (xplor needs r_on^2)");
+    GB_REQUIRE(a->d_head_list || a->interleave <= 1 || a->interleave == 4,
+               "energy between sets: interleave must be 1 or 4");
+    GB_REQUIRE(!Eval::needsCharge() || a->d_charge, "energy between sets: charges needed");
+    const unsigned int grid = energy_sets_blocks(a->N);
+    const bool multi = a->ntypes > 1, xplor = a->shift_mode == 2;
+    auto kern = multi ? (xplor ? k_energy_sets<Eval, true, true> : k_energy_sets<Eval, true, false>)
+                      : (xplor ? k_energy_sets<Eval, false, true> : k_energy_sets<Eval, false, false>);
+    kern<<<grid, 256, 0, s>>>(a->N, reinterpret_cast<const float4*>(a->d_pos), a->box,
+                              a->d_n_neigh, a->d_nlist, a->d_head_list, a->stride,
+                              a->interleave == 4 ? 4u : 1u, d_params, a->d_rcutsq, a->d_ronsq,
+                              a->ntypes, ext, a->d_charge, a->shift_mode == 1, d_set, d_partials);
+    return check_launch("energy between sets");
+    }
+} // namespace gb

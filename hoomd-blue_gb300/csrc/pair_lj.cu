@@ -21,4 +21,16 @@ extern "C"
             return rc;
         return launch_pair<EvalLJ, true>(args, d_params, nullptr, fz, (cudaStream_t)stream);
         }
+
+    int gb_pair_energy_sets_lj(const gb_pair_args* args, const gb_lj_param* d_params,
+                               const uint8_t* d_set, double* d_partials, void* stream)
+        {
+        return launch_energy_sets<EvalLJ>(args, d_params, nullptr, d_set, d_partials,
+                                          (cudaStream_t)stream);
+        }
+
+    unsigned int gb_pair_energy_sets_blocks(unsigned int N)
+        {
+        return energy_sets_blocks(N);
+        }
     }

@@ -9,6 +9,8 @@ namespace gb
 {
 int radial_charged(const gb_pair_args* args, const gb_radial_param* d_params, const FuseArgs& fz,
                    bool fused, cudaStream_t s);
+int radial_energy_sets_charged(const gb_pair_args* args, const gb_radial_param* d_params,
+                               const uint8_t* d_set, double* d_partials, cudaStream_t s);
 }
 
 using namespace gb;
@@ -35,5 +37,15 @@ extern "C"
         if (args->d_charge)
             return radial_charged(args, d_params, fz, true, (cudaStream_t)stream);
         return launch_pair<EvalRadial, true>(args, d_params, nullptr, fz, (cudaStream_t)stream);
+        }
+
+    int gb_pair_energy_sets_radial(const gb_pair_args* args, const gb_radial_param* d_params,
+                                   const uint8_t* d_set, double* d_partials, void* stream)
+        {
+        if (args && args->d_charge)
+            return radial_energy_sets_charged(args, d_params, d_set, d_partials,
+                                              (cudaStream_t)stream);
+        return launch_energy_sets<EvalRadial>(args, d_params, nullptr, d_set, d_partials,
+                                              (cudaStream_t)stream);
         }
     }

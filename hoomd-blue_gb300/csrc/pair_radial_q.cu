@@ -12,4 +12,10 @@ int radial_charged(const gb_pair_args* args, const gb_radial_param* d_params, co
         return launch_pair<EvalRadialQ, true>(args, d_params, nullptr, fz, s);
     return launch_pair<EvalRadialQ, false>(args, d_params, nullptr, fz, s);
     }
+
+int radial_energy_sets_charged(const gb_pair_args* args, const gb_radial_param* d_params,
+                               const uint8_t* d_set, double* d_partials, cudaStream_t s)
+    {
+    return launch_energy_sets<EvalRadialQ>(args, d_params, nullptr, d_set, d_partials, s);
+    }
 } // namespace gb

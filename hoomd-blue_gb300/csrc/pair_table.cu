@@ -21,4 +21,12 @@ extern "C"
             return rc;
         return launch_pair<EvalTable, true>(args, d_params, d_table, fz, (cudaStream_t)stream);
         }
+
+    int gb_pair_energy_sets_table(const gb_pair_args* args, const gb_table_param* d_params,
+                                  const float* d_table,
+                                  const uint8_t* d_set, double* d_partials, void* stream)
+        {
+        return launch_energy_sets<EvalTable>(args, d_params, d_table, d_set, d_partials,
+                                        (cudaStream_t)stream);
+        }
     }

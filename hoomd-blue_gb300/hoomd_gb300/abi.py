@@ -141,6 +141,11 @@ _PROTOS = {
     "gb_sfc_order": (c_int, [c_void, c_uint, _P(Box), c_int, c_void, c_void, c_size, c_void]),
     "gb_gather": (c_int, [c_void, c_void, c_void, c_uint, c_uint, c_void]),
     "gb_pair_forces_radial": (c_int, [c_void, c_void, c_void]),
+    "gb_pair_energy_sets_blocks": (c_uint, [c_uint]),
+    "gb_pair_energy_sets_lj": (c_int, [c_void, c_void, c_void, c_void, c_void]),
+    "gb_pair_energy_sets_table": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void]),
+    "gb_pair_energy_sets_example": (c_int, [c_void, c_void, c_void, c_void, c_void]),
+    "gb_pair_energy_sets_radial": (c_int, [c_void, c_void, c_void, c_void, c_void]),
     "gb_pair_forces_dpd": (c_int, [c_void, c_void, c_void, c_void, c_int, c_u64, ctypes.c_uint16,
                                    c_float, c_float, c_void]),
     "gb_md_pair_step_radial": (c_int, [c_void, c_void, c_void, c_void]),

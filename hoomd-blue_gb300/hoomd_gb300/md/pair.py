@@ -124,6 +124,14 @@ class Pair:
         self._require_run()
         return self._cpp_obj.getForces()
 
+    def compute_energy(self, tags1, tags2):
+        """Energy between two disjoint sets of particles, U = sum over i in tags1 and j in
+        tags2 of V_ij(r) (hoomd/md/pair/pair.py compute_energy), summed on the GPU."""
+        if self._cpp_obj is None or self._simulation is None:
+            raise RuntimeError("compute_energy is available after Simulation.run")
+        self._simulation._attach()
+        return self._cpp_obj.computeEnergyBetweenSets(np.asarray(tags1), np.asarray(tags2))
+
     @property
     def torques(self):
         """(N, 3) torques: zero for these isotropic pair forces."""

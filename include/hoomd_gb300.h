@@ -301,6 +301,24 @@ typedef struct gb_radial_param
 int gb_pair_forces_radial(const gb_pair_args* args, const gb_radial_param* d_params,
                           void* stream);
 
+/* Energy between two sets of particles: replaces PotentialPair<E>::computeEnergyBetweenSets
+ * (hoomd/md/PotentialPair.h, bound as computeEnergyBetweenSets and called by
+ * hoomd/md/pair/pair.py compute_energy), which sums on the host. U = sum over i in set 1, j in
+ * set 2 of V_ij(r) with the force's shift / XPLOR mode, from the full list in args (the forces
+ * and virial fields of args are not used). d_set[i] = 1 or 2 marks particle index i's set (0 =
+ * neither); the sets must be disjoint. d_partials receives gb_pair_energy_sets_blocks(N) doubles
+ * whose sum, in order, is U. With args->d_charge set, the radial entry scales by q_i q_j. */
+unsigned int gb_pair_energy_sets_blocks(unsigned int N);
+int gb_pair_energy_sets_lj(const gb_pair_args* args, const gb_lj_param* d_params,
+                           const uint8_t* d_set, double* d_partials, void* stream);
+int gb_pair_energy_sets_table(const gb_pair_args* args, const gb_table_param* d_params,
+                              const float* d_table, const uint8_t* d_set, double* d_partials,
+                              void* stream);
+int gb_pair_energy_sets_example(const gb_pair_args* args, const gb_example_param* d_params,
+                                const uint8_t* d_set, double* d_partials, void* stream);
+int gb_pair_energy_sets_radial(const gb_pair_args* args, const gb_radial_param* d_params,
+                               const uint8_t* d_set, double* d_partials, void* stream);
+
 /* DPD thermostat pair forces (EvaluatorPairDPDThermoDPD.h:190-272, EvaluatorPairDPDThermoLJ.h:
  * 216-276, PotentialPairDPDThermo.h:160-240): a conservative part (DPD: A (1 - r/r_c); DPDLJ:
  * the LJ force with lj1 = 4 eps sigma^12, lj2 = 4 eps sigma^6), a drag

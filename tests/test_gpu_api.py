@@ -349,3 +349,58 @@ def test_multiple_forces_general_path():
     p1 = sim1.state.get_snapshot().particles.position
     p2 = sim2.state.get_snapshot().particles.position
     assert np.abs(p1 - p2).max() < 1e-4
+
+
+def _brute_energy_sets(pos, L, tags1, tags2, V, r_cut):
+    """FP64 sum of V(r) over i in tags1, j in tags2 within r_cut (minimum image, cubic box)."""
+    a = pos[np.asarray(tags1)][:, None, :] - pos[np.asarray(tags2)][None, :, :]
+    a -= L * np.rint(a / L)
+    r = np.sqrt((a ** 2).sum(-1))
+    m = r < r_cut
+    return V(r[m]).sum()
+
+
+@pytest.mark.parametrize("kind", ["lj_xplor", "lj_shift", "yukawa"])
+def test_compute_energy_between_sets(kind):
+    """Pair.compute_energy (hoomd/md/pair/pair.py, PotentialPair::computeEnergyBetweenSets):
+    the sum over i in one set and j in the other, against an FP64 brute force."""
+    snap = workloads.lj_fluid_sc(10, density=0.8, jitter=0.1, seed=11)
+    N = snap.particles.N
+    L = snap.configuration.box[0]
+    sim = make_sim(snap)
+    rc, ron = 2.5, 2.0
+    if kind.startswith("lj"):
+        f = md.pair.LJ(nlist=md.nlist.Cell(buffer=0.4), default_r_cut=rc,
+                       mode="xplor" if kind == "lj_xplor" else "shift")
+        f.params[("A", "A")] = dict(epsilon=1.2, sigma=0.9)
+        f.r_on[("A", "A")] = ron
+
+        def V0(r):
+            return 4 * 1.2 * ((0.9 / r) ** 12 - (0.9 / r) ** 6)
+        if kind == "lj_xplor":
+            def V(r):
+                s = np.where(r < ron, 1.0, (rc ** 2 - r ** 2) ** 2 * (rc ** 2 + 2 * r ** 2 - 3 * ron ** 2)
+                             / (rc ** 2 - ron ** 2) ** 3)
+                return V0(r) * s
+        else:
+            def V(r):
+                return V0(r) - V0(rc)
+    else:
+        f = md.pair.Yukawa(nlist=md.nlist.Cell(buffer=0.4), default_r_cut=rc)
+        f.params[("A", "A")] = dict(epsilon=2.0, kappa=1.5)
+
+        def V(r):
+            return 2.0 * np.exp(-1.5 * r) / r
+    sim.operations.computes.append(f)
+    sim.run(0)
+    tags = np.arange(N)
+    t1, t2 = tags[0::2], tags[1::2]
+    pos = sim.state.get_snapshot().particles.position.astype(np.float32).astype(np.float64)
+    want = _brute_energy_sets(pos, L, t1, t2, V, rc)
+    got = f.compute_energy(t1, t2)
+    assert got == pytest.approx(want, rel=2e-5)
+    # a subset against the rest, and the symmetry of the two sets
+    s1, s2 = tags[:137], tags[137:]
+    assert f.compute_energy(s1, s2) == pytest.approx(f.compute_energy(s2, s1), rel=1e-5)
+    assert f.compute_energy(s1, s2) == pytest.approx(
+        _brute_energy_sets(pos, L, s1, s2, V, rc), rel=2e-5)
