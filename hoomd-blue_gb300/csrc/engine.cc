@@ -363,7 +363,8 @@ void NeighborList::allocate()
     }
 
 void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count,
-                                 uint32_t* d_cell_cond, uint32_t* d_nl_cond, cudaStream_t s)
+                                 uint32_t* d_cell_cond, uint32_t* d_nl_cond, cudaStream_t s,
+                                 const uint64_t* d_timestep, uint64_t* d_build_steps)
     {
     ParticleData& pd = *pdata;
     gb_cell_list_args c {};
@@ -380,6 +381,8 @@ void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count
     c.d_gate = d_gate;
     c.deterministic = deterministic ? 1 : 0;
     c.d_build_count = d_build_count;
+    c.d_timestep = d_timestep;
+    c.d_build_steps = d_build_steps;
     check(gb_cell_list_build(&c, s), "gb_cell_list_build");
     gb_nlist_args a {};
     a.d_nlist = nlist.get();
@@ -918,6 +921,11 @@ Integrator::Integrator(std::shared_ptr<ParticleData> pd, std::shared_ptr<Neighbo
     {
     d_status.resize(1);
     d_status.zero(pdata->stream);
+    const uint64_t steps[2] = {~0ull, 100};
+    cuda_check(cudaMemcpyAsync(d_status.get()->build_steps, steps, sizeof(steps),
+                               cudaMemcpyHostToDevice, pdata->stream),
+               "build statistics");
+    cuda_check(cudaStreamSynchronize(pdata->stream), "build statistics");
     }
 
 Integrator::~Integrator()
@@ -1283,7 +1291,8 @@ void Integrator::enqueue_step_fused(cudaStream_t s)
     DevStatus* ds = d_status.get();
     const gb_step_one_args o = step_one_args(ds);
     check(gb_md_step_one(&o, s), "gb_md_step_one");
-    nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
+    nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s, &ds->timestep,
+                         ds->build_steps);
     PairForce& f = *forces[0];
     gb_pair_args a = f.pair_args(false);
     const gb_step_fuse fu = fuse_args(ds);
@@ -1302,7 +1311,8 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
         o.timestep = step;
         }
     check(gb_md_step_one(&o, s), "gb_md_step_one");
-    nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s);
+    nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s, &ds->timestep,
+                         ds->build_steps);
     for (auto& f : forces)
         {
         // IntegratorTwoStep::update computes the net force for timestep + 1
@@ -1536,6 +1546,15 @@ void Integrator::sort_particles()
     nb += 1;
     cuda_check(cudaMemcpyAsync(&ds->n_builds, &nb, sizeof(nb), cudaMemcpyHostToDevice, s), "nb");
     cuda_check(cudaStreamSynchronize(s), "sort");
+    }
+
+void Integrator::reset_build_stats()
+    {
+    const uint64_t period = 100;
+    cuda_check(cudaMemcpyAsync(&d_status.get()->build_steps[1], &period, sizeof(period),
+                               cudaMemcpyHostToDevice, pdata->stream),
+               "build statistics");
+    cuda_check(cudaStreamSynchronize(pdata->stream), "build statistics");
     }
 
 void Integrator::run(uint64_t nsteps)

@@ -129,6 +129,7 @@ struct DevStatus
     uint32_t pad[3];
     uint64_t timestep;
     uint64_t n_builds;
+    uint64_t build_steps[2]; // last build's timestep, smallest period between builds (cap 99)
     double factor;         // Bussi rescale factor for the next step one
     double thermo[3];      // KE, PE, W after the last step
     double reservoir;      // Langevin reservoir energy (tally_reservoir_energy)
@@ -183,7 +184,8 @@ class NeighborList
     void allocate();            // cell grid, adjacency, capacities
     void build_sync();          // forced build with host-side overflow retry
     void enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count, uint32_t* d_cell_cond,
-                       uint32_t* d_nl_cond, cudaStream_t s);
+                       uint32_t* d_nl_cond, cudaStream_t s, const uint64_t* d_timestep = nullptr,
+                       uint64_t* d_build_steps = nullptr);
     bool grow(const DevStatus& st); // returns true when a capacity grew
     std::vector<uint32_t> pair_list(bool full); // tag pairs, for tests
     std::vector<uint32_t> dims() const
@@ -383,6 +385,8 @@ class Integrator
         return (uintptr_t)pdata->stream;
         }
     double sum_n_neigh();
+    // restart the smallest-rebuild-period statistic (at each Simulation.run)
+    void reset_build_stats();
     // captured step graphs and the neighbour-list buffer generation they were captured under
     size_t graph_count() const
         {

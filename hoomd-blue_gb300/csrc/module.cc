@@ -261,6 +261,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def_readwrite("compute_virial", &Integrator::compute_virial)
         .def_readonly("n_rollbacks", &Integrator::n_rollbacks)
         .def("graphCount", &Integrator::graph_count)
+        .def("resetBuildStats", &Integrator::reset_build_stats)
         .def("graphGeneration", &Integrator::graph_generation)
         .def_readonly("steps_run", &Integrator::steps_run)
         .def_readonly("launch_count", &Integrator::launch_count)
@@ -283,6 +284,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
                  py::dict d;
                  d["timestep"] = st.timestep;
                  d["n_builds"] = st.n_builds;
+                 d["shortest_rebuild"] = st.build_steps[1];
                  d["factor"] = st.factor;
                  d["kinetic_energy"] = st.thermo[0];
                  d["potential_energy"] = st.thermo[1];

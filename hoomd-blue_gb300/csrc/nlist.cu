@@ -25,12 +25,23 @@ namespace
 {
 constexpr int NL_WARPS = 4; // warps per block in the build kernel
 
-__global__ void k_zero_u32(unsigned int* p, size_t n, const uint32_t* gate, uint64_t* count)
+__global__ void k_zero_u32(unsigned int* p, size_t n, const uint32_t* gate, uint64_t* count,
+                           const uint64_t* timestep, uint64_t* build_steps)
     {
     if (gate && *gate == 0)
         return;
-    if (count && blockIdx.x == 0 && threadIdx.x == 0)
-        *count += 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        {
+        if (count)
+            *count += 1;
+        if (timestep && build_steps)
+            {
+            const uint64_t t = *timestep, last = build_steps[0];
+            if (last != ~0ull && t > last)
+                build_steps[1] = min(build_steps[1], min(t - last, (uint64_t)99));
+            build_steps[0] = t;
+            }
+        }
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x)
         p[i] = 0;
@@ -1001,7 +1012,9 @@ extern "C"
         const int sms = num_sms();
         k_zero_u32<<<min(div_up(ncell, 256), (unsigned)sms * 8), 256, 0, s>>>(a->d_cell_size,
                                                                              ncell, a->d_gate,
-                                                                             a->d_build_count);
+                                                                             a->d_build_count,
+                                                                             a->d_timestep,
+                                                                             a->d_build_steps);
         if (a->N > 0)
             k_cell_bin<<<min(div_up(a->N, 256), (unsigned)sms * 16), 256, 0, s>>>(
                 reinterpret_cast<const float4*>(a->d_pos), a->N, a->box,

@@ -31,7 +31,8 @@ class CellListArgs(ctypes.Structure):
     _fields_ = [("d_pos", c_void), ("N", c_uint), ("box", Box), ("dim", c_uint * 3),
                 ("Nmax", c_uint), ("d_cell_size", c_void), ("d_xyzf", c_void),
                 ("d_cell_type", c_void), ("d_conditions", c_void), ("d_gate", c_void),
-                ("deterministic", c_int), ("d_build_count", c_void)]
+                ("deterministic", c_int), ("d_build_count", c_void), ("d_timestep", c_void),
+                ("d_build_steps", c_void)]
 
 
 class NlistArgs(ctypes.Structure):

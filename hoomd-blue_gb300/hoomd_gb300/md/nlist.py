@@ -58,7 +58,7 @@ def excluded_pairs(topology, exclusions, N):
 
 
 class NeighborList:
-    _loggables = {"num_builds": "scalar", "dimensions": "sequence",
+    _loggables = {"num_builds": "scalar", "shortest_rebuild": "scalar", "dimensions": "sequence",
                   "allocated_particles_per_cell": "scalar"}
 
     def __init__(self, buffer, exclusions, rebuild_check_delay, check_dist, mesh, default_r_cut):
@@ -119,6 +119,15 @@ class NeighborList:
         if self._cpp_obj is None:
             raise RuntimeError("the neighbour list has not been computed yet")
         return self._cpp_obj.getPairList(bool(full))
+
+    @property
+    def shortest_rebuild(self):
+        """Smallest number of timesteps between two builds since the last Simulation.run
+        (NeighborList::getSmallestRebuild: capped at 99; 100 when fewer than two builds)."""
+        sim = self._simulation
+        if sim is None or sim._cpp_integrator is None:
+            raise RuntimeError("shortest_rebuild is available after Simulation.run")
+        return int(sim._cpp_integrator.status()["shortest_rebuild"])
 
     @property
     def num_builds(self):

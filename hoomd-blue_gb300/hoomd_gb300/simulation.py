@@ -216,6 +216,8 @@ class Simulation:
         if steps < 0:
             raise ValueError("steps must be non-negative")
         cpp = self._attach()
+        if cpp is not None and hasattr(cpp, "resetBuildStats"):
+            cpp.resetBuildStats()  # shortest_rebuild counts from this run
         writers = list(self.operations.writers)
         for w in writers:
             w._attach(self)

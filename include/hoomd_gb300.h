@@ -89,6 +89,13 @@ typedef struct gb_cell_list_args
     int deterministic;           /* sort each cell's slots by particle index
                                     (nlist.Cell(deterministic=True), hoomd/CellListGPU.cu:478-540) */
     uint64_t* d_build_count;     /* optional: incremented once per (non-gated-off) call */
+    /* optional, both or neither: the rebuild statistics of NeighborList::needsUpdating
+     * (hoomd/md/NeighborList.cc:1388-1402, getSmallestRebuild :1428-1436). d_build_steps[0] is the
+     * timestep (*d_timestep) of the last build (UINT64_MAX before the first) and
+     * d_build_steps[1] the smallest period between builds, capped at 99; the caller sets it to
+     * 100 when the statistics start. */
+    const uint64_t* d_timestep;
+    uint64_t* d_build_steps;
     } gb_cell_list_args;
 
 int gb_cell_list_build(const gb_cell_list_args* args, void* stream);

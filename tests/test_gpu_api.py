@@ -404,3 +404,22 @@ def test_compute_energy_between_sets(kind):
     assert f.compute_energy(s1, s2) == pytest.approx(f.compute_energy(s2, s1), rel=1e-5)
     assert f.compute_energy(s1, s2) == pytest.approx(
         _brute_energy_sets(pos, L, s1, s2, V, rc), rel=2e-5)
+
+
+def test_shortest_rebuild():
+    """nlist.Cell.shortest_rebuild (NeighborList::getSmallestRebuild): the smallest period
+    between builds since the last run, at most the mean period; 100 before two builds."""
+    snap = workloads.lj_fluid_sc(12, density=0.84)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.5)
+    with pytest.raises(RuntimeError):
+        _ = cell.shortest_rebuild
+    sim.run(1)
+    assert cell.shortest_rebuild == 100
+    b0 = cell.num_builds
+    sim.run(600)
+    nb = cell.num_builds - b0
+    assert nb >= 10
+    shortest = cell.shortest_rebuild
+    assert 1 <= shortest <= 600 / nb
+    sim.run(0)
+    assert cell.shortest_rebuild == 100  # restarted by the run
