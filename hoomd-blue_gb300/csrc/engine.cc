@@ -541,7 +541,7 @@ void NeighborList::build_sync()
     throw std::runtime_error("neighbour list build did not converge");
     }
 
-std::vector<uint32_t> NeighborList::pair_list(bool full)
+std::vector<uint32_t> NeighborList::pair_list(bool full, bool local)
     {
     ParticleData& pd = *pdata;
     std::vector<uint32_t> nn(pd.N), t(pd.N), nl(nlist.size());
@@ -554,7 +554,7 @@ std::vector<uint32_t> NeighborList::pair_list(bool full)
         for (unsigned int k = 0; k < nn[i]; k++)
             {
             uint32_t j = nl[((size_t)(k >> 2) * stride + i) * 4 + (k & 3)];
-            uint32_t a = t[i], b = t[j];
+            uint32_t a = local ? i : t[i], b = local ? j : t[j];
             if (full || a < b)
                 {
                 out.push_back(a);

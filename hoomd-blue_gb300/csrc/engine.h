@@ -187,7 +187,8 @@ class NeighborList
                        uint32_t* d_nl_cond, cudaStream_t s, const uint64_t* d_timestep = nullptr,
                        uint64_t* d_build_steps = nullptr);
     bool grow(const DevStatus& st); // returns true when a capacity grew
-    std::vector<uint32_t> pair_list(bool full); // tag pairs, for tests
+    // pairs of the list as tags (or as the current particle indices with local = true)
+    std::vector<uint32_t> pair_list(bool full, bool local = false);
     std::vector<uint32_t> dims() const
         {
         return {dim[0], dim[1], dim[2]};

@@ -147,12 +147,13 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("getNmaxPerType", [](NeighborList& n) { return n.Nmax; })
         .def("getRList", [](NeighborList& n) { return n.r_listsq; })
         .def("getPairList",
-             [](NeighborList& n, bool full) {
-                 std::vector<uint32_t> v = n.pair_list(full);
+             [](NeighborList& n, bool full, bool local) {
+                 std::vector<uint32_t> v = n.pair_list(full, local);
                  auto out = make_array<uint32_t>({v.size() / 2, 2});
                  std::copy(v.begin(), v.end(), out.mutable_data());
                  return out;
-             })
+             },
+             py::arg("full"), py::arg("local") = false)
         .def("getNNeigh",
              [](NeighborList& n) {
                  ParticleData& pd = *n.pdata;

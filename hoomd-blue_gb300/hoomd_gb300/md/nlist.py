@@ -121,6 +121,14 @@ class NeighborList:
         return self._cpp_obj.getPairList(bool(full))
 
     @property
+    def local_pair_list(self):
+        """Unordered pairs of the list as the engine's current particle indices, not tags
+        (hoomd/md/nlist.py local_pair_list)."""
+        if self._cpp_obj is None:
+            raise RuntimeError("the neighbour list has not been computed yet")
+        return self._cpp_obj.getPairList(False, True)
+
+    @property
     def shortest_rebuild(self):
         """Smallest number of timesteps between two builds since the last Simulation.run
         (NeighborList::getSmallestRebuild: capped at 99; 100 when fewer than two builds)."""

@@ -71,6 +71,10 @@ def test_true_pair_list():
     sim.run(0)
     got = set(frozenset(map(int, p)) for p in nlist.pair_list())
     assert got == truth
+    # nothing has reordered the particles, so the indices of local_pair_list are the tags
+    local = nlist.local_pair_list
+    assert len(local) == len(truth) and np.all(local[:, 0] < local[:, 1])
+    assert set(frozenset(map(int, p)) for p in local) == truth
 
 
 def harm_force_and_energy(dx, k, sigma, r_cut, shift=False):
