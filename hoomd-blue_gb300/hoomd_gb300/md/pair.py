@@ -155,7 +155,7 @@ class Pair:
         """Total energy of this force: the additional energy plus the per-particle energies
         summed in FP64 on the device (ForceCompute::calcEnergySum)."""
         self._require_run()
-        return self.additional_energy + self._cpp_obj.energySum()
+        return self._cpp_obj.tailEnergy() + self._cpp_obj.energySum()
 
 
 class LJ(Pair):
