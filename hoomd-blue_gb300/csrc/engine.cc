@@ -332,7 +332,10 @@ void NeighborList::allocate()
             rl = std::max(rl, r_listsq[t * nt + j]);
         rl = std::sqrt(rl);
         const double shell = (pd.ndim == 3) ? 4.0 / 3.0 * M_PI * rl * rl * rl : M_PI * rl * rl;
-        unsigned int want = (unsigned int)std::ceil(rho * shell * 1.35) + 8;
+        // several types: each type's rows take the largest count among fewer particles, and a
+        // rollback replays a whole chunk, so start those with more room
+        const double headroom = nt > 1 ? 1.5 : 1.35;
+        unsigned int want = (unsigned int)std::ceil(rho * shell * headroom) + 8;
         want = (want + 3) & ~3u;
         if (!capacity_fixed)
             Nmax[t] = std::max(Nmax[t], want);
