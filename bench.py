@@ -355,6 +355,15 @@ def run_gb300(args):
                 "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind ==
                 "measured" else "fallback 6.8 TB/s",
                 "kernel_ms": phases[2], "step_one_ms": phases[0], "rebuild_ms": phases[1]}
+    # the pair and neighbour-list kernels together over a step, the build amortised over the
+    # steps between builds of the timed run: N*(16 pos + 16 + 16 xyzf + 4 n_neigh + 16 last_pos)
+    # + 4*sum(n_neigh) bytes per build
+    per_build = builds / args.steps if builds else 0.0
+    bytes_nl = N * (16 + 16 + 16 + 4 + 16) + 4.0 * sum_n
+    t_pn = t_pair + per_build * phases[1] / 1e3
+    achieved_pn = (bytes_pair + per_build * bytes_nl) / t_pn / 1e9
+    roofline["pair_nlist"] = {"achieved": achieved_pn, "frac": achieved_pn / peak,
+                              "builds_per_step": per_build, "nlist_bytes_per_build": bytes_nl}
 
     line = {"metric": wl.metric, "value": tps * world, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
