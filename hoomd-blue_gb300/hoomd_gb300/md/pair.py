@@ -85,6 +85,16 @@ class Pair:
         self._cpp_obj.mode = _MODES[self._mode]
         types = state.particle_types
         self._cpp_obj.useCharge = bool(self._needs_charge(types))
+        self._send_params()
+        # parameters set after attaching reach the engine before the next step
+        for d in (self.params, self.r_cut, self.r_on):
+            if hasattr(d, "_on_change"):
+                d._on_change = self._typeparam_changed
+        return self._cpp_obj
+
+    def _send_params(self):
+        """Every type pair's parameters, r_cut and r_on to the engine object."""
+        types = self._simulation.state.particle_types
         for i, a in enumerate(types):
             for j, b in enumerate(types):
                 if j < i:
@@ -101,7 +111,17 @@ class Pair:
                 self._cpp_obj.setRCut(i, j, float(rc))
                 self._cpp_obj.setROn(i, j, float(self.r_on[(a, b)]))
         self._update_tail()
-        return self._cpp_obj
+
+    def _typeparam_changed(self, key):
+        if self._cpp_obj is None:
+            return
+        try:
+            self._send_params()
+            self._pending = False
+            # forces at the current positions are recomputed with the new values at the next run
+            self._simulation._state_changed()
+        except RuntimeError:
+            self._pending = True  # other pairs still unset: sent, or reported, at the next run
 
     def _detach(self):
         self._cpp_obj = None

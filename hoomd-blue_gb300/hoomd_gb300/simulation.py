@@ -178,6 +178,10 @@ class Simulation:
                     nl._ex_version != self._state._topology_version:
                 nl._apply_exclusions(self._state)
                 self._needs_prep = True
+        for f in list(integ.forces) + list(self.operations.computes):
+            if getattr(f, "_pending", False) and getattr(f, "_cpp_obj", None) is not None:
+                f._send_params()
+                f._pending = False
         if getattr(self, "_needs_prep", False):
             for f in integ.forces:
                 if getattr(f, "_cpp_obj", None) is not None and hasattr(f, "_update_tail"):

@@ -427,3 +427,32 @@ def test_shortest_rebuild():
     assert 1 <= shortest <= 600 / nb
     sim.run(0)
     assert cell.shortest_rebuild == 100  # restarted by the run
+
+
+def test_parameters_changed_between_runs():
+    """Pair parameters and r_cut set after the simulation started take effect at the next run
+    (the reference's TypeParameters write through to the attached C++ object)."""
+    snap = workloads.lj_fluid_sc(10, density=0.8, jitter=0.05, seed=4)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0)
+    sim.run(5)
+    e1 = lj.energy
+    lj.params[("A", "A")] = dict(epsilon=2.0, sigma=1.0)
+    sim.run(0)
+    assert lj.energy == pytest.approx(2 * e1, rel=1e-5)
+    lj.r_cut[("A", "A")] = 1.5
+    sim.run(0)
+    pos = sim.state.get_snapshot().particles.position.astype(np.float32).astype(np.float64)
+    L = snap.configuration.box[0]
+    N = len(pos)
+    tags = np.arange(N)
+    want = 0.0
+    for i in range(N):
+        d = pos[i] - pos[i + 1:]
+        d -= L * np.rint(d / L)
+        r = np.sqrt((d ** 2).sum(1))
+        r = r[r < 1.5]
+        want += (4 * 2.0 * (r ** -12 - r ** -6)).sum()
+    assert lj.energy == pytest.approx(want, rel=1e-5)
+    sim.run(10)  # the shorter list and the new parameters in the captured step
+    assert np.isfinite(lj.energy)
+    del tags
