@@ -73,16 +73,41 @@ class NeighborList:
         if int(rebuild_check_delay) != 1 or not bool(check_dist):
             raise NotImplementedError("only rebuild_check_delay=1 with check_dist=True (the "
                                       "reference's defaults) is implemented")
-        self.buffer = float(buffer)
-        if self.buffer < 0:
-            raise ValueError("buffer must be non-negative")
+        self._cpp_obj = None
+        self.buffer = buffer
         self.exclusions = exclusions
         self.rebuild_check_delay = int(rebuild_check_delay)
         self.check_dist = bool(check_dist)
         self.r_cut = TypePairDict(default=float(default_r_cut), validator=nonnegative_real)
-        self._cpp_obj = None
+        self.r_cut._on_change = self._r_cut_changed
         self._simulation = None
         self._ex_version = -1
+
+    @property
+    def buffer(self):
+        """Buffer width r_buff; a new value applies from the next run (the list is rebuilt)."""
+        return self._buffer
+
+    @buffer.setter
+    def buffer(self, value):
+        value = float(value)
+        if value < 0:
+            raise ValueError("buffer must be non-negative")
+        self._buffer = value
+        if self._cpp_obj is not None:
+            self._cpp_obj.r_buff = value
+            if self._simulation is not None:
+                self._simulation._state_changed()
+
+    def _r_cut_changed(self, key):
+        if self._cpp_obj is None:
+            return
+        types = self._simulation.state.particle_types
+        for i, a in enumerate(types):
+            for j, b in enumerate(types):
+                if j >= i:
+                    self._cpp_obj.setRCut(i, j, float(self.r_cut[(a, b)]))
+        self._simulation._state_changed()
 
     def _apply_exclusions(self, state):
         pairs = excluded_pairs(state._topology, self.exclusions, state.N_particles)

@@ -456,3 +456,22 @@ def test_parameters_changed_between_runs():
     sim.run(10)  # the shorter list and the new parameters in the captured step
     assert np.isfinite(lj.energy)
     del tags
+
+
+def test_buffer_changed_between_runs():
+    """A new nlist.Cell buffer applies from the next run: the list holds the neighbours within
+    the new r_cut + buffer, and the step keeps running."""
+    snap = workloads.lj_fluid_sc(10, density=0.8, jitter=0.05, seed=5)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0)
+    sim.run(5)
+    integ = sim._cpp_integrator
+    n0 = integ.sumNNeigh()
+    cell.buffer = 0.8
+    sim.run(0)
+    n1 = sim._cpp_integrator.sumNNeigh()
+    rho = snap.particles.N / snap.configuration.box[0] ** 3
+    expect = snap.particles.N * rho * 4 / 3 * np.pi * (2.5 + 0.8) ** 3
+    assert n1 > n0 and abs(n1 / expect - 1) < 0.05
+    e = lj.energy
+    sim.run(20)
+    assert np.isfinite(lj.energy) and abs(lj.energy - e) < 0.2 * abs(e)
