@@ -5,6 +5,34 @@ one neighbour list."""
 from hoomd_gb300._native import _hoomd_gb300
 
 
+class _SyncedList(list):
+    """A list whose changes detach the integrator, so the next run attaches the new contents
+    (the reference's SyncedList behaviour for ``forces`` and ``methods``)."""
+
+    def __init__(self, items, on_change):
+        super().__init__(items)
+        self._on_change = on_change
+
+    def _changed(self):
+        self._on_change()
+
+
+def _wrap(name):
+    base = getattr(list, name)
+
+    def method(self, *args, **kwargs):
+        out = base(self, *args, **kwargs)
+        self._changed()
+        return out
+    method.__name__ = name
+    return method
+
+
+for _name in ("append", "extend", "insert", "remove", "pop", "clear", "__setitem__",
+              "__delitem__", "__iadd__", "sort", "reverse"):
+    setattr(_SyncedList, _name, _wrap(_name))
+
+
 class Integrator:
     def __init__(self, dt, integrate_rotational_dof=False, forces=None, constraints=None,
                  methods=None, rigid=None, half_step_hook=None):
@@ -14,12 +42,34 @@ class Integrator:
             raise NotImplementedError("constraints, rigid bodies and half-step hooks are "
                                       "outside this path")
         self._dt = float(dt)
-        self.forces = list(forces or [])
-        self.methods = list(methods or [])
+        self._forces = _SyncedList(forces or [], self._contents_changed)
+        self._methods = _SyncedList(methods or [], self._contents_changed)
         self.integrate_rotational_dof = False
         self._simulation = None
         self._cpp_obj = None
         self._cpp_nlist = None
+
+    def _contents_changed(self):
+        if self._simulation is not None and self._cpp_obj is not None:
+            self._simulation._detach_all()
+
+    @property
+    def forces(self):
+        return self._forces
+
+    @forces.setter
+    def forces(self, items):
+        self._forces = _SyncedList(items, self._contents_changed)
+        self._contents_changed()
+
+    @property
+    def methods(self):
+        return self._methods
+
+    @methods.setter
+    def methods(self, items):
+        self._methods = _SyncedList(items, self._contents_changed)
+        self._contents_changed()
 
     @property
     def dt(self):

@@ -475,3 +475,22 @@ def test_buffer_changed_between_runs():
     e = lj.energy
     sim.run(20)
     assert np.isfinite(lj.energy) and abs(lj.energy - e) < 0.2 * abs(e)
+
+
+def test_forces_appended_after_a_run():
+    """Forces appended to (or removed from) integrator.forces after a run take part in the next
+    run, as the reference's synced lists do."""
+    snap = workloads.lj_fluid_sc(8, density=0.8, jitter=0.05, seed=6)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0)
+    sim.run(5)
+    pe1 = thermo.potential_energy
+    lj2 = md.pair.LJ(nlist=cell, default_r_cut=2.5)
+    lj2.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+    sim.operations.integrator.forces.append(lj2)
+    sim.run(0)
+    assert thermo.potential_energy == pytest.approx(2 * pe1, rel=1e-5)
+    sim.operations.integrator.forces.remove(lj2)
+    sim.run(0)
+    assert thermo.potential_energy == pytest.approx(pe1, rel=1e-5)
+    sim.run(10)
+    assert np.isfinite(thermo.potential_energy)
