@@ -17,9 +17,17 @@ timed steps. ``replicas_256``: 256 independent LJ systems (N ~ U[500, 20000], de
 U[0.7, 0.9], Bussi kT ~ U[0.8, 2.0], dt 0.005) advanced by one persistent launch per run, with the
 launch shape chosen by the ensemble's tuner during warm-up; reported in particle-timesteps/s.
 
+With no flags (the 1M-particle workload on one GPU) the line also carries, under "workloads",
+the JSON line of each other configuration (ka_262k, table32_524k, replicas_256,
+table32_mlp_524k), each run as its own process of this script with the same --steps/--warmup
+(``--no-secondary`` skips them).
+
 --impl reference times the CPU restatement of the reference's path (oracle/, FP64 Scalar, full
-neighbour list over all host threads) on a bounded sample of the same workload.
-Multi-GPU: the path is run as independent replicas, one per GPU (no collective on the data path).
+neighbour list over all host threads) on a bounded sample of the same workload, after the same
+warm-up sequence; its inputs come from the same numpy-only generators (synthetic_systems), and it
+loads neither torch nor this package's compiled code.
+Multi-GPU: the path is run as independent replicas, one per GPU (no collective on the data path);
+``--gpus N`` without a launcher relaunches itself under torch.distributed.run with N processes.
 """
 
 import argparse
@@ -100,7 +108,7 @@ class Workload:
 
 
 def workloads_registry(fcc_m=64):
-    from hoomd_gb300 import workloads as W
+    import synthetic_systems as W  # numpy only: both arms build their inputs from it
     N_fcc = 4 * fcc_m ** 3
     reg = {}
     reg["lj_fcc_1m"] = Workload(
@@ -228,8 +236,9 @@ def make_sim(wl, snap, seed=1):
     import hoomd_gb300 as hoomd
     from hoomd_gb300 import md
     c = wl.config
+    from hoomd_gb300.workloads import to_snapshot
     sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=seed)
-    sim.create_state_from_snapshot(snap)
+    sim.create_state_from_snapshot(to_snapshot(snap))
     sim.state.thermalize_particle_momenta(hoomd.filter.All(), c["kT"])
     cell = md.nlist.Cell(buffer=c["buffer"])
     force = wl.force(md, cell, snap)
@@ -252,7 +261,9 @@ def traffic_per_launch(wl):
     return None
 
 
-def oracle_sim(wl, snap, full, nthreads):
+def oracle_sim(wl, snap, full, nthreads, bussi=None):
+    """The oracle's whole-step runner on the workload's system, velocities thermalised at the
+    workload's kT; Bussi at that kT when ``bussi`` (default: the timed steps' thermostat)."""
     import numpy as np
     from oracle import oracle as O
     p = snap.particles
@@ -264,7 +275,8 @@ def oracle_sim(wl, snap, full, nthreads):
     vel4 = O.thermalize(vel4, np.arange(N), wl.config["kT"], 0, 1, prec=64)
     return O.Sim(pos4, vel4, np.zeros((N, 3), np.int32), np.arange(N), snap.configuration.box,
                  rc, wl.config["buffer"], wl.config["dt"], kind=kind, params=par, tdata=tdata,
-                 full=full, prec=64, nthreads=nthreads, bussi=wl.timed_thermostat,
+                 full=full, prec=64, nthreads=nthreads,
+                 bussi=wl.timed_thermostat if bussi is None else bussi,
                  kT=wl.config["kT"], seed=1)
 
 
@@ -294,6 +306,9 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     snap = wl.make_snap(1 + rank)
     N = snap.particles.N
+    # clocks sampled from before the warm-up to after the end-to-end run: at 200 ms a sample
+    # the timed region alone (a few ms at K = 20) may fall between two samples
+    clocks = ClockSampler(local) if rank == 0 else None
     sim, force, cell, method = make_sim(wl, snap, seed=1 + rank)
     sim.run(max(3, args.warmup))  # warm-up / equilibration (Bussi)
     if not wl.timed_thermostat:
@@ -308,7 +323,6 @@ def run_gb300(args):
     builds0 = cell.num_builds
     rollbacks0 = integ.n_rollbacks
 
-    clocks = ClockSampler(local) if rank == 0 else None
     barrier(world)
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -318,7 +332,6 @@ def run_gb300(args):
     torch.cuda.synchronize()
     barrier(world)
     ms = ev0.elapsed_time(ev1)
-    clk = clocks.stop() if clocks else None
     ms_max = max_over_ranks(ms, world)
     launches = integ.launch_count - launches0
     builds = cell.num_builds - builds0
@@ -341,6 +354,9 @@ def run_gb300(args):
            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
            "note": "host snapshot -> set_snapshot -> run(K) -> get_snapshot + energy, wall clock"}
     del out, e_pot
+    clk = clocks.stop() if clocks else None
+    if clk:
+        clk["window"] = "warm-up, timed region and end-to-end run"
 
     peak, peak_kind = peaks()
     t_pair = phases[2] / 1e3
@@ -369,13 +385,18 @@ def run_gb300(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic (seeded lattice, jittered, thermalised)",
-            "config": dict(wl.config, parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
+            "config": dict(wl.config),
+            "parallelism": f"independent replicas x{world}" if world > 1 else "1 GPU",
             "pair_evals_per_s": sum_n * tps * world, "nlist_builds": builds,
             "nlist_rollbacks": rollbacks,
             "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk}
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample(wl, snap, args.cpu_seconds)
+        if want_secondary(args, world):
+            del sim, force, cell, method
+            torch.cuda.empty_cache()
+            line["workloads"] = secondary_workloads(args, "gb300")
         print(json.dumps(line), flush=True)
 
 
@@ -405,9 +426,11 @@ def run_mlp(args):
     params = {(types[i], types[j]): dict(r_min=v["r_min"], U=v["U"], F=v["F"])
               for (i, j), v in tabs.items()}
 
+    from hoomd_gb300.workloads import to_snapshot
+
     def make(force_fn, snapshot, thermalize):
         sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=1 + rank)
-        sim.create_state_from_snapshot(snapshot)
+        sim.create_state_from_snapshot(to_snapshot(snapshot))
         if thermalize:
             sim.state.thermalize_particle_momenta(hoomd.filter.All(), c["kT"])
         cell = md.nlist.Cell(buffer=c["buffer"])
@@ -513,7 +536,7 @@ def run_mlp(args):
 
 
 def replica_systems(count=256):
-    from hoomd_gb300 import workloads as W
+    import synthetic_systems as W  # numpy only: both arms build their inputs from it
     return W.replica_systems(count=count, n_min=500, n_max=20000, seed=4)
 
 
@@ -531,9 +554,10 @@ def run_replicas(args):
     import torch
     import hoomd_gb300 as hoomd
     import numpy as np
+    from hoomd_gb300.workloads import to_snapshot
     rank, world, local = dist_init()
     torch.cuda.set_device(local)
-    systems = replica_systems(args.replicas)
+    systems = [(to_snapshot(h), kT, sd) for h, kT, sd in replica_systems(args.replicas)]
 
     def build():
         ens = hoomd.ReplicaEnsemble(dt=0.005, r_cut=2.5, buffer=0.4)
@@ -541,6 +565,7 @@ def run_replicas(args):
             ens.add_replica(snap, kT=kT, seed=seed + 1000 * rank)
         return ens
 
+    clocks = ClockSampler(local) if rank == 0 else None  # warm-up to end-to-end run
     ens = build()
     Ntot = ens.total_particles
     ens.run(0)
@@ -555,7 +580,6 @@ def run_replicas(args):
     builds0 = sum(ens.thermo(r)["n_builds"] for r in range(ens.count))
     launches0 = ens.launch_count
     cyc0 = np.asarray(ens._cpp.phaseClocks(), np.float64).reshape(-1, 4)
-    clocks = ClockSampler(local) if rank == 0 else None
     barrier(world)
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -565,17 +589,9 @@ def run_replicas(args):
     torch.cuda.synchronize()
     barrier(world)
     ms = max_over_ranks(ev0.elapsed_time(ev1), world)
-    clk = clocks.stop() if clocks else None
     builds = sum(ens.thermo(r)["n_builds"] for r in range(ens.count)) - builds0
     cyc = np.asarray(ens._cpp.phaseClocks(), np.float64).reshape(-1, 4) - cyc0
     big = int(np.argmax([ens.record(r)["N"] for r in range(ens.count)]))
-    mhz = (clk or {}).get("sm_mhz") or 2070.0
-    phase_names = ["step_one", "nlist_build", "pair_step", "bussi_draws"]
-    phase_split = {
-        "all_replicas_fraction": dict(zip(phase_names, (cyc.sum(0) / cyc.sum()).round(4).tolist())),
-        "largest_replica": {"N": ens.record(big)["N"], "us_per_step": dict(zip(
-            phase_names, (cyc[big] / mhz / args.steps).round(2).tolist()))},
-        "sm_cycles_total": float(cyc.sum()), "note": "clock64 at phase boundaries, thread 0"}
     launches = ens.launch_count - launches0
     value = Ntot * args.steps / (ms / 1e3) * world
 
@@ -589,6 +605,16 @@ def run_replicas(args):
     th = [e2.thermo(r) for r in range(e2.count)]
     t_e2e = time.perf_counter() - t0
     del out, th, e2
+    clk = clocks.stop() if clocks else None
+    if clk:
+        clk["window"] = "autotune, warm-up, timed region and end-to-end run"
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    phase_names = ["step_one", "nlist_build", "pair_step", "bussi_draws"]
+    phase_split = {
+        "all_replicas_fraction": dict(zip(phase_names, (cyc.sum(0) / cyc.sum()).round(4).tolist())),
+        "largest_replica": {"N": ens.record(big)["N"], "us_per_step": dict(zip(
+            phase_names, (cyc[big] / mhz / args.steps).round(2).tolist()))},
+        "sm_cycles_total": float(cyc.sum()), "note": "clock64 at phase boundaries, thread 0"}
     e2e = {"value": Ntot * args.steps / t_e2e, "unit": REPLICA_UNIT,
            "h2d_bytes_per_step": Ntot * (16 + 16 + 16) / args.steps,
            "d2h_bytes_per_step": (Ntot * (16 + 16 + 16 + 16) + 256 * 240) / args.steps,
@@ -613,9 +639,9 @@ def run_replicas(args):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
             "data": "synthetic (seeded sizes, densities, kT; jittered lattices, MB velocities)",
-            "config": dict(REPLICA_CONFIG, replicas=len(systems), total_particles=Ntot,
-                           launch_shape=ens.launch, tuned_from=len(tune),
-                           parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
+            "config": dict(REPLICA_CONFIG, replicas=len(systems)),
+            "total_particles": Ntot, "launch_shape": ens.launch, "tuned_from": len(tune),
+            "parallelism": f"independent replicas x{world}" if world > 1 else "1 GPU",
             "timesteps_per_s": args.steps / (ms / 1e3), "pair_evals_per_s":
             sum_n * args.steps / (ms / 1e3) * world, "nlist_builds": builds,
             "autotune_best": best, "phases": phase_split, "e2e": e2e, "roofline": roofline,
@@ -626,7 +652,7 @@ def run_replicas(args):
         print(json.dumps(line), flush=True)
 
 
-def replica_cpu_sample(systems, seconds, nthreads):
+def replica_cpu_sample(systems, seconds, nthreads, warm=1):
     """The oracle on a sample of the replicas, one after another (as separate reference runs
     would be): steps until about ``seconds`` have passed, in particle-timesteps/s."""
     import numpy as np
@@ -640,7 +666,7 @@ def replica_cpu_sample(systems, seconds, nthreads):
         sim = O.Sim(pos4, vel4, np.zeros((N, 3), np.int32), np.arange(N),
                     snap.configuration.box, [[2.5]], 0.4, 0.005, params=[[1.0, 1.0]],
                     full=nthreads > 1, prec=64, nthreads=nthreads, bussi=True, kT=kT, seed=seed)
-        sim.run(1)
+        sim.run(warm)
         t0 = time.perf_counter()
         sim.run(10)
         t_tot += time.perf_counter() - t0
@@ -651,9 +677,38 @@ def replica_cpu_sample(systems, seconds, nthreads):
             break
     return {"value": done / t_tot, "unit": REPLICA_UNIT, "cores": nthreads, "kind": "port",
             "sample": f"10 timesteps of each of {k} replicas (N = {names}) one after another, "
-                      f"after one untimed step; oracle FP64, "
+                      f"after {warm} untimed steps; oracle FP64, "
                       + ("half list, single thread" if nthreads == 1 else
                          f"full list, {nthreads} OpenMP threads")}
+
+
+SECONDARY = ("ka_262k", "table32_524k", "replicas_256", "table32_mlp_524k")
+
+
+def want_secondary(args, world):
+    return (world == 1 and not args.no_secondary and args.workload == "lj_fcc_1m"
+            and args.fcc_m == 64)
+
+
+def secondary_workloads(args, impl):
+    """The other benchmark configurations, each as its own process of this script (fresh device
+    state) with the same --steps/--warmup; their JSON lines are kept under the headline line's
+    "workloads" key. The surrogate has no counterpart in the reference's CPU path."""
+    out = {}
+    for w in SECONDARY:
+        if impl == "reference" and w == "table32_mlp_524k":
+            continue
+        cmd = [sys.executable, str(REPO / "bench.py"), "--impl", impl, "--workload", w,
+               "--steps", str(args.steps), "--warmup", str(args.warmup),
+               "--cpu-seconds", str(args.secondary_cpu_seconds), "--no-secondary"]
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=1500)
+            lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+            out[w] = json.loads(lines[-1]) if r.returncode == 0 and lines else {
+                "error": f"rc={r.returncode}", "tail": (r.stdout + r.stderr)[-600:]}
+        except subprocess.TimeoutExpired:
+            out[w] = {"error": "timed out after 1500 s"}
+    return out
 
 
 def run_reference(args):
@@ -663,12 +718,13 @@ def run_reference(args):
         return
     if args.workload == "replicas_256":
         cores = os.cpu_count() or 1
-        cb = replica_cpu_sample(replica_systems(), args.cpu_seconds * 3, cores)
+        warm = max(3, args.warmup)
+        cb = replica_cpu_sample(replica_systems(), args.cpu_seconds * 3, cores, warm=warm)
         v = cb["value"]
         print(json.dumps({
             "metric": "LJ replica ensemble particle-timesteps/s (256 replicas, N 500-20000)",
             "value": v, "unit": REPLICA_UNIT, "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "warmup": warm, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
             "data": "synthetic (seeded sizes, densities, kT; jittered lattices, MB velocities)",
             "config": REPLICA_CONFIG, "impl": "reference", "cpu_baseline": cb,
@@ -678,9 +734,14 @@ def run_reference(args):
     wl = workloads_registry(args.fcc_m)[args.workload]
     cores = os.cpu_count() or 1
     snap = wl.make_snap(1)
-    sim = oracle_sim(wl, snap, full=True, nthreads=cores)
-    warm = max(1, min(args.warmup, 3))
-    sim.run(warm)  # includes the first neighbour-list build
+    # the same sequence as the GPU arm: W Bussi warm-up steps from the thermalised lattice, then
+    # (for the 1M-particle NVE workload) the thermostat removed and 3 settling steps
+    sim = oracle_sim(wl, snap, full=True, nthreads=cores, bussi=True)
+    warm = max(3, args.warmup)
+    sim.run(warm)
+    if not wl.timed_thermostat:
+        sim.set_thermostat(None)
+    sim.run(3)
     t0 = time.perf_counter()
     sim.run(1)
     per = time.perf_counter() - t0
@@ -689,7 +750,7 @@ def run_reference(args):
     sim.run(n)
     dt = time.perf_counter() - t0
     v = n / dt
-    print(json.dumps({
+    line = {
         "metric": wl.metric, "value": v, "unit": UNIT, "n_gpus": 0, "steps": n, "warmup": warm,
         "ms_per_step": 1e3 * dt / n, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp64",
@@ -698,9 +759,13 @@ def run_reference(args):
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{n} of the {args.steps} requested timesteps (bounded to a "
                                    f"few minutes) of the {snap.particles.N}-particle {wl.name} "
-                                   f"system; oracle FP64, full list, {cores} OpenMP threads"},
-        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
-        flush=True)
+                                   f"system after {warm} + 3 untimed steps; oracle FP64, full "
+                                   f"list, {cores} OpenMP threads"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    del sim
+    if want_secondary(args, int(os.environ.get("WORLD_SIZE", "1"))):
+        line["workloads"] = secondary_workloads(args, "reference")
+    print(json.dumps(line), flush=True)
 
 
 def run_drift(args):
@@ -766,6 +831,11 @@ def main():
                     help="activations as one bfloat16 (0) or the sum of two (1)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="lj_fcc_1m at one GPU: skip the other workloads' lines (by default each "
+                         "runs as its own process and is reported under \"workloads\")")
+    ap.add_argument("--secondary-cpu-seconds", type=float, default=5.0,
+                    help="CPU-baseline sample length of each secondary workload")
     ap.add_argument("--fcc-m", type=int, default=64,
                     help="FCC cells per side of lj_fcc_1m (64 = the 1,048,576-particle workload; "
                          "smaller values are for profiling captures only)")
@@ -779,6 +849,19 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch this command under torch.distributed.run
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+               f"--nproc-per-node={args.gpus}", "--master-addr", "127.0.0.1",
+               "--master-port", str(port), str(pathlib.Path(__file__).resolve()), *sys.argv[1:]]
+        sys.exit(subprocess.call(cmd))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world != args.gpus:
+        sys.exit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}")
     if args.nve_drift:
         run_drift(args)
     elif args.impl == "reference":

@@ -588,17 +588,19 @@ void nlist_binned(unsigned int N,
                         {
                         if (cur_n_neigh < Nmax_i)
                             nlist[head_i + cur_n_neigh] = j;
-                        else
-                            {
-#ifdef _OPENMP
-#pragma omp critical(orc_nlist_cond)
-#endif
-                            conditions[type_i] = std::max(conditions[type_i], cur_n_neigh + 1);
-                            }
                         cur_n_neigh++;
                         }
                     }
                 }
+            }
+        // overflow: the per-type condition is the largest count seen (one update per particle
+        // instead of one per overflowing neighbour; the result is the same)
+        if (cur_n_neigh > Nmax_i)
+            {
+#ifdef _OPENMP
+#pragma omp critical(orc_nlist_cond)
+#endif
+            conditions[type_i] = std::max(conditions[type_i], cur_n_neigh);
             }
         n_neigh[i] = cur_n_neigh;
         }
@@ -1582,13 +1584,13 @@ using namespace orc;
         const unsigned int* cell_size, const R* xyzf, unsigned int Nmax_cell,                      \
         const unsigned int* adj, unsigned int adj_w, const unsigned int* Nmax,                     \
         const uint64_t* head_list, unsigned int* nlist, unsigned int* n_neigh,                     \
-        unsigned int* conditions, int rint_min_image)                                              \
+        unsigned int* conditions, int rint_min_image, int nthreads)                                \
         {                                                                                          \
         Box<R> box;                                                                                \
         box.set(b6, per);                                                                          \
         nlist_binned<R>(N, pos, box, ntypes, r_cut, r_listsq, full != 0, dim3, cell_size, xyzf,    \
                         Nmax_cell, adj, adj_w, Nmax, head_list, nlist, n_neigh, conditions,        \
-                        rint_min_image != 0);                                                      \
+                        rint_min_image != 0, nthreads);                                            \
         }                                                                                          \
     ORC_EXPORT void orc_lj_eval_##SUF(int n, const double* rsq, double rcutsq, double sigma,       \
                                       double eps, int shift, R* fdivr, R* eng, int* evaluated)     \

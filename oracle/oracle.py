@@ -199,9 +199,11 @@ def rlist_matrices(r_cut, r_buff, prec):
 
 
 def build_nlist(pos4, box, r_cut, r_buff, full=True, ndim=3, prec=32, periodic=(1, 1, 1),
-                rint_min_image=True):
+                rint_min_image=True, nthreads=1):
     """One neighbour-list build with the overflow retry loops of hoomd/CellList.cc:133-200 and
-    hoomd/md/NeighborList.cc:412-427. Returns (n_neigh, nlist, head_list, extra-info dict)."""
+    hoomd/md/NeighborList.cc:412-427. Returns (n_neigh, nlist, head_list, extra-info dict).
+    ``nthreads`` OpenMP threads each build whole particle lists (the result does not depend on
+    the thread count)."""
     R = rdtype(prec)
     pos4 = np.ascontiguousarray(pos4, R)
     N = len(pos4)
@@ -237,7 +239,7 @@ def build_nlist(pos4, box, r_cut, r_buff, full=True, ndim=3, prec=32, periodic=(
         getattr(lib(), f"orc_nlist_binned_{suf(prec)}")(
             N, ptr(pos4), ptr(b), ptr(p), ntypes, ptr(rc), ptr(rlsq), int(full), ptr(dim),
             ptr(cell_size), ptr(xyzf), Nmax_cell, ptr(adj), adj.shape[1], ptr(Nmax), ptr(head),
-            ptr(nlist), ptr(n_neigh), ptr(conditions), int(rint_min_image))
+            ptr(nlist), ptr(n_neigh), ptr(conditions), int(rint_min_image), int(nthreads))
         over = conditions > Nmax
         if not over.any():
             break
@@ -497,6 +499,13 @@ class Sim:
             g = np.ascontiguousarray(langevin, np.float64)
             self._keep.append(g)
             getattr(L, f"orc_sim_set_langevin_{self._s}")(self.h, d(kT), ptr(g))
+
+    def set_thermostat(self, thermostat, kT=1.0, tau=0.0):
+        """Replace the ConstantVolume thermostat: None (NVE), "bussi", "berendsen" or "mttk"."""
+        kind = {None: 0, "bussi": 1, "berendsen": 2, "mttk": 3}[thermostat]
+        getattr(lib(), f"orc_sim_set_thermostat_{self._s}")(
+            self.h, ctypes.c_int(kind), ctypes.c_double(kT), ctypes.c_double(tau),
+            ctypes.c_double(0.0), ctypes.c_double(0.0))
 
     @property
     def mttk_state(self):

@@ -125,6 +125,17 @@ class GpuNlist:
                             Nmax).astype(np.uint32)
         self.Nmax = Nmax
 
+    def word_index(self):
+        """index(i, k) -> word offset of particle i's k-th neighbour in this list's layout."""
+        if self.head is None and self.interleave == 4:
+            st = self.stride
+            return lambda i, k: ((k >> 2) * st + i) * 4 + (k & 3)
+        if self.head is None:
+            st = self.stride
+            return lambda i, k: i + k * st
+        hd = host(self.head).astype(np.int64)
+        return lambda i, k: hd[i] + k
+
     def sets(self):
         nn = host(self.n_neigh).astype(np.int64)
         nl = host(self.nlist).astype(np.int64)
@@ -149,6 +160,57 @@ class GpuNlist:
                          shift_mode=shift, compute_virial=int(virial is not None),
                          threads_per_particle=tpp)
         return a
+
+
+RTOL = 1e-5  # relative tolerance of FP32 forces, energies, virials vs the FP64 oracle
+
+
+def assert_close_f64(got, ref, rtol=RTOL, what=""):
+    """|got - ref| <= rtol |ref| + rtol max|ref| elementwise (a relative bar with an absolute
+    floor scaled to the largest reference value)."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    floor = rtol * max(np.abs(ref).max(), 1e-30)
+    err = np.abs(got - ref)
+    bad = err > rtol * np.abs(ref) + floor
+    assert not bad.any(), (f"{what}: {bad.sum()} of {bad.size} outside tolerance; worst "
+                           f"{err.max():.3e} (ref scale {np.abs(ref).max():.3e})")
+
+
+PAD = np.uint32(0xFFFFFFFF)
+
+
+def padded_sorted_rows(n_neigh, nlist, index, lo, hi):
+    """Rows lo..hi-1 of a neighbour list as a (hi-lo, max n) array of sorted indices padded with
+    0xFFFFFFFF. ``index(i, k)`` maps particle and slot arrays to word offsets in ``nlist``."""
+    nn = np.asarray(n_neigh[lo:hi], np.int64)
+    K = int(nn.max()) if len(nn) else 0
+    i = np.arange(lo, hi, dtype=np.int64)[:, None]
+    k = np.arange(K, dtype=np.int64)[None, :]
+    valid = k < nn[:, None]
+    idx = np.where(valid, index(i, k), 0)
+    rows = np.where(valid, nlist[idx], PAD).astype(np.uint32)
+    rows.sort(axis=1)
+    return rows
+
+
+def compare_neighbor_sets(nn_a, nl_a, index_a, nn_b, nl_b, index_b, chunk=65536):
+    """Indices of the particles whose neighbour sets differ between two lists (vectorised over
+    chunks of particles, so a million-particle list compares in seconds)."""
+    nn_a = np.asarray(nn_a)
+    nn_b = np.asarray(nn_b)
+    bad = [np.nonzero(nn_a != nn_b)[0]]
+    N = len(nn_a)
+    for lo in range(0, N, chunk):
+        hi = min(N, lo + chunk)
+        ra = padded_sorted_rows(nn_a, nl_a, index_a, lo, hi)
+        rb = padded_sorted_rows(nn_b, nl_b, index_b, lo, hi)
+        if ra.shape != rb.shape:
+            w = max(ra.shape[1], rb.shape[1])
+            ra = np.pad(ra, ((0, 0), (0, w - ra.shape[1])), constant_values=PAD)
+            rb = np.pad(rb, ((0, 0), (0, w - rb.shape[1])), constant_values=PAD)
+        bad.append(lo + np.nonzero((ra != rb).any(axis=1))[0])
+    return np.unique(np.concatenate(bad))
 
 
 def lj_params_dev(par):

@@ -53,8 +53,8 @@ def test_force_energy_accuracy(pot):
             e = f.energies
             forces = f.forces
             ref_e = fe["energies"][i][k]
-            assert np.isclose(e.sum(), ref_e, rtol=2e-5, atol=1e-6 if ref_e == 0 else 0)
-            assert np.allclose(forces[0], np.array([0, 0, 1.0]) * fe["forces"][i][k], rtol=2e-5,
+            assert np.isclose(e.sum(), ref_e, rtol=1e-5, atol=1e-6 if ref_e == 0 else 0)
+            assert np.allclose(forces[0], np.array([0, 0, 1.0]) * fe["forces"][i][k], rtol=1e-5,
                                atol=1e-5)
 
 

@@ -1,0 +1,144 @@
+"""Parity at the benchmark configurations' own sizes.
+
+Each system is built from the same seeds as the benchmark:
+
+* the 1,048,576-particle LJ fluid (64^3 FCC, density 0.84, r_cut 2.5, buffer 0.4);
+* the 262,144-particle Kob-Andersen mixture (80:20, density 1.2, r_cut 2.5 sigma_ij, buffer 0.3);
+* the 524,288-particle 32-type system with 528 tabulated potentials (density 0.8, r_cut 3.0,
+  buffer 0.4).
+
+For each, the GPU neighbour list (cell list + lane-per-particle build through the C ABI, the
+layout the engine runs) must equal the FP32 oracle's full list as per-particle sorted sets, bit
+for bit, and one evaluation of the pair forces, per-particle energies and virials over that list
+must lie within 1e-5 relative of the FP64 oracle (absolute floor 1e-5 x the largest value). This
+follows the reference's CPU-vs-GPU list comparison (hoomd/md/test/test_neighborlist.cc:1060-1148)
+and its force/energy accuracy test (hoomd/md/pytest/test_potential.py:952-1058), at full size.
+The oracle runs on every host core (OpenMP); the comparisons are vectorised over particle chunks.
+
+The 1M-particle fluid is also checked after 200 steps of the product's own run (Bussi at
+kT 1.5, Hilbert sort every 100 steps): the engine's forces, energies and virials through the
+Python API against the FP64 oracle at the resulting positions.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+import synthetic_systems as S  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from gpu_util import (GpuNlist, assert_close_f64, compare_neighbor_sets,  # noqa: E402
+                      gpu_pair_forces, table_params)
+
+CORES = os.cpu_count() or 1
+
+
+def _pos4(system):
+    p = system.particles
+    return O.make_pos4(p.position, p.typeid, 32), tuple(system.configuration.box)
+
+
+def _lj_case(system, pairs):
+    """pairs: {(i, j): (epsilon, sigma, r_cut)} -> (r_cut matrix, oracle/ABI params)."""
+    nt = len(system.particles.types)
+    rc = np.zeros((nt, nt))
+    par = np.zeros((nt * nt, 2))
+    for (i, j), (eps, sig, r) in pairs.items():
+        for a, b in ((i, j), (j, i)):
+            rc[a, b] = r
+            par[a * nt + b] = (sig, eps)
+    return rc, par
+
+
+def _systems():
+    fcc = S.lj_fluid_fcc(m=64, density=0.84, jitter=0.05, seed=1)
+    ka = S.binary_mixture(N=262144, density=1.2, seed=1)
+    t32 = S.multitype_system(N=524288, ntypes=32, density=0.8, seed=1)
+    return {
+        "lj_fcc_1m": (fcc, "lj", _lj_case(fcc, {(0, 0): (1.0, 1.0, 2.5)}), 0.4),
+        "ka_262k": (ka, "lj", _lj_case(ka, {(0, 0): (1.0, 1.0, 2.5), (0, 1): (1.5, 0.8, 2.0),
+                                            (1, 1): (0.5, 0.88, 2.2)}), 0.3),
+        "table32_524k": (t32, "table", None, 0.4),
+    }
+
+
+@pytest.fixture(scope="module")
+def systems():
+    return _systems()
+
+
+@pytest.mark.parametrize("case", ["lj_fcc_1m", "ka_262k", "table32_524k"])
+def test_fullsize_nlist_and_forces_vs_oracle(systems, case):
+    system, kind, lj, r_buff = systems[case]
+    pos4, box6 = _pos4(system)
+    N = len(pos4)
+    nt = len(system.particles.types)
+    if kind == "lj":
+        rc, par = lj
+        tables = opar = odata = None
+    else:
+        tabs = S.mixture_tables(32, r_min=0.8, r_cut=3.0, width=1000, seed=2)
+        recs, data, opar, odata = table_params(
+            nt, {k: (v["r_min"], v["U"], v["F"]) for k, v in tabs.items()})
+        tables = (recs, data)
+        rc = np.full((nt, nt), 3.0)
+        par = None
+
+    # neighbour sets: GPU (interleaved column-major list, lane-per-particle build) vs FP32 oracle
+    nl = GpuNlist(pos4, box6, rc, r_buff, layout="col4")
+    n_o, l_o, h_o, info = O.build_nlist(pos4, box6, rc, r_buff, full=True, prec=32,
+                                        nthreads=CORES)
+    assert nl.dim == info["dim"].tolist()
+    nn_g = nl.n_neigh.cpu().numpy().view(np.uint32)
+    nl_g = nl.nlist.cpu().numpy().view(np.uint32)
+    ho = h_o.astype(np.int64)
+    bad = compare_neighbor_sets(nn_g, nl_g, nl.word_index(), n_o, l_o, lambda i, k: ho[i] + k)
+    assert len(bad) == 0, f"{case}: {len(bad)} of {N} particles' sets differ, first {bad[:5]}"
+    sum_n = int(n_o.astype(np.int64).sum())
+    assert sum_n > 50 * N  # a dense liquid: tens of neighbours each
+    del l_o, h_o, ho
+
+    # one force evaluation over the GPU list vs the FP64 oracle (own FP64 list at r_cut + buffer)
+    f, v = gpu_pair_forces(nl, kind, par, rc, virial=True, tables=tables)
+    pos64 = pos4.astype(np.float64)
+    pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
+    n6, l6, h6, _ = O.build_nlist(pos64, box6, rc, r_buff, full=True, prec=64, nthreads=CORES)
+    fo, vo = O.pair_forces(kind, pos64, box6, opar if kind == "table" else par, rc ** 2, n6, l6,
+                           h6, third_law=False, compute_virial=True, tdata=odata, prec=64,
+                           nthreads=CORES)
+    assert_close_f64(f[:, :3], fo[:, :3], what=f"{case} force")
+    assert_close_f64(f[:, 3], fo[:, 3], what=f"{case} energy")
+    assert_close_f64(v, vo, what=f"{case} virial")
+
+
+def test_fullsize_fcc_after_run_vs_oracle():
+    import hoomd_gb300 as hoomd
+    from hoomd_gb300 import md
+    from hoomd_gb300.workloads import to_snapshot
+
+    system = S.lj_fluid_fcc(m=64, density=0.84, jitter=0.05, seed=1)
+    sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=1)
+    sim.create_state_from_snapshot(to_snapshot(system))
+    sim.state.thermalize_particle_momenta(hoomd.filter.All(), 1.5)
+    cell = md.nlist.Cell(buffer=0.4)
+    lj = md.pair.LJ(nlist=cell, default_r_cut=2.5)
+    lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+    sim.operations.integrator = md.Integrator(dt=0.005, forces=[lj], methods=[
+        md.methods.ConstantVolume(hoomd.filter.All(), md.methods.thermostats.Bussi(kT=1.5))])
+    sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=100))
+    sim.run(200)
+    F, E, W = lj.forces, lj.energies, lj.virials
+    snap = sim.state.get_snapshot()
+    box6 = tuple(snap.configuration.box)
+    pos4 = O.make_pos4(snap.particles.position, snap.particles.typeid, 64)
+    n6, l6, h6, _ = O.build_nlist(pos4, box6, [[2.5]], 0.4, full=True, prec=64, nthreads=CORES)
+    fo, vo = O.pair_forces("lj", pos4, box6, [[1.0, 1.0]], [[6.25]], n6, l6, h6, third_law=False,
+                           compute_virial=True, prec=64, nthreads=CORES)
+    assert cell.num_builds >= 2
+    assert_close_f64(F, fo[:, :3], what="force after 200 steps")
+    assert_close_f64(E, fo[:, 3], what="energy after 200 steps")
+    assert_close_f64(W, vo.T, what="virial after 200 steps")

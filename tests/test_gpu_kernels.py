@@ -24,17 +24,7 @@ from gpu_util import (GpuNlist, dev, gpu_pair_forces, host, lj_params_dev, p, st
                       table_params, zeros)
 
 GOLD = pathlib.Path(__file__).resolve().parent / "golden"
-RTOL = 1e-5  # relative tolerance of FP32 forces, energies, virials vs the FP64 oracle
-
-
-def assert_close_f64(got, ref, rtol=RTOL, what=""):
-    got = np.asarray(got, np.float64)
-    ref = np.asarray(ref, np.float64)
-    floor = rtol * max(np.abs(ref).max(), 1e-30)
-    err = np.abs(got - ref)
-    bad = err > rtol * np.abs(ref) + floor
-    assert not bad.any(), (f"{what}: {bad.sum()} of {bad.size} outside tolerance; worst "
-                           f"{err.max():.3e} (ref scale {np.abs(ref).max():.3e})")
+from gpu_util import RTOL, assert_close_f64  # noqa: E402,F401
 
 
 def random_system(N, L, ntypes=1, seed=0, tilts=(0, 0, 0), lattice=False):
@@ -216,8 +206,8 @@ def test_forces_and_energies_golden_through_abi(kind):
                 f, _ = gpu_pair_forces(nl, "table", None, [[2.5]], tables=(recs, data))
             e = float(f[:, 3].astype(np.float64).sum())
             ref_e = fe["energies"][i][k]
-            assert np.isclose(e, ref_e, rtol=2e-5, atol=1e-6 if ref_e == 0 else 0), (i, d, e)
-            assert np.allclose(f[0, :3], np.array([0, 0, 1.0]) * fe["forces"][i][k], rtol=2e-5,
+            assert np.isclose(e, ref_e, rtol=1e-5, atol=1e-6 if ref_e == 0 else 0), (i, d, e)
+            assert np.allclose(f[0, :3], np.array([0, 0, 1.0]) * fe["forces"][i][k], rtol=1e-5,
                                atol=1e-5)
 
 
