@@ -863,35 +863,49 @@ double PairForce::energy_between_sets(const std::vector<uint32_t>& tags1,
     upload();
     nlist->ensure_consumer(&r_cut);
     nlist->build_sync();
+    if (tags1.empty() || tags2.empty())
+        return 0.0;
     const std::vector<uint32_t> rt = pd.rtag();
-    std::vector<uint8_t> set(pd.N, 0);
-    for (int which = 1; which <= 2; which++)
-        for (uint32_t t : (which == 1 ? tags1 : tags2))
+    // occurrences of each particle index's tag in the two sets (the reference's double loop
+    // over the tag lists counts duplicates and overlaps)
+    std::vector<uint32_t> mult((size_t)2 * pd.N, 0u);
+    for (int which = 0; which < 2; which++)
+        for (uint32_t t : (which == 0 ? tags1 : tags2))
             {
             if (t >= pd.N)
                 throw std::invalid_argument("compute_energy: tag out of range");
-            set[rt[t]] = (uint8_t)which;
+            mult[(size_t)which * pd.N + rt[t]]++;
             }
-    DeviceArray<uint8_t> d_set;
-    d_set.resize(std::max(1u, pd.N));
-    d_set.upload(set.data(), pd.N, s);
+    DeviceArray<uint32_t> d_mult;
+    d_mult.resize(std::max<size_t>(2, mult.size()));
+    d_mult.upload(mult.data(), mult.size(), s);
+    nlist->refresh_exclusions();
+    gb_energy_sets sets{};
+    sets.d_mult1 = d_mult.get();
+    sets.d_mult2 = d_mult.get() + pd.N;
+    if (nlist->ex_pitch > 0)
+        {
+        sets.d_n_ex = nlist->n_ex.get();
+        sets.d_ex_list = nlist->ex_list.get();
+        sets.ex_pitch = nlist->ex_pitch;
+        }
     const unsigned int nb = gb_pair_energy_sets_blocks(pd.N);
     DeviceArray<double> parts;
     parts.resize(nb);
     gb_pair_args a = pair_args(false);
     int rc;
     if (kind == PairKind::LJ)
-        rc = gb_pair_energy_sets_lj(&a, (const gb_lj_param*)d_params.get(), d_set.get(),
-                                    parts.get(), s);
+        rc = gb_pair_energy_sets_lj(&a, (const gb_lj_param*)d_params.get(), &sets, parts.get(),
+                                    s);
     else if (kind == PairKind::Example)
-        rc = gb_pair_energy_sets_example(&a, (const gb_example_param*)d_params.get(), d_set.get(),
+        rc = gb_pair_energy_sets_example(&a, (const gb_example_param*)d_params.get(), &sets,
                                          parts.get(), s);
     else if (kind == PairKind::Radial)
-        rc = gb_pair_energy_sets_radial(&a, (const gb_radial_param*)d_params.get(), d_set.get(),
+        rc = gb_pair_energy_sets_radial(&a, (const gb_radial_param*)d_params.get(), &sets,
                                         parts.get(), s);
     else
         rc = gb_pair_energy_sets_table(&a, (const gb_table_param*)d_params.get(), d_table.get(),
-                                       d_set.get(), parts.get(), s);
+                                       &sets, parts.get(), s);
     check(rc, "energy between sets");
     std::vector<double> h(nb);
     parts.download(h.data(), nb, s);

@@ -864,12 +864,45 @@ int launch_pair(const gb_pair_args* a, const typename Eval::param_type* d_params
 
 namespace gb
 {
-// PotentialPair::computeEnergyBetweenSets (hoomd/md/PotentialPair.h, exported as
-// computeEnergyBetweenSets; hoomd/md/pair/pair.py compute_energy): U = sum over i in set 1 and
-// j in set 2 of V_ij(r), with the force's shift / XPLOR mode. d_set[i] is 1 or 2 for the two
-// sets (0 otherwise); every unordered pair appears once, from its set-1 particle's row of the
-// full list. Each block writes its partial sum to d_partials[blockIdx.x]; the caller adds them in
-// order.
+// PotentialPair::computeEnergyBetweenSets (hoomd/md/PotentialPair.h:833-990, exported as
+// computeEnergyBetweenSets; hoomd/md/pair/pair.py compute_energy): the reference loops over every
+// tag of set 1 and every tag of set 2 (duplicates and tags in both sets included, no exclusions
+// applied) and adds V_ij(r) with the force's shift / XPLOR mode. Here d_mult1[i] / d_mult2[i]
+// count how often particle index i's tag appears in each set, and the sum is
+//   sum_i m1[i] * ( sum_{j in list(i) + excluded(i)} m2[j] V_ij + m2[i] V_ii(r = 0) ):
+// the full list holds every ordered pair within r_list except the excluded ones, which are added
+// back from the exclusion rows (each distinct partner once); pairs beyond r_cut contribute
+// nothing. The i == j term is the evaluator at zero distance, as the reference evaluates it when
+// a tag is in both sets. Each block writes its partial sum to d_partials[blockIdx.x]; the caller
+// adds them in order.
+template<class Eval, bool XPLOR>
+__device__ __forceinline__ double sets_pair_energy(float rsq, unsigned int tp,
+                                                   const typename Eval::param_type* d_params,
+                                                   const float* d_rcutsq, const float* d_ronsq,
+                                                   const float* ext, float qi, float qj,
+                                                   bool SHIFT1)
+    {
+    typename Eval::param_type param = d_params[tp];
+    const float rcutsq = d_rcutsq[tp];
+    Eval::prepare_param(param, rcutsq);
+    const float ronsq = XPLOR ? d_ronsq[tp] : 0.0f;
+    float force_divr = 0.0f, pair_eng = 0.0f;
+    Eval eval(rsq, rcutsq, param, ext);
+    if (Eval::needsCharge())
+        eval.setCharge(qi, qj);
+    if (!eval.evalForceAndEnergy(force_divr, pair_eng, XPLOR ? (ronsq > rcutsq) : SHIFT1))
+        return 0.0;
+    if (XPLOR && rsq >= ronsq && rsq < rcutsq)
+        {
+        // smoothing factor S(r) = (rc^2 - r^2)^2 (rc^2 + 2 r^2 - 3 ron^2) / (rc^2 - ron^2)^3
+        const float width = rcutsq - ronsq;
+        const float below_cut = rcutsq - rsq;
+        pair_eng *= below_cut * below_cut * (rcutsq + 2.0f * rsq - 3.0f * ronsq)
+                    / (width * width * width);
+        }
+    return (double)pair_eng;
+    }
+
 template<class Eval, bool MULTI, bool XPLOR>
 __global__ void __launch_bounds__(256)
     k_energy_sets(unsigned int N, const float4* __restrict__ d_pos, gb_box box,
@@ -879,52 +912,67 @@ __global__ void __launch_bounds__(256)
                   const float* __restrict__ d_rcutsq, const float* __restrict__ d_ronsq,
                   unsigned int ntypes, const float* __restrict__ ext,
                   const float* __restrict__ d_charge, bool SHIFT1,
-                  const uint8_t* __restrict__ d_set, double* __restrict__ d_partials)
+                  const uint32_t* __restrict__ d_mult1, const uint32_t* __restrict__ d_mult2,
+                  const unsigned int* __restrict__ d_n_ex, const unsigned int* __restrict__ d_ex_list,
+                  unsigned int ex_pitch, double* __restrict__ d_partials)
     {
-    using P = typename Eval::param_type;
     const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
     double u = 0.0;
-    if (i < N && d_set[i] == 1)
+    const uint32_t m1 = i < N ? d_mult1[i] : 0u;
+    if (m1)
         {
         const float4 pi = d_pos[i];
         const unsigned int ti = __float_as_uint(pi.w);
-        const unsigned int nn = d_n_neigh[i];
         const float qi = Eval::needsCharge() ? d_charge[i] : 0.0f;
-        for (unsigned int k = 0; k < nn; k++)
+        const unsigned int nn = d_n_neigh[i];
+        const unsigned int nex = d_n_ex ? d_n_ex[i] : 0u;
+        double ui = 0.0;
+        for (unsigned int k = 0; k < nn + nex; k++)
             {
-            size_t w;
-            if (d_head_list)
-                w = d_head_list[i] + k;
-            else if (interleave == 4)
-                w = (((size_t)(k >> 2) * stride + i) << 2) + (k & 3u);
+            unsigned int j;
+            if (k < nn)
+                {
+                size_t w;
+                if (d_head_list)
+                    w = d_head_list[i] + k;
+                else if (interleave == 4)
+                    w = (((size_t)(k >> 2) * stride + i) << 2) + (k & 3u);
+                else
+                    w = (size_t)k * stride + i;
+                j = d_nlist[w];
+                }
             else
-                w = (size_t)k * stride + i;
-            const unsigned int j = d_nlist[w];
-            if (d_set[j] != 2)
+                {
+                // an excluded partner (filtered out of the list): count each distinct one once
+                const unsigned int* row = d_ex_list + (size_t)i * ex_pitch;
+                const unsigned int e = k - nn;
+                j = row[e];
+                bool seen = (j == i);
+                for (unsigned int e2 = 0; e2 < e && !seen; e2++)
+                    seen = row[e2] == j;
+                if (seen)
+                    continue;
+                }
+            const uint32_t m2 = d_mult2[j];
+            if (!m2)
                 continue;
             const float4 pj = d_pos[j];
             float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             min_image(box, dx, dy, dz);
             const float rsq = dx * dx + dy * dy + dz * dz;
             const unsigned int tp = MULTI ? ti * ntypes + __float_as_uint(pj.w) : 0u;
-            P param = d_params[tp];
-            const float rcutsq = d_rcutsq[tp];
-            Eval::prepare_param(param, rcutsq);
-            const float ronsq = XPLOR ? d_ronsq[tp] : 0.0f;
-            float force_divr = 0.0f, pair_eng = 0.0f;
-            Eval eval(rsq, rcutsq, param, ext);
-            if (Eval::needsCharge())
-                eval.setCharge(qi, d_charge[j]);
-            eval.evalForceAndEnergy(force_divr, pair_eng, XPLOR ? (ronsq > rcutsq) : SHIFT1);
-            if (XPLOR && rsq >= ronsq && rsq < rcutsq)
-                {
-                // the XPLOR smoothing of the energy (hoomd/md/PotentialPair.h:711-737)
-                const float d = rcutsq - ronsq;
-                const float m = rsq - rcutsq;
-                pair_eng *= m * m * (rcutsq + 2.0f * rsq - 3.0f * ronsq) / (d * d * d);
-                }
-            u += (double)pair_eng;
+            ui += (double)m2 * sets_pair_energy<Eval, XPLOR>(
+                                   rsq, tp, d_params, d_rcutsq, d_ronsq, ext, qi,
+                                   Eval::needsCharge() ? d_charge[j] : 0.0f, SHIFT1);
             }
+        const uint32_t m2i = d_mult2[i];
+        if (m2i)
+            {
+            const unsigned int tp = MULTI ? ti * ntypes + ti : 0u;
+            ui += (double)m2i * sets_pair_energy<Eval, XPLOR>(0.0f, tp, d_params, d_rcutsq,
+                                                              d_ronsq, ext, qi, qi, SHIFT1);
+            }
+        u = (double)m1 * ui;
         }
     __shared__ double s_red[32];
     u = block_sum_d<1>(u, s_red);
@@ -939,10 +987,13 @@ inline unsigned int energy_sets_blocks(unsigned int N)
 
 template<class Eval>
 int launch_energy_sets(const gb_pair_args* a, const typename Eval::param_type* d_params,
-                       const float* ext, const uint8_t* d_set, double* d_partials,
+                       const float* ext, const gb_energy_sets* sets, double* d_partials,
                        cudaStream_t s)
     {
-    GB_REQUIRE(a && d_set && d_partials, "energy between sets: null argument");
+    GB_REQUIRE(a && sets && d_partials, "energy between sets: null argument");
+    GB_REQUIRE(sets->d_mult1 && sets->d_mult2, "energy between sets: null multiplicity array");
+    GB_REQUIRE(!sets->d_n_ex || (sets->d_ex_list && sets->ex_pitch > 0),
+               "energy between sets: exclusion rows need d_ex_list and ex_pitch");
     GB_REQUIRE(a->d_pos && a->d_n_neigh && a->d_nlist && a->d_rcutsq && d_params,
                "energy between sets: null device pointer");
     GB_REQUIRE(a->shift_mode <= 2 && (a->shift_mode != 2 || a->d_ronsq),
@@ -957,7 +1008,9 @@ int launch_energy_sets(const gb_pair_args* a, const typename Eval::param_type* d
     kern<<<grid, 256, 0, s>>>(a->N, reinterpret_cast<const float4*>(a->d_pos), a->box,
                               a->d_n_neigh, a->d_nlist, a->d_head_list, a->stride,
                               a->interleave == 4 ? 4u : 1u, d_params, a->d_rcutsq, a->d_ronsq,
-                              a->ntypes, ext, a->d_charge, a->shift_mode == 1, d_set, d_partials);
+                              a->ntypes, ext, a->d_charge, a->shift_mode == 1, sets->d_mult1,
+                              sets->d_mult2, sets->d_n_ex, sets->d_ex_list,
+                              sets->d_n_ex ? sets->ex_pitch : 0u, d_partials);
     return check_launch("energy between sets");
     }
 } // namespace gb

@@ -23,9 +23,9 @@ extern "C"
         }
 
     int gb_pair_energy_sets_lj(const gb_pair_args* args, const gb_lj_param* d_params,
-                               const uint8_t* d_set, double* d_partials, void* stream)
+                               const gb_energy_sets* sets, double* d_partials, void* stream)
         {
-        return launch_energy_sets<EvalLJ>(args, d_params, nullptr, d_set, d_partials,
+        return launch_energy_sets<EvalLJ>(args, d_params, nullptr, sets, d_partials,
                                           (cudaStream_t)stream);
         }
 

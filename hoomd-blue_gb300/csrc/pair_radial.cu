@@ -10,7 +10,7 @@ namespace gb
 int radial_charged(const gb_pair_args* args, const gb_radial_param* d_params, const FuseArgs& fz,
                    bool fused, cudaStream_t s);
 int radial_energy_sets_charged(const gb_pair_args* args, const gb_radial_param* d_params,
-                               const uint8_t* d_set, double* d_partials, cudaStream_t s);
+                               const gb_energy_sets* sets, double* d_partials, cudaStream_t s);
 }
 
 using namespace gb;
@@ -40,12 +40,12 @@ extern "C"
         }
 
     int gb_pair_energy_sets_radial(const gb_pair_args* args, const gb_radial_param* d_params,
-                                   const uint8_t* d_set, double* d_partials, void* stream)
+                                   const gb_energy_sets* sets, double* d_partials, void* stream)
         {
         if (args && args->d_charge)
-            return radial_energy_sets_charged(args, d_params, d_set, d_partials,
+            return radial_energy_sets_charged(args, d_params, sets, d_partials,
                                               (cudaStream_t)stream);
-        return launch_energy_sets<EvalRadial>(args, d_params, nullptr, d_set, d_partials,
+        return launch_energy_sets<EvalRadial>(args, d_params, nullptr, sets, d_partials,
                                               (cudaStream_t)stream);
         }
     }

@@ -14,8 +14,8 @@ int radial_charged(const gb_pair_args* args, const gb_radial_param* d_params, co
     }
 
 int radial_energy_sets_charged(const gb_pair_args* args, const gb_radial_param* d_params,
-                               const uint8_t* d_set, double* d_partials, cudaStream_t s)
+                               const gb_energy_sets* sets, double* d_partials, cudaStream_t s)
     {
-    return launch_energy_sets<EvalRadialQ>(args, d_params, nullptr, d_set, d_partials, s);
+    return launch_energy_sets<EvalRadialQ>(args, d_params, nullptr, sets, d_partials, s);
     }
 } // namespace gb

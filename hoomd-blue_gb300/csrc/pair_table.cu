@@ -24,9 +24,9 @@ extern "C"
 
     int gb_pair_energy_sets_table(const gb_pair_args* args, const gb_table_param* d_params,
                                   const float* d_table,
-                                  const uint8_t* d_set, double* d_partials, void* stream)
+                                  const gb_energy_sets* sets, double* d_partials, void* stream)
         {
-        return launch_energy_sets<EvalTable>(args, d_params, d_table, d_set, d_partials,
+        return launch_energy_sets<EvalTable>(args, d_params, d_table, sets, d_partials,
                                         (cudaStream_t)stream);
         }
     }

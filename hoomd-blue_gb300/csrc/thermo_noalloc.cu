@@ -12,8 +12,10 @@
 // Limits and rules:
 //  * N must not exceed GB_NOALLOC_MAX_N (4,194,304 particles); larger N is rejected with
 //    GB_ERR_TOO_LARGE before anything is launched.
-//  * The first call on a device looks up the array's device address (cudaGetSymbolAddress, with
-//    that device current) and caches it; make that first call before any stream capture.
+//  * The first call in each CUDA context looks up the array's device address
+//    (cudaGetSymbolAddress, with that context current) and caches it under the context's id;
+//    that is once per device, and once more after a cudaDeviceReset. Make that first call
+//    before any stream capture.
 //  * All calls share the one array and it keeps the previous call's contents. The call clears
 //    the completion counter on its stream before the reduction starts; calls that overlap on the
 //    GPU (issued on different streams without ordering between them) race on the array and give
@@ -21,6 +23,8 @@
 //  * No cudaMalloc, cudaFree or allocating library routine is called.
 #include <cstdint>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "gb_device.cuh"
 #include "gb_host.h"
@@ -114,31 +118,69 @@ __global__ void __launch_bounds__(NA_BLOCK)
         }
     }
 
-// Device address of g_noalloc_scratch per device, looked up once per device.
+// Device address of g_noalloc_scratch, looked up once per CUDA context. The cache is keyed by
+// the driver's context id (cuCtxGetId: unique for the life of the process), not by the device
+// ordinal, so a context created after cudaDeviceReset, or another context made current on the
+// same device, gets its own lookup instead of a stale address. The two driver functions are
+// resolved through the runtime (cudaGetDriverEntryPointByVersion), so the library needs no link
+// to libcuda; where they cannot be resolved, the address is looked up on every call.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+
 std::mutex g_na_mutex;
-void* g_na_ptr[64] = {};
+bool g_na_resolved = false;
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+std::vector<std::pair<unsigned long long, void*>> g_na_cache;
+
+// the current context's id, or false when there is none (or the driver functions are missing)
+bool current_context_id(unsigned long long* id)
+    {
+    if (!g_na_resolved)
+        {
+        g_na_resolved = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q)
+                == cudaSuccess
+            && q == cudaDriverEntryPointSuccess)
+            g_ctx_current = (CtxGetCurrentFn)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q)
+                == cudaSuccess
+            && q == cudaDriverEntryPointSuccess)
+            g_ctx_id = (CtxGetIdFn)f;
+        cudaGetLastError();
+        }
+    if (!g_ctx_current || !g_ctx_id)
+        return false;
+    void* ctx = nullptr;
+    if (g_ctx_current(&ctx) != 0 || ctx == nullptr)
+        return false;
+    return g_ctx_id(ctx, id) == 0;
+    }
 
 int noalloc_scratch_ptr(void** ptr)
     {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess)
-        return fail(GB_ERR_CUDA, std::string("gb_thermo_reduce_noalloc: cudaGetDevice: ")
-                                     + cudaGetErrorString(e));
-    if (dev < 0 || dev >= 64)
-        return fail(GB_ERR_UNSUPPORTED, "gb_thermo_reduce_noalloc: device ordinal >= 64");
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev])
-        {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr)
-            return fail(GB_ERR_CUDA,
-                        std::string("gb_thermo_reduce_noalloc: cudaGetSymbolAddress: ")
-                            + cudaGetErrorString(e));
-        g_na_ptr[dev] = p;
-        }
-    *ptr = g_na_ptr[dev];
+    unsigned long long id = 0;
+    if (current_context_id(&id))
+        for (const auto& kv : g_na_cache)
+            if (kv.first == id)
+                {
+                *ptr = kv.second;
+                return GB_OK;
+                }
+    // first call in this context (the lookup also initialises the device's primary context when
+    // none is current yet)
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr)
+        return fail(GB_ERR_CUDA, std::string("gb_thermo_reduce_noalloc: cudaGetSymbolAddress: ")
+                                     + cudaGetErrorString(e));
+    if (current_context_id(&id))
+        g_na_cache.emplace_back(id, p);
+    *ptr = p;
     return GB_OK;
     }
 } // namespace

@@ -79,6 +79,11 @@ class StepFuse(ctypes.Structure):
                 ("brownian", c_int)]
 
 
+class EnergySets(ctypes.Structure):
+    _fields_ = [("d_mult1", c_void), ("d_mult2", c_void), ("d_n_ex", c_void),
+                ("d_ex_list", c_void), ("ex_pitch", c_uint)]
+
+
 class RadialParam(ctypes.Structure):
     _fields_ = [("v", c_float * 6), ("kind", c_uint), ("aux", c_float)]
 

@@ -48,9 +48,17 @@ class Integrator:
         self._simulation = None
         self._cpp_obj = None
         self._cpp_nlist = None
+        self._attached_forces = []
 
     def _contents_changed(self):
         if self._simulation is not None and self._cpp_obj is not None:
+            # forces taken out of the list lose their engine objects (reading them raises until
+            # they are attached again); the ones still listed are re-attached at the next run
+            current = {id(f) for f in self._forces}
+            for f in self._attached_forces:
+                if id(f) not in current:
+                    f._detach()
+            self._detach()
             self._simulation._detach_all()
 
     @property
@@ -95,6 +103,7 @@ class Integrator:
         integ = _hoomd_gb300.IntegratorTwoStep(simulation.state._cpp_pdata, cpp_nl, self._dt)
         for f in self.forces:
             integ.addForce(f._attach(simulation, cpp_nl))
+        self._attached_forces = list(self.forces)
         self.methods[0]._attach(integ, simulation.state)
         self._cpp_obj = integ
         return integ

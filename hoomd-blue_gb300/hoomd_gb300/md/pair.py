@@ -145,12 +145,18 @@ class Pair:
         return self._cpp_obj.getForces()
 
     def compute_energy(self, tags1, tags2):
-        """Energy between two disjoint sets of particles, U = sum over i in tags1 and j in
-        tags2 of V_ij(r) (hoomd/md/pair/pair.py compute_energy), summed on the GPU."""
+        """Energy between two sets of particles, U = sum over every tag in tags1 and every tag
+        in tags2 of V_ij(r) (hoomd/md/pair/pair.py compute_energy, PotentialPair::
+        computeEnergyBetweenSets): no exclusions apply, repeated tags count each time, and a tag
+        in both lists is also paired with itself, as in the reference. Summed on the GPU."""
         if self._cpp_obj is None or self._simulation is None:
             raise RuntimeError("compute_energy is available after Simulation.run")
         self._simulation._attach()
-        return self._cpp_obj.computeEnergyBetweenSets(np.asarray(tags1), np.asarray(tags2))
+        t1 = np.asarray(tags1, dtype=np.int64).ravel()
+        t2 = np.asarray(tags2, dtype=np.int64).ravel()
+        if (t1 < 0).any() or (t2 < 0).any():
+            raise ValueError("compute_energy: tags are non-negative")
+        return self._cpp_obj.computeEnergyBetweenSets(t1, t2)
 
     @property
     def torques(self):

@@ -182,6 +182,8 @@ class Simulation:
             if getattr(f, "_pending", False) and getattr(f, "_cpp_obj", None) is not None:
                 f._send_params()
                 f._pending = False
+                # accelerations at the current positions follow the new parameters
+                self._needs_prep = True
         if getattr(self, "_needs_prep", False):
             for f in integ.forces:
                 if getattr(f, "_cpp_obj", None) is not None and hasattr(f, "_update_tail"):

@@ -49,3 +49,8 @@ def replica_systems(count=256, n_min=500, n_max=20000, rho=(0.7, 0.9), kT=(0.8, 
     """[(snapshot, kT, seed)] for ``count`` replicas drawn from one seeded generator."""
     return [(to_snapshot(h), kt, sd) for h, kt, sd in
             _S.replica_systems(count, n_min, n_max, rho, kT, jitter, seed)]
+
+
+def _snapshot(pos, L, types, typeid):
+    """N particles at ``pos`` in a cubic box of side L, as a Snapshot."""
+    return to_snapshot(_S.HostSystem(pos, L, types, typeid))

@@ -309,22 +309,36 @@ int gb_pair_forces_radial(const gb_pair_args* args, const gb_radial_param* d_par
                           void* stream);
 
 /* Energy between two sets of particles: replaces PotentialPair<E>::computeEnergyBetweenSets
- * (hoomd/md/PotentialPair.h, bound as computeEnergyBetweenSets and called by
- * hoomd/md/pair/pair.py compute_energy), which sums on the host. U = sum over i in set 1, j in
- * set 2 of V_ij(r) with the force's shift / XPLOR mode, from the full list in args (the forces
- * and virial fields of args are not used). d_set[i] = 1 or 2 marks particle index i's set (0 =
- * neither); the sets must be disjoint. d_partials receives gb_pair_energy_sets_blocks(N) doubles
- * whose sum, in order, is U. With args->d_charge set, the radial entry scales by q_i q_j. */
+ * (hoomd/md/PotentialPair.h:833-990, bound as computeEnergyBetweenSets and called by
+ * hoomd/md/pair/pair.py compute_energy), which sums on the host over every tag of set 1 and
+ * every tag of set 2. U = sum_i m1[i] (sum_j m2[j] V_ij(r) + m2[i] V_ii(0)) with the force's
+ * shift / XPLOR mode, j over particle i's row of the full list in args plus its exclusion row
+ * (the reference applies no exclusions; the list has the excluded pairs filtered out, so they
+ * are added back, each distinct partner once). d_mult1[i] / d_mult2[i] count how often particle
+ * index i's tag appears in set 1 / set 2 (duplicates and overlapping sets count as the
+ * reference's double loop counts them; a tag in both sets adds the evaluator at r = 0, as
+ * there). d_n_ex may be NULL (no exclusions). The forces and virial fields of args are not
+ * used. d_partials receives gb_pair_energy_sets_blocks(N) doubles whose sum, in order, is U.
+ * With args->d_charge set, the radial entry scales by q_i q_j. */
+typedef struct gb_energy_sets
+    {
+    const uint32_t* d_mult1;       /* [N] occurrences of index i's tag in set 1 */
+    const uint32_t* d_mult2;       /* [N] occurrences of index i's tag in set 2 */
+    const unsigned int* d_n_ex;    /* [N] exclusion row lengths (as gb_nlist_filter), or NULL */
+    const unsigned int* d_ex_list; /* [N * ex_pitch] excluded indices */
+    unsigned int ex_pitch;
+    } gb_energy_sets;
+
 unsigned int gb_pair_energy_sets_blocks(unsigned int N);
 int gb_pair_energy_sets_lj(const gb_pair_args* args, const gb_lj_param* d_params,
-                           const uint8_t* d_set, double* d_partials, void* stream);
+                           const gb_energy_sets* sets, double* d_partials, void* stream);
 int gb_pair_energy_sets_table(const gb_pair_args* args, const gb_table_param* d_params,
-                              const float* d_table, const uint8_t* d_set, double* d_partials,
-                              void* stream);
+                              const float* d_table, const gb_energy_sets* sets,
+                              double* d_partials, void* stream);
 int gb_pair_energy_sets_example(const gb_pair_args* args, const gb_example_param* d_params,
-                                const uint8_t* d_set, double* d_partials, void* stream);
+                                const gb_energy_sets* sets, double* d_partials, void* stream);
 int gb_pair_energy_sets_radial(const gb_pair_args* args, const gb_radial_param* d_params,
-                               const uint8_t* d_set, double* d_partials, void* stream);
+                               const gb_energy_sets* sets, double* d_partials, void* stream);
 
 /* DPD thermostat pair forces (EvaluatorPairDPDThermoDPD.h:190-272, EvaluatorPairDPDThermoLJ.h:
  * 216-276, PotentialPairDPDThermo.h:160-240): a conservative part (DPD: A (1 - r/r_c); DPDLJ:
@@ -380,7 +394,8 @@ int gb_thermo_reduce(const float* d_vel, const float* d_force, const float* d_vi
  * the device), and so cannot pass the d_scratch buffer gb_thermo_reduce needs. Its scratch is a
  * fixed array inside the library (GB_NOALLOC_MAX_N particles' worth, 384.25 KiB), resident on
  * every GPU that loads the library until the process exits. N > GB_NOALLOC_MAX_N returns
- * GB_ERR_TOO_LARGE. The first call on a device looks up the array's address with that device
+ * GB_ERR_TOO_LARGE. The first call in each CUDA context (once per device; again after a
+ * cudaDeviceReset or under another context) looks up the array's address with that context
  * current; make it before any stream capture. All calls share the array: calls that overlap on
  * the GPU race. Outputs as gb_thermo_reduce; no cudaMalloc or cudaFree is ever called. */
 #define GB_NOALLOC_MAX_N 4194304u

@@ -410,6 +410,51 @@ def test_compute_energy_between_sets(kind):
         _brute_energy_sets(pos, L, s1, s2, V, rc), rel=2e-5)
 
 
+def _brute_energy_tag_lists(pos, L, tags1, tags2, V, r_cut):
+    """The reference's double loop over the two tag lists (hoomd/md/PotentialPair.h:833-990):
+    every (tag in tags1, tag in tags2) combination, duplicates and shared tags included, no
+    exclusions; V(r) within r_cut, minimum image, FP64."""
+    a = pos[np.asarray(tags1)][:, None, :] - pos[np.asarray(tags2)][None, :, :]
+    a -= L * np.rint(a / L)
+    r = np.sqrt((a ** 2).sum(-1))
+    return V(r[r < r_cut]).sum()
+
+
+def test_compute_energy_counts_excluded_and_repeated_pairs():
+    """compute_energy applies no exclusions (bonded pairs count), counts a tag as often as it
+    appears, counts both orders of a pair when both tags are in both sets, and adds V(0) for a
+    tag paired with itself, as the reference's double loop does."""
+    snap = workloads.lj_fluid_sc(8, density=0.84, jitter=0.05, seed=3)
+    N = snap.particles.N
+    b = [(i, i + 1) for i in range(0, N - 1, 2)]
+    snap.bonds.N = len(b)
+    snap.bonds.types = ["b"]
+    snap.bonds.group[:] = b
+    L = snap.configuration.box[0]
+    sim = make_sim(snap)
+    rc = 2.5
+    f = md.pair.Gaussian(nlist=md.nlist.Cell(buffer=0.4), default_r_cut=rc)  # bonds excluded
+    f.params[("A", "A")] = dict(epsilon=1.3, sigma=0.8)
+
+    def V(r):
+        return 1.3 * np.exp(-0.5 * r * r / 0.64)
+    sim.operations.computes.append(f)
+    sim.run(0)
+    pos = sim.state.get_snapshot().particles.position.astype(np.float32).astype(np.float64)
+    tags = np.arange(N)
+    # disjoint: every bonded pair (2k, 2k+1) joins the two sets
+    t1, t2 = tags[0::2], tags[1::2]
+    assert f.compute_energy(t1, t2) == pytest.approx(
+        _brute_energy_tag_lists(pos, L, t1, t2, V, rc), rel=2e-5)
+    # overlapping sets with repeated tags
+    s1 = np.concatenate([tags[:200], [3, 3, 7, 150]])
+    s2 = np.concatenate([tags[100:300], [150, 3]])
+    want = _brute_energy_tag_lists(pos, L, s1, s2, V, rc)
+    assert f.compute_energy(s1, s2) == pytest.approx(want, rel=2e-5)
+    assert f.compute_energy(s2, s1) == pytest.approx(want, rel=2e-5)
+    assert f.compute_energy(s1, []) == 0.0
+
+
 def test_shortest_rebuild():
     """nlist.Cell.shortest_rebuild (NeighborList::getSmallestRebuild): the smallest period
     between builds since the last run, at most the mean period; 100 before two builds."""
@@ -490,7 +535,34 @@ def test_forces_appended_after_a_run():
     sim.run(0)
     assert thermo.potential_energy == pytest.approx(2 * pe1, rel=1e-5)
     sim.operations.integrator.forces.remove(lj2)
+    # a removed force no longer reports values from the discarded engine
+    with pytest.raises(RuntimeError, match="available after"):
+        _ = lj2.energy
     sim.run(0)
     assert thermo.potential_energy == pytest.approx(pe1, rel=1e-5)
     sim.run(10)
     assert np.isfinite(thermo.potential_energy)
+    with pytest.raises(RuntimeError, match="available after"):
+        _ = lj2.forces
+
+
+def test_params_changed_between_runs_apply_to_the_first_step():
+    """Parameters set after a run are sent before the next one, and the accelerations the next
+    step starts from are recomputed with them."""
+    snap = workloads.lj_fluid_sc(8, density=0.8, jitter=0.05, seed=6)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0)
+    sim.run(5)
+    lj.params[("A", "A")] = dict(epsilon=2.0, sigma=1.0)
+    sim.run(0)
+    f_now = lj.forces
+    # a fresh simulation from the same state with epsilon = 2 from the start
+    snap2 = sim.state.get_snapshot()
+    sim2, lj_b, cell2, thermo2 = lj_sim(snap2, kT=None, thermalize=None)
+    lj_b.params[("A", "A")] = dict(epsilon=2.0, sigma=1.0)
+    sim2.run(0)
+    assert np.allclose(f_now, lj_b.forces, rtol=1e-5, atol=1e-5 * np.abs(f_now).max())
+    sim.run(1)
+    sim2.run(1)
+    a = sim.state.get_snapshot().particles.velocity
+    b = sim2.state.get_snapshot().particles.velocity
+    assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
