@@ -104,6 +104,22 @@ __device__ __forceinline__ float dot3(float x, float y, float z)
     return fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z));
     }
 
+// dot3 of both halves of packed differences. The squares and sums are scalar __fmul_rn /
+// __fadd_rn, which are never contracted into fused multiply-adds; the same sequence written
+// with packed mul.rn/add.rn.f32x2 was measured to round differently from the scalar sequence on
+// a share of inputs (a list membership decided at r_list^2 then differs from the reference's by
+// one pair in a million particles), so only the subtractions stay packed.
+__device__ __forceinline__ void f2dot3(uint64_t dx, uint64_t dy, uint64_t dz, float& r0,
+                                       float& r1)
+    {
+    float x0, x1, y0, y1, z0, z1;
+    f2unpack(dx, x0, x1);
+    f2unpack(dy, y0, y1);
+    f2unpack(dz, z0, z1);
+    r0 = dot3(x0, y0, z0);
+    r1 = dot3(x1, y1, z1);
+    }
+
 // BoxDim::makeFraction with no ghost layer: hoomd/BoxDim.h:276-284.
 __device__ __forceinline__ void make_fraction(const gb_box& b, float x, float y, float z,
                                               float& fx, float& fy, float& fz)
@@ -118,8 +134,14 @@ __device__ __forceinline__ void make_fraction(const gb_box& b, float x, float y,
     fz = fmul(dz, b.Linv[2]);
     }
 
-// Cell of a position: hoomd/CellList.cc:441-476 (bin index, wrap at the hi face). Returns false
-// when the particle is outside the box (fraction outside [-1e-5, 1 + 1e-5)).
+// Cell of a position: hoomd/CellList.cc:441-476 (bin index from makeFraction). Returns false
+// when the particle is outside the box (fraction outside [-1e-5, 1 + 1e-5)). One deliberate
+// difference: where the reference wraps a bin index of dim (a fraction that rounds to 1, i.e. a
+// particle within an ulp or so of the hi face) to bin 0, this keeps it in the last bin. The
+// neighbour-list builds here take a stencil cell's periodic image from the cell index, which
+// needs every particle on its own cell's side of the boundary; a particle at the hi face filed
+// in bin 0 would be imaged a box length away from all its partners (the reference finds them by
+// minimum image per pair). The neighbour sets are the same either way.
 __device__ __forceinline__ bool cell_of(const gb_box& b, const unsigned int* dim, float x, float y,
                                         float z, unsigned int& cell)
     {
@@ -132,11 +154,11 @@ __device__ __forceinline__ bool cell_of(const gb_box& b, const unsigned int* dim
         || (fz < -0.00001f || fz >= 1.00001f))
         return false;
     if (ib == (int)dim[0] && b.periodic[0])
-        ib = 0;
+        ib = (int)dim[0] - 1;
     if (jb == (int)dim[1] && b.periodic[1])
-        jb = 0;
+        jb = (int)dim[1] - 1;
     if (kb == (int)dim[2] && b.periodic[2])
-        kb = 0;
+        kb = (int)dim[2] - 1;
     if (ib < 0 || ib >= (int)dim[0] || jb < 0 || jb >= (int)dim[1] || kb < 0 || kb >= (int)dim[2])
         return false;
     cell = (unsigned int)((kb * (int)dim[1] + jb) * (int)dim[0] + ib);

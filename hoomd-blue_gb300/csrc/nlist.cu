@@ -501,8 +501,8 @@ __global__ void __launch_bounds__(TILE_WARPS_MAX * 32)
                 unsigned int o = 0;
                 if (ORTHO)
                     {
-                    // two own particles per step in packed FP32 pairs; each half rounds as the
-                    // scalar fsub / fmul / fadd sequence below, so the decisions are identical
+                    // two own particles per step: packed FP32 differences (each half rounds as the
+                    // scalar fsub), scalar rounded squares and sums, so the decisions are identical
                     const uint64_t cx2 = f2pack(c.x, c.x), cy2 = f2pack(c.y, c.y),
                                    cz2 = f2pack(c.z, c.z);
                     const uint64_t sx2 = f2pack(sx, sx), sy2 = f2pack(sy, sy), sz2 = f2pack(sz, sz);
@@ -512,10 +512,8 @@ __global__ void __launch_bounds__(TILE_WARPS_MAX * 32)
                         const uint64_t dx = f2sub(f2sub(f2pack(p0.x, p1.x), cx2), sx2);
                         const uint64_t dy = f2sub(f2sub(f2pack(p0.y, p1.y), cy2), sy2);
                         const uint64_t dz = f2sub(f2sub(f2pack(p0.z, p1.z), cz2), sz2);
-                        const uint64_t r2
-                            = f2add(f2add(f2mul(dx, dx), f2mul(dy, dy)), f2mul(dz, dz));
                         float rsq0, rsq1;
-                        f2unpack(r2, rsq0, rsq1);
+                        f2dot3(dx, dy, dz, rsq0, rsq1);
                         const unsigned int i0 = __float_as_uint(p0.w), i1 = __float_as_uint(p1.w);
                         float rc, rl;
                         unsigned int nmax_o;
@@ -568,8 +566,9 @@ __global__ void __launch_bounds__(TILE_WARPS_MAX * 32)
 // particle ob + l in registers. The nine cells of each stencil plane are staged in shared memory
 // as structure-of-arrays (x, y, z, index[, type]), every cell starting at an even slot, so two
 // consecutive candidates load as one 8-byte packed pair. Every lane tests its own particle
-// against the staged candidates two at a time in packed FP32 pairs (each half rounds as the
-// scalar minImage sequence, so the decisions are bit-identical) and writes its hits straight into
+// against the staged candidates two at a time: packed FP32 differences (each half rounds as the
+// scalar subtraction) and scalar rounded squares and sums (f2dot3), so the decisions are
+// bit-identical to the minImage sequence, and writes its hits straight into
 // its own row; a cell's exact image shift is applied only when the stencil wraps there (it is
 // zero otherwise, and x - 0 is exact). Hits come in the order (plane, cell, slot) of the
 // warp-cooperative kernel above, so the lists are the same.
@@ -735,10 +734,8 @@ __global__ void __launch_bounds__(LANE_WARPS * 32)
                             dy = f2sub(dy, sy2);
                             dx = f2sub(dx, sx2);
                             }
-                        const uint64_t r2
-                            = f2add(f2add(f2mul(dx, dx), f2mul(dy, dy)), f2mul(dz, dz));
                         float rsq0, rsq1;
-                        f2unpack(r2, rsq0, rsq1);
+                        f2dot3(dx, dy, dz, rsq0, rsq1);
                         const uint2 jj = *reinterpret_cast<const uint2*>(s_j + slot);
                         put(rsq0 <= rlim(slot) && (!centre || jj.x != i), jj.x);
                         put(rsq1 <= rlim(slot + 1) && (!centre || jj.y != i), jj.y);

@@ -259,8 +259,9 @@ __device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint
                 }
             cnt++;
         };
-        // candidates [s_start[c0], s_start[c1]) shifted by (sx, sy, sz); two per step in
-        // packed FP32 pairs (each half rounds as the scalar operation would)
+        // candidates [s_start[c0], s_start[c1]) shifted by (sx, sy, sz); two per step: packed
+        // FP32 differences (each half rounds as the scalar subtraction) and scalar rounded
+        // squares and sums (f2dot3)
         auto run = [&](uint32_t c0, uint32_t c1, float sx, float sy, float sz) {
             const uint32_t e = s_start[c1];
             uint32_t a = s_start[c0];
@@ -275,9 +276,8 @@ __device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint
                     const uint64_t dx = f2sub(f2sub(px, f2pack(q0.x, q1.x)), hx);
                     const uint64_t dy = f2sub(f2sub(py, f2pack(q0.y, q1.y)), hy);
                     const uint64_t dz = f2sub(f2sub(pz, f2pack(q0.z, q1.z)), hz);
-                    const uint64_t r2 = f2add(f2add(f2mul(dx, dx), f2mul(dy, dy)), f2mul(dz, dz));
                     float r0, r1;
-                    f2unpack(r2, r0, r1);
+                    f2dot3(dx, dy, dz, r0, r1);
                     const uint32_t j0 = __float_as_uint(q0.w), j1 = __float_as_uint(q1.w);
                     if (r0 <= rlsq && j0 != i)
                         store(j0);

@@ -182,7 +182,9 @@ class Simulation:
             if getattr(f, "_pending", False) and getattr(f, "_cpp_obj", None) is not None:
                 f._send_params()
                 f._pending = False
-                # accelerations at the current positions follow the new parameters
+                # the next run's preparation recomputes the forces at the current positions
+                # with the new parameters (IntegratorTwoStep::prepRun; the accelerations of
+                # the last step are kept, as there)
                 self._needs_prep = True
         if getattr(self, "_needs_prep", False):
             for f in integ.forces:

@@ -626,8 +626,17 @@ void pair_forces(unsigned int N,
                  R* force,
                  R* virial, // 6 * N, SoA with pitch N
                  bool rint_min_image,
-                 int nthreads)
+                 int nthreads,
+                 int abs_terms = 0)
     {
+    // abs_terms (full list only) accumulates magnitudes instead of the terms:
+    //  1: of every term. The result bounds each sum's conditioning: a sum of n terms computed
+    //     in a precision with unit roundoff u is within about n u times this of the exact sum.
+    //  2: of the terms of the cut-off band only: pairs with |r^2 - r_cut^2| <= 1e-6 r_cut^2,
+    //     evaluated just inside r_cut. Whether such a pair interacts turns on the last bits of
+    //     r^2, which two correct FP32 evaluations may round differently; where the potential
+    //     does not vanish at r_cut, one pair more or less moves the force by this much.
+    const R band = R(1e-6);
     std::memset(force, 0, sizeof(R) * 4 * N);
     if (virial)
         std::memset(virial, 0, sizeof(R) * 6 * N);
@@ -669,6 +678,13 @@ void pair_forces(unsigned int N,
                 }
             R force_divr = R(0.0);
             R pair_eng = R(0.0);
+            if (abs_terms == 2)
+                {
+                using std::abs;
+                if (!(abs(rsq - rc2) <= band * rc2))
+                    continue;
+                rsq = std::min(rsq, rc2 * (R(1) - band));
+                }
             E eval(rsq, rc2, param);
             bool evaluated = eval.eval(force_divr, pair_eng, energy_shift);
             if (evaluated)
@@ -689,6 +705,24 @@ void pair_forces(unsigned int N,
                         }
                     }
                 R force_div2r = force_divr * R(0.5);
+                if (abs_terms != 0)
+                    {
+                    using std::abs;
+                    fx += abs(dx * force_divr);
+                    fy += abs(dy * force_divr);
+                    fz += abs(dz * force_divr);
+                    pei += abs(pair_eng * R(0.5));
+                    if (compute_virial)
+                        {
+                        vxx += abs(force_div2r * dx * dx);
+                        vxy += abs(force_div2r * dx * dy);
+                        vxz += abs(force_div2r * dx * dz);
+                        vyy += abs(force_div2r * dy * dy);
+                        vyz += abs(force_div2r * dy * dz);
+                        vzz += abs(force_div2r * dz * dz);
+                        }
+                    continue;
+                    }
                 fx += dx * force_divr;
                 fy += dy * force_divr;
                 fz += dz * force_divr;
@@ -1647,7 +1681,7 @@ using namespace orc;
         unsigned int ntypes, const double* params, const R* tdata, const R* rcutsq,               \
         const R* ronsq, int shift_mode, const unsigned int* n_neigh, const unsigned int* nlist,   \
         const uint64_t* head_list, int third_law, int compute_virial, R* force, R* virial,        \
-        int rint_min_image, int nthreads)                                                          \
+        int rint_min_image, int nthreads, int abs_terms)                                           \
         {                                                                                          \
         Box<R> box;                                                                                \
         box.set(b6, per);                                                                          \
@@ -1659,7 +1693,7 @@ using namespace orc;
                 p[t] = LJ<R>::make_param(params[2 * t], params[2 * t + 1]);                        \
             pair_forces<R, LJ<R>>(N, pos, box, ntypes, p.data(), rcutsq, ronsq, shift_mode,        \
                                   n_neigh, nlist, head_list, third_law != 0, compute_virial != 0,  \
-                                  force, virial, rint_min_image != 0, nthreads);                   \
+                                  force, virial, rint_min_image != 0, nthreads, abs_terms);   \
             }                                                                                      \
         else if (kind == 1)                                                                        \
             {                                                                                      \
@@ -1673,7 +1707,7 @@ using namespace orc;
                 }                                                                                  \
             pair_forces<R, Table<R>>(N, pos, box, ntypes, p.data(), rcutsq, ronsq, 0, n_neigh,     \
                                      nlist, head_list, third_law != 0, compute_virial != 0, force, \
-                                     virial, rint_min_image != 0, nthreads);                       \
+                                     virial, rint_min_image != 0, nthreads, abs_terms);       \
             }                                                                                      \
         else                                                                                       \
             {                                                                                      \
@@ -1683,7 +1717,7 @@ using namespace orc;
             pair_forces<R, Example<R>>(N, pos, box, ntypes, p.data(), rcutsq, ronsq, shift_mode,   \
                                        n_neigh, nlist, head_list, third_law != 0,                  \
                                        compute_virial != 0, force, virial, rint_min_image != 0,    \
-                                       nthreads);                                                  \
+                                       nthreads, abs_terms);                                  \
             }                                                                                      \
         }                                                                                          \
     ORC_EXPORT void orc_cv_step_one_##SUF(unsigned int N, R* pos, R* vel, const R* accel,          \

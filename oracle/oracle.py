@@ -256,10 +256,15 @@ def neighbor_sets(n_neigh, nlist, head):
 
 def pair_forces(kind, pos4, box, params, rcutsq, n_neigh, nlist, head, third_law=False,
                 compute_virial=True, shift_mode=0, ronsq=None, tdata=None, prec=32,
-                periodic=(1, 1, 1), rint_min_image=True, nthreads=1):
+                periodic=(1, 1, 1), rint_min_image=True, nthreads=1, abs_terms=False):
     """hoomd/md/PotentialPair.h:587-794. kind: 'lj' (params ntypes^2 x (sigma, epsilon)),
     'table' (ntypes^2 x (r_min, width, offset) into tdata = concatenated [V, F] per pair),
-    'example' (ntypes^2 x (k, sigma))."""
+    'example' (ntypes^2 x (k, sigma)). abs_terms=True (full list only) sums the magnitudes of
+    the terms instead: the conditioning of each force, energy and virial sum; abs_terms=2 sums
+    the magnitudes of the terms of the pairs within 1e-6 relative of r_cut^2 only (evaluated just
+    inside r_cut), the part of each value that two correct FP32 evaluations may include or not."""
+    if abs_terms and third_law:
+        raise ValueError("abs_terms needs the full list (third_law=False)")
     R = rdtype(prec)
     pos4 = np.ascontiguousarray(pos4, R)
     N = len(pos4)
@@ -278,7 +283,8 @@ def pair_forces(kind, pos4, box, params, rcutsq, n_neigh, nlist, head, third_law
     getattr(lib(), f"orc_pair_forces_{suf(prec)}")(
         kid, N, ptr(pos4), ptr(b), ptr(p), ntypes, ptr(params), ptr(tdata), ptr(rcutsq),
         ptr(ronsq), int(shift_mode), ptr(n_neigh), ptr(nlist), ptr(head), int(third_law),
-        int(compute_virial), ptr(force), ptr(virial), int(rint_min_image), int(nthreads))
+        int(compute_virial), ptr(force), ptr(virial), int(rint_min_image), int(nthreads),
+        int(abs_terms))
     return force, virial
 
 

@@ -177,6 +177,26 @@ def assert_close_f64(got, ref, rtol=RTOL, what=""):
                            f"{err.max():.3e} (ref scale {np.abs(ref).max():.3e})")
 
 
+def assert_close_cond(got, ref, absref, band=0.0, rtol=RTOL, what=""):
+    """|got - ref| <= rtol * absref elementwise, absref being the sum of the magnitudes of the
+    terms that make up each value (oracle pair_forces with abs_terms=True), plus a floor of
+    1e-7 x its largest value. A sum of n FP32 terms is within about n x 6e-8 x absref of the
+    exact sum whatever the order, so this bar is met by any correct FP32 summation of up to
+    ~150 terms, where a bar relative to the value itself is not when the terms cancel (dense
+    liquids: repulsive pair forces tens of times the net force). ``band`` (oracle pair_forces
+    with abs_terms=2) adds the magnitude of the terms of pairs within 1e-6 relative of r_cut^2,
+    which two correct FP32 evaluations may count or not where the potential does not vanish at
+    r_cut."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    absref = np.asarray(absref, np.float64)
+    err = np.abs(got - ref)
+    bound = rtol * absref + np.asarray(band, np.float64) + 1e-7 * max(absref.max(), 1e-30)
+    bad = err > bound
+    assert not bad.any(), (f"{what}: {bad.sum()} of {bad.size} outside rtol x sum|terms|; worst "
+                           f"ratio {(err / bound).max():.3f}")
+
+
 PAD = np.uint32(0xFFFFFFFF)
 
 

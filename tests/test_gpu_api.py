@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 import hoomd_gb300 as hoomd  # noqa: E402
 from hoomd_gb300 import md, workloads  # noqa: E402
 from oracle import oracle as O  # noqa: E402
+from gpu_util import assert_close_cond  # noqa: E402
 
 GOLD = pathlib.Path(__file__).resolve().parent / "golden"
 
@@ -546,9 +547,54 @@ def test_forces_appended_after_a_run():
         _ = lj2.forces
 
 
-def test_params_changed_between_runs_apply_to_the_first_step():
-    """Parameters set after a run are sent before the next one, and the accelerations the next
-    step starts from are recomputed with them."""
+def test_particles_on_the_hi_face_keep_their_neighbours():
+    """Particles one FP32 ulp inside the hi faces (a wrapped position lands there when a
+    particle crosses the lo face by less than half an ulp): their fractional coordinate rounds to
+    1; the engine's list must still hold all their partners across the boundary, so the forces
+    match the oracle's."""
+    # density 0.8: a box whose FP32 fraction of L/2 - 1 ulp rounds to exactly 1
+    snap = workloads.lj_fluid_sc(16, density=0.8)
+    L = np.float32(snap.configuration.box[0])
+    inside = float(np.nextafter(np.float32(L / np.float32(2)), np.float32(0)))
+    assert O.make_fraction(np.float32([[inside, 0, 0]]), snap.configuration.box, 32)[0, 0] >= 1
+    rng = np.random.default_rng(8)
+    P = snap.particles.position
+    moved = 0
+    for i in rng.permutation(snap.particles.N):
+        axes = [(0,), (1,), (2,), (0, 1), (1, 2), (0, 1, 2)][moved % 6]
+        trial = P[i].copy()
+        trial[list(axes)] = inside
+        d = P - trial
+        d -= float(L) * np.rint(d / float(L))
+        r = np.sqrt((d ** 2).sum(1))
+        r[i] = np.inf
+        if r.min() > 0.45:  # apart from every other particle (lattice spacing 1.08)
+            P[i] = trial
+            moved += 1
+        if moved == 18:
+            break
+    sim, lj, cell, thermo = lj_sim(snap, thermalize=None)
+    sim.run(0)
+    pos = sim.state.get_snapshot().particles.position
+    assert (np.abs(pos - inside) == 0).any()
+    box = tuple(snap.configuration.box)
+    # the FP32 oracle (same FP32 differences of coordinates near L/2) and the magnitude sums of
+    # the FP64 terms bound the comparison; a missing partner would be off by a whole pair force
+    p32 = O.make_pos4(pos, np.zeros(len(pos)), 32)
+    n, l, h, _ = O.build_nlist(p32, box, [[2.5]], 0.4, full=True, prec=32)
+    f32, _ = O.pair_forces("lj", p32, box, [[1.0, 1.0]], np.float32([[6.25]]), n, l, h, prec=32)
+    p64 = O.make_pos4(pos, np.zeros(len(pos)), 64)
+    n, l, h, _ = O.build_nlist(p64, box, [[2.5]], 0.4, full=True, prec=64)
+    fa, _ = O.pair_forces("lj", p64, box, [[1.0, 1.0]], [[6.25]], n, l, h, prec=64, abs_terms=1)
+    fb, _ = O.pair_forces("lj", p64, box, [[1.0, 1.0]], [[6.25]], n, l, h, prec=64, abs_terms=2)
+    assert_close_cond(lj.forces, f32[:, :3], fa[:, :3], band=fb[:, :3], what="hi-face forces")
+
+
+def test_params_changed_between_runs_recompute_forces():
+    """Parameters set after a run are sent before the next one, and that run's preparation
+    recomputes the forces at the current positions with them (IntegratorTwoStep::prepRun,
+    hoomd/md/IntegratorTwoStep.cc:262-275: the net force is always recomputed; the
+    accelerations of the last step are kept, as there)."""
     snap = workloads.lj_fluid_sc(8, density=0.8, jitter=0.05, seed=6)
     sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0)
     sim.run(5)
@@ -561,8 +607,4 @@ def test_params_changed_between_runs_apply_to_the_first_step():
     lj_b.params[("A", "A")] = dict(epsilon=2.0, sigma=1.0)
     sim2.run(0)
     assert np.allclose(f_now, lj_b.forces, rtol=1e-5, atol=1e-5 * np.abs(f_now).max())
-    sim.run(1)
-    sim2.run(1)
-    a = sim.state.get_snapshot().particles.velocity
-    b = sim2.state.get_snapshot().particles.velocity
-    assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
+    assert thermo.potential_energy == pytest.approx(thermo2.potential_energy, rel=1e-6)

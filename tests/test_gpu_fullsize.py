@@ -9,15 +9,31 @@ Each system is built from the same seeds as the benchmark:
 
 For each, the GPU neighbour list (cell list + lane-per-particle build through the C ABI, the
 layout the engine runs) must equal the FP32 oracle's full list as per-particle sorted sets, bit
-for bit, and one evaluation of the pair forces, per-particle energies and virials over that list
-must lie within 1e-5 relative of the FP64 oracle (absolute floor 1e-5 x the largest value). This
-follows the reference's CPU-vs-GPU list comparison (hoomd/md/test/test_neighborlist.cc:1060-1148)
-and its force/energy accuracy test (hoomd/md/pytest/test_potential.py:952-1058), at full size.
-The oracle runs on every host core (OpenMP); the comparisons are vectorised over particle chunks.
+for bit. One evaluation of the pair forces, per-particle energies and virials over that list is
+then held to two bars:
+
+* against the FP32 oracle (the reference's arithmetic at HOOMD_LONGREAL_SIZE=32 on the same
+  FP32 positions): within 1e-5 of the sum of the magnitudes of the terms of each value (the
+  only differences left are the evaluator's reciprocal and the summation order), plus the terms
+  of pairs within 1e-6 relative of r_cut^2 (LJ does not vanish at r_cut in mode "none", and
+  whether such a pair counts turns on the last bit of r^2);
+* against the FP64 oracle: no worse than the FP32 oracle itself (largest error at most 1.5x
+  the FP32 oracle's; values outside 1e-5 relative at most twice as many as the FP32 oracle's,
+  plus 1e-4 of the values).
+
+A bar of 1e-5 relative to the FP64 value alone cannot be met by any FP32 evaluation of these
+dense systems: the difference x_i - x_j of FP32 coordinates up to L/2 ~ 54 is off by up to
+~4e-6, and the r^-13 LJ force of a close pair magnifies that thirteen-fold, so the FP32 oracle
+itself misses it on about 0.2 % of the Kob-Andersen force components.
+
+This follows the reference's CPU-vs-GPU list comparison
+(hoomd/md/test/test_neighborlist.cc:1060-1148) and its force/energy accuracy test
+(hoomd/md/pytest/test_potential.py:952-1058), at full size. The oracle runs on every host core
+(OpenMP); the comparisons are vectorised over particle chunks.
 
 The 1M-particle fluid is also checked after 200 steps of the product's own run (Bussi at
 kT 1.5, Hilbert sort every 100 steps): the engine's forces, energies and virials through the
-Python API against the FP64 oracle at the resulting positions.
+Python API against the oracles at the resulting positions, with the same bars.
 """
 
 import os
@@ -31,7 +47,7 @@ torch = pytest.importorskip("torch")
 
 import synthetic_systems as S  # noqa: E402
 from oracle import oracle as O  # noqa: E402
-from gpu_util import (GpuNlist, assert_close_f64, compare_neighbor_sets,  # noqa: E402
+from gpu_util import (RTOL, GpuNlist, assert_close_cond, compare_neighbor_sets,  # noqa: E402
                       gpu_pair_forces, table_params)
 
 CORES = os.cpu_count() or 1
@@ -100,19 +116,49 @@ def test_fullsize_nlist_and_forces_vs_oracle(systems, case):
     assert len(bad) == 0, f"{case}: {len(bad)} of {N} particles' sets differ, first {bad[:5]}"
     sum_n = int(n_o.astype(np.int64).sum())
     assert sum_n > 50 * N  # a dense liquid: tens of neighbours each
-    del l_o, h_o, ho
 
-    # one force evaluation over the GPU list vs the FP64 oracle (own FP64 list at r_cut + buffer)
+    # one force evaluation over the GPU list vs the FP32 and FP64 oracles
     f, v = gpu_pair_forces(nl, kind, par, rc, virial=True, tables=tables)
+    oparams = opar if kind == "table" else par
+    f32, v32 = O.pair_forces(kind, pos4, box6, oparams, (rc ** 2).astype(np.float32), n_o, l_o,
+                             h_o, third_law=False, compute_virial=True,
+                             tdata=None if odata is None else odata.astype(np.float32), prec=32,
+                             nthreads=CORES)
+    del l_o, h_o, ho
     pos64 = pos4.astype(np.float64)
     pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
+    check_against_oracles(kind, pos64, box6, oparams, rc, r_buff, odata,
+                          (f[:, :3], f[:, 3], v), (f32[:, :3], f32[:, 3], v32), case)
+
+
+def check_against_oracles(kind, pos64, box6, oparams, rc, r_buff, odata, got, f32, case):
+    """got / f32: (forces (N, 3), energies (N,), virials (6, N)) of the GPU and of the FP32
+    oracle; the FP64 oracle's values, the sums of term magnitudes and the cut-off band terms are
+    computed here."""
     n6, l6, h6, _ = O.build_nlist(pos64, box6, rc, r_buff, full=True, prec=64, nthreads=CORES)
-    fo, vo = O.pair_forces(kind, pos64, box6, opar if kind == "table" else par, rc ** 2, n6, l6,
-                           h6, third_law=False, compute_virial=True, tdata=odata, prec=64,
-                           nthreads=CORES)
-    assert_close_f64(f[:, :3], fo[:, :3], what=f"{case} force")
-    assert_close_f64(f[:, 3], fo[:, 3], what=f"{case} energy")
-    assert_close_f64(v, vo, what=f"{case} virial")
+    kw = dict(third_law=False, compute_virial=True, tdata=odata, prec=64, nthreads=CORES)
+    fo, vo = O.pair_forces(kind, pos64, box6, oparams, rc ** 2, n6, l6, h6, **kw)
+    fa, va = O.pair_forces(kind, pos64, box6, oparams, rc ** 2, n6, l6, h6, abs_terms=1, **kw)
+    fb, vb = O.pair_forces(kind, pos64, box6, oparams, rc ** 2, n6, l6, h6, abs_terms=2, **kw)
+    ref = (fo[:, :3], fo[:, 3], vo)
+    absref = (fa[:, :3], fa[:, 3], va)
+    bands = (fb[:, :3], fb[:, 3], vb)
+    for name, g, r32, r64, a, b in zip(("force", "energy", "virial"), got, f32, ref, absref,
+                                       bands):
+        g = np.asarray(g, np.float64)
+        r32 = np.asarray(r32, np.float64)
+        assert_close_cond(g, r32, a, band=b, what=f"{case} {name} vs FP32 oracle")
+        e_gpu = np.abs(g - r64)
+        e_32 = np.abs(r32 - r64)
+        over = e_gpu - (1.5 * e_32.max() + b + 1e-7 * np.abs(r64).max())
+        assert (over <= 0).all(), (
+            f"{case} {name}: GPU error vs FP64 {e_gpu.max():.3e} beyond 1.5 x the FP32 oracle's "
+            f"{e_32.max():.3e} plus the cut-off band")
+        plain = RTOL * np.abs(r64) + RTOL * np.abs(r64).max()
+        out_gpu, out_32 = int((e_gpu > plain + b).sum()), int((e_32 > plain + b).sum())
+        assert out_gpu <= 2 * out_32 + 1e-4 * e_gpu.size, (
+            f"{case} {name}: {out_gpu} values outside 1e-5 relative of FP64 on the GPU against "
+            f"{out_32} for the FP32 oracle")
 
 
 def test_fullsize_fcc_after_run_vs_oracle():
@@ -134,11 +180,14 @@ def test_fullsize_fcc_after_run_vs_oracle():
     F, E, W = lj.forces, lj.energies, lj.virials
     snap = sim.state.get_snapshot()
     box6 = tuple(snap.configuration.box)
-    pos4 = O.make_pos4(snap.particles.position, snap.particles.typeid, 64)
-    n6, l6, h6, _ = O.build_nlist(pos4, box6, [[2.5]], 0.4, full=True, prec=64, nthreads=CORES)
-    fo, vo = O.pair_forces("lj", pos4, box6, [[1.0, 1.0]], [[6.25]], n6, l6, h6, third_law=False,
-                           compute_virial=True, prec=64, nthreads=CORES)
+    pos4 = O.make_pos4(snap.particles.position, snap.particles.typeid, 32)
+    rc = np.array([[2.5]])
+    n, l, h, _ = O.build_nlist(pos4, box6, rc, 0.4, full=True, prec=32, nthreads=CORES)
+    f32, v32 = O.pair_forces("lj", pos4, box6, [[1.0, 1.0]], np.float32([[6.25]]), n, l, h,
+                             third_law=False, compute_virial=True, prec=32, nthreads=CORES)
+    del l, h
     assert cell.num_builds >= 2
-    assert_close_f64(F, fo[:, :3], what="force after 200 steps")
-    assert_close_f64(E, fo[:, 3], what="energy after 200 steps")
-    assert_close_f64(W, vo.T, what="virial after 200 steps")
+    pos64 = pos4.astype(np.float64)
+    pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
+    check_against_oracles("lj", pos64, box6, [[1.0, 1.0]], rc, 0.4, None,
+                          (F, E, W.T), (f32[:, :3], f32[:, 3], v32), "fcc after 200 steps")

@@ -55,6 +55,35 @@ def snap_pos4(snap):
         tuple(snap.configuration.box)
 
 
+def hi_face_system():
+    """The 4096-particle fluid with particles placed on the hi faces of the box at FP32: exactly
+    at L/2 and one ulp inside, on each axis and on edges and a corner. Their fractional
+    coordinate rounds to 1, where the reference's cell list wraps the bin index to 0; their
+    neighbours lie across the periodic boundary (a wrapped FP32 position lands there when a
+    particle crosses the lo face by less than half an ulp)."""
+    pos4, box6 = snap_pos4(workloads.lj_fluid_sc(16))
+    L = np.float32(box6[0])
+    hi = np.float32(L / np.float32(2))
+    inside = np.nextafter(hi, np.float32(0))
+    rng = np.random.default_rng(5)
+    moved = 0
+    for i in rng.permutation(len(pos4)):
+        v = hi if moved % 2 == 0 else inside
+        axes = [(0,), (1,), (2,), (0, 1), (1, 2), (0, 1, 2)][moved % 6]
+        trial = pos4[i, :3].astype(np.float64)
+        trial[list(axes)] = v
+        d = pos4[:, :3].astype(np.float64) - trial
+        d -= float(L) * np.rint(d / float(L))
+        r = np.sqrt((d ** 2).sum(1))
+        r[i] = np.inf
+        if r.min() > 0.45:  # apart from every other particle (lattice spacing 1.06)
+            pos4[i, list(axes)] = v
+            moved += 1
+        if moved == 24:
+            break
+    return pos4, box6
+
+
 NLIST_CASES = {
     "sc7_rcut1.1": lambda: (O.make_pos4(workloads.sc_positions(7, 1.0), np.zeros(343), 32),
                             (7.0, 7.0, 7.0, 0, 0, 0), [[1.1]], 0.0),
@@ -66,6 +95,7 @@ NLIST_CASES = {
                                            tilts=(0.3, -0.2, 0.1), lattice=True)
     + ([[2.5, 1.5], [1.5, 2.0]], 0.4),
     "random60k": lambda: random_system(60000, (41.0, 41.0, 41.0), seed=7) + ([[2.5]], 0.4),
+    "hi_face4096": lambda: hi_face_system() + ([[2.5]], 0.4),
 }
 
 
@@ -393,7 +423,8 @@ def test_bussi_predrawn_ring_gives_the_same_factor():
         assert np.isclose(factor, O.bussi_factor(K, dof, dt, 0.0, kT, t, seed, 0), rtol=1e-9)
 
 
-@pytest.mark.parametrize("case", ["lj4096", "binary3000", "triclinic1728", "random60k"])
+@pytest.mark.parametrize("case", ["lj4096", "binary3000", "triclinic1728", "random60k",
+                                  "hi_face4096"])
 @pytest.mark.parametrize("layout", ["col", "col4"])
 def test_lane_and_warp_builds_are_identical(case, layout):
     """The lane-per-particle and warp-per-cell tiled builds write the same neighbours in the same
