@@ -31,7 +31,7 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["box_common.cu", "nlist.cu", "integrate.cu", "pair_lj.cu", "pair_table.cu",
-              "pair_example.cu", "pair_radial.cu", "pair_radial_q.cu", "pair_dpd.cu", "sfc_sort.cu", "thermo_noalloc.cu", "replica.cu",
+              "pair_example.cu", "pair_radial.cu", "pair_radial_q.cu", "pair_dpd.cu", "sfc_sort.cu", "thermo_noalloc.cu", "replica.cu", "snapshot_io.cu",
               "mlp.cu"]
 HOST_SOURCES = ["engine.cc", "npt.cc", "ensemble.cc", "surrogate.cc", "module.cc"]
 LIB_NAME = "libhoomd_gb300.so"

@@ -62,90 +62,80 @@ ParticleData::ParticleData(unsigned int N_, unsigned int ntypes_, unsigned int n
     scratch.zero(stream);
     }
 
-void ParticleData::set_particles(const double* p, const double* v, const double* m,
-                                 const uint32_t* t, const int32_t* img)
+ParticleData::Stage ParticleData::stage()
     {
-    std::vector<float> hp(4 * (size_t)N), hv(4 * (size_t)N);
-    std::vector<int32_t> hi(3 * (size_t)N);
-    std::vector<uint32_t> ht(N);
-    for (unsigned int i = 0; i < N; i++)
+    const size_t need = gb_snapshot_stage_bytes(N) + 256;
+    if (io_stage.size() < need)
+        io_stage.resize(need);
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t n = N;
+    char* b = io_stage.get();
+    Stage st;
+    st.pos = reinterpret_cast<double*>(b);
+    b += up(24 * n);
+    st.vel = reinterpret_cast<double*>(b);
+    b += up(24 * n);
+    st.mass = reinterpret_cast<double*>(b);
+    b += up(8 * n);
+    st.charge = reinterpret_cast<double*>(b);
+    b += up(8 * n);
+    st.typeid_ = reinterpret_cast<uint32_t*>(b);
+    b += up(4 * n);
+    st.image = reinterpret_cast<int32_t*>(b);
+    b += up(12 * n);
+    st.rtag = reinterpret_cast<uint32_t*>(b);
+    b += up(4 * n);
+    st.err = reinterpret_cast<uint32_t*>(b);
+    return st;
+    }
+
+// initializeFromSnapshot's per-particle part on the device: one bulk copy per snapshot array into
+// the staging block, then gb_snapshot_scatter (conversion to FP32, wrap into the box, images).
+void ParticleData::set_particles(const double* p, const double* v, const double* m,
+                                 const uint32_t* t, const int32_t* img, const double* q)
+    {
+    if (!p || !v || !m || !t || !img)
+        throw std::invalid_argument("set_particles: position, velocity, mass, typeid and image "
+                                    "arrays are required");
+    const Stage st = stage();
+    const size_t n = N;
+    auto h2d = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes)
+            cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream),
+                       "set_particles copy");
+    };
+    h2d(st.pos, p, 24 * n);
+    h2d(st.vel, v, 24 * n);
+    h2d(st.mass, m, 8 * n);
+    h2d(st.typeid_, t, 4 * n);
+    h2d(st.image, img, 12 * n);
+    if (charge.size() != N)
+        charge.resize(N);
+    if (q)
+        h2d(st.charge, q, 8 * n);
+    else
+        charge.zero(stream); // the snapshot's charges are all at their default, 0
+    const uint32_t* rt = nullptr;
+    if (tags_set)
         {
-        if (t[i] >= ntypes)
-            throw std::invalid_argument("typeid out of range");
-        float x = (float)p[3 * i], y = (float)p[3 * i + 1], z = (float)p[3 * i + 2];
-        int ix = img ? img[3 * i] : 0, iy = img ? img[3 * i + 1] : 0, iz = img ? img[3 * i + 2] : 0;
-        // wrap into the box once, as ParticleData::initializeFromSnapshot does (orthorhombic
-        // and triclinic, one image at most)
-        for (int pass = 0; pass < 2; pass++)
-            {
-            if (periodic[2])
-                {
-                if (z >= box.hi[2])
-                    {
-                    z -= box.L[2];
-                    y -= box.L[2] * box.yz;
-                    x -= box.L[2] * box.xz;
-                    iz++;
-                    }
-                else if (z < box.lo[2])
-                    {
-                    z += box.L[2];
-                    y += box.L[2] * box.yz;
-                    x += box.L[2] * box.xz;
-                    iz--;
-                    }
-                }
-            if (periodic[1])
-                {
-                float ty = box.yz * z;
-                if (y >= box.hi[1] + ty)
-                    {
-                    y -= box.L[1];
-                    x -= box.L[1] * box.xy;
-                    iy++;
-                    }
-                else if (y < box.lo[1] + ty)
-                    {
-                    y += box.L[1];
-                    x += box.L[1] * box.xy;
-                    iy--;
-                    }
-                }
-            if (periodic[0])
-                {
-                float tx = (box.xz - box.xy * box.yz) * z + box.xy * y;
-                if (x >= box.hi[0] + tx)
-                    {
-                    x -= box.L[0];
-                    ix++;
-                    }
-                else if (x < box.lo[0] + tx)
-                    {
-                    x += box.L[0];
-                    ix--;
-                    }
-                }
-            }
-        hp[4 * i] = x;
-        hp[4 * i + 1] = y;
-        hp[4 * i + 2] = z;
-        hp[4 * i + 3] = u2f(t[i]);
-        hv[4 * i] = v ? (float)v[3 * i] : 0.0f;
-        hv[4 * i + 1] = v ? (float)v[3 * i + 1] : 0.0f;
-        hv[4 * i + 2] = v ? (float)v[3 * i + 2] : 0.0f;
-        hv[4 * i + 3] = m ? (float)m[i] : 1.0f;
-        hi[3 * i] = ix;
-        hi[3 * i + 1] = iy;
-        hi[3 * i + 2] = iz;
-        ht[i] = i;
+        check(gb_rtag(tag.get(), N, st.rtag, stream), "gb_rtag");
+        rt = st.rtag;
         }
-    pos.upload(hp.data(), hp.size(), stream);
-    vel.upload(hv.data(), hv.size(), stream);
-    image.upload(hi.data(), hi.size(), stream);
-    tag.upload(ht.data(), ht.size(), stream);
+    cuda_check(cudaMemsetAsync(st.err, 0xFF, sizeof(uint32_t), stream), "set_particles err");
+    check(gb_snapshot_scatter(st.pos, st.vel, st.mass, st.typeid_, st.image,
+                              q ? st.charge : nullptr, rt, N, ntypes, &box, pos.get(), vel.get(),
+                              image.get(), tag.get(), q ? charge.get() : nullptr, st.err, stream),
+          "gb_snapshot_scatter");
+    uint32_t err = 0;
+    cuda_check(cudaMemcpyAsync(&err, st.err, sizeof(err), cudaMemcpyDeviceToHost, stream),
+               "set_particles err");
     accel.zero(stream);
     accel_set = false;
     cuda_check(cudaStreamSynchronize(stream), "set_particles");
+    if (err != 0xFFFFFFFFu)
+        throw std::invalid_argument("typeid out of range (particle tag " + std::to_string(err)
+                                    + ")");
+    tags_set = true;
     }
 
 void ParticleData::set_charges(const double* q)
@@ -176,31 +166,26 @@ std::vector<uint32_t> ParticleData::rtag()
     return r;
     }
 
+// takeSnapshot's per-particle part on the device: gb_snapshot_gather writes the tag-ordered FP64
+// arrays into the staging block, then one bulk copy per array to the host.
 void ParticleData::get_particles(double* p, double* v, double* m, uint32_t* t, int32_t* img)
     {
-    std::vector<float> hp(4 * (size_t)N), hv(4 * (size_t)N);
-    std::vector<int32_t> hi(3 * (size_t)N);
-    pos.download(hp.data(), hp.size(), stream);
-    vel.download(hv.data(), hv.size(), stream);
-    image.download(hi.data(), hi.size(), stream);
-    std::vector<uint32_t> r = rtag();
-    for (unsigned int tg = 0; tg < N; tg++)
-        {
-        const size_t i = r[tg];
-        if (p)
-            for (int d = 0; d < 3; d++)
-                p[3 * tg + d] = hp[4 * i + d];
-        if (v)
-            for (int d = 0; d < 3; d++)
-                v[3 * tg + d] = hv[4 * i + d];
-        if (m)
-            m[tg] = hv[4 * i + 3];
-        if (t)
-            t[tg] = f2u(hp[4 * i + 3]);
-        if (img)
-            for (int d = 0; d < 3; d++)
-                img[3 * tg + d] = hi[3 * i + d];
-        }
+    const Stage st = stage();
+    const size_t n = N;
+    check(gb_snapshot_gather(pos.get(), vel.get(), image.get(), tag.get(), N, st.pos, st.vel,
+                             st.mass, st.typeid_, st.image, stream),
+          "gb_snapshot_gather");
+    auto d2h = [&](void* dst, const void* src, size_t bytes) {
+        if (dst && bytes)
+            cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream),
+                       "get_particles copy");
+    };
+    d2h(p, st.pos, 24 * n);
+    d2h(v, st.vel, 24 * n);
+    d2h(m, st.mass, 8 * n);
+    d2h(t, st.typeid_, 4 * n);
+    d2h(img, st.image, 12 * n);
+    cuda_check(cudaStreamSynchronize(stream), "get_particles");
     }
 
 void ParticleData::thermalize(double kT, uint64_t ts)

@@ -143,9 +143,12 @@ class ParticleData
     public:
     ParticleData(unsigned int N, unsigned int ntypes, unsigned int ndim,
                  const std::vector<double>& box6, const std::vector<int>& periodic);
-    // host arrays in tag order: pos xyz (3N), vel xyz (3N), mass (N), typeid (N), image (3N)
+    // host arrays in tag order: pos xyz (3N), vel xyz (3N), mass (N), typeid (N), image (3N),
+    // optional charge (N). Particles that already exist keep their current index (a snapshot
+    // written back keeps the sorted order); positions are wrapped into the box.
     void set_particles(const double* pos, const double* vel, const double* mass,
-                       const uint32_t* typeid_, const int32_t* image);
+                       const uint32_t* typeid_, const int32_t* image,
+                       const double* charge = nullptr);
     void get_particles(double* pos, double* vel, double* mass, uint32_t* typeid_,
                        int32_t* image);
     std::vector<uint32_t> rtag(); // tag -> index
@@ -167,7 +170,20 @@ class ParticleData
     DeviceArray<int32_t> image;
     DeviceArray<uint32_t> tag;
     DeviceArray<char> scratch;
+    DeviceArray<char> io_stage; // snapshot staging block (gb_snapshot_stage_bytes(N) + 256)
+    bool tags_set = false;      // the particles exist (tags hold a permutation of 0..N-1)
     uint64_t sort_generation = 0;
+
+    private:
+    // section pointers of io_stage: pos, vel, mass, charge, typeid, image, rtag, error word
+    struct Stage
+        {
+        double *pos, *vel, *mass, *charge;
+        uint32_t* typeid_;
+        int32_t* image;
+        uint32_t *rtag, *err;
+        };
+    Stage stage();
     };
 
 class NeighborList

@@ -72,15 +72,28 @@ PYBIND11_MODULE(_hoomd_gb300, m)
                 py::array_t<double, py::array::c_style | py::array::forcecast> vel,
                 py::array_t<double, py::array::c_style | py::array::forcecast> mass,
                 py::array_t<uint32_t, py::array::c_style | py::array::forcecast> typeid_,
-                py::array_t<int32_t, py::array::c_style | py::array::forcecast> image) {
+                py::array_t<int32_t, py::array::c_style | py::array::forcecast> image,
+                py::object charge) {
                  const size_t N = pd.N;
                  if ((size_t)pos.size() != 3 * N || (size_t)vel.size() != 3 * N
                      || (size_t)mass.size() != N || (size_t)typeid_.size() != N
                      || (size_t)image.size() != 3 * N)
                      throw std::invalid_argument("particle array sizes do not match N");
+                 if (charge.is_none())
+                     {
+                     pd.set_particles(pos.data(), vel.data(), mass.data(), typeid_.data(),
+                                      image.data(), nullptr);
+                     return;
+                     }
+                 auto q = py::array_t<double, py::array::c_style | py::array::forcecast>::ensure(
+                     charge);
+                 if (!q || (size_t)q.size() != N)
+                     throw std::invalid_argument("charge array size does not match N");
                  pd.set_particles(pos.data(), vel.data(), mass.data(), typeid_.data(),
-                                  image.data());
-             })
+                                  image.data(), q.data());
+             },
+             py::arg("pos"), py::arg("vel"), py::arg("mass"), py::arg("typeid"),
+             py::arg("image"), py::arg("charge") = py::none())
         .def("setCharges",
              [](ParticleData& pd, py::array_t<double, py::array::c_style | py::array::forcecast> q) {
                  if ((size_t)q.size() != pd.N)

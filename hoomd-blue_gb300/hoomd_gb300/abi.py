@@ -123,6 +123,13 @@ _PROTOS = {
                                c_void]),
     "gb_thermalize": (c_int, [c_void, c_void, c_uint, c_double, c_u64, ctypes.c_uint16, c_uint,
                               c_void, c_void]),
+    "gb_snapshot_stage_bytes": (c_size, [c_uint]),
+    "gb_snapshot_gather": (c_int, [c_void, c_void, c_void, c_void, c_uint, c_void, c_void, c_void,
+                                   c_void, c_void, c_void]),
+    "gb_rtag": (c_int, [c_void, c_uint, c_void, c_void]),
+    "gb_snapshot_scatter": (c_int, [c_void, c_void, c_void, c_void, c_void, c_void, c_void, c_uint,
+                                    c_uint, _P(Box), c_void, c_void, c_void, c_void, c_void,
+                                    c_void, c_void]),
     "gb_md_step_one": (c_int, [_P(StepOneArgs), c_void]),
     "gb_abi_struct_sizes": (c_uint, [_P(c_size), c_uint]),
     "gb_npt_step_one": (c_int, [c_void, c_void, c_void, c_void, c_uint, _P(Box), c_float, c_float,

@@ -41,21 +41,29 @@ class _Particles:
         self.typeid = np.zeros(N, np.uint32)
         self.mass = np.ones(N, np.float64)
         self.image = np.zeros((N, 3), np.int32)
-        # carried with the particles (GSD files, snapshots) but not used by the pair step
-        for name in PASSIVE_DEFAULTS:
-            setattr(self, name, passive_default(name, N))
+        # carried with the particles (GSD files, snapshots) but not used by the pair step; each
+        # is created at its default on first access, so a field nobody touched is known to hold
+        # its default without looking at N values
+        self._passive = {}
 
     def _adopt(self, N, arrays):
         """Take ``arrays`` (name -> array of the right shape, owned by this snapshot from now
-        on) as the particle data of N particles; fields not given get their defaults."""
+        on) as the particle data of N particles; passive fields not given hold their defaults."""
         self._N = int(N)
+        self._passive = {}
         for name, m in PARTICLE_FIELDS:
             a = arrays.get(name)
-            if a is None:
-                a = passive_default(name, self._N) if name in PASSIVE_DEFAULTS else None
+            if name in PASSIVE_DEFAULTS:
+                if a is not None:
+                    self._passive[name] = a
+                continue
             if a is None:
                 raise ValueError(f"_adopt: {name} is required")
             setattr(self, name, a)
+
+    def _passive_array(self, name):
+        """The passive field ``name`` if it was ever accessed or set, else None (all defaults)."""
+        return self._passive.get(name)
 
     @property
     def N(self):
@@ -65,6 +73,19 @@ class _Particles:
     def N(self, n):
         self._N = int(n)
         self._alloc(self._N)
+
+
+def _passive_property(name):
+    def get(self):
+        a = self._passive.get(name)
+        if a is None:
+            a = self._passive[name] = passive_default(name, self._N)
+        return a
+
+    def set(self, value):
+        self._passive[name] = value
+    return property(get, set, doc=f"snapshot.particles.{name} (created at its default on first "
+                                  f"access)")
 
 
 class _Group:
@@ -120,6 +141,9 @@ def is_passive_default(name, a):
     return not np.any(a[:, 0] != v[0]) and not np.any(a[:, 1:])
 
 
+for _name in PASSIVE_DEFAULTS:
+    setattr(_Particles, _name, _passive_property(_name))
+
 PARTICLE_FIELDS = (("position", 3), ("velocity", 3), ("typeid", 1), ("mass", 1), ("image", 3),
                    ("charge", 1), ("diameter", 1), ("body", 1), ("moment_inertia", 3),
                    ("orientation", 4), ("angmom", 4))
@@ -146,7 +170,8 @@ class Snapshot:
         N = p.N
         for name, m in PARTICLE_FIELDS:
             shape = (N,) if m == 1 else (N, m)
-            if np.shape(getattr(p, name)) != shape:
+            a = p._passive_array(name) if name in PASSIVE_DEFAULTS else getattr(p, name)
+            if a is not None and np.shape(a) != shape:
                 raise ValueError(f"snapshot.particles.{name} must have shape {shape}")
         if N and int(np.max(p.typeid)) >= len(p.types):
             raise ValueError("typeid refers to a type not in snapshot.particles.types")

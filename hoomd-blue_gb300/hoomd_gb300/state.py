@@ -29,13 +29,14 @@ class State:
 
     def _upload(self, snapshot):
         p = snapshot.particles
+        q = self._passive.get("charge")  # None: every charge at its default, 0
         self._cpp_pdata.setParticles(
             np.ascontiguousarray(p.position, np.float64),
             np.ascontiguousarray(p.velocity, np.float64),
             np.ascontiguousarray(p.mass, np.float64),
             np.ascontiguousarray(p.typeid, np.uint32),
-            np.ascontiguousarray(p.image, np.int32))
-        self._cpp_pdata.setCharges(np.ascontiguousarray(p.charge, np.float64))
+            np.ascontiguousarray(p.image, np.int32),
+            None if q is None else np.ascontiguousarray(q, np.float64))
         self._counts = None
         self._simulation._state_changed()
 
@@ -108,11 +109,13 @@ _PASSIVE = ("charge", "diameter", "body", "moment_inertia", "orientation", "angm
 
 
 def _copy_passive(snapshot):
-    """Host copies of the passive fields that differ from their defaults."""
+    """Host copies of the passive fields that differ from their defaults (a field the snapshot
+    never created holds its defaults)."""
     out = {}
+    p = snapshot.particles
     for name in _PASSIVE:
-        a = getattr(snapshot.particles, name)
-        if not is_passive_default(name, a):
+        a = p._passive_array(name) if hasattr(p, "_passive_array") else getattr(p, name)
+        if a is not None and not is_passive_default(name, a):
             out[name] = np.array(a, copy=True)
     return out
 

@@ -416,6 +416,33 @@ int gb_thermalize(float* d_vel, const uint32_t* d_tag, unsigned int N, double kT
                   uint64_t timestep, uint16_t seed, unsigned int ndim, void* d_scratch,
                   void* stream);
 
+/* Snapshot transfer on the device: the per-particle loops of ParticleData::takeSnapshot
+ * (hoomd/ParticleData.cc:1388-1617) and ParticleData::initializeFromSnapshot
+ * (hoomd/ParticleData.cc:982-1379), which the reference runs on the host. Snapshot arrays are in
+ * tag order and FP64 (positions and velocities 3 per particle, images 3 int32); the particle
+ * arrays are in index order (positions float4 x, y, z, type bits; velocities float4 with the
+ * mass; images int3; tags).
+ * gb_snapshot_gather writes the tag-ordered arrays from the particle arrays.
+ * gb_rtag writes rtag[tag[i]] = i (the reference's reverse-tag table).
+ * gb_snapshot_scatter places tag t at index d_rtag[t] (d_rtag NULL: index t), wrapping the
+ * position into the box with the image updated; d_in_charge may be NULL (charges left as they
+ * are). A type id >= ntypes is not written: *d_err receives the smallest such tag (set *d_err to
+ * 0xFFFFFFFF before the call). gb_snapshot_stage_bytes(N) is the size of one staging block that
+ * holds every snapshot array of N particles, each section 256-byte aligned (pos, vel, mass,
+ * charge, typeid, image, rtag). */
+size_t gb_snapshot_stage_bytes(unsigned int N);
+int gb_snapshot_gather(const float* d_pos, const float* d_vel, const int32_t* d_image,
+                       const uint32_t* d_tag, unsigned int N, double* d_out_pos,
+                       double* d_out_vel, double* d_out_mass, uint32_t* d_out_typeid,
+                       int32_t* d_out_image, void* stream);
+int gb_rtag(const uint32_t* d_tag, unsigned int N, uint32_t* d_rtag, void* stream);
+int gb_snapshot_scatter(const double* d_in_pos, const double* d_in_vel, const double* d_in_mass,
+                        const uint32_t* d_in_typeid, const int32_t* d_in_image,
+                        const double* d_in_charge, const uint32_t* d_rtag, unsigned int N,
+                        unsigned int ntypes, const gb_box* box, float* d_pos, float* d_vel,
+                        int32_t* d_image, uint32_t* d_tag, float* d_charge, uint32_t* d_err,
+                        void* stream);
+
 
 /* ---------------------------------------------------------------------------------------------
  * Fused whole-step kernels (GB300 design; no single reference counterpart). One MD step of

@@ -608,3 +608,52 @@ def test_params_changed_between_runs_recompute_forces():
     sim2.run(0)
     assert np.allclose(f_now, lj_b.forces, rtol=1e-5, atol=1e-5 * np.abs(f_now).max())
     assert thermo.potential_energy == pytest.approx(thermo2.potential_energy, rel=1e-6)
+
+def test_snapshot_round_trip_on_the_device():
+    """get_snapshot / set_snapshot convert on the device (takeSnapshot / initializeFromSnapshot's
+    per-particle loops): values come back as their FP32 roundings in tag order, positions out of
+    the box are wrapped with their images counted, a snapshot written into a sorted system keeps
+    its order and gives the oracle's forces, and a type id out of range is refused."""
+    snap = workloads.lj_fluid_sc(12, density=0.84, jitter=0.05, seed=21)
+    N = snap.particles.N
+    L = snap.configuration.box[0]
+    sim, lj, cell, thermo = lj_sim(snap, kT=1.5, sorter=10)
+    sim.run(25)  # sorted twice: index order is no longer tag order
+    s = sim.state.get_snapshot()
+    rng = np.random.default_rng(3)
+    pos = s.particles.position + rng.uniform(-0.02, 0.02, (N, 3))
+    pos[0] += [L, 0, 0]          # one box length beyond +x
+    pos[1] += [0, -1.2 * L, 0]   # beyond -y by more than the box
+    vel = rng.normal(size=(N, 3))
+    mass = rng.uniform(0.5, 2.0, N)
+    s.particles.position[:] = pos
+    s.particles.velocity[:] = vel
+    s.particles.mass[:] = mass
+    img0 = s.particles.image.copy()
+    sim.state.set_snapshot(s)
+    out = sim.state.get_snapshot()
+    f32 = np.float32
+    want = pos.astype(f32).astype(np.float64)
+    shift = np.zeros((N, 3))
+    shift[0, 0] = -L
+    k = 2 if pos[1, 1] + L < -L / 2 else 1  # box lengths added to bring it in
+    shift[1, 1] = k * L
+    assert np.allclose(out.particles.position, want + shift, atol=2e-5)
+    assert np.array_equal(out.particles.image[0], img0[0] + [1, 0, 0])
+    assert np.array_equal(out.particles.image[1], img0[1] + [0, -k, 0])
+    assert np.array_equal(out.particles.image[2:], img0[2:])
+    assert np.array_equal(out.particles.velocity, vel.astype(f32).astype(np.float64))
+    assert np.array_equal(out.particles.mass, mass.astype(f32).astype(np.float64))
+    assert np.array_equal(out.particles.typeid, s.particles.typeid)
+    sim.run(0)
+    p = out.particles.position
+    pos4 = O.make_pos4(p, np.zeros(N), 64)
+    box = tuple(snap.configuration.box)
+    n, l, h, _ = O.build_nlist(pos4, box, [[2.5]], 0.4, full=False, prec=64)
+    fo, _ = O.pair_forces("lj", pos4, box, [[1.0, 1.0]], [[6.25]], n, l, h, third_law=True,
+                          compute_virial=False, prec=64)
+    assert np.allclose(lj.forces, fo[:, :3], rtol=1e-5, atol=1e-5 * np.abs(fo[:, :3]).max())
+    bad = sim.state.get_snapshot()
+    bad.particles.typeid[7] = 3
+    with pytest.raises(Exception):
+        sim.state._upload(bad)
