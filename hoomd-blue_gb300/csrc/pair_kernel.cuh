@@ -214,6 +214,22 @@ __device__ inline void fuse_finish(const FuseArgs& fz, double ke, double pe, dou
 
 // Template parameters select the data path (evaluator, threads per particle, layout, type
 // tables, fused epilogue); shift mode, virial and box shape are uniform runtime branches.
+// XPLOR smoothing between r_on and r_cut (applied by the reference's force loop,
+// hoomd/md/PotentialPair.h:711-737). With w = r_cut^2 - r_on^2 and u = r_cut^2 - r^2, the energy is
+// multiplied by S = u^2 (r_cut^2 + 2 r^2 - 3 r_on^2) / w^3, and since dS/d(r^2) =
+// -6 u (r^2 - r_on^2) / w^3, the force over r becomes S F/r + 12 V u (r^2 - r_on^2) / w^3.
+__device__ __forceinline__ void xplor_smooth(float rsq, float rcutsq, float ronsq,
+                                             float& force_divr, float& pair_eng)
+    {
+    const float w = rcutsq - ronsq;
+    const float inv_w3 = 1.0f / (w * w * w);
+    const float u = rcutsq - rsq;
+    const float smooth = u * u * (rcutsq + 2.0f * rsq - 3.0f * ronsq) * inv_w3;
+    const float slope = 12.0f * u * (rsq - ronsq) * inv_w3;
+    force_divr = smooth * force_divr + slope * pair_eng;
+    pair_eng *= smooth;
+    }
+
 template<class Eval, int TPP, bool FLAT, bool MULTI, bool FUSE>
 __global__ void __launch_bounds__(256)
     k_pair(float4* __restrict__ d_force, float* __restrict__ d_virial, size_t pitch,
@@ -302,20 +318,7 @@ __global__ void __launch_bounds__(256)
             if (SHIFT == 2)
                 {
                 if (rsq >= ronsq && rsq < rcutsq)
-                    {
-                    // XPLOR smoothing (hoomd/md/PotentialPairGPU.cuh:318-338)
-                    const float old_pair_eng = pair_eng;
-                    const float old_force_divr = force_divr;
-                    const float xplor_denom_inv
-                        = 1.0f / ((rcutsq - ronsq) * (rcutsq - ronsq) * (rcutsq - ronsq));
-                    const float rsq_minus_r_cut_sq = rsq - rcutsq;
-                    const float s = rsq_minus_r_cut_sq * rsq_minus_r_cut_sq
-                                    * (rcutsq + 2.0f * rsq - 3.0f * ronsq) * xplor_denom_inv;
-                    const float ds_dr_divr
-                        = 12.0f * (rsq - ronsq) * rsq_minus_r_cut_sq * xplor_denom_inv;
-                    pair_eng = old_pair_eng * s;
-                    force_divr = s * old_force_divr - ds_dr_divr * old_pair_eng;
-                    }
+                    xplor_smooth(rsq, rcutsq, ronsq, force_divr, pair_eng);
                 }
             if (VIRIAL)
                 {
@@ -538,18 +541,7 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
                 eval.setCharge(qi, __ldg(d_charge + j));
             eval.evalForceAndEnergy(force_divr, pair_eng, energy_shift);
             if (XPLOR && rsq >= ronsq && rsq < rcutsq)
-                {
-                const float old_pair_eng = pair_eng;
-                const float old_force_divr = force_divr;
-                const float xplor_denom_inv
-                    = 1.0f / ((rcutsq - ronsq) * (rcutsq - ronsq) * (rcutsq - ronsq));
-                const float rsq_minus_r_cut_sq = rsq - rcutsq;
-                const float s = rsq_minus_r_cut_sq * rsq_minus_r_cut_sq
-                                * (rcutsq + 2.0f * rsq - 3.0f * ronsq) * xplor_denom_inv;
-                const float ds_dr_divr = 12.0f * (rsq - ronsq) * rsq_minus_r_cut_sq * xplor_denom_inv;
-                pair_eng = old_pair_eng * s;
-                force_divr = s * old_force_divr - ds_dr_divr * old_pair_eng;
-                }
+                xplor_smooth(rsq, rcutsq, ronsq, force_divr, pair_eng);
             if (!valid)
                 {
                 force_divr = 0.0f;
@@ -893,13 +885,7 @@ __device__ __forceinline__ double sets_pair_energy(float rsq, unsigned int tp,
     if (!eval.evalForceAndEnergy(force_divr, pair_eng, XPLOR ? (ronsq > rcutsq) : SHIFT1))
         return 0.0;
     if (XPLOR && rsq >= ronsq && rsq < rcutsq)
-        {
-        // smoothing factor S(r) = (rc^2 - r^2)^2 (rc^2 + 2 r^2 - 3 ron^2) / (rc^2 - ron^2)^3
-        const float width = rcutsq - ronsq;
-        const float below_cut = rcutsq - rsq;
-        pair_eng *= below_cut * below_cut * (rcutsq + 2.0f * rsq - 3.0f * ronsq)
-                    / (width * width * width);
-        }
+        xplor_smooth(rsq, rcutsq, ronsq, force_divr, pair_eng);
     return (double)pair_eng;
     }
 

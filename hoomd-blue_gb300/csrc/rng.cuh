@@ -129,35 +129,34 @@ __device__ inline float normal_f(Philox& rng)
 // Marsaglia-Tsang gamma with squeeze test (hoomd/RandomNumbers.h:454-534). The rejection loop is
 // bounded (acceptance is > 95% per iteration for alpha >= 1); after 64 rejections the last
 // candidate is returned rather than spinning.
-__device__ inline double gamma_d(Philox& rng, double m_alpha, double m_b)
+__device__ inline double gamma_d(Philox& rng, double shape, double scale)
     {
-    double alpha = m_alpha;
-    if (m_alpha < 1.0)
-        alpha += 1.0;
-    const double d = alpha - 1. / 3.;
+    // shape < 1: draw at shape + 1 and scale by U^(1/shape) (Marsaglia and Tsang, sect. 6)
+    const double a = shape < 1.0 ? shape + 1.0 : shape;
+    const double d = a - 1. / 3.;
     const double c = (1.0 / sqrt(d)) / 3.;
-    double v = 1.0;
+    double cube = 1.0;
     for (int it = 0; it < 64; it++)
         {
-        double x;
+        double z;
         int tries = 0;
         do
             {
-            x = normal_d(rng);
-            v = 1.0 + c * x;
-            } while (v <= 0. && ++tries < 64);
-        v = v * v * v;
-        const double x2 = x * x;
+            z = normal_d(rng);
+            cube = 1.0 + c * z;
+            } while (cube <= 0. && ++tries < 64);
+        cube = cube * cube * cube;
+        const double z2 = z * z;
         const double u = u01<double>(rng.u64());
-        if (u < 1.0 - 0.0331 * x2 * x2)
+        if (u < 1.0 - 0.0331 * z2 * z2) // squeeze
             break;
-        if (log(u) < 0.5 * x2 + d * (1.0 - v + log(v)))
+        if (log(u) < 0.5 * z2 + d * (1.0 - cube + log(cube)))
             break;
         }
-    v *= d * m_b;
-    if (m_alpha < 1.0)
-        v *= pow(u01<double>(rng.u64()), 1.0 / m_alpha);
-    return v;
+    double g = cube * d * scale;
+    if (shape < 1.0)
+        g *= pow(u01<double>(rng.u64()), 1.0 / shape);
+    return g;
     }
 
 // hoomd/md/Thermostat.h:357-391 (key id 45, counter = first member tag) and :416-446, split in
@@ -168,28 +167,26 @@ __device__ inline double2 bussi_draws_d(double dof, uint64_t timestep, uint16_t 
                                         uint32_t instance_id)
     {
     Philox rng(45, timestep, seed, instance_id);
-    const double r_normal_one = normal_d(rng);
-    double r_gamma = 0.0;
+    const double gauss = normal_d(rng);
+    double chi2 = 0.0; // chi-squared with dof - 1 degrees of freedom, as 2 Gamma((dof - 1) / 2)
     if (dof > 1.0)
-        r_gamma = 2.0 * gamma_d(rng, (dof - 1.0) / 2.0, 1.0);
-    return make_double2(r_normal_one, r_gamma);
+        chi2 = 2.0 * gamma_d(rng, (dof - 1.0) / 2.0, 1.0);
+    return make_double2(gauss, chi2);
     }
 
+// Bussi, Donadio and Parrinello (2007), eq. A7: with c = exp(-dt / tau) (0 for tau = 0) and
+// w = kT / (2 K), alpha^2 = c + (1 - c) w (chi2 + g^2) + 2 g sqrt(c (1 - c) w).
 __device__ inline double bussi_factor_from_draws(double K, double dof, double dt, double tau,
                                                  double set_T, double2 draws)
     {
     if (dt == 0.0 || dof == 0.0 || K <= 0.0)
         return 1.0;
-    double time_decay_factor = 0.0;
-    if (tau != 0.0)
-        time_decay_factor = exp(-dt / tau);
-    const double r_normal_one = draws.x;
-    const double r_gamma = draws.y;
-    const double v = set_T / 2.0 / K;
-    const double term1 = v * (1.0 - time_decay_factor) * (r_gamma + r_normal_one * r_normal_one);
-    const double term2
-        = 2.0 * r_normal_one * sqrt(v * (1.0 - time_decay_factor) * time_decay_factor);
-    return sqrt(time_decay_factor + term1 + term2);
+    const double c = tau != 0.0 ? exp(-dt / tau) : 0.0;
+    const double g = draws.x, chi2 = draws.y;
+    const double w = set_T / 2.0 / K;
+    const double stochastic = w * (1.0 - c) * (chi2 + g * g);
+    const double cross = 2.0 * g * sqrt(w * (1.0 - c) * c);
+    return sqrt(c + stochastic + cross);
     }
 
 __device__ inline double bussi_factor_d(double K, double dof, double dt, double tau, double set_T,

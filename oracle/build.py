@@ -23,7 +23,10 @@ import sys
 import sysconfig
 
 HERE = pathlib.Path(__file__).resolve().parent
-REF_ROOT = pathlib.Path(os.environ.get("HOOMD_REFERENCE_ROOT", "/root/reference"))
+# the reference source tree: $HOOMD_REFERENCE_ROOT, else a directory named "reference" beside
+# this repository's root
+REF_ROOT = pathlib.Path(os.environ.get("HOOMD_REFERENCE_ROOT",
+                                       str(HERE.parent.parent / "reference")))
 
 ORACLE_SRC = HERE / "md_oracle.cc"
 ORACLE_LIB = HERE / "_build" / "libmd_oracle.so"
