@@ -707,6 +707,13 @@ void PairForce::upload()
                                    cudaMemcpyHostToDevice, s),
                    "params");
         }
+    else if (kind == PairKind::Plugin)
+        {
+        d_params.resize(std::max<size_t>(1, plugin_params.size()));
+        cuda_check(cudaMemcpyAsync(d_params.get(), plugin_params.data(), plugin_params.size(),
+                                   cudaMemcpyHostToDevice, s),
+                   "params");
+        }
     else if (kind == PairKind::Example)
         {
         d_params.resize(np * sizeof(gb_example_param));
@@ -822,7 +829,15 @@ void PairForce::compute(cudaStream_t s, bool with_virial)
         }
     gb_pair_args a = pair_args(with_virial);
     int rc;
-    if (kind == PairKind::LJ)
+    if (kind == PairKind::Plugin)
+        {
+        gb_pair_plugin_call c {};
+        c.op = 0;
+        c.args = &a;
+        c.stream = s;
+        rc = plugin_call(c);
+        }
+    else if (kind == PairKind::LJ)
         rc = gb_pair_forces_lj(&a, (const gb_lj_param*)d_params.get(), s);
     else if (kind == PairKind::Example)
         rc = gb_pair_forces_example(&a, (const gb_example_param*)d_params.get(), s);
@@ -879,7 +894,17 @@ double PairForce::energy_between_sets(const std::vector<uint32_t>& tags1,
     parts.resize(nb);
     gb_pair_args a = pair_args(false);
     int rc;
-    if (kind == PairKind::LJ)
+    if (kind == PairKind::Plugin)
+        {
+        gb_pair_plugin_call c {};
+        c.op = 2;
+        c.args = &a;
+        c.sets = &sets;
+        c.d_partials = parts.get();
+        c.stream = s;
+        rc = plugin_call(c);
+        }
+    else if (kind == PairKind::LJ)
         rc = gb_pair_energy_sets_lj(&a, (const gb_lj_param*)d_params.get(), &sets, parts.get(),
                                     s);
     else if (kind == PairKind::Example)
@@ -901,8 +926,40 @@ double PairForce::energy_between_sets(const std::vector<uint32_t>& tags1,
     return u;
     }
 
+int PairForce::plugin_call(gb_pair_plugin_call& c)
+    {
+    if (!plugin || !plugin->call)
+        return GB_ERR_INVALID;
+    c.status = GB_OK;
+    const int rc = plugin->call(&c, d_params.get());
+    return rc != GB_OK ? rc : c.status;
+    }
+
+void PairForce::set_params_plugin(unsigned int i, unsigned int j, const void* record, size_t bytes)
+    {
+    if (kind != PairKind::Plugin || !plugin)
+        throw std::logic_error("set_params_plugin: not a plugin pair force");
+    if (bytes != plugin->param_size)
+        throw std::invalid_argument("plugin parameter record has the wrong size");
+    if (i >= ntypes || j >= ntypes)
+        throw std::invalid_argument("type index out of range");
+    const unsigned char* r = static_cast<const unsigned char*>(record);
+    std::copy(r, r + bytes, plugin_params.begin() + (size_t)(i * ntypes + j) * bytes);
+    std::copy(r, r + bytes, plugin_params.begin() + (size_t)(j * ntypes + i) * bytes);
+    params_dirty = true;
+    }
+
 int PairForce::launch_fused(const gb_pair_args& a, const gb_step_fuse& f, cudaStream_t s)
     {
+    if (kind == PairKind::Plugin)
+        {
+        gb_pair_plugin_call c {};
+        c.op = 1;
+        c.args = &a;
+        c.fuse = &f;
+        c.stream = s;
+        return plugin_call(c);
+        }
     if (kind == PairKind::LJ)
         return gb_md_pair_step_lj(&a, (const gb_lj_param*)d_params.get(), &f, s);
     if (kind == PairKind::Example)

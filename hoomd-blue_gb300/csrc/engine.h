@@ -172,6 +172,7 @@ class ParticleData
     DeviceArray<char> scratch;
     DeviceArray<char> io_stage; // snapshot staging block (gb_snapshot_stage_bytes(N) + 256)
     bool tags_set = false;      // the particles exist (tags hold a permutation of 0..N-1)
+    std::vector<std::string> type_names; // particle type names, by type id (when known)
     uint64_t sort_generation = 0;
 
     private:
@@ -251,7 +252,8 @@ enum class PairKind
     Example = 2,
     MLP = 3, // radial MLP surrogate of Table (unfused path: pair list + tensor-core tiles)
     Radial = 4, // the other radial evaluators (gb_radial_param.kind)
-    DPD = 5  // DPD thermostat pair forces (unfused: they read the velocities step two writes)
+    DPD = 5, // DPD thermostat pair forces (unfused: they read the velocities step two writes)
+    Plugin = 6 // an evaluator compiled in a plugin module (gb_pair_plugin)
     };
 
 class MlpSurrogate;
@@ -310,6 +312,11 @@ class PairForce
     std::vector<std::vector<double>> t_U, t_F;
     bool params_dirty = true;
     std::shared_ptr<MlpSurrogate> mlp;
+    // plugin evaluator: its record and ntypes^2 parameter records of param_size bytes each
+    const gb_pair_plugin* plugin = nullptr;
+    std::vector<unsigned char> plugin_params;
+    void set_params_plugin(unsigned int i, unsigned int j, const void* record, size_t bytes);
+    int plugin_call(gb_pair_plugin_call& c);
     DeviceArray<char> d_params, mlp_scratch, d_esum_scratch;
     DeviceArray<float> d_rcutsq, d_ronsq, d_table, force, virial;
     DeviceArray<double> d_esum;

@@ -1,6 +1,8 @@
 // pybind11 module _hoomd_gb300: the host engine classes under the names of the reference's
 // C++ classes that the Python layer looks up (hoomd/md/pair/pair.py:126-146,
 // hoomd/md/nlist.py:390-397, hoomd/md/integrate.py:287-293).
+#include <map>
+
 #include <pybind11/numpy.h>
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
@@ -56,6 +58,185 @@ py::array_t<double> force_by_tag(PairForce& f, int what)
     for (unsigned int t = 0; t < N; t++)
         o(t) = h[4 * (size_t)r[t] + 3];
     return out;
+    }
+// The reference's Python-facing pair force (export_PotentialPair[GPU]<E>,
+// hoomd/md/PotentialPair.h:1017-1036): the engine's PairForce plus per-type-pair parameters set
+// and read as dicts keyed by type names, r_cut / r_on per type pair, mode by name and the
+// tail-correction flag.
+struct PyPairForce : PairForce
+    {
+    PyPairForce(std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborList> nl, PairKind k,
+                int radial = -1, bool lj_dpd = false)
+        : PairForce(std::move(pd), std::move(nl), k), radial_kind(radial), dpd_is_lj(lj_dpd)
+        {
+        }
+    ~PyPairForce()
+        {
+        if (Py_IsInitialized())
+            {
+            py::gil_scoped_acquire gil;
+            py_params.clear();
+            to_bytes = py::object();
+            to_dict = py::object();
+            }
+        }
+    int radial_kind;     // the closed form of PairKind::Radial
+    bool dpd_is_lj;      // PairKind::DPD: DPDLJ (epsilon, sigma) instead of DPD (A)
+    bool tail_correction = false;
+    std::map<std::pair<unsigned int, unsigned int>, py::object> py_params; // as given
+    py::object to_bytes, to_dict; // PairKind::Plugin: param_type(dict) and param_type::asDict
+    };
+
+// parameter names of the radial closed forms, in gb_radial_param.v order (by radial kind)
+const std::vector<std::vector<const char*>>& radial_keys()
+    {
+    static const std::vector<std::vector<const char*>> k = {
+        {"epsilon", "sigma"},                       // 0 Gauss
+        {"epsilon", "kappa"},                       // 1 Yukawa
+        {"D0", "alpha", "r0"},                      // 2 Morse
+        {"sigma", "epsilon"},                       // 3 ForceShiftedLJ
+        {"epsilon", "sigma", "n", "m"},             // 4 Mie
+        {"epsilon", "sigma", "n", "m", "delta"},    // 5 ExpandedMie
+        {"sigma", "epsilon", "delta"},              // 6 ExpandedLJ
+        {"A", "rho", "C"},                          // 7 Buckingham
+        {"sigma", "epsilon"},                       // 8 LJ1208
+        {"sigma", "epsilon"},                       // 9 LJ0804
+        {"epsilon", "sigma", "r0"},                 // 10 LJGauss
+        {"epsilon", "sigma", "delta"},              // 11 ExpandedGaussian
+        {"C1", "C2", "eta1", "eta2", "k", "phi"},   // 12 OPP
+        {"sigma", "epsilon", "alpha"},              // 13 TWF
+        {"A"},                                      // 14 DPDConservative
+        {"kappa", "Z", "A", "a1", "a2"},            // 15 DLVO
+        {},                                         // 16 Fourier (a, b: three each)
+        {"qi", "qj", "aF"},                         // 17 Moliere
+        {"qi", "qj", "aF"},                         // 18 ZBL
+        {"epsilon", "eps_rf"},                      // 19 ReactionField
+        {"kappa"}};                                 // 20 Ewald (+ alpha, default 0)
+    return k;
+    }
+
+unsigned int type_of(const ParticleData& pd, const py::handle& h)
+    {
+    if (py::isinstance<py::str>(h))
+        {
+        const std::string name = h.cast<std::string>();
+        for (size_t t = 0; t < pd.type_names.size(); t++)
+            if (pd.type_names[t] == name)
+                return (unsigned int)t;
+        throw py::key_error("unknown particle type " + name);
+        }
+    const long t = h.cast<long>();
+    if (t < 0 || (unsigned long)t >= pd.ntypes)
+        throw py::index_error("particle type index out of range");
+    return (unsigned int)t;
+    }
+
+std::pair<unsigned int, unsigned int> type_pair(const PyPairForce& f, const py::tuple& t)
+    {
+    if (t.size() != 2)
+        throw py::value_error("a type pair is a tuple of two particle types");
+    unsigned int a = type_of(*f.pdata, t[0]), b = type_of(*f.pdata, t[1]);
+    return {std::min(a, b), std::max(a, b)};
+    }
+
+std::vector<double> doubles(const py::handle& h)
+    {
+    auto a = py::array_t<double, py::array::c_style | py::array::forcecast>::ensure(h);
+    if (!a)
+        throw py::value_error("expected an array of numbers");
+    return std::vector<double>(a.data(), a.data() + a.size());
+    }
+
+// PotentialPair<E>::setParamsPython: the evaluator's param_type from a dict
+void apply_params(PyPairForce& f, unsigned int i, unsigned int j, const py::dict& d)
+    {
+    auto num = [&](const char* k) {
+        if (!d.contains(k))
+            throw py::key_error(std::string("missing parameter ") + k);
+        return d[k].cast<double>();
+    };
+    switch (f.kind)
+        {
+    case PairKind::LJ:
+        f.set_params_lj(i, j, num("sigma"), num("epsilon"));
+        break;
+    case PairKind::Example:
+        f.set_params_example(i, j, num("k"), num("sigma"));
+        break;
+    case PairKind::Table:
+        {
+        std::vector<double> U = doubles(d["U"]), F = doubles(d["F"]);
+        if (U.size() != F.size())
+            throw py::value_error("The length of V and F arrays must be equal.");
+        if (U.empty())
+            throw py::value_error("The length of V and F must not be zero.");
+        f.set_params_table(i, j, num("r_min"), U, F);
+        break;
+        }
+    case PairKind::DPD:
+        if (f.dpd_is_lj)
+            f.set_params_dpd(i, j, true, num("epsilon"), num("sigma"), num("gamma"));
+        else
+            f.set_params_dpd(i, j, false, num("A"), 0.0, num("gamma"));
+        break;
+    case PairKind::Radial:
+        {
+        std::vector<double> v;
+        if (f.radial_kind == 16)
+            {
+            std::vector<double> a = doubles(d["a"]), b = doubles(d["b"]);
+            if (a.size() != 3 || b.size() != 3)
+                throw py::value_error("Fourier: a and b are three coefficients each");
+            v = {a[0], a[1], a[2], b[0], b[1], b[2]};
+            }
+        else
+            {
+            for (const char* k : radial_keys().at(f.radial_kind))
+                v.push_back(num(k));
+            if (f.radial_kind == 20)
+                v.push_back(d.contains("alpha") ? d["alpha"].cast<double>() : 0.0);
+            }
+        f.set_params_radial(i, j, (unsigned int)f.radial_kind, v);
+        break;
+        }
+    case PairKind::Plugin:
+        {
+        const std::string rec = py::bytes(f.to_bytes(d));
+        f.set_params_plugin(i, j, rec.data(), rec.size());
+        break;
+        }
+    default:
+        throw py::type_error("this pair force takes no per-type-pair parameters");
+        }
+    f.py_params[{i, j}] = py::dict(d);
+    }
+
+py::dict read_params(PyPairForce& f, unsigned int i, unsigned int j)
+    {
+    if (f.kind == PairKind::Plugin)
+        {
+        const size_t b = f.plugin->param_size;
+        const unsigned char* r = f.plugin_params.data() + (size_t)(i * f.ntypes + j) * b;
+        return f.to_dict(py::bytes(reinterpret_cast<const char*>(r), b));
+        }
+    auto it = f.py_params.find({i, j});
+    if (it == f.py_params.end())
+        throw py::key_error("parameters of this type pair are not set");
+    return py::dict(it->second);
+    }
+
+std::shared_ptr<PyPairForce> make_pair_force(std::shared_ptr<ParticleData> pd,
+                                             std::shared_ptr<NeighborList> nl, PairKind k,
+                                             int radial = -1, bool lj_dpd = false)
+    {
+    auto f = std::make_shared<PyPairForce>(std::move(pd), std::move(nl), k, radial, lj_dpd);
+    f->uses_charge = k == PairKind::Plugin;
+    return f;
+    }
+
+const char* mode_name(int m)
+    {
+    return m == 1 ? "shift" : (m == 2 ? "xplor" : "none");
     }
 } // namespace
 
@@ -125,6 +306,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def_readonly("ntypes", &ParticleData::ntypes)
         .def_readonly("ndim", &ParticleData::ndim)
         .def_readonly("sort_generation", &ParticleData::sort_generation)
+        .def_readwrite("types", &ParticleData::type_names)
         .def("getBox",
              [](ParticleData& pd) {
                  return std::vector<double>(pd.box6, pd.box6 + 6);
@@ -198,10 +380,14 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .value("Example", PairKind::Example)
         .value("MLP", PairKind::MLP)
         .value("Radial", PairKind::Radial)
-        .value("DPD", PairKind::DPD);
+        .value("DPD", PairKind::DPD)
+        .value("Plugin", PairKind::Plugin);
 
     py::class_<PairForce, std::shared_ptr<PairForce>>(m, "PotentialPairGPU")
-        .def(py::init<std::shared_ptr<ParticleData>, std::shared_ptr<NeighborList>, PairKind>())
+        .def(py::init([](std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborList> nl,
+                         PairKind k) -> std::shared_ptr<PairForce> {
+            return make_pair_force(std::move(pd), std::move(nl), k);
+        }))
         .def("setParamsLJ", &PairForce::set_params_lj)
         .def("setParamsExample", &PairForce::set_params_example)
         .def("setParamsTable", &PairForce::set_params_table)
@@ -220,11 +406,19 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setROn", &PairForce::set_r_on)
         .def("setSurrogate", [](PairForce& f, std::shared_ptr<MlpSurrogate> m) { f.mlp = m; })
         .def_property(
-            "mode", [](PairForce& f) { return f.shift_mode; },
-            [](PairForce& f, int v) {
-                if (v < 0 || v > 2)
-                    throw std::invalid_argument("mode must be 0 (none), 1 (shift) or 2 (xplor)");
-                f.shift_mode = v;
+            "mode", [](PairForce& f) { return std::string(mode_name(f.shift_mode)); },
+            [](PairForce& f, py::object v) {
+                int mv = -1;
+                if (py::isinstance<py::str>(v))
+                    {
+                    const std::string s = v.cast<std::string>();
+                    mv = s == "none" ? 0 : (s == "shift" ? 1 : (s == "xplor" ? 2 : -1));
+                    }
+                else
+                    mv = v.cast<int>();
+                if (mv < 0 || mv > 2)
+                    throw std::invalid_argument("mode must be 'none', 'shift' or 'xplor'");
+                f.shift_mode = mv;
                 f.params_dirty = true;
             })
         .def("compute", &PairForce::compute_standalone)
@@ -248,6 +442,110 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("getEnergies", [](PairForce& f) { return force_by_tag(f, 1); })
         .def("energySum", &PairForce::energy_sum)
         .def("getVirials", [](PairForce& f) { return force_by_tag(f, 2); });
+
+    // one class for every evaluator; the reference's per-evaluator class names
+    // (PotentialPair<Name>GPU, hoomd/md/pair/pair.py _cpp_class_name + "GPU") construct it
+    py::class_<PyPairForce, PairForce, std::shared_ptr<PyPairForce>>(m, "PotentialPairEvaluatorGPU")
+        .def("setParams",
+             [](PyPairForce& f, py::tuple typ, py::dict d) {
+                 auto ij = type_pair(f, typ);
+                 apply_params(f, ij.first, ij.second, d);
+             })
+        .def("getParams",
+             [](PyPairForce& f, py::tuple typ) {
+                 auto ij = type_pair(f, typ);
+                 return read_params(f, ij.first, ij.second);
+             })
+        .def("setRCut",
+             [](PyPairForce& f, py::tuple typ, double r) {
+                 auto ij = type_pair(f, typ);
+                 f.set_r_cut(ij.first, ij.second, r);
+             })
+        .def("getRCut",
+             [](PyPairForce& f, py::tuple typ) {
+                 auto ij = type_pair(f, typ);
+                 return (double)f.r_cut[ij.first * f.ntypes + ij.second];
+             })
+        .def("setROn",
+             [](PyPairForce& f, py::tuple typ, double r) {
+                 auto ij = type_pair(f, typ);
+                 f.set_r_on(ij.first, ij.second, r);
+             })
+        .def("getROn",
+             [](PyPairForce& f, py::tuple typ) {
+                 auto ij = type_pair(f, typ);
+                 return (double)f.r_on[ij.first * f.ntypes + ij.second];
+             })
+        .def_readwrite("tail_correction", &PyPairForce::tail_correction)
+        .def_property_readonly("evaluator_name", [](PyPairForce& f) {
+            return f.kind == PairKind::Plugin && f.plugin && f.plugin->name
+                       ? std::string(f.plugin->name)
+                       : std::string();
+        });
+    {
+    struct Named
+        {
+        const char* name;
+        PairKind kind;
+        int radial;
+        bool lj_dpd;
+        };
+    static const Named named[] = {
+        {"PotentialPairLJGPU", PairKind::LJ, -1, false},
+        {"PotentialPairTableGPU", PairKind::Table, -1, false},
+        {"PotentialPairExampleGPU", PairKind::Example, -1, false},
+        {"PotentialPairGaussGPU", PairKind::Radial, 0, false},
+        {"PotentialPairYukawaGPU", PairKind::Radial, 1, false},
+        {"PotentialPairMorseGPU", PairKind::Radial, 2, false},
+        {"PotentialPairForceShiftedLJGPU", PairKind::Radial, 3, false},
+        {"PotentialPairMieGPU", PairKind::Radial, 4, false},
+        {"PotentialPairExpandedMieGPU", PairKind::Radial, 5, false},
+        {"PotentialPairExpandedLJGPU", PairKind::Radial, 6, false},
+        {"PotentialPairBuckinghamGPU", PairKind::Radial, 7, false},
+        {"PotentialPairLJ1208GPU", PairKind::Radial, 8, false},
+        {"PotentialPairLJ0804GPU", PairKind::Radial, 9, false},
+        {"PotentialPairLJGaussGPU", PairKind::Radial, 10, false},
+        {"PotentialPairExpandedGaussianGPU", PairKind::Radial, 11, false},
+        {"PotentialPairOPPGPU", PairKind::Radial, 12, false},
+        {"PotentialPairTWFGPU", PairKind::Radial, 13, false},
+        {"PotentialPairConservativeDPDGPU", PairKind::Radial, 14, false},
+        {"PotentialPairDLVOGPU", PairKind::Radial, 15, false},
+        {"PotentialPairFourierGPU", PairKind::Radial, 16, false},
+        {"PotentialPairMoliereGPU", PairKind::Radial, 17, false},
+        {"PotentialPairZBLGPU", PairKind::Radial, 18, false},
+        {"PotentialPairReactionFieldGPU", PairKind::Radial, 19, false},
+        {"PotentialPairEwaldGPU", PairKind::Radial, 20, false},
+        {"PotentialPairDPDThermoDPDGPU", PairKind::DPD, -1, false},
+        {"PotentialPairDPDThermoLJGPU", PairKind::DPD, -1, true}};
+    for (const Named& n : named)
+        {
+        const Named c = n;
+        m.def(c.name,
+              [c](std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborList> nl) {
+                  return make_pair_force(std::move(pd), std::move(nl), c.kind, c.radial,
+                                         c.lj_dpd);
+              },
+              py::arg("sysdef"), py::arg("nlist"));
+        }
+    }
+    // a plugin evaluator's pair force: built by the plugin module's export_PotentialPairGPU<E>
+    // (include/hoomd/md/PotentialPairGPU.h) from its gb_pair_plugin record and its param_type
+    // conversions
+    m.def("PotentialPairPluginGPU",
+          [](std::shared_ptr<ParticleData> pd, std::shared_ptr<NeighborList> nl, py::capsule rec,
+             py::object to_bytes, py::object to_dict) {
+              if (std::string(rec.name() ? rec.name() : "") != "gb_pair_plugin")
+                  throw py::type_error("expected a gb_pair_plugin capsule");
+              const auto* r = static_cast<const gb_pair_plugin*>(rec.get_pointer());
+              if (!r || r->abi != GB_PAIR_PLUGIN_ABI || !r->call || r->param_size == 0)
+                  throw py::value_error("pair plugin record of an incompatible ABI version");
+              auto f = make_pair_force(std::move(pd), std::move(nl), PairKind::Plugin);
+              f->plugin = r;
+              f->plugin_params.assign((size_t)f->ntypes * f->ntypes * r->param_size, 0);
+              f->to_bytes = std::move(to_bytes);
+              f->to_dict = std::move(to_dict);
+              return f;
+          });
 
     py::class_<Integrator, std::shared_ptr<Integrator>>(m, "IntegratorTwoStep")
         .def(py::init<std::shared_ptr<ParticleData>, std::shared_ptr<NeighborList>, double>())

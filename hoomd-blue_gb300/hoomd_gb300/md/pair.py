@@ -1,11 +1,16 @@
-"""Pair forces (hoomd/md/pair/pair.py): ``Pair`` with ``LJ`` and ``Table``, plus ``ExamplePair``,
-the evaluator of the reference's pair-plugin template
-(example_plugins/pair_plugin/EvaluatorPairExample.h), as a worked plugin.
+"""Pair forces (hoomd/md/pair/pair.py): ``Pair`` with ``LJ``, ``Table``, the other radial
+potentials, DPD, and ``ExamplePair``, the evaluator of the reference's pair-plugin template
+(example_plugins/pair_plugin/EvaluatorPairExample.h).
 
 Attribute names, parameter keys, accepted modes and the per-particle outputs (``forces``,
-``energies``, ``virials``, ``energy``) follow the reference. On attach each force becomes a
-PotentialPairGPU engine object; its kernels are instantiated per evaluator
-(gb_pair_forces_lj / _table / _example in include/hoomd_gb300.h).
+``energies``, ``virials``, ``energy``) follow the reference. On attach each force looks up its
+engine class as the reference does (hoomd/md/pair/pair.py:126-146): ``_ext_module`` (this
+package's compiled module, or a plugin's own module) and ``_cpp_class_name`` + "GPU", constructed
+from the state and the neighbour list; every type pair's parameters then go through the engine
+object's ``setParams((a, b), dict)``, ``setRCut`` and ``setROn`` (PotentialPair<E>'s pybind
+methods, hoomd/md/PotentialPair.h:1017-1036). A plugin's Python class declares its parameters
+with ``hoomd_gb300.data.TypeParameter`` / ``TypeParameterDict`` and ``_add_typeparam``, as
+example_plugins/pair_plugin/pair.py does.
 """
 
 import numpy as np
@@ -20,7 +25,8 @@ class Pair:
     """Base pair force (hoomd/md/pair/pair.py:18-161)."""
 
     _accepted_modes = ("none", "shift", "xplor")
-    _kind = None
+    _ext_module = _hoomd_gb300
+    _cpp_class_name = None
     _loggables = {"energy": "scalar", "energies": "particle", "forces": "particle",
                   "torques": "particle", "virials": "particle", "additional_energy": "scalar",
                   "additional_virial": "sequence"}
@@ -46,7 +52,7 @@ class Pair:
             raise ValueError(f"mode must be one of {self._accepted_modes}")
         self._mode = m
         if self._cpp_obj is not None:
-            self._cpp_obj.mode = _MODES[m]
+            self._cpp_obj.mode = m
             self._update_tail()
 
     def _tail_coefficients(self, state):
@@ -74,17 +80,25 @@ class Pair:
         w = self._cpp_obj.tailVirial()
         return [w, 0.0, 0.0, w, 0.0, w]
 
-    def _set_pair_params(self, cpp, i, j, value):
-        raise NotImplementedError
+    def _add_typeparam(self, typeparam):
+        """Expose a ``hoomd_gb300.data.TypeParameter`` as the attribute of its name (the
+        reference's Operation._add_typeparam)."""
+        setattr(self, typeparam.name, typeparam.make_container())
+
+    def _cpp_params(self, value):
+        """The dict handed to the engine object's setParams for one type pair."""
+        return dict(value)
 
     def _attach(self, simulation, cpp_nlist):
         self._simulation = simulation
         self._standalone = False
         state = simulation.state
-        self._cpp_obj = _hoomd_gb300.PotentialPairGPU(state._cpp_pdata, cpp_nlist, self._kind)
-        self._cpp_obj.mode = _MODES[self._mode]
+        cls = getattr(self._ext_module, self._cpp_class_name + "GPU")
+        self._cpp_obj = cls(state._cpp_pdata, cpp_nlist)
+        self._cpp_obj.mode = self._mode
         types = state.particle_types
-        self._cpp_obj.useCharge = bool(self._needs_charge(types))
+        if self._cpp_obj.useCharge is False:
+            self._cpp_obj.useCharge = bool(self._needs_charge(types))
         self._send_params()
         # parameters set after attaching reach the engine before the next step
         for d in (self.params, self.r_cut, self.r_on):
@@ -103,13 +117,13 @@ class Pair:
                     value = self.params[(a, b)]
                 except KeyError:
                     raise RuntimeError(f"{type(self).__name__}: params[({a!r}, {b!r})] is not set")
-                self._set_pair_params(self._cpp_obj, i, j, value)
+                self._cpp_obj.setParams((a, b), self._cpp_params(value))
                 try:
                     rc = self.r_cut[(a, b)]
                 except KeyError:
                     raise RuntimeError(f"{type(self).__name__}: r_cut[({a!r}, {b!r})] is not set")
-                self._cpp_obj.setRCut(i, j, float(rc))
-                self._cpp_obj.setROn(i, j, float(self.r_on[(a, b)]))
+                self._cpp_obj.setRCut((a, b), float(rc))
+                self._cpp_obj.setROn((a, b), float(self.r_on[(a, b)]))
         self._update_tail()
 
     def _typeparam_changed(self, key):
@@ -187,7 +201,7 @@ class Pair:
 class LJ(Pair):
     """Lennard-Jones (hoomd/md/pair/pair.py:163-228); params: epsilon, sigma."""
 
-    _kind = _hoomd_gb300.PairKind.LJ
+    _cpp_class_name = "PotentialPairLJ"
 
     def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none',
                  tail_correction=False):
@@ -203,10 +217,14 @@ class LJ(Pair):
     @tail_correction.setter
     def tail_correction(self, value):
         self._tail_correction = bool(value)
+        if self._cpp_obj is not None:
+            self._cpp_obj.tail_correction = self._tail_correction
         self._update_tail()
 
-    def _set_pair_params(self, cpp, i, j, v):
-        cpp.setParamsLJ(i, j, v["sigma"], v["epsilon"])
+    def _attach(self, simulation, cpp_nlist):
+        obj = super()._attach(simulation, cpp_nlist)
+        obj.tail_correction = self._tail_correction
+        return obj
 
     def _tail_coefficients(self, state):
         """PotentialPair::computeTailCorrection (hoomd/md/PotentialPair.h:255-341) with the LJ
@@ -241,7 +259,7 @@ class LJ(Pair):
 class Table(Pair):
     """Tabulated potential (hoomd/md/pair/pair.py:520-619); params: r_min, U, F. Mode 'none'."""
 
-    _kind = _hoomd_gb300.PairKind.Table
+    _cpp_class_name = "PotentialPairTable"
     _accepted_modes = ("none",)
 
     def __init__(self, nlist, default_r_cut=None):
@@ -249,28 +267,25 @@ class Table(Pair):
         self.params = TypePairDict(validator=dict_validator(("r_min", "U", "F"),
                                                             arrays=("U", "F")))
 
-    def _set_pair_params(self, cpp, i, j, v):
+    def _cpp_params(self, v):
         U = np.asarray(v["U"], np.float64)
         F = np.asarray(v["F"], np.float64)
         if U.shape != F.shape or U.ndim != 1:
             raise RuntimeError("The length of V and F arrays must be equal.")
         if len(U) == 0:
             raise RuntimeError("The length of V and F must not be zero.")
-        cpp.setParamsTable(i, j, float(v["r_min"]), U.tolist(), F.tolist())
+        return dict(r_min=float(v["r_min"]), U=U, F=F)
 
 
 class ExamplePair(Pair):
     """The reference's pair-plugin example evaluator: V = k/2 (sigma - r)^2 inside r_cut
     (example_plugins/pair_plugin/pair.py:15-28); params: k, sigma."""
 
-    _kind = _hoomd_gb300.PairKind.Example
+    _cpp_class_name = "PotentialPairExample"
 
     def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
         super().__init__(nlist, default_r_cut, default_r_on, mode)
         self.params = TypePairDict(validator=dict_validator(("k", "sigma")))
-
-    def _set_pair_params(self, cpp, i, j, v):
-        cpp.setParamsExample(i, j, v["k"], v["sigma"])
 
 
 class TableSurrogate(Pair):
@@ -280,7 +295,6 @@ class TableSurrogate(Pair):
     closer than its r_min feel no force, as in ``Table``. Mode 'none', no virials. On attach the
     force becomes a PotentialPairGPU of kind MLP (gb_mlp_forces in include/hoomd_gb300.h)."""
 
-    _kind = _hoomd_gb300.PairKind.MLP
     _accepted_modes = ("none",)
 
     def __init__(self, nlist, surrogate):
@@ -295,7 +309,8 @@ class TableSurrogate(Pair):
         if ntypes != self.surrogate.ntypes:
             raise RuntimeError(f"the surrogate was trained for {self.surrogate.ntypes} types, "
                                f"the state has {ntypes}")
-        self._cpp_obj = _hoomd_gb300.PotentialPairGPU(state._cpp_pdata, cpp_nlist, self._kind)
+        self._cpp_obj = _hoomd_gb300.PotentialPairGPU(state._cpp_pdata, cpp_nlist,
+                                                      _hoomd_gb300.PairKind.MLP)
         self._cpp_obj.setSurrogate(self.surrogate._cpp)
         for i in range(ntypes):
             for j in range(i, ntypes):
@@ -312,21 +327,22 @@ class _Radial(Pair):
     in include/hoomd_gb300.h selects the closed form by kind). Parameter keys and modes follow
     hoomd.md.pair."""
 
-    _kind = _hoomd_gb300.PairKind.Radial
-    _radial_kind = None
     _keys = ()
 
     def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
         super().__init__(nlist, default_r_cut, default_r_on, mode)
         self.params = TypePairDict(validator=dict_validator(self._keys))
 
-    def _set_pair_params(self, cpp, i, j, v):
-        cpp.setParamsRadial(i, j, self._radial_kind, [float(v[k]) for k in self._keys])
+
+# the reference's engine class of each radial potential (hoomd/md/pair/pair.py _cpp_class_name)
+_CPP_NAMES = {"Gaussian": "PotentialPairGauss", "DPDConservative": "PotentialPairConservativeDPD"}
 
 
 def _radial(name, kind, keys, doc, modes=("none", "shift", "xplor")):
     cls = type(name, (_Radial,), {"_radial_kind": kind, "_keys": tuple(keys),
-                                  "_accepted_modes": modes, "__doc__": doc})
+                                  "_accepted_modes": modes, "__doc__": doc,
+                                  "_cpp_class_name": _CPP_NAMES.get(name,
+                                                                    "PotentialPair" + name)})
     cls.__module__ = __name__
     return cls
 
@@ -374,17 +390,12 @@ class Fourier(_Radial):
     coefficients of n = 2, 3, 4 (those of n = 1 make the force and energy vanish at r_c)."""
 
     _radial_kind = 16
+    _cpp_class_name = "PotentialPairFourier"
     _accepted_modes = ("none", "xplor")
 
     def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
         super().__init__(nlist, default_r_cut, default_r_on, mode)
         self.params = TypePairDict(validator=dict_validator(("a", "b"), arrays=("a", "b")))
-
-    def _set_pair_params(self, cpp, i, j, v):
-        a, b = np.asarray(v["a"], np.float64), np.asarray(v["b"], np.float64)
-        if a.shape != (3,) or b.shape != (3,):
-            raise ValueError("Fourier: a and b are three coefficients each")
-        cpp.setParamsRadial(i, j, self._radial_kind, [float(x) for x in (*a, *b)])
 
 
 class ReactionField(_Radial):
@@ -394,14 +405,12 @@ class ReactionField(_Radial):
     pair (one kernel instantiation scales all pairs or none)."""
 
     _radial_kind = 19
+    _cpp_class_name = "PotentialPairReactionField"
 
     def __init__(self, nlist, default_r_cut=None, default_r_on=0., mode='none'):
         super().__init__(nlist, default_r_cut, default_r_on, mode)
         self.params = TypePairDict(validator=dict_validator(("epsilon", "eps_rf"),
                                                             optional={"use_charge": False}))
-
-    def _set_pair_params(self, cpp, i, j, v):
-        cpp.setParamsRadial(i, j, self._radial_kind, [float(v["epsilon"]), float(v["eps_rf"])])
 
     def _needs_charge(self, types):
         flags = {bool(self.params[(a, b)].get("use_charge")) for a in types for b in types}
@@ -417,6 +426,7 @@ class Ewald(_Radial):
     is the plain erfc(kappa r) / r. Reads the particle charges."""
 
     _radial_kind = 20
+    _cpp_class_name = "PotentialPairEwald"
     _keys = ("kappa", "alpha")
     _accepted_modes = ("none",)
 
@@ -434,8 +444,6 @@ class _DPDBase(Pair):
     random numbers come from both particles' tags and the timestep. They read the velocities, so
     the integrator runs them on its unfused path."""
 
-    _kind = _hoomd_gb300.PairKind.DPD
-    _lj = False
 
     def __init__(self, nlist, kT, default_r_cut=None, mode='none'):
         super().__init__(nlist, default_r_cut, 0.0, mode)
@@ -461,24 +469,20 @@ class DPD(_DPDBase):
     """DPD (EvaluatorPairDPDThermoDPD.h): conservative force A (1 - r/r_c), drag
     -gamma w^2 (r . v) / r and random force sqrt(6 gamma kT / dt) w alpha, w = 1 - r/r_c."""
 
+    _cpp_class_name = "PotentialPairDPDThermoDPD"
     _accepted_modes = ("none",)
 
     def __init__(self, nlist, kT, default_r_cut=None):
         super().__init__(nlist, kT, default_r_cut, 'none')
         self.params = TypePairDict(validator=dict_validator(("A", "gamma")))
 
-    def _set_pair_params(self, cpp, i, j, v):
-        cpp.setParamsDPD(i, j, False, float(v["A"]), 0.0, float(v["gamma"]))
-
 
 class DPDLJ(_DPDBase):
     """DPD thermostat with a Lennard-Jones conservative force (EvaluatorPairDPDThermoLJ.h)."""
 
+    _cpp_class_name = "PotentialPairDPDThermoLJ"
     _accepted_modes = ("none", "shift")
 
     def __init__(self, nlist, kT, default_r_cut=None, mode='none'):
         super().__init__(nlist, kT, default_r_cut, mode)
         self.params = TypePairDict(validator=dict_validator(("epsilon", "sigma", "gamma")))
-
-    def _set_pair_params(self, cpp, i, j, v):
-        cpp.setParamsDPD(i, j, True, float(v["epsilon"]), float(v["sigma"]), float(v["gamma"]))

@@ -20,6 +20,7 @@ class State:
             int(p.N), len(self._types), int(self._dimensions),
             [float(x) for x in snapshot.configuration.box], [1, 1, 1])
         self._cpp_pdata.seed = simulation.seed & 0xFFFF
+        self._cpp_pdata.types = list(self._types)
         self._cpp_pdata.timestep = simulation._initial_timestep
         self._topology = _copy_topology(snapshot)
         self._topology_version = 0

@@ -785,6 +785,41 @@ typedef struct gb_mlp_force_args
 size_t gb_mlp_forces_scratch_bytes(unsigned int N, unsigned int Nmax);
 int gb_mlp_forces(const gb_mlp_force_args* args, void* stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Pair-evaluator plugins. The reference's example_plugins/pair_plugin compiles an evaluator with
+ * the reference's concept (EvaluatorPairExample.h: param_type, a three-argument constructor,
+ * evalForceAndEnergy, ...) into its own module: PotentialPairExampleGPUKernel.cu explicitly
+ * instantiates gpu_compute_pair_forces<Evaluator> (hoomd/md/PotentialPairGPU.cuh:579-656) and
+ * module.cc calls export_PotentialPairGPU<Evaluator> (example_plugins/pair_plugin/module.cc:
+ * 20-26). The headers under include/hoomd/ give those two files the same names here: the
+ * instantiation compiles this library's pair kernels for the evaluator, and the export hands the
+ * engine one gb_pair_plugin record. Every kernel call of the evaluator goes through its `call`
+ * function with one gb_pair_plugin_call.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct gb_pair_plugin_call
+    {
+    int op;                        /* 0: forces (+ virial if args->compute_virial), as
+                                      gb_pair_forces_*; 1: the fused pair step, as
+                                      gb_md_pair_step_*; 2: energy between sets, as
+                                      gb_pair_energy_sets_* */
+    const gb_pair_args* args;
+    const gb_step_fuse* fuse;      /* op 1 */
+    const gb_energy_sets* sets;    /* op 2 */
+    double* d_partials;            /* op 2 */
+    void* stream;
+    int status;                    /* out: GB_OK or the gb_status of the failure */
+    } gb_pair_plugin_call;
+
+#define GB_PAIR_PLUGIN_ABI 1
+typedef struct gb_pair_plugin
+    {
+    uint32_t abi;                  /* GB_PAIR_PLUGIN_ABI */
+    uint32_t param_size;           /* sizeof(Evaluator::param_type) at FP32 */
+    /* runs one call on the evaluator's kernels; d_params: ntypes^2 param_type records */
+    int (*call)(gb_pair_plugin_call* call, const void* d_params);
+    const char* name;              /* Evaluator::getName() */
+    } gb_pair_plugin;
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,6 +29,23 @@ def test_engine_module_imports():
         assert hasattr(hoomd_gb300._hoomd_gb300, cls)
 
 
+def test_every_pair_force_has_its_reference_engine_class():
+    """Each md.pair class finds its engine class as the reference's does
+    (hoomd/md/pair/pair.py:126-146: _ext_module, _cpp_class_name + "GPU")."""
+    import inspect
+
+    from hoomd_gb300.md import pair
+    names = []
+    for name, cls in vars(pair).items():
+        if inspect.isclass(cls) and issubclass(cls, pair.Pair) and cls._cpp_class_name:
+            assert hasattr(cls._ext_module, cls._cpp_class_name + "GPU"), name
+            names.append(cls._cpp_class_name)
+    for ref in ("PotentialPairLJ", "PotentialPairTable", "PotentialPairGauss", "PotentialPairYukawa",
+                "PotentialPairEwald", "PotentialPairDPDThermoDPD", "PotentialPairConservativeDPD",
+                "PotentialPairLJGauss", "PotentialPairReactionField", "PotentialPairFourier"):
+        assert ref in names, ref
+
+
 @pytest.mark.parametrize("box6", [(16.957, 16.957, 16.957, 0, 0, 0), (10, 11, 12, 0.3, -0.2, 0.1),
                                   (107.67, 107.67, 107.67, 0, 0, 0)])
 def test_box_make_matches_oracle_fp32(box6):
