@@ -1563,14 +1563,15 @@ void Integrator::sort_particles()
     {
     ParticleData& pd = *pdata;
     cudaStream_t s = pd.stream;
-    const size_t need = gb_sfc_scratch_bytes(pd.N, sort_bits);
+    const size_t need = gb_sfc_scratch_bytes_dim(pd.N, sort_bits, pd.ndim == 2 ? 2 : 3);
     if (pd.scratch.size() < need + 4 * (size_t)pd.N + 256)
         {
         pd.scratch.resize(need + 4 * (size_t)pd.N + 256);
         pd.scratch.zero(s);
         }
     uint32_t* order = reinterpret_cast<uint32_t*>(pd.scratch.get() + need);
-    check(gb_sfc_order(pd.pos.get(), pd.N, &pd.box, sort_bits, order, pd.scratch.get(), need, s),
+    check(gb_sfc_order_dim(pd.pos.get(), pd.N, &pd.box, sort_bits, pd.ndim == 2 ? 2 : 3, order,
+                           pd.scratch.get(), need, s),
           "gb_sfc_order");
     pd.alt.resize(4 * (size_t)pd.N);
     auto apply = [&](void* arr, unsigned int bytes) {

@@ -1,14 +1,23 @@
-// Space-filling-curve particle sort (replaces SFCPackTunerGPU: hoomd/SFCPackTunerGPU.cu:26-160
-// bins particles on a grid^3 lattice, orders them along a Hilbert curve with thrust::sort_by_key
-// and gathers every per-particle array).
+// Space-filling-curve particle sort (replaces SFCPackTunerGPU: hoomd/SFCPackTunerGPU.cu:26-160,
+// hoomd/SFCPackTuner.cc:289-486): particles are binned on a grid^3 lattice of the box, ordered by
+// the position of their bin along the reference's Hilbert traversal, ties by old index, and every
+// per-particle array is gathered into the new order.
 //
-// Here the Hilbert index of each particle's grid cell is computed arithmetically with Skilling's
-// transpose algorithm (J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004)
-// instead of the reference's recursive traversal table, and the order is produced by a counting
-// sort over the grid^3 buckets: histogram, exclusive scan, scatter. Buckets are far smaller than
-// a particle's volume at liquid densities, so ties are rare; a final pass orders the members of
-// any shared bucket by old index, which makes the permutation deterministic.
+// The reference builds the traversal as a grid^3 table by recursion (SFCPackTuner::
+// generateTraversalOrder): a cube is split into eight octants visited in the order `cell_order`,
+// and octant m's own order is cell_order permuted by rule m. Here the position of a bin along
+// that traversal is computed directly: the orders the recursion can reach form a small set of
+// states, so a state table (state, octant) -> (rank among the eight children, next state), built
+// once on the host by walking the rules from the identity order, turns the bin's coordinates into
+// its traversal position with one table step per level (8 levels for the default grid of 256).
+// The order then comes from a counting sort over the grid^3 buckets: histogram, exclusive scan,
+// scatter, and a pass that orders the members of a shared bucket by old index (the reference
+// sorts (key, index) pairs). In two dimensions the reference orders bins row by row
+// (SFCPackTuner::getSortedOrder2D, grid 4096), and so does this sort.
 #include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "gb_device.cuh"
 #include "gb_host.h"
@@ -18,47 +27,75 @@ namespace gb
 namespace
 {
 constexpr unsigned int SCAN_TILE = 4096; // elements per block in the scan (1024 threads x 4)
+constexpr int MAX_STATES = 64;
 
-// Skilling: axes -> transposed Hilbert index, then interleave to a 3*bits-bit key.
-__device__ inline uint32_t hilbert3(uint32_t x, uint32_t y, uint32_t z, int bits)
+// Octant o of a cube at (x, y, z) offsets (the reference's istep / jstep / kstep walking tables:
+// a Gray-code tour of the eight corners).
+constexpr int OCT_X[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+constexpr int OCT_Y[8] = {0, 0, 1, 1, 1, 1, 0, 0};
+constexpr int OCT_Z[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+// Permutation rules: the order inside child m is child[k] = parent[RULE[m][k]]
+// (SFCPackTuner.cc permute1 ... permute8).
+constexpr int RULE[8][8] = {{0, 3, 4, 7, 6, 5, 2, 1}, {0, 7, 6, 1, 2, 5, 4, 3},
+                            {0, 7, 6, 1, 2, 5, 4, 3}, {2, 3, 0, 1, 6, 7, 4, 5},
+                            {2, 3, 0, 1, 6, 7, 4, 5}, {4, 3, 2, 5, 6, 1, 0, 7},
+                            {4, 3, 2, 5, 6, 1, 0, 7}, {6, 5, 2, 1, 0, 3, 4, 7}};
+
+// rank[state][octant]: which child (0..7) visits that octant; next[state][rank]: the child's state
+struct HilbertTable
     {
-    uint32_t X[3] = {x, y, z};
-    const uint32_t M = 1u << (bits - 1);
-    // inverse undo
-    for (uint32_t Q = M; Q > 1; Q >>= 1)
-        {
-        const uint32_t P = Q - 1;
-        for (int i = 0; i < 3; i++)
+    uint8_t rank[MAX_STATES][8];
+    uint8_t next[MAX_STATES][8];
+    };
+
+const HilbertTable& hilbert_table()
+    {
+    static HilbertTable table;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        std::vector<std::vector<int>> states;
+        states.push_back({0, 1, 2, 3, 4, 5, 6, 7});
+        std::memset(&table, 0, sizeof(table));
+        for (size_t s = 0; s < states.size(); s++)
             {
-            if (X[i] & Q)
-                X[0] ^= P;
-            else
+            const std::vector<int> order = states[s];
+            for (int m = 0; m < 8; m++)
                 {
-                const uint32_t t = (X[0] ^ X[i]) & P;
-                X[0] ^= t;
-                X[i] ^= t;
+                table.rank[s][order[m]] = (uint8_t)m;
+                std::vector<int> child(8);
+                for (int k = 0; k < 8; k++)
+                    child[k] = order[RULE[m][k]];
+                size_t c = 0;
+                while (c < states.size() && states[c] != child)
+                    c++;
+                if (c == states.size())
+                    states.push_back(child);
+                table.next[s][m] = (uint8_t)c;
                 }
             }
-        }
-    // Gray encode
-    for (int i = 1; i < 3; i++)
-        X[i] ^= X[i - 1];
-    uint32_t t = 0;
-    for (uint32_t Q = M; Q > 1; Q >>= 1)
-        if (X[2] & Q)
-            t ^= Q - 1;
-    for (int i = 0; i < 3; i++)
-        X[i] ^= t;
-    // interleave: bit b of X[i] -> key bit 3*b + (2 - i)
-    uint32_t key = 0;
+        });
+    return table;
+    }
+
+// position of bin (x, y, z) of a 2^bits grid along the traversal
+__device__ inline uint32_t hilbert_rank(const HilbertTable& t, uint32_t x, uint32_t y, uint32_t z,
+                                        int bits)
+    {
+    uint32_t key = 0, state = 0;
     for (int b = bits - 1; b >= 0; b--)
-        for (int i = 0; i < 3; i++)
-            key = (key << 1) | ((X[i] >> b) & 1u);
+        {
+        const uint32_t bx = (x >> b) & 1u, by = (y >> b) & 1u, bz = (z >> b) & 1u;
+        // octant id from the corner bits (inverse of the Gray-code tour)
+        const uint32_t oct = bx ? (by ? 4u + bz : 7u - bz) : (by ? 3u - bz : bz);
+        const uint32_t m = t.rank[state][oct];
+        key = (key << 3) | m;
+        state = t.next[state][m];
+        }
     return key;
     }
 
 __global__ void k_sfc_keys(const float4* __restrict__ pos, unsigned int N, gb_box box, int bits,
-                           uint32_t* keys, uint32_t* hist)
+                           unsigned int ndim, HilbertTable table, uint32_t* keys, uint32_t* hist)
     {
     const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N)
@@ -66,11 +103,19 @@ __global__ void k_sfc_keys(const float4* __restrict__ pos, unsigned int N, gb_bo
     const float4 p = pos[i];
     float fx, fy, fz;
     make_fraction(box, p.x, p.y, p.z, fx, fy, fz);
-    const int G = 1 << bits;
-    int c[3] = {(int)(fx * G), (int)(fy * G), (int)(fz * G)};
-    for (int d = 0; d < 3; d++)
-        c[d] = c[d] < 0 ? 0 : (c[d] >= G ? G - 1 : c[d]);
-    const uint32_t key = hilbert3(c[0], c[1], c[2], bits);
+    const uint32_t G = 1u << bits;
+    // (unsigned int)(f * grid) % grid, as the reference bins (a fraction that rounds to 1 lands
+    // in bin 0)
+    const uint32_t cx = __float2uint_rz(fmul(fx, (float)G)) % G;
+    const uint32_t cy = __float2uint_rz(fmul(fy, (float)G)) % G;
+    uint32_t key;
+    if (ndim == 2)
+        key = cx * G + cy;
+    else
+        {
+        const uint32_t cz = __float2uint_rz(fmul(fz, (float)G)) % G;
+        key = hilbert_rank(table, cx, cy, cz, bits);
+        }
     keys[i] = key;
     atomicAdd(&hist[key], 1u);
     }
@@ -218,10 +263,10 @@ struct alignas(4) b12
     };
 } // namespace
 
-static size_t sfc_layout(unsigned int N, int bits, size_t* off_keys, size_t* off_hist,
-                         size_t* off_tiles)
+static size_t sfc_layout(unsigned int N, int bits, unsigned int ndim, size_t* off_keys,
+                         size_t* off_hist, size_t* off_tiles)
     {
-    const size_t nbins = (size_t)1 << (3 * bits);
+    const size_t nbins = (size_t)1 << ((ndim == 2 ? 2 : 3) * bits);
     const size_t ntiles = (nbins + SCAN_TILE - 1) / SCAN_TILE;
     size_t o = 0;
     *off_keys = o;
@@ -238,19 +283,27 @@ using namespace gb;
 
 extern "C"
     {
-    size_t gb_sfc_scratch_bytes(unsigned int N, int grid_bits)
+    size_t gb_sfc_scratch_bytes_dim(unsigned int N, int grid_bits, unsigned int ndim)
         {
         size_t a, b, c;
-        return sfc_layout(N, grid_bits, &a, &b, &c);
+        return sfc_layout(N, grid_bits, ndim, &a, &b, &c);
         }
 
-    int gb_sfc_order(const float* d_pos, unsigned int N, const gb_box* box, int grid_bits,
-                     uint32_t* d_order, void* d_scratch, size_t scratch_bytes, void* stream)
+    size_t gb_sfc_scratch_bytes(unsigned int N, int grid_bits)
+        {
+        return gb_sfc_scratch_bytes_dim(N, grid_bits, 3);
+        }
+
+    int gb_sfc_order_dim(const float* d_pos, unsigned int N, const gb_box* box, int grid_bits,
+                         unsigned int ndim, uint32_t* d_order, void* d_scratch,
+                         size_t scratch_bytes, void* stream)
         {
         GB_REQUIRE(box && d_order && d_scratch && (d_pos || N == 0), "gb_sfc_order: null argument");
-        GB_REQUIRE(grid_bits >= 1 && grid_bits <= 9, "gb_sfc_order: 1 <= grid_bits <= 9");
+        GB_REQUIRE(ndim == 2 || ndim == 3, "gb_sfc_order: ndim must be 2 or 3");
+        GB_REQUIRE(grid_bits >= 1 && grid_bits <= (ndim == 2 ? 12 : 9),
+                   "gb_sfc_order: 1 <= grid_bits <= 9 (3D) or 12 (2D)");
         size_t ok, oh, ot;
-        const size_t need = sfc_layout(N, grid_bits, &ok, &oh, &ot);
+        const size_t need = sfc_layout(N, grid_bits, ndim, &ok, &oh, &ot);
         GB_REQUIRE(scratch_bytes >= need, "gb_sfc_order: scratch too small");
         if (N == 0)
             return GB_OK;
@@ -259,18 +312,25 @@ extern "C"
         uint32_t* keys = reinterpret_cast<uint32_t*>(base + ok);
         uint32_t* hist = reinterpret_cast<uint32_t*>(base + oh);
         uint32_t* tiles = reinterpret_cast<uint32_t*>(base + ot);
-        const size_t nbins = (size_t)1 << (3 * grid_bits);
+        const size_t nbins = (size_t)1 << ((ndim == 2 ? 2 : 3) * grid_bits);
         const unsigned int ntiles = (unsigned int)((nbins + SCAN_TILE - 1) / SCAN_TILE);
         if (cudaMemsetAsync(hist, 0, nbins * 4, s) != cudaSuccess)
             return fail(GB_ERR_CUDA, "gb_sfc_order: memset");
         k_sfc_keys<<<div_up(N, 256), 256, 0, s>>>(reinterpret_cast<const float4*>(d_pos), N, *box,
-                                                  grid_bits, keys, hist);
+                                                  grid_bits, ndim, hilbert_table(), keys, hist);
         k_scan_tile<<<ntiles, 1024, 0, s>>>(hist, nbins, tiles);
         k_scan_sums<<<1, 1024, 0, s>>>(tiles, ntiles);
         k_scan_add<<<ntiles, 256, 0, s>>>(hist, nbins, tiles);
         k_sfc_scatter<<<div_up(N, 256), 256, 0, s>>>(keys, N, hist, d_order);
         k_sfc_fix_ties<<<div_up(N, 256), 256, 0, s>>>(keys, N, d_order);
         return check_launch("gb_sfc_order");
+        }
+
+    int gb_sfc_order(const float* d_pos, unsigned int N, const gb_box* box, int grid_bits,
+                     uint32_t* d_order, void* d_scratch, size_t scratch_bytes, void* stream)
+        {
+        return gb_sfc_order_dim(d_pos, N, box, grid_bits, 3, d_order, d_scratch, scratch_bytes,
+                                stream);
         }
 
     int gb_gather(void* d_dst, const void* d_src, const uint32_t* d_order, unsigned int N,

@@ -151,6 +151,9 @@ _PROTOS = {
     "gb_md_pair_step_example": (c_int, [_P(PairArgs), c_void, _P(StepFuse), c_void]),
     "gb_sum_net_force": (c_int, [c_void, _P(c_void), c_uint, c_uint, c_void]),
     "gb_sfc_scratch_bytes": (c_size, [c_uint, c_int]),
+    "gb_sfc_scratch_bytes_dim": (c_size, [c_uint, c_int, c_uint]),
+    "gb_sfc_order_dim": (c_int, [c_void, c_uint, _P(Box), c_int, c_uint, c_void, c_void, c_size,
+                                 c_void]),
     "gb_sfc_order": (c_int, [c_void, c_uint, _P(Box), c_int, c_void, c_void, c_size, c_void]),
     "gb_gather": (c_int, [c_void, c_void, c_void, c_uint, c_uint, c_void]),
     "gb_pair_forces_radial": (c_int, [c_void, c_void, c_void]),

@@ -170,7 +170,8 @@ class Simulation:
             self._cpp_integrator = integ._attach(self)
             sorter = next((t for t in self.operations.tuners if hasattr(t, "grid_bits")), None)
             if sorter is not None:
-                self._cpp_integrator.setSorter(sorter.trigger.period, sorter.grid_bits)
+                self._cpp_integrator.setSorter(sorter.trigger.period,
+                                               sorter._grid_bits(self.state.dimensions))
             self._needs_prep = True
         for f in integ.forces:
             nl = getattr(f, "nlist", None)

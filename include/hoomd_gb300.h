@@ -613,15 +613,23 @@ int gb_md_pair_step_radial(const gb_pair_args* args, const gb_radial_param* d_pa
                            const gb_step_fuse* fuse, void* stream);
 
 /* ---------------------------------------------------------------------------------------------
- * Space-filling-curve sort. Replaces SFCPackTunerGPU (hoomd/SFCPackTunerGPU.cu:26-160): a
- * Hilbert order over a 2^grid_bits per side lattice of the box (the reference's default grid is
- * 256 = 2^8). d_order[new] = old index; deterministic. d_scratch of gb_sfc_scratch_bytes().
+ * Space-filling-curve sort. Replaces SFCPackTunerGPU (hoomd/SFCPackTunerGPU.cu:26-160) and
+ * SFCPackTuner::getSortedOrder3D / 2D (hoomd/SFCPackTuner.cc:289-651): particles binned on a
+ * 2^grid_bits per side lattice of the box as the reference bins them ((unsigned)(f * grid) %
+ * grid), ordered by their bin's position along the reference's Hilbert traversal
+ * (generateTraversalOrder; in 2D, bins row by row), ties by old index -- the reference's order.
+ * The reference's default grid is 256 = 2^8 (3D), 4096 = 2^12 (2D). d_order[new] = old index;
+ * deterministic. d_scratch of gb_sfc_scratch_bytes[_dim](). gb_sfc_order is the 3D form.
  * gb_gather applies the order to one per-particle array (dst[i] = src[order[i]]; elements of
  * 4, 8, 12 or 16 bytes; dst and src must differ), as gpu_apply_sorted_order does.
  * ------------------------------------------------------------------------------------------- */
 size_t gb_sfc_scratch_bytes(unsigned int N, int grid_bits);
 int gb_sfc_order(const float* d_pos, unsigned int N, const gb_box* box, int grid_bits,
                  uint32_t* d_order, void* d_scratch, size_t scratch_bytes, void* stream);
+size_t gb_sfc_scratch_bytes_dim(unsigned int N, int grid_bits, unsigned int ndim);
+int gb_sfc_order_dim(const float* d_pos, unsigned int N, const gb_box* box, int grid_bits,
+                     unsigned int ndim, uint32_t* d_order, void* d_scratch, size_t scratch_bytes,
+                     void* stream);
 int gb_gather(void* d_dst, const void* d_src, const uint32_t* d_order, unsigned int N,
               unsigned int elem_bytes, void* stream);
 

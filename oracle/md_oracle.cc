@@ -1229,6 +1229,81 @@ void npt_step_two(unsigned int N, R* vel, R* accel, const R* net_force, R dt, R 
     }
 
 // ------------------------------------------------------------------------------------------------
+// Particle sort: hoomd/SFCPackTuner.cc:289-486 (Hilbert traversal by recursion over octants with
+// the walking tables and the eight permutation rules), :541-651 (getSortedOrder3D: bin with
+// (unsigned)(f * grid) % grid, clamp, key = traversal position, sort (key, index) pairs) and
+// :489-539 (getSortedOrder2D: key = row-major bin). Positions and fractions at the precision R.
+// ------------------------------------------------------------------------------------------------
+namespace sfc
+{
+const int istep[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+const int jstep[8] = {0, 0, 1, 1, 1, 1, 0, 0};
+const int kstep[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+// child order of rule m: result[k] = in[perm[m][k]]
+const int perm[8][8] = {{0, 3, 4, 7, 6, 5, 2, 1}, {0, 7, 6, 1, 2, 5, 4, 3},
+                        {0, 7, 6, 1, 2, 5, 4, 3}, {2, 3, 0, 1, 6, 7, 4, 5},
+                        {2, 3, 0, 1, 6, 7, 4, 5}, {4, 3, 2, 5, 6, 1, 0, 7},
+                        {4, 3, 2, 5, 6, 1, 0, 7}, {6, 5, 2, 1, 0, 3, 4, 7}};
+
+// appends the grid index i*M*M + j*M + k of every cell of the w-wide cube at (i, j, k) in
+// traversal order
+void traverse(int i, int j, int k, int w, int M, const unsigned int order[8],
+              std::vector<unsigned int>& out)
+    {
+    if (w == 1)
+        {
+        out.push_back((unsigned int)(i * M * M + j * M + k));
+        return;
+        }
+    w /= 2;
+    for (int m = 0; m < 8; m++)
+        {
+        const unsigned int cur = order[m];
+        unsigned int child[8];
+        for (int q = 0; q < 8; q++)
+            child[q] = order[perm[m][q]];
+        traverse(i + w * istep[cur], j + w * jstep[cur], k + w * kstep[cur], w, M, child, out);
+        }
+    }
+} // namespace sfc
+
+template<class R>
+void sfc_order(unsigned int N, const R* pos, const Box<R>& box, unsigned int grid, int ndim,
+               unsigned int* order)
+    {
+    std::vector<unsigned int> rank;
+    if (ndim == 3)
+        {
+        std::vector<unsigned int> seq;
+        seq.reserve((size_t)grid * grid * grid);
+        const unsigned int identity[8] = {0, 1, 2, 3, 4, 5, 6, 7};
+        sfc::traverse(0, 0, 0, (int)grid, (int)grid, identity, seq);
+        rank.assign(seq.size(), 0u);
+        for (size_t n = 0; n < seq.size(); n++)
+            rank[seq[n]] = (unsigned int)n;
+        }
+    std::vector<std::pair<unsigned int, unsigned int>> keys(N);
+    for (unsigned int n = 0; n < N; n++)
+        {
+        R fx, fy, fz;
+        box.make_fraction(pos[4 * n], pos[4 * n + 1], pos[4 * n + 2], fx, fy, fz);
+        int ib = (int)((unsigned int)(fx * R(grid)) % grid);
+        int jb = (int)((unsigned int)(fy * R(grid)) % grid);
+        int kb = ndim == 3 ? (int)((unsigned int)(fz * R(grid)) % grid) : 0;
+        ib = std::min(std::max(ib, 0), (int)grid - 1);
+        jb = std::min(std::max(jb, 0), (int)grid - 1);
+        kb = std::min(std::max(kb, 0), (int)grid - 1);
+        const unsigned int key = ndim == 3
+                                     ? rank[(size_t)ib * grid * grid + (size_t)jb * grid + kb]
+                                     : (unsigned int)(ib * grid + jb);
+        keys[n] = {key, n};
+        }
+    std::sort(keys.begin(), keys.end());
+    for (unsigned int n = 0; n < N; n++)
+        order[n] = keys[n].second;
+    }
+
+// ------------------------------------------------------------------------------------------------
 // Whole-step runner: hoomd/md/IntegratorTwoStep.cc:51-139 (update), :226-298 (prepRun),
 // hoomd/md/NeighborList.cc:363-435 (compute), :452-529 (updateRList), :1220-1289 (distanceCheck),
 // :1325-1418 (needsUpdating, rebuild_check_delay = 1, check_dist = true), :1544-1617 (head list,
@@ -1954,6 +2029,15 @@ using namespace orc;
 
 ORC_GEOMETRY(f32, float)
 ORC_GEOMETRY(f64, double)
+
+ORC_EXPORT void orc_sfc_order_f32(unsigned int N, const float* pos, const double* b6,
+                                  const int* per, unsigned int grid, int ndim,
+                                  unsigned int* order)
+    {
+    Box<float> box;
+    box.set(b6, per);
+    sfc_order<float>(N, pos, box, grid, ndim, order);
+    }
 
 ORC_EXPORT unsigned int orc_cell_adj(const unsigned int* dim3, int ndim, int radius,
                                      unsigned int* adj)

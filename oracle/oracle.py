@@ -249,6 +249,17 @@ def build_nlist(pos4, box, r_cut, r_buff, full=True, ndim=3, prec=32, periodic=(
     return n_neigh, nlist, head, info
 
 
+def sfc_order(pos4, box, grid=256, ndim=3, periodic=(1, 1, 1)):
+    """hoomd/SFCPackTuner.cc:489-651: the new order (order[new] = old index) of the particle sort
+    on a grid^3 Hilbert traversal (grid^2 row-major in 2D), FP32 fractions."""
+    pos4 = np.ascontiguousarray(pos4, np.float32)
+    N = len(pos4)
+    out = np.zeros(N, np.uint32)
+    b, p = box6(box), periodic3(periodic)
+    lib().orc_sfc_order_f32(N, ptr(pos4), ptr(b), ptr(p), int(grid), int(ndim), ptr(out))
+    return out
+
+
 def neighbor_sets(n_neigh, nlist, head):
     """Per-particle sorted neighbour index arrays."""
     return [np.sort(nlist[int(h): int(h) + int(n)]) for n, h in zip(n_neigh, head)]

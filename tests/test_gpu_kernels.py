@@ -385,6 +385,53 @@ def test_sfc_order_is_deterministic_permutation_with_locality():
     assert np.array_equal(host(dst).reshape(-1, 4), pos4[orders[0]])
 
 
+SORT_CASES = {
+    "fcc16k_shuffled": lambda: (lambda s: snap_pos4(s))(workloads.lj_fluid_fcc(m=16)),
+    "random60k": lambda: random_system(60000, (41.0, 41.0, 41.0), seed=7),
+    "triclinic1728": lambda: random_system(1728, (11.0, 12.0, 13.0), 2, seed=4,
+                                           tilts=(0.3, -0.2, 0.1), lattice=True),
+    "fcc1m": lambda: snap_pos4(workloads.lj_fluid_fcc(m=64)),
+    "hi_face4096": lambda: hi_face_system(),
+}
+
+
+@pytest.mark.parametrize("case", sorted(SORT_CASES))
+@pytest.mark.parametrize("grid_bits", [8, 5])
+def test_sfc_order_equals_oracle(case, grid_bits):
+    """The particle sort's permutation is the reference's (SFCPackTuner::getSortedOrder3D:
+    Hilbert traversal of the grid, ties by old index), element for element."""
+    L_ = abi.load()
+    pos4, box6 = SORT_CASES[case]()
+    N = len(pos4)
+    pos4 = pos4[np.random.default_rng(1).permutation(N)]
+    box = abi.make_box(box6[:3], box6[3:])
+    need = L_.gb_sfc_scratch_bytes(N, grid_bits)
+    scratch = zeros(need, torch.uint8)
+    order = zeros(N)
+    abi.check(L_.gb_sfc_order(p(dev(pos4)), N, ctypes.byref(box), grid_bits, p(order),
+                              p(scratch), need, stream()), "sfc")
+    want = O.sfc_order(pos4, box6, grid=1 << grid_bits)
+    got = host(order).astype(np.uint32)
+    assert np.array_equal(got, want), f"{(got != want).sum()} of {N} positions differ"
+
+
+def test_sfc_order_2d_equals_oracle():
+    """2D: the reference's row-major bin order on a 4096 grid (getSortedOrder2D)."""
+    L_ = abi.load()
+    rng = np.random.default_rng(9)
+    N = 20000
+    xy = rng.uniform(-50.0, 50.0, (N, 2))
+    pos4 = O.make_pos4(np.column_stack([xy, np.zeros(N)]), np.zeros(N), 32)
+    box = abi.make_box((100.0, 100.0, 1.0), (0, 0, 0))
+    need = L_.gb_sfc_scratch_bytes_dim(N, 12, 2)
+    scratch = zeros(need, torch.uint8)
+    order = zeros(N)
+    abi.check(L_.gb_sfc_order_dim(p(dev(pos4)), N, ctypes.byref(box), 12, 2, p(order),
+                                  p(scratch), need, stream()), "sfc 2d")
+    want = O.sfc_order(pos4, (100.0, 100.0, 1.0, 0, 0, 0), grid=4096, ndim=2)
+    assert np.array_equal(host(order).astype(np.uint32), want)
+
+
 def test_needs_update_kernel():
     L_ = abi.load()
     pos4, vel4, acc, img, box6 = _integrator_state(N=2000)
