@@ -1186,7 +1186,7 @@ void Integrator::drop_graphs()
     }
 
 // IntegratorTwoStep::prepRun (hoomd/md/IntegratorTwoStep.cc:226-298)
-void Integrator::prepare()
+void Integrator::prepare(bool keep_graphs)
     {
     ParticleData& pd = *pdata;
     cudaStream_t s = pd.stream;
@@ -1198,7 +1198,8 @@ void Integrator::prepare()
     for (auto& f : forces)
         nlist->add_consumer(&f->r_cut);
     nlist->build_sync();
-    drop_graphs();
+    if (!keep_graphs)
+        drop_graphs();
     for (auto& f : forces)
         {
         f->force_timestep = pd.timestep;

@@ -363,7 +363,10 @@ class Integrator
         {
         chunk = steps ? (steps > 1024 ? 1024 : steps) : 1;
         }
-    void prepare();
+    // IntegratorTwoStep::prepRun. keep_graphs: only the particle state changed since the step
+    // graphs were captured (positions, velocities, images, charges), so they stay valid; every
+    // setter of a value the graphs hold (time step, thermostat, parameters) drops them itself
+    void prepare(bool keep_graphs = false);
     void run(uint64_t nsteps);
     std::vector<double> thermo(bool with_virial); // KE, PE, W (W only when with_virial)
     double dof() const;
@@ -420,6 +423,7 @@ class Integrator
         {
         return graph_nlist_generation;
         }
+    void drop_graphs(); // the captured step graphs are rebuilt at the next run
 
     private:
     void sort_particles();
@@ -435,7 +439,6 @@ class Integrator
     void checkpoint();
     void restore();
     cudaGraphExec_t graph_for(unsigned int k);
-    void drop_graphs();
 
     DeviceArray<DevStatus> d_status;
     DeviceArray<char> d_step_scratch, d_thermo_scratch;

@@ -1,7 +1,12 @@
 // pybind11 module _hoomd_gb300: the host engine classes under the names of the reference's
 // C++ classes that the Python layer looks up (hoomd/md/pair/pair.py:126-146,
 // hoomd/md/nlist.py:390-397, hoomd/md/integrate.py:287-293).
+#include <cstdlib>
 #include <map>
+#include <memory>
+#include <mutex>
+#include <type_traits>
+#include <vector>
 
 #include <pybind11/numpy.h>
 #include <pybind11/pybind11.h>
@@ -19,6 +24,79 @@ namespace
 template<class T> py::array_t<T> make_array(std::vector<size_t> shape)
     {
     return py::array_t<T>(shape);
+    }
+
+// Page-locked host blocks for snapshot arrays. A block is handed out wrapped in a capsule that
+// owns it; numpy arrays viewing the block keep the capsule alive, and when the last one goes the
+// block returns to a small free list (at most POOL_KEEP blocks are kept; more are released).
+// Blocks are never shared by two live snapshots. Where page-locked memory cannot be had the
+// block is ordinary heap memory.
+struct PinnedBlock
+    {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    bool pinned = false;
+    };
+std::mutex g_pool_mutex;
+std::vector<PinnedBlock> g_pool;
+constexpr size_t POOL_KEEP = 4;
+
+void release_block(PinnedBlock* b)
+    {
+    std::unique_ptr<PinnedBlock> own(b);
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (g_pool.size() < POOL_KEEP)
+        {
+        g_pool.push_back(*b);
+        return;
+        }
+    if (b->pinned)
+        cudaFreeHost(b->ptr);
+    else
+        std::free(b->ptr);
+    }
+
+py::capsule pinned_block(size_t bytes)
+    {
+    PinnedBlock blk;
+        {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        // the smallest free block that is large enough
+        size_t best = g_pool.size();
+        for (size_t k = 0; k < g_pool.size(); k++)
+            if (g_pool[k].bytes >= bytes && (best == g_pool.size() || g_pool[k].bytes < g_pool[best].bytes))
+                best = k;
+        if (best < g_pool.size())
+            {
+            blk = g_pool[best];
+            g_pool.erase(g_pool.begin() + (long)best);
+            }
+        }
+    if (!blk.ptr)
+        {
+        blk.bytes = std::max<size_t>(bytes, 256);
+        blk.pinned = cudaHostAlloc(&blk.ptr, blk.bytes, cudaHostAllocDefault) == cudaSuccess;
+        if (!blk.pinned)
+            {
+            cudaGetLastError();
+            blk.ptr = std::malloc(blk.bytes);
+            if (!blk.ptr)
+                throw std::bad_alloc();
+            }
+        }
+    auto* holder = new PinnedBlock(blk);
+    return py::capsule(holder, "gb_snapshot_block",
+                       [](PyObject* o) {
+                           auto* h = static_cast<PinnedBlock*>(
+                               PyCapsule_GetPointer(o, "gb_snapshot_block"));
+                           if (h)
+                               release_block(h);
+                       });
+    }
+
+void* pinned_ptr(const py::capsule& c)
+    {
+    return static_cast<PinnedBlock*>(PyCapsule_GetPointer(c.ptr(), "gb_snapshot_block"))->ptr;
     }
 
 // Per-particle float4 (or 6 x pitch) device array -> numpy in tag order.
@@ -284,11 +362,23 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("getParticles",
              [](ParticleData& pd) {
                  const size_t N = pd.N;
-                 auto pos = make_array<double>({N, 3});
-                 auto vel = make_array<double>({N, 3});
-                 auto mass = make_array<double>({N});
-                 auto tid = make_array<uint32_t>({N});
-                 auto img = make_array<int32_t>({N, 3});
+                 // the five arrays share one page-locked block (the device writes them at full
+                 // link speed, no page faults), recycled when the arrays are released
+                 auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+                 const size_t o_vel = up(24 * N), o_mass = o_vel + up(24 * N),
+                              o_tid = o_mass + up(8 * N), o_img = o_tid + up(4 * N),
+                              total = o_img + up(12 * N);
+                 py::capsule owner = pinned_block(total);
+                 char* base = static_cast<char*>(pinned_ptr(owner));
+                 auto view = [&](auto* ptr, std::vector<size_t> shape) {
+                     using T = std::remove_pointer_t<decltype(ptr)>;
+                     return py::array_t<T>(shape, ptr, owner);
+                 };
+                 auto pos = view(reinterpret_cast<double*>(base), {N, 3});
+                 auto vel = view(reinterpret_cast<double*>(base + o_vel), {N, 3});
+                 auto mass = view(reinterpret_cast<double*>(base + o_mass), {N});
+                 auto tid = view(reinterpret_cast<uint32_t*>(base + o_tid), {N});
+                 auto img = view(reinterpret_cast<int32_t*>(base + o_img), {N, 3});
                  pd.get_particles(pos.mutable_data(), vel.mutable_data(), mass.mutable_data(),
                                   tid.mutable_data(), img.mutable_data());
                  py::dict d;
@@ -584,9 +674,10 @@ PYBIND11_MODULE(_hoomd_gb300, m)
             "dt", [](Integrator& i) { return i.dt; },
             [](Integrator& i, double v) {
                 i.dt = v;
-                i.prepared = false; // prepare() drops the captured graphs
+                i.prepared = false;
+                i.drop_graphs(); // the captured steps hold the time step
             })
-        .def("prepRun", &Integrator::prepare)
+        .def("prepRun", &Integrator::prepare, py::arg("keep_graphs") = false)
         .def("run", &Integrator::run, py::call_guard<py::gil_scoped_release>())
         .def("thermo", &Integrator::thermo)
         .def("dof", &Integrator::dof)

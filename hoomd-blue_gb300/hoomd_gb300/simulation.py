@@ -191,7 +191,9 @@ class Simulation:
             for f in integ.forces:
                 if getattr(f, "_cpp_obj", None) is not None and hasattr(f, "_update_tail"):
                     f._update_tail()
-            self._cpp_integrator.prepRun()
+            # the particle state or parameters changed: the engine's setters of values its
+            # captured step graphs hold drop those graphs themselves, so they are kept here
+            self._cpp_integrator.prepRun(True)
             self._needs_prep = False
         for op in self.operations.computes:
             op._simulation = self

@@ -657,3 +657,25 @@ def test_snapshot_round_trip_on_the_device():
     bad.particles.typeid[7] = 3
     with pytest.raises(Exception):
         sim.state._upload(bad)
+
+
+def test_time_step_change_after_a_run_applies():
+    """A new Integrator.dt set between runs reaches the captured fused steps (they hold the time
+    step): the second run equals a fresh simulation started from the same state at the new dt."""
+    snap = workloads.lj_fluid_sc(8, density=0.8, jitter=0.05, seed=13)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.0)
+    sim.run(10)
+    mid = sim.state.get_snapshot()
+    sim.operations.integrator.dt = 0.0025
+    sim.run(10)
+    a = sim.state.get_snapshot()
+    sim2, lj2, cell2, thermo2 = lj_sim(mid, kT=None, dt=0.0025, thermalize=None)
+    sim2.run(10)
+    b = sim2.state.get_snapshot()
+    assert np.allclose(a.particles.position, b.particles.position, atol=1e-4)
+    assert np.allclose(a.particles.velocity, b.particles.velocity, atol=1e-3)
+    # and a state written back between runs keeps the same captured steps valid
+    sim.state.set_snapshot(mid)
+    sim.run(10)
+    c = sim.state.get_snapshot()
+    assert np.allclose(c.particles.position, b.particles.position, atol=1e-4)
