@@ -990,6 +990,10 @@ Integrator::Integrator(std::shared_ptr<ParticleData> pd, std::shared_ptr<Neighbo
 Integrator::~Integrator()
     {
     drop_graphs();
+    if (body_stream)
+        cudaStreamDestroy(body_stream);
+    if (h_builds)
+        cudaFreeHost(h_builds);
     }
 
 void Integrator::add_force(std::shared_ptr<PairForce> f)
@@ -1359,6 +1363,53 @@ void Integrator::enqueue_step_fused(cudaStream_t s)
     check(f.launch_fused(a, fu, s), "fused pair step");
     }
 
+// One fused step inside a graph capture on stream s, its neighbour-list build in the body of an
+// IF conditional node whose value the step's rebuild flag sets (gb_graph_set_conditional).
+void Integrator::capture_step_conditional(cudaStream_t s, unsigned long long handle)
+    {
+    DevStatus* ds = d_status.get();
+    const gb_step_one_args o = step_one_args(ds);
+    check(gb_md_step_one(&o, s), "gb_md_step_one");
+    check(gb_graph_set_conditional(handle, &ds->rebuild, s), "gb_graph_set_conditional");
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cap = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cuda_check(cudaStreamGetCaptureInfo(s, &st, nullptr, &cap, &deps, nullptr, &ndeps),
+               "capture info");
+    cudaGraphNodeParams p {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = (cudaGraphConditionalHandle)handle;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    cuda_check(cudaGraphAddNode(&node, cap, deps, nullptr, ndeps, &p), "conditional node");
+    cuda_check(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                                                   cudaStreamSetCaptureDependencies),
+               "capture dependencies");
+    if (!body_stream)
+        cuda_check(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking), "stream");
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    cuda_check(cudaStreamBeginCaptureToGraph(body_stream, body, nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal),
+               "body capture");
+    try
+        {
+        nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond,
+                             body_stream, &ds->timestep, ds->build_steps);
+        }
+    catch (...)
+        {
+        cudaStreamEndCapture(body_stream, &body);
+        throw;
+        }
+    cuda_check(cudaStreamEndCapture(body_stream, &body), "body capture end");
+    PairForce& f = *forces[0];
+    gb_pair_args a = f.pair_args(false);
+    const gb_step_fuse fu = fuse_args(ds);
+    check(f.launch_fused(a, fu, s), "fused pair step");
+    }
+
 void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
     {
     ParticleData& pd = *pdata;
@@ -1441,23 +1492,66 @@ cudaGraphExec_t Integrator::graph_for(unsigned int k)
     cudaGraph_t g;
     if (k > BUSSI_RING)
         throw std::runtime_error("chunk longer than the Bussi draw ring");
-    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
-    try
+    // with conditional nodes, a step's build runs only when its rebuild check fired (the gated
+    // build kernels otherwise cost a wave of empty blocks each, every step); each step's node has
+    // a handle of its own (a handle belongs to one conditional node). A runtime that refuses
+    // any part of it gets the gated capture instead.
+    auto capture = [&](bool conditional) {
+        cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+        try
+            {
+            if (bussi)
+                enqueue_bussi_draws(*this, d_status.get(), d_bussi_ring.get(), BUSSI_RING, k, s);
+            std::vector<cudaGraphConditionalHandle> handles(conditional ? k : 0);
+            if (conditional)
+                {
+                cudaStreamCaptureStatus st;
+                cudaGraph_t cap = nullptr;
+                cuda_check(cudaStreamGetCaptureInfo(s, &st, nullptr, &cap, nullptr, nullptr,
+                                                    nullptr),
+                           "capture info");
+                for (unsigned int i = 0; i < k; i++)
+                    cuda_check(cudaGraphConditionalHandleCreate(&handles[i], cap, 0, 0),
+                               "conditional handle");
+                }
+            for (unsigned int i = 0; i < k; i++)
+                {
+                if (conditional)
+                    capture_step_conditional(s, handles[i]);
+                else
+                    enqueue_step_fused(s);
+                }
+            }
+        catch (...)
+            {
+            g = nullptr;
+            cudaStreamEndCapture(s, &g);
+            if (g)
+                cudaGraphDestroy(g);
+            throw;
+            }
+        cuda_check(cudaStreamEndCapture(s, &g), "end capture");
+        cudaGraphExec_t e;
+        const cudaError_t err = cudaGraphInstantiate(&e, g, 0);
+        cudaGraphDestroy(g);
+        cuda_check(err, "graph instantiate");
+        return e;
+    };
+    cudaGraphExec_t exec = nullptr;
+    if (use_conditional_build)
         {
-        if (bussi)
-            enqueue_bussi_draws(*this, d_status.get(), d_bussi_ring.get(), BUSSI_RING, k, s);
-        for (unsigned int i = 0; i < k; i++)
-            enqueue_step_fused(s);
+        try
+            {
+            exec = capture(true);
+            }
+        catch (const std::exception&)
+            {
+            cudaGetLastError();
+            use_conditional_build = false;
+            }
         }
-    catch (...)
-        {
-        cudaStreamEndCapture(s, &g);
-        throw;
-        }
-    cuda_check(cudaStreamEndCapture(s, &g), "end capture");
-    cudaGraphExec_t exec;
-    cuda_check(cudaGraphInstantiate(&exec, g, 0), "graph instantiate");
-    cudaGraphDestroy(g);
+    if (!exec)
+        exec = capture(false);
     graphs[k] = exec;
     return exec;
     }
@@ -1496,10 +1590,25 @@ void Integrator::run_chunk(unsigned int k)
         cuda_check(cudaMemsetAsync(ds->nl_cond, 0, sizeof(ds->nl_cond), s), "zero cond");
         cuda_check(cudaMemsetAsync(&ds->status, 0, sizeof(uint32_t), s), "zero status");
         const uint64_t cell_kernels = (nlist->deterministic ? 3 : 2) + (nlist->ex_pitch ? 1 : 0);
+        bool conditional = false;
         if (fused && use_graph)
             {
-            cuda_check(cudaGraphLaunch(graph_for(k), s), "graph launch");
-            launch_count += (uint64_t)k * (1 + cell_kernels + 1 + 1) + (bussi ? 1 : 0);
+            cudaGraphExec_t exec = graph_for(k);
+            conditional = use_conditional_build;
+            if (conditional)
+                {
+                if (!h_builds)
+                    cuda_check(cudaHostAlloc((void**)&h_builds, sizeof(uint64_t), 0), "host alloc");
+                cuda_check(cudaMemcpyAsync(h_builds, &ds->n_builds, sizeof(uint64_t),
+                                           cudaMemcpyDeviceToHost, s),
+                           "build count");
+                }
+            cuda_check(cudaGraphLaunch(exec, s), "graph launch");
+            // conditional graphs: step one, the conditional's value and the pair step each step;
+            // the build kernels are added below for the builds that ran
+            launch_count += conditional
+                                ? (uint64_t)k * 3 + (bussi ? 1 : 0)
+                                : (uint64_t)k * (1 + cell_kernels + 1 + 1) + (bussi ? 1 : 0);
             }
         else if (fused)
             {
@@ -1520,6 +1629,8 @@ void Integrator::run_chunk(unsigned int k)
                                + (langevin || brownian ? 1 : 2) + ((bussi || berendsen) ? 1 : 0));
             }
         DevStatus st = read_status();
+        if (conditional)
+            launch_count += (st.n_builds - *h_builds) * (cell_kernels + 1);
         if (st.cell_cond[1])
             throw std::runtime_error(tag_message(pd, st.cell_cond[1], "has NaN for its position."));
         if (st.cell_cond[2])

@@ -398,6 +398,14 @@ class Integrator
     int sort_bits = 8;
     unsigned int chunk = 50;
     bool use_graph = true;
+    // captured fused steps put the neighbour-list build in the body of a conditional graph node
+    // (run only on rebuild steps) instead of launching the gated build kernels every step; falls
+    // back to the gated kernels when the runtime refuses conditional nodes. Off by default: on
+    // the 1M-particle fluid the conditional nodes cost more per step (0.296 against 0.290 ms at
+    // one build in eight steps) than the early-exit blocks of the gated kernels they remove.
+    bool use_conditional_build = false;
+    cudaStream_t body_stream = nullptr; // captures the conditional node bodies
+    uint64_t* h_builds = nullptr;       // page-locked copy of the build count at a chunk's start
     bool compute_virial = false;
     bool prepared = false;
     uint64_t n_rollbacks = 0;
@@ -439,6 +447,7 @@ class Integrator
     void checkpoint();
     void restore();
     cudaGraphExec_t graph_for(unsigned int k);
+    void capture_step_conditional(cudaStream_t s, unsigned long long handle);
 
     DeviceArray<DevStatus> d_status;
     DeviceArray<char> d_step_scratch, d_thermo_scratch;

@@ -566,8 +566,30 @@ __global__ void k_sum_net_force(float4* __restrict__ net, ForcePtrs fp, unsigned
 
 using namespace gb;
 
+namespace gb
+{
+namespace
+{
+// The value of a conditional graph node from a device flag (0 or not): the rebuild flag the
+// step's check kernel raised decides whether the node's body (the cell list and neighbour-list
+// build) runs in this replay of the graph.
+__global__ void k_set_conditional(cudaGraphConditionalHandle handle, const uint32_t* flag)
+    {
+    cudaGraphSetConditional(handle, *flag != 0u ? 1u : 0u);
+    }
+} // namespace
+} // namespace gb
+
 extern "C"
     {
+    int gb_graph_set_conditional(uint64_t handle, const uint32_t* d_flag, void* stream)
+        {
+        GB_REQUIRE(d_flag, "gb_graph_set_conditional: null flag");
+        gb::k_set_conditional<<<1, 1, 0, (cudaStream_t)stream>>>(
+            (cudaGraphConditionalHandle)handle, d_flag);
+        return check_launch("gb_graph_set_conditional");
+        }
+
     int gb_cv_step_one(float* d_pos, float* d_vel, const float* d_accel, int* d_image,
                        unsigned int N, const gb_box* box, float dt, float scale,
                        const double* d_scale, void* stream)

@@ -660,6 +660,12 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setSorter", &Integrator::set_sorter)
         .def("setChunk", &Integrator::set_chunk)
         .def_readwrite("use_graph", &Integrator::use_graph)
+        .def_property(
+            "conditional_build", [](const Integrator& in) { return in.use_conditional_build; },
+            [](Integrator& in, bool v) {
+                in.use_conditional_build = v;
+                in.drop_graphs();
+            })
         .def_readwrite("compute_virial", &Integrator::compute_virial)
         .def_readonly("n_rollbacks", &Integrator::n_rollbacks)
         .def("graphCount", &Integrator::graph_count)

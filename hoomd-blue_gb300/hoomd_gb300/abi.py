@@ -123,6 +123,7 @@ _PROTOS = {
                                c_void]),
     "gb_thermalize": (c_int, [c_void, c_void, c_uint, c_double, c_u64, ctypes.c_uint16, c_uint,
                               c_void, c_void]),
+    "gb_graph_set_conditional": (c_int, [c_u64, c_void, c_void]),
     "gb_snapshot_stage_bytes": (c_size, [c_uint]),
     "gb_snapshot_gather": (c_int, [c_void, c_void, c_void, c_void, c_uint, c_void, c_void, c_void,
                                    c_void, c_void, c_void]),

@@ -416,6 +416,13 @@ int gb_thermalize(float* d_vel, const uint32_t* d_tag, unsigned int N, double kT
                   uint64_t timestep, uint16_t seed, unsigned int ndim, void* d_scratch,
                   void* stream);
 
+/* Conditional graph nodes (GB300 design, no reference counterpart): inside a captured CUDA graph,
+ * sets the value of the conditional node `handle` (a cudaGraphConditionalHandle created on that
+ * graph) to (*d_flag != 0). The captured MD step uses it to run the cell-list and neighbour-list
+ * build of a step only when the step's rebuild check raised the flag, instead of launching the
+ * gated build kernels every step. */
+int gb_graph_set_conditional(uint64_t handle, const uint32_t* d_flag, void* stream);
+
 /* Snapshot transfer on the device: the per-particle loops of ParticleData::takeSnapshot
  * (hoomd/ParticleData.cc:1388-1617) and ParticleData::initializeFromSnapshot
  * (hoomd/ParticleData.cc:982-1379), which the reference runs on the host. Snapshot arrays are in

@@ -254,6 +254,41 @@ def test_graphs_follow_list_reallocation():
     assert np.abs(ua - ub).max() < 1e-3
 
 
+@pytest.mark.parametrize("kT", [None, 1.2])
+def test_conditional_build_graphs_match_gated_kernels(kT):
+    """The captured step graphs put the neighbour-list build in a conditional node that runs
+    only on rebuild steps; graphs that launch the gated build kernels every step must give the
+    same trajectory bit for bit (deterministic cell list) and the same number of builds, across
+    chunks, a sort and a run continued from the first."""
+    snap = workloads.lj_fluid_sc(16)
+    res = []
+    for conditional in (True, False):
+        sim = make_sim(snap, seed=9)
+        sim.state.thermalize_particle_momenta(hoomd.filter.All(), 1.5)
+        cell = md.nlist.Cell(buffer=0.3, deterministic=True)
+        lj = md.pair.LJ(nlist=cell, default_r_cut=2.5)
+        lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+        th = None if kT is None else md.methods.thermostats.Bussi(kT=kT)
+        sim.operations.integrator = md.Integrator(
+            dt=0.005, forces=[lj], methods=[md.methods.ConstantVolume(hoomd.filter.All(), th)])
+        sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=150))
+        sim.run(0)
+        integ = sim._cpp_integrator
+        integ.conditional_build = conditional
+        l0 = integ.launch_count
+        sim.run(230)
+        sim.run(70)
+        res.append((sim.state.get_snapshot(), cell.num_builds, integ.launch_count - l0))
+    (a, nb_a, la), (b, nb_b, lb) = res
+    assert nb_a == nb_b and nb_a >= 5
+    assert np.array_equal(a.particles.position, b.particles.position)
+    assert np.array_equal(a.particles.velocity, b.particles.velocity)
+    assert np.array_equal(a.particles.image, b.particles.image)
+    # the gated graphs launch every build kernel on all 300 steps, the conditional ones only on
+    # the rebuild steps (plus one kernel a step that sets the condition)
+    assert la < lb
+
+
 def test_adding_to_operations():
     """hoomd/md/pytest/test_potential.py:1296-1305: a force added to the operations (no
     integrator) is a compute evaluated at the current positions."""
