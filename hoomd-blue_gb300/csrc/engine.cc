@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <iostream>
 #include <sstream>
 
 namespace gbe
@@ -352,10 +353,14 @@ void NeighborList::allocate()
 
 void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count,
                                  uint32_t* d_cell_cond, uint32_t* d_nl_cond, cudaStream_t s,
-                                 const uint64_t* d_timestep, uint64_t* d_build_steps)
+                                 const uint64_t* d_timestep, uint64_t* d_build_steps,
+                                 uint64_t* d_dangerous)
     {
     ParticleData& pd = *pdata;
     gb_cell_list_args c {};
+    c.d_dangerous = d_dangerous;
+    c.check_delay = rebuild_check_delay;
+    c.check_dist = check_dist ? 1 : 0;
     c.d_pos = pd.pos.get();
     c.N = pd.N;
     c.box = pd.box;
@@ -521,10 +526,7 @@ void NeighborList::build_sync()
         for (unsigned int t = 0; t < pd.ntypes; t++)
             st.nl_cond[t] = h[3 + t];
         if (!grow(st))
-            {
-            n_builds_host++;
             return;
-            }
         }
     throw std::runtime_error("neighbour list build did not converge");
     }
@@ -1201,6 +1203,11 @@ void Integrator::prepare(bool keep_graphs)
     nlist->clear_consumers();
     for (auto& f : forces)
         nlist->add_consumer(&f->r_cut);
+    // the build statistics and the check schedule carry over from the last run unless the list
+    // must be rebuilt anyway (first run, new r_cut or capacities: the reference's forced update
+    // at this step, which the build count leaves out)
+    const bool forced = nlist->dirty || !nlist->allocated;
+    const DevStatus old = read_status();
     nlist->build_sync();
     if (!keep_graphs)
         drop_graphs();
@@ -1235,7 +1242,10 @@ void Integrator::prepare(bool keep_graphs)
     d_bussi_ring.resize(2 * (size_t)BUSSI_RING);
     DevStatus st {};
     st.timestep = pd.timestep;
-    st.n_builds = nlist->n_builds_host;
+    st.n_builds = old.n_builds;
+    st.build_steps[0] = (forced || old.build_steps[0] == ~0ull) ? pd.timestep : old.build_steps[0];
+    st.build_steps[1] = old.build_steps[1];
+    st.n_dangerous = old.n_dangerous;
     st.factor = 1.0;
     st.reservoir = reservoir;
     st.mttk[0] = mttk_host[0];
@@ -1281,6 +1291,13 @@ gb_step_one_args Integrator::step_one_args(DevStatus* ds) const
     o.d_rcut_max = nlist->d_rcut_max.get();
     o.r_buff = nlist->r_buff;
     o.d_rebuild = &ds->rebuild;
+    if (nlist->rebuild_check_delay != 1 || !nlist->check_dist)
+        {
+        o.d_check_step = &ds->timestep;
+        o.d_last_update = &ds->build_steps[0];
+        o.check_delay = nlist->rebuild_check_delay;
+        o.check_dist = nlist->check_dist ? 1 : 0;
+        }
     o.nve_order = langevin ? 1 : 0;
     o.max_displacement = (float)max_disp;
     if (brownian)
@@ -1356,7 +1373,7 @@ void Integrator::enqueue_step_fused(cudaStream_t s)
     const gb_step_one_args o = step_one_args(ds);
     check(gb_md_step_one(&o, s), "gb_md_step_one");
     nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s, &ds->timestep,
-                         ds->build_steps);
+                         ds->build_steps, &ds->n_dangerous);
     PairForce& f = *forces[0];
     gb_pair_args a = f.pair_args(false);
     const gb_step_fuse fu = fuse_args(ds);
@@ -1396,7 +1413,7 @@ void Integrator::capture_step_conditional(cudaStream_t s, unsigned long long han
     try
         {
         nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond,
-                             body_stream, &ds->timestep, ds->build_steps);
+                             body_stream, &ds->timestep, ds->build_steps, &ds->n_dangerous);
         }
     catch (...)
         {
@@ -1423,7 +1440,7 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
         }
     check(gb_md_step_one(&o, s), "gb_md_step_one");
     nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s, &ds->timestep,
-                         ds->build_steps);
+                         ds->build_steps, &ds->n_dangerous);
     for (auto& f : forces)
         {
         // IntegratorTwoStep::update computes the net force for timestep + 1
@@ -1465,6 +1482,8 @@ void Integrator::enqueue_step_general(cudaStream_t s, uint64_t step)
                                ds->thermo, s),
               "thermo");
         }
+    if (!langevin) // the Langevin step two advances the counter itself
+        check(gb_step_counter_advance(&ds->timestep, s), "step counter");
     if (bussi)
         check(gb_bussi_factor(&ds->thermo[0], dof(), dt, tau, kT, step + 1, pd.seed, 0u,
                               &ds->factor, s),
@@ -1626,9 +1645,21 @@ void Integrator::run_chunk(unsigned int k)
                 enqueue_step_general(s, pd.timestep + i);
             launch_count += (uint64_t)k
                             * (1 + cell_kernels + 1 + forces.size() + (forces.size() > 1 ? 1 : 0)
-                               + (langevin || brownian ? 1 : 2) + ((bussi || berendsen) ? 1 : 0));
+                               + (langevin ? 1 : (brownian ? 2 : 3))
+                               + ((bussi || berendsen) ? 1 : 0));
             }
         DevStatus st = read_status();
+        if (st.n_dangerous > dangerous_seen && notice_level >= 2)
+            {
+            // NeighborList::needsUpdating's notice (hoomd/md/NeighborList.cc:1405-1414)
+            std::cerr << "notice(2): nlist: " << (st.n_dangerous - dangerous_seen)
+                      << " dangerous neighbor list build(s): the first check after "
+                         "rebuild_check_delay steps found the list stale. Continuing this "
+                         "simulation may produce incorrect results; decrease "
+                         "rebuild_check_delay and rerun."
+                      << std::endl;
+            }
+        dangerous_seen = st.n_dangerous;
         if (conditional)
             launch_count += (st.n_builds - *h_builds) * (cell_kernels + 1);
         if (st.cell_cond[1])
@@ -1711,21 +1742,29 @@ void Integrator::sort_particles()
     pd.scratch.zero(s);
     pd.sort_generation++;
     nlist->build_sync();
+    // a forced update (not counted in num_builds): the reference makes it at the next step's
+    // force computation, the step the check schedule and the build periods count from
     DevStatus* ds = d_status.get();
-    uint64_t nb = 0;
-    cuda_check(cudaMemcpyAsync(&nb, &ds->n_builds, sizeof(nb), cudaMemcpyDeviceToHost, s), "nb");
-    cuda_check(cudaStreamSynchronize(s), "sort");
-    nb += 1;
-    cuda_check(cudaMemcpyAsync(&ds->n_builds, &nb, sizeof(nb), cudaMemcpyHostToDevice, s), "nb");
+    const uint64_t upd = pd.timestep + 1;
+    cuda_check(cudaMemcpyAsync(&ds->build_steps[0], &upd, sizeof(upd), cudaMemcpyHostToDevice, s),
+               "last update");
     cuda_check(cudaStreamSynchronize(s), "sort");
     }
 
+// System::run's resetStats (hoomd/System.cc:90, hoomd/md/NeighborList.cc:1420-1426): builds,
+// dangerous builds and the smallest period count from the start of each run
 void Integrator::reset_build_stats()
     {
     const uint64_t period = 100;
-    cuda_check(cudaMemcpyAsync(&d_status.get()->build_steps[1], &period, sizeof(period),
+    DevStatus* ds = d_status.get();
+    cuda_check(cudaMemcpyAsync(&ds->build_steps[1], &period, sizeof(period),
                                cudaMemcpyHostToDevice, pdata->stream),
                "build statistics");
+    cuda_check(cudaMemsetAsync(&ds->n_builds, 0, sizeof(uint64_t), pdata->stream),
+               "build statistics");
+    cuda_check(cudaMemsetAsync(&ds->n_dangerous, 0, sizeof(uint64_t), pdata->stream),
+               "build statistics");
+    dangerous_seen = 0;
     cuda_check(cudaStreamSynchronize(pdata->stream), "build statistics");
     }
 

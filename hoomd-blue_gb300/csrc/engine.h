@@ -129,7 +129,10 @@ struct DevStatus
     uint32_t pad[3];
     uint64_t timestep;
     uint64_t n_builds;
-    uint64_t build_steps[2]; // last build's timestep, smallest period between builds (cap 99)
+    // step of the last build (NeighborList m_last_updated_tstep), smallest period between
+    // builds (capped at 99)
+    uint64_t build_steps[2];
+    uint64_t n_dangerous; // dangerous builds (delayed checks that found the list stale)
     double factor;         // Bussi rescale factor for the next step one
     double thermo[3];      // KE, PE, W after the last step
     double reservoir;      // Langevin reservoir energy (tally_reservoir_energy)
@@ -202,7 +205,7 @@ class NeighborList
     void build_sync();          // forced build with host-side overflow retry
     void enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count, uint32_t* d_cell_cond,
                        uint32_t* d_nl_cond, cudaStream_t s, const uint64_t* d_timestep = nullptr,
-                       uint64_t* d_build_steps = nullptr);
+                       uint64_t* d_build_steps = nullptr, uint64_t* d_dangerous = nullptr);
     bool grow(const DevStatus& st); // returns true when a capacity grew
     // pairs of the list as tags (or as the current particle indices with local = true)
     std::vector<uint32_t> pair_list(bool full, bool local = false);
@@ -223,7 +226,6 @@ class NeighborList
     unsigned int adj_w = 0, Nmax_cell = 0;
     std::vector<uint32_t> Nmax;
     uint64_t stride = 0;
-    uint64_t n_builds_host = 0;
     bool allocated = false;
     bool dirty = true; // r_cut or capacities changed: graphs must be rebuilt
     bool capacity_fixed = false; // start from exactly Nmax_cell / Nmax (tests of the growth path)
@@ -411,6 +413,8 @@ class Integrator
     uint64_t n_rollbacks = 0;
     uint64_t steps_run = 0;
     uint64_t launch_count = 0; // kernels this engine launched (graph replays included)
+    int notice_level = 2;      // the device's notice level (dangerous-build notices at >= 2)
+    uint64_t dangerous_seen = 0;
     // average device time (ms) of each phase of one fused step, launched outside the graph on
     // the engine's stream with CUDA events: [step one + rebuild check, cell list + neighbour
     // list build, fused pair step]; the state is checkpointed before and restored after

@@ -80,7 +80,27 @@ struct StepOneCheck
     const float* rcut_max;
     float r_buff;
     uint32_t* rebuild;
+    // delayed-check schedule (gb_step_one_args); last_update NULL: check every step
+    const uint64_t* check_step;
+    const uint64_t* last_update;
+    uint32_t delay;
+    int dist_check;
     };
+
+// NeighborList::shouldCheckDistance / needsUpdating (hoomd/md/NeighborList.cc:1313-1403) for the
+// step T = *check_step + 1: 0 = no rebuild, 1 = rebuild without a check, 2 = distance check
+__device__ __forceinline__ int check_schedule(const StepOneCheck& c)
+    {
+    if (!c.last_update)
+        return 2;
+    const uint64_t T = *c.check_step + 1, last = *c.last_update;
+    if (T < last + c.delay)
+        return 0;
+    if (c.r_buff < 1e-6f
+        || (!c.dist_check && (c.delay == 0 || (c.delay > 1 && T == last + c.delay))))
+        return 1;
+    return 2;
+    }
 
 // Brownian dynamics (TwoStepBD) and the DisplacementCapped limit of step one.
 struct StepOneExtra
@@ -220,7 +240,10 @@ __global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
             ke = (double)v.w
                  * ((double)v.x * (double)v.x + (double)v.y * (double)v.y
                     + (double)v.z * (double)v.z);
-        if (CHECK)
+        const int sched = CHECK ? check_schedule(chk) : 0;
+        if (CHECK && sched == 1)
+            moved = true;
+        if (CHECK && sched == 2)
             {
             // hoomd/md/NeighborListGPU.cu:42-83 with lambda = 1 (fixed box)
             const float4 lp = chk.last_pos[j];
@@ -577,6 +600,11 @@ __global__ void k_set_conditional(cudaGraphConditionalHandle handle, const uint3
     {
     cudaGraphSetConditional(handle, *flag != 0u ? 1u : 0u);
     }
+
+__global__ void k_step_counter_advance(uint64_t* step)
+    {
+    *step += 1;
+    }
 } // namespace
 } // namespace gb
 
@@ -590,6 +618,13 @@ extern "C"
         return check_launch("gb_graph_set_conditional");
         }
 
+    int gb_step_counter_advance(uint64_t* d_timestep, void* stream)
+        {
+        GB_REQUIRE(d_timestep, "gb_step_counter_advance: null counter");
+        gb::k_step_counter_advance<<<1, 1, 0, (cudaStream_t)stream>>>(d_timestep);
+        return check_launch("gb_step_counter_advance");
+        }
+
     int gb_cv_step_one(float* d_pos, float* d_vel, const float* d_accel, int* d_image,
                        unsigned int N, const gb_box* box, float dt, float scale,
                        const double* d_scale, void* stream)
@@ -598,7 +633,7 @@ extern "C"
                    "gb_cv_step_one: null argument");
         if (N == 0)
             return GB_OK;
-        StepOneCheck none {nullptr, nullptr, 0.0f, nullptr};
+        StepOneCheck none {nullptr, nullptr, 0.0f, nullptr, nullptr, nullptr, 1u, 1};
         k_step_one<false, false, false, false><<<div_up(N, 256), 256, 0, (cudaStream_t)stream>>>(
             reinterpret_cast<float4*>(d_pos), reinterpret_cast<float4*>(d_vel), d_accel, d_image,
             N, *box, dt, scale, d_scale, none, MttkStep {}, StepOneExtra {});
@@ -614,8 +649,16 @@ extern "C"
                    "gb_md_step_one: rebuild check needs r_cut max and a flag");
         if (a->N == 0)
             return GB_OK;
-        StepOneCheck chk {reinterpret_cast<const float4*>(a->d_last_pos), a->d_rcut_max,
-                          a->r_buff, a->d_rebuild};
+        GB_REQUIRE(!a->d_last_update || a->d_check_step,
+                   "gb_md_step_one: a check schedule needs the device step counter");
+        StepOneCheck chk {reinterpret_cast<const float4*>(a->d_last_pos),
+                          a->d_rcut_max,
+                          a->r_buff,
+                          a->d_rebuild,
+                          a->d_check_step,
+                          a->d_last_update,
+                          a->check_delay,
+                          a->check_dist};
         cudaStream_t s = (cudaStream_t)stream;
         const bool mttk = a->d_mttk_state != nullptr;
         GB_REQUIRE(!mttk || (a->d_mttk_scale2 && a->d_mttk_scratch && !a->nve_order),

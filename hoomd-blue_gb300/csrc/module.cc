@@ -660,6 +660,7 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("setSorter", &Integrator::set_sorter)
         .def("setChunk", &Integrator::set_chunk)
         .def_readwrite("use_graph", &Integrator::use_graph)
+        .def_readwrite("notice_level", &Integrator::notice_level)
         .def_property(
             "conditional_build", [](const Integrator& in) { return in.use_conditional_build; },
             [](Integrator& in, bool v) {
@@ -694,6 +695,8 @@ PYBIND11_MODULE(_hoomd_gb300, m)
                  d["timestep"] = st.timestep;
                  d["n_builds"] = st.n_builds;
                  d["shortest_rebuild"] = st.build_steps[1];
+                 d["last_update"] = st.build_steps[0];
+                 d["dangerous_builds"] = st.n_dangerous;
                  d["factor"] = st.factor;
                  d["kinetic_energy"] = st.thermo[0];
                  d["potential_energy"] = st.thermo[1];

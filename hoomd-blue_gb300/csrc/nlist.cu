@@ -25,8 +25,16 @@ namespace
 {
 constexpr int NL_WARPS = 4; // warps per block in the build kernel
 
+// dangerous-build accounting of a delayed rebuild check (gb_cell_list_args)
+struct BuildRecord
+    {
+    uint64_t* dangerous;
+    uint32_t delay;
+    int dist_check;
+    };
+
 __global__ void k_zero_u32(unsigned int* p, size_t n, const uint32_t* gate, uint64_t* count,
-                           const uint64_t* timestep, uint64_t* build_steps)
+                           const uint64_t* timestep, uint64_t* build_steps, BuildRecord rec)
     {
     if (gate && *gate == 0)
         return;
@@ -36,10 +44,15 @@ __global__ void k_zero_u32(unsigned int* p, size_t n, const uint32_t* gate, uint
             *count += 1;
         if (timestep && build_steps)
             {
-            const uint64_t t = *timestep, last = build_steps[0];
-            if (last != ~0ull && t > last)
-                build_steps[1] = min(build_steps[1], min(t - last, (uint64_t)99));
-            build_steps[0] = t;
+            // NeighborList::needsUpdating (hoomd/md/NeighborList.cc:1349-1356, 1388-1414) for the
+            // step whose forces follow
+            const uint64_t T = *timestep + 1, last = build_steps[0];
+            if (last != ~0ull && T > last)
+                build_steps[1] = min(build_steps[1], min(T - last, (uint64_t)99));
+            if (rec.dangerous && rec.dist_check && rec.delay > 1 && last != ~0ull
+                && T == last + rec.delay)
+                *rec.dangerous += 1;
+            build_steps[0] = T;
             }
         }
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -1006,12 +1019,13 @@ extern "C"
         const unsigned int ncell = a->dim[0] * a->dim[1] * a->dim[2];
         GB_REQUIRE(ncell > 0, "gb_cell_list_build: empty cell grid");
         cudaStream_t s = (cudaStream_t)stream;
+        GB_REQUIRE(!a->d_timestep == !a->d_build_steps,
+                   "gb_cell_list_build: the build statistics need both the step and the record");
         const int sms = num_sms();
-        k_zero_u32<<<min(div_up(ncell, 256), (unsigned)sms * 8), 256, 0, s>>>(a->d_cell_size,
-                                                                             ncell, a->d_gate,
-                                                                             a->d_build_count,
-                                                                             a->d_timestep,
-                                                                             a->d_build_steps);
+        const BuildRecord rec {a->d_dangerous, a->check_delay, a->check_dist};
+        k_zero_u32<<<min(div_up(ncell, 256), (unsigned)sms * 8), 256, 0, s>>>(
+            a->d_cell_size, ncell, a->d_gate, a->d_build_count, a->d_timestep, a->d_build_steps,
+            rec);
         if (a->N > 0)
             k_cell_bin<<<min(div_up(a->N, 256), (unsigned)sms * 16), 256, 0, s>>>(
                 reinterpret_cast<const float4*>(a->d_pos), a->N, a->box,

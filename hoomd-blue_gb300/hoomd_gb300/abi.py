@@ -32,7 +32,8 @@ class CellListArgs(ctypes.Structure):
                 ("Nmax", c_uint), ("d_cell_size", c_void), ("d_xyzf", c_void),
                 ("d_cell_type", c_void), ("d_conditions", c_void), ("d_gate", c_void),
                 ("deterministic", c_int), ("d_build_count", c_void), ("d_timestep", c_void),
-                ("d_build_steps", c_void)]
+                ("d_build_steps", c_void), ("d_dangerous", c_void),
+                ("check_delay", ctypes.c_uint32), ("check_dist", c_int)]
 
 
 class NlistArgs(ctypes.Structure):
@@ -64,7 +65,9 @@ class StepOneArgs(ctypes.Structure):
                 ("max_displacement", c_float), ("brownian", c_int), ("d_bd_force", c_void),
                 ("d_tag", c_void), ("d_gamma", c_void), ("bd_kT", c_float),
                 ("ndim", ctypes.c_uint32), ("seed", ctypes.c_uint32), ("d_timestep", c_void),
-                ("timestep", c_u64), ("noiseless", c_int)]
+                ("timestep", c_u64), ("noiseless", c_int), ("d_check_step", c_void),
+                ("d_last_update", c_void), ("check_delay", ctypes.c_uint32),
+                ("check_dist", c_int)]
 
 
 class StepFuse(ctypes.Structure):
@@ -124,6 +127,7 @@ _PROTOS = {
     "gb_thermalize": (c_int, [c_void, c_void, c_uint, c_double, c_u64, ctypes.c_uint16, c_uint,
                               c_void, c_void]),
     "gb_graph_set_conditional": (c_int, [c_u64, c_void, c_void]),
+    "gb_step_counter_advance": (c_int, [c_void, c_void]),
     "gb_snapshot_stage_bytes": (c_size, [c_uint]),
     "gb_snapshot_gather": (c_int, [c_void, c_void, c_void, c_void, c_uint, c_void, c_void, c_void,
                                    c_void, c_void, c_void]),

@@ -101,6 +101,7 @@ class Integrator:
         cpp_nl = nl._attach(simulation)
         self._cpp_nlist = cpp_nl
         integ = _hoomd_gb300.IntegratorTwoStep(simulation.state._cpp_pdata, cpp_nl, self._dt)
+        integ.notice_level = int(getattr(simulation.device, "notice_level", 2))
         for f in self.forces:
             integ.addForce(f._attach(simulation, cpp_nl))
         self._attached_forces = list(self.forces)

@@ -70,14 +70,11 @@ class NeighborList:
             raise ValueError(f"invalid exclusions {bad}")
         if mesh is not None:
             raise NotImplementedError("mesh exclusions are outside the short-range LJ/Table path")
-        if int(rebuild_check_delay) != 1 or not bool(check_dist):
-            raise NotImplementedError("only rebuild_check_delay=1 with check_dist=True (the "
-                                      "reference's defaults) is implemented")
         self._cpp_obj = None
         self.buffer = buffer
         self.exclusions = exclusions
-        self.rebuild_check_delay = int(rebuild_check_delay)
-        self.check_dist = bool(check_dist)
+        self.rebuild_check_delay = rebuild_check_delay
+        self.check_dist = check_dist
         self.r_cut = TypePairDict(default=float(default_r_cut), validator=nonnegative_real)
         self.r_cut._on_change = self._r_cut_changed
         self._simulation = None
@@ -98,6 +95,45 @@ class NeighborList:
             self._cpp_obj.r_buff = value
             if self._simulation is not None:
                 self._simulation._state_changed()
+
+    @property
+    def rebuild_check_delay(self):
+        """Check whether the list needs a rebuild only every this many steps after a build
+        (NeighborList::shouldCheckDistance); 0 with ``check_dist=False`` rebuilds every step."""
+        return self._rebuild_check_delay
+
+    @rebuild_check_delay.setter
+    def rebuild_check_delay(self, value):
+        value = int(value)
+        if value < 0:
+            raise ValueError("rebuild_check_delay must be non-negative")
+        self._rebuild_check_delay = value
+        if self._cpp_obj is not None:
+            self._cpp_obj.rebuild_check_delay = value
+            self._simulation._state_changed()
+
+    @property
+    def check_dist(self):
+        """Decide rebuilds by the distance check (True) or rebuild every ``rebuild_check_delay``
+        steps (False)."""
+        return self._check_dist
+
+    @check_dist.setter
+    def check_dist(self, value):
+        self._check_dist = bool(value)
+        if self._cpp_obj is not None:
+            self._cpp_obj.check_dist = self._check_dist
+            self._simulation._state_changed()
+
+    @property
+    def dangerous_builds(self):
+        """Builds found necessary at the first check after a delayed-check period: particles
+        may have moved further than half the buffer before the check (the reference's
+        'dangerous neighborlist build' notice)."""
+        sim = self._simulation
+        if sim is None or sim._cpp_integrator is None:
+            return 0
+        return int(sim._cpp_integrator.status()["dangerous_builds"])
 
     def _r_cut_changed(self, key):
         if self._cpp_obj is None:
@@ -120,6 +156,8 @@ class NeighborList:
         self._simulation = simulation
         state = simulation.state
         self._cpp_obj = _hoomd_gb300.NeighborListGPUBinned(state._cpp_pdata, self.buffer)
+        self._cpp_obj.rebuild_check_delay = self.rebuild_check_delay
+        self._cpp_obj.check_dist = self.check_dist
         types = state.particle_types
         for i, a in enumerate(types):
             for j, b in enumerate(types):

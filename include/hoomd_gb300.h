@@ -90,12 +90,20 @@ typedef struct gb_cell_list_args
                                     (nlist.Cell(deterministic=True), hoomd/CellListGPU.cu:478-540) */
     uint64_t* d_build_count;     /* optional: incremented once per (non-gated-off) call */
     /* optional, both or neither: the rebuild statistics of NeighborList::needsUpdating
-     * (hoomd/md/NeighborList.cc:1388-1402, getSmallestRebuild :1428-1436). d_build_steps[0] is the
-     * timestep (*d_timestep) of the last build (UINT64_MAX before the first) and
-     * d_build_steps[1] the smallest period between builds, capped at 99; the caller sets it to
-     * 100 when the statistics start. */
+     * (hoomd/md/NeighborList.cc:1388-1402, getSmallestRebuild :1428-1436). The step of a build
+     * is *d_timestep + 1 (the step whose forces follow, the reference's needsUpdating(timestep +
+     * 1)). d_build_steps[0] is the step of the last build (m_last_updated_tstep; UINT64_MAX
+     * before the first) and d_build_steps[1] the smallest period between builds, capped at 99;
+     * the caller sets it to 100 when the statistics start. */
     const uint64_t* d_timestep;
     uint64_t* d_build_steps;
+    /* optional, with d_build_steps: dangerous builds. When check_dist is set, check_delay > 1 and
+     * this build's step is exactly d_build_steps[0] + check_delay (the first check after the
+     * delay found the list stale), *d_dangerous is incremented (hoomd/md/NeighborList.cc:
+     * 1349-1356, 1405-1414). */
+    uint64_t* d_dangerous;
+    uint32_t check_delay;
+    int check_dist;
     } gb_cell_list_args;
 
 int gb_cell_list_build(const gb_cell_list_args* args, void* stream);
@@ -423,6 +431,11 @@ int gb_thermalize(float* d_vel, const uint32_t* d_tag, unsigned int N, double kT
  * gated build kernels every step. */
 int gb_graph_set_conditional(uint64_t handle, const uint32_t* d_flag, void* stream);
 
+/* Advances the device step counter by one (the steps of methods whose second half is not the
+ * fused pair step, which advances it itself), so the rebuild-check schedule and the rebuild
+ * statistics see the current step. */
+int gb_step_counter_advance(uint64_t* d_timestep, void* stream);
+
 /* Snapshot transfer on the device: the per-particle loops of ParticleData::takeSnapshot
  * (hoomd/ParticleData.cc:1388-1617) and ParticleData::initializeFromSnapshot
  * (hoomd/ParticleData.cc:982-1379), which the reference runs on the host. Snapshot arrays are in
@@ -510,6 +523,18 @@ typedef struct gb_step_one_args
     const uint64_t* d_timestep; /* current step on the device; NULL = use timestep */
     uint64_t timestep;
     int noiseless;
+    /* Schedule of the rebuild check, NeighborList::shouldCheckDistance / needsUpdating
+     * (hoomd/md/NeighborList.cc:1313-1403), applied when d_last_update is non-NULL (NULL: the
+     * distance check every step, i.e. rebuild_check_delay = 1 with check_dist). The check is for
+     * step T = *d_check_step + 1 (the step whose forces follow); *d_last_update is the step of
+     * the last build (d_build_steps[0] of gb_cell_list_args). While T < last + check_delay nothing is checked. Otherwise the flag is
+     * raised without a distance check when r_buff < 1e-6, or without check_dist when
+     * check_delay is 0 or T == last + check_delay (check_delay > 1); in every other case the
+     * distance check decides. */
+    const uint64_t* d_check_step;
+    const uint64_t* d_last_update;
+    uint32_t check_delay;
+    int check_dist;
     } gb_step_one_args;
 
 int gb_md_step_one(const gb_step_one_args* args, void* stream);

@@ -1339,6 +1339,11 @@ template<class R> struct Sim
     R last_L[3] = {0, 0, 0};
     bool force_update = true;
     uint64_t n_builds = 0;
+    // rebuild-check schedule (nlist rebuild_check_delay, check_dist) and its counters: builds
+    // decided by a check (the reference's num_builds), dangerous builds
+    unsigned int check_delay = 1;
+    bool dist_check = true;
+    uint64_t last_updated = 0, n_updates = 0, n_dangerous = 0;
     // integrator
     R dt = 0;
     bool langevin = false;
@@ -1492,14 +1497,44 @@ template<class R> struct Sim
         return true;
         }
 
-    bool compute_forces()
+    // NeighborList::shouldCheckDistance / needsUpdating (hoomd/md/NeighborList.cc:1313-1418) for
+    // the forces of step T: a forced update builds at once; otherwise nothing is checked until
+    // check_delay steps after the last build, the list is rebuilt without a check when r_buff is
+    // tiny or (without dist_check) when the delay is 0 or just ran out, and the distance check
+    // decides in every other case. A build at the first check after a delay > 1 is dangerous.
+    bool needs_updating(uint64_t T)
         {
-        bool rebuild = force_update;
+        if (force_update)
+            {
+            force_update = false;
+            last_updated = T;
+            return true;
+            }
+        if (T < last_updated + check_delay)
+            return false;
+        const bool dangerous = dist_check && check_delay > 1 && T == last_updated + check_delay;
+        bool result;
+        if (r_buff < R(1e-6)
+            || (!dist_check
+                && (check_delay == 0 || (check_delay > 1 && T == last_updated + check_delay))))
+            result = true;
+        else
+            result = distance_check();
+        if (result)
+            {
+            last_updated = T;
+            n_updates++;
+            if (dangerous)
+                n_dangerous++;
+            }
+        return result;
+        }
+
+    bool compute_forces(uint64_t T)
+        {
         if (force_update)
             build_head_list();
-        force_update = false;
-        if (!rebuild)
-            rebuild = (r_buff < R(1e-6)) || distance_check();
+        const bool rebuild = needs_updating(T);
         if (rebuild)
             {
             // NeighborList::checkBoxSize (hoomd/md/NeighborList.cc:535-561)
@@ -1531,7 +1566,7 @@ template<class R> struct Sim
 
     bool prep_run()
         {
-        if (!compute_forces())
+        if (!compute_forces(timestep))
             return false;
         for (unsigned int j = 0; j < N; j++)
             {
@@ -1556,7 +1591,7 @@ template<class R> struct Sim
         if (langevin)
             {
             nve_step_one(N, pos.data(), vel.data(), accel.data(), image.data(), box, dt, nthreads);
-            if (!compute_forces())
+            if (!compute_forces(timestep + 1))
                 return false;
             const double e = langevin_step_two(N, vel.data(), accel.data(), pos.data(),
                                                tags.data(), force.data(), gamma.data(),
@@ -1578,7 +1613,7 @@ template<class R> struct Sim
             R s = R(std::sqrt(1.0 + double(dt) / tau * (kT / T_cur - 1.0)));
             cv_step_one(N, pos.data(), vel.data(), accel.data(), image.data(), box, dt, s,
                         nthreads);
-            if (!compute_forces())
+            if (!compute_forces(timestep + 1))
                 return false;
             cv_step_two(N, vel.data(), accel.data(), force.data(), dt, R(1.0), nthreads);
             timestep++;
@@ -1597,7 +1632,7 @@ template<class R> struct Sim
             double xi_prime = xi + drive;
             xi = xi_prime + drive;
             eta += xi_prime * ddt;
-            if (!compute_forces())
+            if (!compute_forces(timestep + 1))
                 return false;
             R s2 = R(std::exp(-(1.0 / 2.0) * xi * ddt));
             cv_step_two(N, vel.data(), accel.data(), force.data(), dt, s2, nthreads);
@@ -1616,7 +1651,7 @@ template<class R> struct Sim
             s = R(bussi_factor(K, dof(), double(dt), tau, kT, timestep, seed, tags[0]));
             }
         cv_step_one(N, pos.data(), vel.data(), accel.data(), image.data(), box, dt, s, nthreads);
-        if (!compute_forces())
+        if (!compute_forces(timestep + 1))
             return false;
         cv_step_two(N, vel.data(), accel.data(), force.data(), dt, R(1.0), nthreads);
         timestep++;
@@ -2006,7 +2041,14 @@ using namespace orc;
         if (accel)                                                                                 \
             std::copy(s->accel.begin(), s->accel.end(), accel);                                    \
         }                                                                                          \
-    /* stats: [timestep, n_builds, sum n_neigh, kinetic energy, potential energy] */               \
+    ORC_EXPORT void orc_sim_set_check_##SUF(void* h, unsigned int delay, int dist_check)           \
+        {                                                                                          \
+        auto* s = (Sim<R>*)h;                                                                      \
+        s->check_delay = delay;                                                                    \
+        s->dist_check = dist_check != 0;                                                           \
+        }                                                                                          \
+    /* stats: [timestep, n_builds, sum n_neigh, kinetic energy, potential energy, checked builds,  \
+       dangerous builds, step of the last build] */                                               \
     ORC_EXPORT void orc_sim_stats_##SUF(void* h, double* out5)                                     \
         {                                                                                          \
         auto* s = (Sim<R>*)h;                                                                      \
@@ -2021,6 +2063,9 @@ using namespace orc;
         out5[2] = nn;                                                                              \
         out5[3] = kinetic_energy<R>(s->N, s->vel.data());                                          \
         out5[4] = pe;                                                                              \
+        out5[5] = double(s->n_updates);                                                            \
+        out5[6] = double(s->n_dangerous);                                                          \
+        out5[7] = double(s->last_updated);                                                         \
         }                                                                                          \
     ORC_EXPORT void orc_sim_destroy_##SUF(void* h)                                                 \
         {                                                                                          \

@@ -551,11 +551,20 @@ class Sim:
                                                  ptr(accel))
         return dict(pos=pos, vel=vel, image=img, force=force, accel=accel)
 
+    def set_check(self, rebuild_check_delay=1, check_dist=True):
+        """The neighbour list's rebuild-check schedule (nlist rebuild_check_delay, check_dist)."""
+        getattr(lib(), f"orc_sim_set_check_{self._s}")(self.h, ctypes.c_uint(rebuild_check_delay),
+                                                        ctypes.c_int(int(check_dist)))
+
     def stats(self):
-        out = np.zeros(5, np.float64)
+        """n_builds counts every build, forced ones included; checked_builds only those a check
+        decided (the reference's num_builds), dangerous_builds those at the first check after a
+        delay > 1; last_update is the step of the last build."""
+        out = np.zeros(8, np.float64)
         getattr(lib(), f"orc_sim_stats_{self._s}")(self.h, ptr(out))
         return dict(timestep=int(out[0]), n_builds=int(out[1]), sum_n_neigh=out[2],
-                    kinetic_energy=out[3], potential_energy=out[4])
+                    kinetic_energy=out[3], potential_energy=out[4], checked_builds=int(out[5]),
+                    dangerous_builds=int(out[6]), last_update=int(out[7]))
 
     def __del__(self):
         try:

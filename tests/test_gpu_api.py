@@ -277,8 +277,10 @@ def test_conditional_build_graphs_match_gated_kernels(kT):
         integ.conditional_build = conditional
         l0 = integ.launch_count
         sim.run(230)
+        nb = cell.num_builds
         sim.run(70)
-        res.append((sim.state.get_snapshot(), cell.num_builds, integ.launch_count - l0))
+        nb += cell.num_builds
+        res.append((sim.state.get_snapshot(), nb, integ.launch_count - l0))
     (a, nb_a, la), (b, nb_b, lb) = res
     assert nb_a == nb_b and nb_a >= 5
     assert np.array_equal(a.particles.position, b.particles.position)
@@ -287,6 +289,66 @@ def test_conditional_build_graphs_match_gated_kernels(kT):
     # the gated graphs launch every build kernel on all 300 steps, the conditional ones only on
     # the rebuild steps (plus one kernel a step that sets the condition)
     assert la < lb
+
+
+def _schedule_run(r_buff, delay, dist_check, steps=40):
+    """The 512-particle fluid of the oracle's schedule test, run through the API."""
+    from test_oracle import sc_lattice
+    pos, (L, _, _) = sc_lattice(8, 1.2, 0.05, seed=3)
+    N = len(pos)
+    vel = np.zeros((N, 4), np.float32)
+    vel[:, 3] = 1.0
+    vel = O.thermalize(vel, np.arange(N), 1.5, 0, 9, prec=32)
+    snap = hoomd.Snapshot()
+    snap.configuration.box = [L, L, L, 0, 0, 0]
+    snap.particles.N = N
+    snap.particles.types = ["A"]
+    snap.particles.position[:] = np.asarray(pos, np.float32)
+    snap.particles.velocity[:] = vel[:, :3]
+    sim = make_sim(snap)
+    cell = md.nlist.Cell(buffer=r_buff, rebuild_check_delay=delay, check_dist=dist_check)
+    lj = md.pair.LJ(nlist=cell, default_r_cut=2.5)
+    lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+    sim.operations.integrator = md.Integrator(
+        dt=0.005, forces=[lj], methods=[md.methods.ConstantVolume(hoomd.filter.All())])
+    sim.run(steps)
+    return sim, cell
+
+
+@pytest.mark.parametrize("r_buff,delay,dist_check,builds,dangerous", [
+    (0.002, 4, True, 10, 10),   # thin buffer: every check after the delay finds the list stale
+    (0.002, 4, False, 10, 0),   # no distance check: a build every 4 steps, never dangerous
+    (0.4, 0, False, 40, 0),     # delay 0 without the distance check: every step
+    (0.002, 1, True, 40, 0),    # the default schedule with the thin buffer: every step
+])
+def test_rebuild_check_schedule(r_buff, delay, dist_check, builds, dangerous, capfd):
+    """rebuild_check_delay / check_dist (NeighborList::needsUpdating,
+    hoomd/md/NeighborList.cc:1313-1418) on the GPU: the same builds and dangerous builds as the
+    oracle's schedule on the same system, and the reference's notice for dangerous builds."""
+    sim, cell = _schedule_run(r_buff, delay, dist_check)
+    assert (cell.num_builds, cell.dangerous_builds) == (builds, dangerous)
+    assert sim._cpp_integrator.status()["last_update"] == 40
+    err = capfd.readouterr().err
+    assert ("dangerous neighbor list build" in err) == (dangerous > 0)
+    if delay > 1:
+        assert cell.shortest_rebuild == delay
+
+
+def test_delayed_check_matches_oracle():
+    """A check every third step with the 0.4 buffer: the GPU builds as often as the oracle from
+    the same state, never dangerously, and the trajectory follows the oracle's."""
+    from test_oracle import _schedule_sim
+    sim, cell = _schedule_run(0.4, 3, True, steps=60)
+    ref = _schedule_sim(0.4, 3, True, steps=60)
+    st = ref.stats()
+    assert cell.num_builds == st["checked_builds"] and cell.dangerous_builds == 0
+    assert cell.shortest_rebuild >= 3
+    snap = sim.state.get_snapshot()
+    pos = snap.particles.position + snap.particles.image * snap.configuration.box[:3]
+    r = ref.get()
+    L = np.array(snap.configuration.box[:3])
+    ref_pos = r["pos"][:, :3] + r["image"] * L
+    assert np.abs(pos - ref_pos).max() < 1e-3
 
 
 def test_adding_to_operations():

@@ -326,3 +326,51 @@ def test_bussi_thermostat_holds_temperature():
     sim.run(300)
     T = 2 * sim.stats()["kinetic_energy"] / (3 * N - 3)
     assert abs(T - 1.5) < 0.3
+
+
+def _schedule_sim(r_buff, delay, dist_check, steps=40):
+    """NeighborList::needsUpdating's schedule (hoomd/md/NeighborList.cc:1313-1418) in the
+    oracle: a fluid run of ``steps`` steps with the given buffer and rebuild-check settings."""
+    pos, L = sc_lattice(8, 1.2, 0.05, seed=3)
+    N = len(pos)
+    pos4 = O.make_pos4(pos, np.zeros(N), 32)
+    vel = np.zeros((N, 4), np.float32)
+    vel[:, 3] = 1.0
+    vel = O.thermalize(vel, np.arange(N), 1.5, 0, 9, prec=32)
+    sim = O.Sim(pos4, vel, np.zeros((N, 3), np.int32), np.arange(N), L, [[2.5]], r_buff, 0.005,
+                params=[[1.0, 1.0]], prec=32)
+    sim.set_check(delay, dist_check)
+    sim.run(steps)
+    return sim
+
+
+def test_oracle_rebuild_check_schedule():
+    # a buffer so thin that every check finds the list stale: with a delay of 4 the list is
+    # built at steps 4, 8, ..., 40, each at the first check after the delay (dangerous)
+    st = _schedule_sim(0.002, 4, True).stats()
+    assert (st["checked_builds"], st["dangerous_builds"], st["last_update"]) == (10, 10, 40)
+    # without the distance check: the same builds, none of them dangerous
+    st = _schedule_sim(0.002, 4, False).stats()
+    assert (st["checked_builds"], st["dangerous_builds"], st["last_update"]) == (10, 0, 40)
+    # rebuild_check_delay = 0 without the distance check: every step
+    st = _schedule_sim(0.4, 0, False).stats()
+    assert (st["checked_builds"], st["dangerous_builds"]) == (40, 0)
+    # the default (check every step) with the thin buffer: a build every step, none dangerous
+    st = _schedule_sim(0.002, 1, True).stats()
+    assert (st["checked_builds"], st["dangerous_builds"]) == (40, 0)
+    # check_dist=False with rebuild_check_delay = 1 still checks the distance (the reference's
+    # condition only skips the check for a delay of 0 or above 1)
+    a = _schedule_sim(0.4, 1, False).stats()
+    b = _schedule_sim(0.4, 1, True).stats()
+    assert a["checked_builds"] == b["checked_builds"] < 40
+
+
+def test_oracle_delayed_check_keeps_the_physics():
+    """With a buffer wide enough for the delay, a list checked every third step holds every
+    pair within r_cut, so the trajectory follows the every-step one to FP32 round-off."""
+    a = _schedule_sim(0.4, 3, True, steps=60)
+    b = _schedule_sim(0.4, 1, True, steps=60)
+    sa, sb = a.stats(), b.stats()
+    assert sa["dangerous_builds"] == 0
+    assert sa["checked_builds"] <= 60 // 3
+    assert np.abs(a.get()["pos"][:, :3] - b.get()["pos"][:, :3]).max() < 1e-3
