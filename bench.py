@@ -314,7 +314,11 @@ def run_gb300(args):
     if not wl.timed_thermostat:
         method.thermostat = None  # NVE for the timed steps
         sim._needs_prep = True
+    # the reference tunes its kernels' launch parameters during its first steps
+    # (hoomd/Autotuner.h); here the search runs once, on the warmed-up state, before the timing
+    sim.operations.tune_kernel_parameters()
     sim.run(3)
+    kernel_parameters = {**force.kernel_parameters, **cell.kernel_parameters}
     integ = sim._cpp_integrator
     stream = torch.cuda.ExternalStream(integ.streamHandle())
     sum_n = integ.sumNNeigh()
@@ -393,7 +397,7 @@ def run_gb300(args):
             "config": dict(wl.config),
             "parallelism": f"independent replicas x{world}" if world > 1 else "1 GPU",
             "pair_evals_per_s": sum_n * tps * world, "nlist_builds": builds,
-            "nlist_rollbacks": rollbacks,
+            "nlist_rollbacks": rollbacks, "kernel_parameters": kernel_parameters,
             "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk}
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <iostream>
 #include <sstream>
 
@@ -401,6 +402,7 @@ void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count
     a.d_r_listsq = d_r_listsq.get();
     a.ntypes = pd.ntypes;
     a.d_gate = d_gate;
+    a.block_size = kp_block;
     a.nlist_capacity = nlist.size();
     check(gb_nlist_build_binned(&a, s), "gb_nlist_build_binned");
     if (ex_pitch > 0)
@@ -786,6 +788,8 @@ gb_pair_args PairForce::pair_args(bool with_virial)
     a.ntypes = ntypes;
     a.shift_mode = (unsigned int)shift_mode;
     a.compute_virial = with_virial ? 1 : 0;
+    a.block_size = kp_block;
+    a.threads_per_particle = kp_tpp;
     if (uses_charge)
         {
         if (pd.charge.size() != pd.N)
@@ -1779,6 +1783,11 @@ void Integrator::run(uint64_t nsteps)
             f->upload();
             drop_graphs();
             }
+    bool tune = nlist->tune_requested;
+    for (auto& f : forces)
+        tune = tune || f->tune_requested;
+    if (tune && !npt)
+        last_tuning = autotune();
     if (npt)
         {
         run_npt(nsteps);
@@ -1810,6 +1819,122 @@ double Integrator::sum_n_neigh()
     for (uint32_t v : h)
         s += v;
     return s;
+    }
+
+std::vector<Integrator::TuneSample> Integrator::autotune()
+    {
+    ParticleData& pd = *pdata;
+    cudaStream_t s = pd.stream;
+    if (!prepared || nlist->dirty)
+        prepare();
+    checkpoint();
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "event");
+    cuda_check(cudaEventCreate(&e1), "event");
+    DevStatus* ds = d_status.get();
+    std::vector<TuneSample> out;
+    // two untimed launches, then the mean of five
+    auto time_it = [&](const std::function<void()>& fn) {
+        fn();
+        fn();
+        cuda_check(cudaEventRecord(e0, s), "record");
+        for (int r = 0; r < 5; r++)
+            fn();
+        cuda_check(cudaEventRecord(e1, s), "record");
+        cuda_check(cudaEventSynchronize(e1), "sync");
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms / 5.0;
+    };
+    try
+        {
+        if (nlist->tune_requested)
+            {
+            // a build at the current positions, as the forced build before the run made
+            double best = 1e30;
+            unsigned int pick = 0;
+            for (unsigned int b : {32u, 64u, 128u})
+                {
+                nlist->kp_block = b;
+                const double ms = time_it([&] {
+                    cuda_check(cudaMemsetAsync(ds->cell_cond, 0, sizeof(ds->cell_cond), s),
+                               "cond");
+                    cuda_check(cudaMemsetAsync(ds->nl_cond, 0, sizeof(ds->nl_cond), s), "cond");
+                    nlist->enqueue_build(nullptr, nullptr, ds->cell_cond, ds->nl_cond, s);
+                });
+                out.push_back({"nlist", b, 1u, ms});
+                if (ms < best)
+                    {
+                    best = ms;
+                    pick = b;
+                    }
+                }
+            nlist->kp_block = pick;
+            nlist->tune_requested = false;
+            }
+        const bool fused_path = forces.size() == 1 && !compute_virial
+                                && forces[0]->kind != PairKind::MLP
+                                && forces[0]->kind != PairKind::DPD;
+        for (auto& fp : forces)
+            {
+            PairForce& f = *fp;
+            if (!f.tune_requested)
+                continue;
+            // several lanes per particle serve the interleaved list of an orthorhombic box
+            // without XPLOR smoothing or virials
+            const bool split = pd.box.xy == 0.0f && pd.box.xz == 0.0f && pd.box.yz == 0.0f
+                               && f.shift_mode != 2 && !(compute_virial && !fused_path)
+                               && f.kind != PairKind::MLP;
+            std::vector<unsigned int> tpps = {1u};
+            if (split)
+                tpps = {1u, 4u, 8u};
+            double best = 1e30;
+            unsigned int pb = 0, pt = 0;
+            for (unsigned int b : {128u, 256u})
+                for (unsigned int t : tpps)
+                    {
+                    f.kp_block = b;
+                    f.kp_tpp = t;
+                    const double ms = time_it([&] {
+                        if (fused_path)
+                            {
+                            gb_pair_args a = f.pair_args(false);
+                            const gb_step_fuse fu = fuse_args(ds);
+                            check(f.launch_fused(a, fu, s), "fused pair step");
+                            }
+                        else
+                            f.compute(s, compute_virial);
+                    });
+                    out.push_back({"pair", b, t, ms});
+                    if (ms < best)
+                        {
+                        best = ms;
+                        pb = b;
+                        pt = t;
+                        }
+                    }
+            f.kp_block = pb;
+            f.kp_tpp = pt;
+            f.tune_requested = false;
+            }
+        }
+    catch (...)
+        {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        restore();
+        throw;
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    restore();
+    // the candidates' forces were computed at the restored positions; recompute them with the
+    // kept configuration so that every array matches it
+    for (auto& f : forces)
+        f->compute(s, compute_virial);
+    drop_graphs();
+    cuda_check(cudaStreamSynchronize(s), "autotune");
+    return out;
     }
 
 std::vector<double> Integrator::time_phases(unsigned int reps)

@@ -229,6 +229,10 @@ class NeighborList
     bool allocated = false;
     bool dirty = true; // r_cut or capacities changed: graphs must be rebuilt
     bool capacity_fixed = false; // start from exactly Nmax_cell / Nmax (tests of the growth path)
+    // kernel parameters (Autotuner): threads per block of the lane build (0 = default); a
+    // search on the live state runs at the next run when requested
+    unsigned int kp_block = 0;
+    bool tune_requested = false;
     // exclusions (NeighborList::addExclusion / filterNlist): unordered tag pairs, and per
     // particle index the excluded indices (rebuilt when a sort permutes the indices)
     void set_exclusions(const std::vector<uint32_t>& tag_pairs);
@@ -313,6 +317,10 @@ class PairForce
     std::vector<double> t_rmin;
     std::vector<std::vector<double>> t_U, t_F;
     bool params_dirty = true;
+    // kernel parameters (Autotuner): block size and threads per particle of the pair kernel
+    // (0 = the kernel's defaults); a search on the live state runs at the next run when requested
+    unsigned int kp_block = 0, kp_tpp = 0;
+    bool tune_requested = false;
     std::shared_ptr<MlpSurrogate> mlp;
     // plugin evaluator: its record and ntypes^2 parameter records of param_size bytes each
     const gb_pair_plugin* plugin = nullptr;
@@ -419,6 +427,17 @@ class Integrator
     // the engine's stream with CUDA events: [step one + rebuild check, cell list + neighbour
     // list build, fused pair step]; the state is checkpointed before and restored after
     std::vector<double> time_phases(unsigned int reps);
+    // the Autotuner's search (hoomd/Autotuner.h:49-668) for every pair force and the list that
+    // asked for one: each candidate launch configuration timed on the current state (the state
+    // restored afterwards), the fastest kept; returns {name, block, tpp, ms} per candidate
+    struct TuneSample
+        {
+        std::string kernel;
+        unsigned int block, tpp;
+        double ms;
+        };
+    std::vector<TuneSample> autotune();
+    std::vector<TuneSample> last_tuning;
     uintptr_t stream_handle() const
         {
         return (uintptr_t)pdata->stream;

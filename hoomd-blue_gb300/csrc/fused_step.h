@@ -6,10 +6,11 @@
 namespace gb
 {
 // Scratch layout: [0, 256) counter word; [256, ...) 3 doubles per block of the pair kernel. The
-// kernel may run up to 8 lanes per particle (small systems), so room for 8 N threads.
+// kernel may run up to 8 lanes per particle (small systems) in blocks of 128 or 256 threads, so
+// room for 8 N threads in blocks of 128.
 inline size_t step_scratch_bytes(unsigned int N)
     {
-    return 256 + 3 * sizeof(double) * (size_t)div_up(8ull * (N > 0 ? N : 1), 256);
+    return 256 + 3 * sizeof(double) * (size_t)div_up(8ull * (N > 0 ? N : 1), 128);
     }
 
 inline int make_fuse_args(const gb_pair_args* a, const gb_step_fuse* f, FuseArgs& fz)
@@ -18,7 +19,8 @@ inline int make_fuse_args(const gb_pair_args* a, const gb_step_fuse* f, FuseArgs
     GB_REQUIRE(f->d_vel && f->d_accel && f->d_scratch && f->d_thermo,
                "fused step: velocities, accelerations, scratch and thermo output are required");
     GB_REQUIRE(a->d_head_list == nullptr, "fused step: column-major neighbour list required");
-    GB_REQUIRE(a->block_size == 0 || a->block_size == 256, "fused step: block size 256");
+    GB_REQUIRE(a->block_size == 0 || a->block_size == 128 || a->block_size == 256,
+               "fused step: block size 128 or 256");
     GB_REQUIRE(!f->bussi || (f->d_timestep && f->d_factor && f->d_status),
                "fused step: Bussi needs timestep, factor and status buffers");
     fz.vel = reinterpret_cast<float4*>(f->d_vel);

@@ -428,6 +428,27 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def_readwrite("check_dist", &NeighborList::check_dist)
         .def_readwrite("rebuild_check_delay", &NeighborList::rebuild_check_delay)
         .def("getDim", &NeighborList::dims)
+        .def("getAutotunerParameters",
+             [](NeighborList& n) {
+                 py::dict d;
+                 d["nlist"] = py::make_tuple(n.kp_block ? n.kp_block : 128u);
+                 return d;
+             })
+        .def("setAutotunerParameters",
+             [](NeighborList& n, py::dict d) {
+                 for (auto kv : d)
+                     {
+                     if (py::str(kv.first).cast<std::string>() != "nlist")
+                         throw py::key_error("no kernel " + py::str(kv.first).cast<std::string>());
+                     auto t = kv.second.cast<std::vector<unsigned int>>();
+                     if (t.size() != 1 || (t[0] != 32 && t[0] != 64 && t[0] != 128))
+                         throw py::value_error("nlist: (block size 32, 64 or 128)");
+                     n.kp_block = t[0];
+                     }
+                 n.tune_requested = false;
+             })
+        .def("isAutotuningComplete", [](NeighborList& n) { return !n.tune_requested; })
+        .def("startAutotuning", [](NeighborList& n) { n.tune_requested = true; })
         .def("getNmax", [](NeighborList& n) { return n.Nmax_cell; })
         .def("getNmaxPerType", [](NeighborList& n) { return n.Nmax; })
         .def("getRList", [](NeighborList& n) { return n.r_listsq; })
@@ -480,6 +501,35 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         }))
         .def("setParamsLJ", &PairForce::set_params_lj)
         .def("setParamsExample", &PairForce::set_params_example)
+        // Autotuner interface (hoomd/Autotuner.h, AutotunedObject in hoomd/operation.py)
+        .def("getAutotunerParameters",
+             [](PairForce& f) {
+                 // the values in use: the set ones, else the kernel's defaults
+                 const unsigned int N = f.pdata->N;
+                 const unsigned int tpp
+                     = f.kp_tpp ? f.kp_tpp : (N <= 16384 ? 8u : (N <= 65536 ? 4u : 1u));
+                 py::dict d;
+                 d["pair"] = py::make_tuple(f.kp_block ? f.kp_block : 256u, tpp);
+                 return d;
+             })
+        .def("setAutotunerParameters",
+             [](PairForce& f, py::dict d) {
+                 for (auto kv : d)
+                     {
+                     if (py::str(kv.first).cast<std::string>() != "pair")
+                         throw py::key_error("no kernel " + py::str(kv.first).cast<std::string>());
+                     auto t = kv.second.cast<std::vector<unsigned int>>();
+                     if (t.size() != 2 || (t[0] != 128 && t[0] != 256)
+                         || (t[1] != 1 && t[1] != 4 && t[1] != 8))
+                         throw py::value_error("pair: (block size 128 or 256, threads per "
+                                               "particle 1, 4 or 8)");
+                     f.kp_block = t[0];
+                     f.kp_tpp = t[1];
+                     }
+                 f.tune_requested = false;
+             })
+        .def("isAutotuningComplete", [](PairForce& f) { return !f.tune_requested; })
+        .def("startAutotuning", [](PairForce& f) { f.tune_requested = true; })
         .def("setParamsTable", &PairForce::set_params_table)
         .def("setParamsRadial", &PairForce::set_params_radial)
         .def("setParamsDPD", &PairForce::set_params_dpd)
@@ -640,6 +690,13 @@ PYBIND11_MODULE(_hoomd_gb300, m)
     py::class_<Integrator, std::shared_ptr<Integrator>>(m, "IntegratorTwoStep")
         .def(py::init<std::shared_ptr<ParticleData>, std::shared_ptr<NeighborList>, double>())
         .def("addForce", &Integrator::add_force)
+        .def("lastTuning",
+             [](Integrator& in) {
+                 py::list out;
+                 for (auto& t : in.last_tuning)
+                     out.append(py::make_tuple(t.kernel, t.block, t.tpp, t.ms));
+                 return out;
+             })
         .def("setBussi", &Integrator::set_thermostat_bussi)
         .def("setNoThermostat", &Integrator::set_thermostat_none)
         .def("setLangevin", &Integrator::set_langevin)

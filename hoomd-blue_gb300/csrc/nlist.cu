@@ -815,7 +815,7 @@ bool launch_nlist_tile(const gb_nlist_args& a, unsigned int ncell, cudaStream_t 
     const bool ortho = a.box.xy == 0.0f && a.box.xz == 0.0f && a.box.yz == 0.0f;
     if (a.nlist_capacity != 0 && a.nlist_capacity <= 0xffffffffull)
         {
-        int wpb = LANE_WARPS;
+        int wpb = a.block_size ? (int)(a.block_size / 32) : LANE_WARPS;
         size_t smem = lane_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, wpb);
         while (smem > 96 * 1024 && wpb > 1)
             smem = lane_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, --wpb);
@@ -1077,6 +1077,9 @@ extern "C"
                    "gb_nlist_build_binned: column-major stride must be >= N");
         GB_REQUIRE(a->adj_width >= 1 && a->adj_width <= 27, "gb_nlist_build_binned: adj width");
         GB_REQUIRE(a->ntypes <= 64, "gb_nlist_build_binned: at most 64 types");
+        GB_REQUIRE(a->block_size == 0 || a->block_size == 32 || a->block_size == 64
+                       || a->block_size == 128,
+                   "gb_nlist_build_binned: block_size must be 32, 64 or 128");
         const unsigned int ncell = a->dim[0] * a->dim[1] * a->dim[2];
         if (ncell == 0 || a->N == 0)
             return GB_OK;

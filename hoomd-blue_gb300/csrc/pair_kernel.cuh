@@ -676,17 +676,18 @@ __global__ void __launch_bounds__(256, (FUSE || VIRIAL || XPLOR) ? 4 : 5)
     }
 
 // Blocks of one kernel resident on the current GPU at once (SM count x blocks per SM), cached
-// per kernel, dynamic shared memory size and device.
+// per kernel, block size, dynamic shared memory size and device.
 struct ResidentGrid
     {
     int dev = -1;
     size_t smem = ~size_t(0);
+    unsigned int blk = 0;
     unsigned int n = 0;
     unsigned int blocks(const void* kern, unsigned int block, size_t smem_bytes)
         {
         int d = 0;
         cudaGetDevice(&d);
-        if (d != dev || smem_bytes != smem)
+        if (d != dev || smem_bytes != smem || block != blk)
             {
             int sms = 0, per_sm = 0;
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d);
@@ -694,6 +695,7 @@ struct ResidentGrid
             n = (unsigned int)std::max(1, sms * std::max(1, per_sm));
             dev = d;
             smem = smem_bytes;
+            blk = block;
             }
         return n;
         }
@@ -703,7 +705,7 @@ template<class Eval, bool MULTI, bool ORTHO, bool FUSE, bool VIRIAL, bool XPLOR,
 int launch_pair_i4_inst(const gb_pair_args& a, const typename Eval::param_type* d_params,
                         const float* ext, const FuseArgs& fz, cudaStream_t s)
     {
-    const unsigned int block = 256;
+    const unsigned int block = a.block_size ? a.block_size : 256u;
     const size_t smem = i4_param_bytes<typename Eval::param_type>(a.ntypes, MULTI);
     auto kern = k_pair_i4<Eval, MULTI, ORTHO, FUSE, VIRIAL, XPLOR, TPP>;
     if (smem > 48 * 1024)
@@ -754,8 +756,8 @@ int dispatch_pair_i4(const gb_pair_args& a, const typename Eval::param_type* d_p
                      const float* ext, const FuseArgs& fz, cudaStream_t s)
     {
     GB_REQUIRE(a.shift_mode <= 2, "pair force: shift_mode must be 0, 1 or 2");
-    GB_REQUIRE(a.block_size == 0 || a.block_size == 256,
-               "pair force: the interleaved-list kernel runs 256-thread blocks");
+    GB_REQUIRE(a.block_size == 0 || a.block_size == 128 || a.block_size == 256,
+               "pair force: the interleaved-list kernel runs 128- or 256-thread blocks");
     GB_REQUIRE(!(FUSE && a.compute_virial), "fused step: the virial is not computed");
     GB_REQUIRE(a.box.periodic[0] && a.box.periodic[1] && a.box.periodic[2],
                "pair force: the interleaved-list kernel needs a box periodic in every direction");

@@ -19,7 +19,7 @@ C++) on hand-written sm_103a kernels reached through the C ABI of include/hoomd_
 """
 
 from hoomd_gb300._native import _hoomd_gb300  # noqa: F401  (fails loudly when not built)
-from hoomd_gb300 import device, filter, trigger, tune  # noqa: E402
+from hoomd_gb300 import device, error, filter, operation, trigger, tune  # noqa: E402
 from hoomd_gb300.box import Box  # noqa: E402
 from hoomd_gb300.snapshot import Snapshot  # noqa: E402
 from hoomd_gb300.simulation import Simulation  # noqa: E402

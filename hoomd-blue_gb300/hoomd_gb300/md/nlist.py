@@ -5,6 +5,7 @@ import numpy as np
 
 from hoomd_gb300._native import _hoomd_gb300
 from hoomd_gb300.md.data import TypePairDict, nonnegative_real
+from hoomd_gb300.operation import AutotunedObject
 
 
 def excluded_pairs(topology, exclusions, N):
@@ -57,7 +58,7 @@ def excluded_pairs(topology, exclusions, N):
     return np.unique(np.concatenate(out), axis=0).astype(np.uint32)
 
 
-class NeighborList:
+class NeighborList(AutotunedObject):
     _loggables = {"num_builds": "scalar", "shortest_rebuild": "scalar", "dimensions": "sequence",
                   "allocated_particles_per_cell": "scalar"}
 

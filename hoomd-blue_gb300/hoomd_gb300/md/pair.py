@@ -17,11 +17,12 @@ import numpy as np
 
 from hoomd_gb300._native import _hoomd_gb300
 from hoomd_gb300.md.data import TypePairDict, dict_validator, nonnegative_real
+from hoomd_gb300.operation import AutotunedObject
 
 _MODES = {"none": 0, "shift": 1, "xplor": 2}
 
 
-class Pair:
+class Pair(AutotunedObject):
     """Base pair force (hoomd/md/pair/pair.py:18-161)."""
 
     _accepted_modes = ("none", "shift", "xplor")

@@ -21,6 +21,33 @@ class Operations:
     def integrator(self):
         return self._integrator
 
+    def _tuned_objects(self):
+        integ = self._integrator
+        out = []
+        if integ is not None:
+            for f in integ.forces:
+                out.append(f)
+                if getattr(f, "nlist", None) is not None and f.nlist not in out:
+                    out.append(f.nlist)
+        return [o for o in out if getattr(o, "_cpp_obj", None) is not None]
+
+    @property
+    def is_tuning_complete(self):
+        """hoomd.Operations.is_tuning_complete: every attached object's kernel parameters are
+        settled."""
+        if self._simulation._cpp_integrator is None:
+            from hoomd_gb300.error import DataAccessError
+            raise DataAccessError("is_tuning_complete")
+        return all(o.is_tuning_complete for o in self._tuned_objects())
+
+    def tune_kernel_parameters(self):
+        """hoomd.Operations.tune_kernel_parameters: search every attached object's kernel
+        parameters at the start of the next run."""
+        if self._simulation._cpp_integrator is None:
+            raise RuntimeError("Call Simulation.run() before tune_kernel_parameters.")
+        for o in self._tuned_objects():
+            o.tune_kernel_parameters()
+
     @integrator.setter
     def integrator(self, integrator):
         if self._integrator is not None:

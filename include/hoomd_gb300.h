@@ -150,6 +150,9 @@ typedef struct gb_nlist_args
     const float* d_r_listsq;          /* [ntypes^2] (r_cut + r_buff)^2, 0 where r_cut <= 0 */
     unsigned int ntypes;
     const uint32_t* d_gate;           /* optional no-op gate, as for the cell list */
+    /* threads per block of the lane-per-particle build: 32, 64 or 128 (0 = 128), a warp per cell
+       (the kernel parameter the reference's Autotuner varies, hoomd/md/NeighborListGPUBinned.h) */
+    uint32_t block_size;
     uint64_t nlist_capacity;          /* words allocated at d_nlist, or 0 when unknown; below 2^32
                                          the tiled build addresses slots with 32-bit offsets
                                          (one lane per particle), else it uses the warp-per-cell
@@ -188,7 +191,9 @@ int gb_nlist_head_list(uint64_t* d_head_list, uint64_t* d_total, const float* d_
  * The evaluator parameter structs below are byte-for-byte the FP32 param_type of the reference
  * evaluators. threads_per_particle: flat head lists take 1-32 (0 = 8); plain column-major lists
  * take 1; the interleaved list takes 1, 4 or 8 lanes per particle (0 = by N: 8 up to 16,384
- * particles, 4 up to 65,536, else 1; virials and XPLOR use 1).
+ * particles, 4 up to 65,536, else 1; virials and XPLOR use 1). block_size: the interleaved list
+ * takes 128 or 256 threads (0 = 256), the others a multiple of 32 up to 1024 (0 = 256); these
+ * are the kernel parameters the reference's Autotuner varies (hoomd/md/PotentialPairGPU.h:76-81).
  * ------------------------------------------------------------------------------------------- */
 typedef struct gb_pair_args
     {

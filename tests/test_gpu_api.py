@@ -351,6 +351,50 @@ def test_delayed_check_matches_oracle():
     assert np.abs(pos - ref_pos).max() < 1e-3
 
 
+def test_kernel_parameters_and_tuning():
+    """AutotunedObject (hoomd/operation.py:391-497) on the pair force and the list: the values in
+    use, setting them (validated), and the search, which times every candidate launch
+    configuration on the live state and keeps the fastest. Forces and neighbour sets do not
+    depend on the configuration beyond FP32 summation order."""
+    snap = workloads.lj_fluid_sc(16)
+    sim, lj, cell, thermo = lj_sim(snap, kT=None, thermalize=1.5)
+    with pytest.raises(hoomd.error.DataAccessError):
+        _ = lj.kernel_parameters
+    sim.run(0)
+    assert lj.kernel_parameters == {"pair": (256, 8)}  # 4096 particles: 8 lanes per particle
+    assert cell.kernel_parameters == {"nlist": (128,)}
+    assert lj.is_tuning_complete and cell.is_tuning_complete
+    assert sim.operations.is_tuning_complete
+    with pytest.raises(ValueError):
+        lj.kernel_parameters = {"pair": (64, 1)}
+    with pytest.raises(KeyError):
+        cell.kernel_parameters = {"pair": (64,)}
+    pairs0 = {tuple(p) for p in np.sort(cell.pair_list(), axis=1)}
+    f0 = lj.forces
+
+    sim.operations.tune_kernel_parameters()
+    assert not sim.operations.is_tuning_complete
+    sim.run(10)
+    assert sim.operations.is_tuning_complete
+    samples = sim._cpp_integrator.lastTuning()
+    pair = [s for s in samples if s[0] == "pair"]
+    nl = [s for s in samples if s[0] == "nlist"]
+    assert len(pair) == 6 and len(nl) == 3 and all(s[3] > 0 for s in samples)
+    best = min(pair, key=lambda s: s[3])
+    assert lj.kernel_parameters["pair"] == (best[1], best[2])
+    assert cell.kernel_parameters["nlist"] == (min(nl, key=lambda s: s[3])[1],)
+
+    sim2, lj2, cell2, _ = lj_sim(snap, kT=None, thermalize=1.5)
+    sim2.run(0)
+    for pcfg, ncfg in [((128, 1), (32,)), ((256, 4), (64,)), ((128, 8), (128,))]:
+        lj2.kernel_parameters = {"pair": pcfg}
+        cell2.kernel_parameters = {"nlist": ncfg}
+        sim2.run(0)
+        assert lj2.kernel_parameters == {"pair": pcfg}
+        assert {tuple(p) for p in np.sort(cell2.pair_list(), axis=1)} == pairs0
+        assert np.allclose(lj2.forces, f0, rtol=1e-5, atol=1e-5 * np.abs(f0).max())
+
+
 def test_adding_to_operations():
     """hoomd/md/pytest/test_potential.py:1296-1305: a force added to the operations (no
     integrator) is a compute evaluated at the current positions."""
