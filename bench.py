@@ -506,6 +506,11 @@ def run_mlp(args):
     ms_m, launches_m = timed(sim_m, args.steps)
     clk_m = clocks.stop() if clocks else None
     phases_m = sim_m._cpp_integrator.timePhases(10)
+    # the same run on the legacy warp-level mma.sync path, for comparison
+    sur._cpp.tensor_kernel = "mma.sync"
+    ms_ms, _ = timed(sim_m, args.steps)
+    phases_ms = sim_m._cpp_integrator.timePhases(10)
+    sur._cpp.tensor_kernel = "tcgen05"
     tps_t = args.steps / (ms_t / 1e3)
     tps_m = args.steps / (ms_m / 1e3)
     # tensor-pipe roofline of the surrogate force: FLOPs of the per-pair products
@@ -528,14 +533,18 @@ def run_mlp(args):
                            train_steps=args.mlp_train_steps, train_batch=8192,
                            train_samples=int(len(samples["r"])), train_frames=args.mlp_frames),
             "table_tps": tps_t, "mlp_over_table": tps_m / tps_t,
+            "tensor_kernel": "tcgen05 (128-pair tiles, TMEM accumulators)",
+            "mma_sync_tps": args.steps / (ms_ms / 1e3),
             "force_rmse": rmse, "force_rms": frms, "force_rmse_target": 1e-3,
             "force_rmse_ref": "GPU Table path (FP32; within 1e-5 of the FP64 oracle)",
             "train_s": t_train, "sample_s": t_sample, "train_loss": losses[-3:],
             "phases_ms": {"table": dict(zip(["step_one", "rebuild", "pair_step"], phases_t)),
-                          "mlp": dict(zip(["step_one", "rebuild", "force+step_two"], phases_m))},
+                          "mlp": dict(zip(["step_one", "rebuild", "force+step_two"], phases_m)),
+                          "mlp_mma_sync": dict(zip(["step_one", "rebuild", "force+step_two"],
+                                                   phases_ms))},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_mlp_forces (+ pair list, step two, thermo)",
+                         "kernel": "k_mlp_forces_tc (+ pair list, step two, thermo)",
                          "flops_formula": "pairs in [r_min, r_cut) (0.5 N rho 4/3 pi (rc^3 - "
                                           "rmin^3)) x 2 x 2 x (32x64 + 64x64)",
                          "peak_kind": pk},

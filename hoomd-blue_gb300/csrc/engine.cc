@@ -829,6 +829,7 @@ void PairForce::compute(cudaStream_t s, bool with_virial)
         m.act_split = mlp->act_split;
         m.d_infer = mlp->infer_block();
         m.d_scratch = mlp_scratch.get();
+        m.mma_sync = mlp->mma_sync;
         check(gb_mlp_forces(&m, s), "gb_mlp_forces");
         virial_valid = false;
         return;

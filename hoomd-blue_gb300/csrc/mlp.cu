@@ -30,8 +30,19 @@ constexpr int S_GZ2 = 0, S_H1 = 64, S_GDZ2 = 128, S_DH1 = 192, S_GZ1 = 256, S_GD
               S_H2 = 384, S_DH2 = 448, S_PHI = 512, S_DPHI = 544, S_E = 576, S_GU = 592,
               S_GD = 593, S_LOSS = 594, SW = 596;
 
-// inference block (bytes)
-constexpr size_t I_FW1 = 0, I_FW2 = 4096, I_B2 = 12288, I_W3 = 12544, I_B3 = 12800, I_C = 12816;
+// inference block (bytes): mma.sync fragments of W1r and W2, b2, w3, b3, the tcgen05 operand
+// images of W1r and W2 (K-major core-matrix layout), then C[p] per type pair
+constexpr size_t I_FW1 = 0, I_FW2 = 4096, I_B2 = 12288, I_W3 = 12544, I_B3 = 12800,
+                 I_TW1 = 12816, I_TW2 = 16912, I_C = 25104;
+
+// Byte offset of element (row, k) of a K-major tcgen05 operand with K columns in the
+// no-swizzle layout: core matrices of 8 rows x 16 bytes, K-adjacent core matrices 128 bytes
+// apart (the descriptor's leading-dimension offset), row groups K / 8 * 128 bytes apart (its
+// stride-dimension offset).
+__host__ __device__ constexpr uint32_t tc_off(int row, int k, int K)
+    {
+    return (uint32_t)((row >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+    }
 
 __host__ __device__ inline size_t param_count(uint32_t n_pairs)
     {
@@ -288,6 +299,19 @@ __global__ void k_prepare(const float* __restrict__ th, uint32_t n_pairs, unsign
         {
         b2[tid] = th[O_B2 + tid];
         w3[tid] = q_bf16(th[O_W3 + tid]);
+        }
+    // tcgen05 B operands: B[k][n] = W[n][k], stored as the K-major N x K matrix W
+    if (tid < HID * RBF)
+        {
+        const uint32_t n = tid / RBF, k = tid % RBF;
+        *reinterpret_cast<__nv_bfloat16*>(inf + I_TW1 + tc_off((int)n, (int)k, RBF))
+            = __float2bfloat16_rn(th[O_W1R + n * RBF + k]);
+        }
+    if (tid < HID * HID)
+        {
+        const uint32_t n = tid / HID, k = tid % HID;
+        *reinterpret_cast<__nv_bfloat16*>(inf + I_TW2 + tc_off((int)n, (int)k, HID))
+            = __float2bfloat16_rn(th[O_W2 + n * HID + k]);
         }
     if (tid == 0)
         *reinterpret_cast<float*>(inf + I_B3) = th[O_B3];
@@ -687,6 +711,340 @@ __global__ void __launch_bounds__(128)
         __syncwarp();
         }
     }
+
+// ------------------------------------------------------------------------------------------------
+// tcgen05 inference: tiles of 128 pairs, one pair per TMEM lane
+// ------------------------------------------------------------------------------------------------
+// A CTA of 256 threads walks tiles of 128 pairs. Rows (pairs) are the M = 128 lanes of the
+// tensor memory; warp w serves lanes 32 (w % 4) .. + 31 and hidden units 32 (w / 4) .. + 31, so
+// two threads share a row. Per tile: the radial features (value and r-derivative, each as a
+// bfloat16 high part and its bfloat16 remainder) go to shared memory as K-major operands; one
+// thread issues the layer-1 products (M = 128, N = 64, K = 32 in two K = 16 steps, high and low
+// parts accumulated into the same FP32 accumulator) into tensor memory and commits them to an
+// mbarrier; after the wait every thread reads its row's accumulators with tcgen05.ld, adds C[p],
+// applies SiLU and its derivative and writes the layer-2 operands (K = 64) over the layer-1 ones;
+// the layer-2 products go to four more accumulator columns; the output layer, the radial
+// derivative and the forces follow in registers, and each pair adds its force to both particles
+// with float4 atomics. Tensor memory: 4 accumulators x 64 FP32 columns = 256 columns per CTA,
+// two CTAs per SM. Every wait on the mbarrier is bounded; a wait that runs out records an error
+// and all threads leave the tile loop together, free the tensor memory and return.
+constexpr int TC_THREADS = 256;
+constexpr uint32_t TC_OP = 0;                        // operands: 4 x (128 x 64) bf16 = 64 KB
+constexpr uint32_t TC_W1 = 65536;                    // W1r image, 64 x 32 bf16
+constexpr uint32_t TC_W2 = TC_W1 + 4096;             // W2 image, 64 x 64 bf16
+constexpr uint32_t TC_B2 = TC_W2 + 8192;             // b2, w3 (64 floats each)
+constexpr uint32_t TC_W3 = TC_B2 + 256;
+constexpr uint32_t TC_PART = TC_W3 + 256;            // 128 x float2: second-half partial sums
+constexpr uint32_t TC_MISC = TC_PART + 1024;         // mbarrier, tensor-memory base, b3
+constexpr uint32_t TC_SMEM = TC_MISC + 64;
+constexpr uint32_t TC_TMEM_COLS = 256;
+// instruction descriptor (kind::f16): FP32 accumulator, BF16 A and B, both K-major,
+// N = 64 (N >> 3 at bit 17), M = 128 (M >> 4 at bit 24)
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17)
+                              | ((128u >> 4) << 24);
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+    {
+    return (uint32_t)__cvta_generic_to_shared(p);
+    }
+
+// shared-memory matrix descriptor of a K-major operand with K columns (no swizzle)
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, int K)
+    {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16)
+           | ((uint64_t)(((uint32_t)K / 8u * 128u) >> 4) << 32) | ((uint64_t)1 << 46);
+    }
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc)
+    {
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                 ::"r"(tmem_d), "l"(a), "l"(b), "r"(TC_IDESC), "r"(acc));
+    }
+
+__device__ __forceinline__ void tc_commit(uint64_t* mbar)
+    {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(smem_addr(mbar)));
+    }
+
+// bounded wait for the mbarrier phase with the given parity; true when it completed
+__device__ __forceinline__ bool tc_wait(uint64_t* mbar, uint32_t parity)
+    {
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < TC_WAIT_LIMIT && !done; it++)
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     "selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(smem_addr(mbar)), "r"(parity));
+    return done != 0;
+    }
+
+// 32 consecutive FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32])
+    {
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+                 "%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,"
+                 "%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                   "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                   "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]),
+                   "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                   "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+                   "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+        v[c] = __uint_as_float(r[c]);
+    }
+
+// eight values as a 16-byte row of a core matrix: the high bfloat16 parts, or the remainders
+__device__ __forceinline__ uint4 bf16x8(const float* v, bool remainder)
+    {
+    float x[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++)
+        x[e] = remainder ? bf16_rem(v[e]) : v[e];
+    return make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]),
+                      pack_bf16(x[6], x[7]));
+    }
+
+template<bool SPLIT>
+__global__ void __launch_bounds__(TC_THREADS, 2)
+    k_mlp_forces_tc(const unsigned char* __restrict__ inf, const float4* __restrict__ pos,
+                    gb_box box, unsigned int ntypes, uint32_t n_pairs, float r_min, float r_cut,
+                    const uint2* __restrict__ pairs, const unsigned int* __restrict__ count,
+                    float4* __restrict__ force, uint32_t* __restrict__ err)
+    {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    const uint32_t tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    const uint32_t quarter = warp & 3u, half = warp >> 2;
+    const uint32_t row = 32u * quarter + lane;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + TC_MISC);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + TC_MISC + 8);
+    float* b3s = reinterpret_cast<float*>(sm + TC_MISC + 12);
+    const float* b2 = reinterpret_cast<const float*>(sm + TC_B2);
+    const float* w3 = reinterpret_cast<const float*>(sm + TC_W3);
+    float2* part = reinterpret_cast<float2*>(sm + TC_PART);
+
+    // weights and biases into shared memory
+    {
+    const uint4* src1 = reinterpret_cast<const uint4*>(inf + I_TW1);
+    const uint4* src2 = reinterpret_cast<const uint4*>(inf + I_TW2);
+    uint4* dst1 = reinterpret_cast<uint4*>(sm + TC_W1);
+    uint4* dst2 = reinterpret_cast<uint4*>(sm + TC_W2);
+    for (uint32_t k = tid; k < 4096 / 16; k += TC_THREADS)
+        dst1[k] = src1[k];
+    for (uint32_t k = tid; k < 8192 / 16; k += TC_THREADS)
+        dst2[k] = src2[k];
+    if (tid < HID)
+        {
+        reinterpret_cast<float*>(sm + TC_B2)[tid] = reinterpret_cast<const float*>(inf + I_B2)[tid];
+        reinterpret_cast<float*>(sm + TC_W3)[tid] = reinterpret_cast<const float*>(inf + I_W3)[tid];
+        }
+    if (tid == 0)
+        {
+        *b3s = *reinterpret_cast<const float*>(inf + I_B3);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        }
+    if (warp == 0)
+        {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_addr(tmem_slot)), "r"(TC_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        }
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t t_lane = tmem + ((32u * quarter) << 16);
+    const uint32_t op = smem_addr(sm + TC_OP), w1a = smem_addr(sm + TC_W1),
+                   w2a = smem_addr(sm + TC_W2);
+    const float* C = reinterpret_cast<const float*>(inf + I_C);
+    const float hstep = (r_cut - r_min) / (float)(RBF - 1);
+    const float gamma = 1.0f / (2.0f * hstep * hstep);
+    const unsigned int n = *count;
+    uint32_t parity = 0;
+
+    for (uint32_t tile = blockIdx.x; tile * 128u < n; tile += gridDim.x)
+        {
+        // geometry of this thread's row (both threads of a row compute it)
+        const uint32_t s = tile * 128u + row;
+        const bool v = s < n;
+        const uint2 pr = v ? pairs[s] : make_uint2(0u, 0u);
+        const float4 pi = pos[pr.x], pj = pos[pr.y];
+        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        min_image(box, dx, dy, dz);
+        const float r = v ? sqrtf(dx * dx + dy * dy + dz * dz) : r_min;
+        uint32_t p;
+        {
+        const unsigned int ta = __float_as_uint(pi.w), tb = __float_as_uint(pj.w);
+        const unsigned int a = min(ta, tb), b = max(ta, tb);
+        p = v ? min(a * ntypes - a * (a - 1) / 2 + (b - a), n_pairs - 1) : 0u;
+        }
+        // layer-1 operands: features 16 half .. 16 half + 15 of this row
+        {
+        float ph[16], dph[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++)
+            {
+            const int k = 16 * (int)half + q;
+            const float mu = r_min + (float)k * hstep;
+            const float d = r - mu;
+            const float e = __expf(-gamma * d * d);
+            ph[q] = e;
+            dph[q] = -2.0f * gamma * d * e;
+            }
+#pragma unroll
+        for (int g = 0; g < 2; g++)
+            {
+            const uint32_t off = tc_off((int)row, 16 * (int)half + 8 * g, RBF);
+            *reinterpret_cast<uint4*>(sm + TC_OP + 0 * 8192 + off) = bf16x8(ph + 8 * g, false);
+            *reinterpret_cast<uint4*>(sm + TC_OP + 2 * 8192 + off) = bf16x8(dph + 8 * g, false);
+            if (SPLIT)
+                {
+                *reinterpret_cast<uint4*>(sm + TC_OP + 1 * 8192 + off) = bf16x8(ph + 8 * g, true);
+                *reinterpret_cast<uint4*>(sm + TC_OP + 3 * 8192 + off) = bf16x8(dph + 8 * g, true);
+                }
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (tid == 0)
+            {
+#pragma unroll
+            for (int k = 0; k < RBF / 16; k++)
+                {
+                const uint64_t bw = tc_desc(w1a + 256u * k, RBF);
+                tc_mma(tmem + 0, tc_desc(op + 0 * 8192 + 256u * k, RBF), bw, k > 0);
+                tc_mma(tmem + 64, tc_desc(op + 2 * 8192 + 256u * k, RBF), bw, k > 0);
+                if (SPLIT)
+                    {
+                    tc_mma(tmem + 0, tc_desc(op + 1 * 8192 + 256u * k, RBF), bw, 1u);
+                    tc_mma(tmem + 64, tc_desc(op + 3 * 8192 + 256u * k, RBF), bw, 1u);
+                    }
+                }
+            tc_commit(mbar);
+            }
+        if (!__syncthreads_and(tc_wait(mbar, parity)))
+            {
+            if (tid == 0)
+                atomicExch(err, 1u);
+            break;
+            }
+        parity ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // layer 1 epilogue: hidden units 32 half .. 32 half + 31 of this row
+        {
+        float z[32], dzv[32];
+        tc_ld32(t_lane + 0 + 32u * half, z);
+        tc_ld32(t_lane + 64 + 32u * half, dzv);
+        const float4* Cp = reinterpret_cast<const float4*>(C + (size_t)p * HID + 32 * half);
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            {
+            const float4 c = __ldg(Cp + q);
+            z[4 * q] += c.x;
+            z[4 * q + 1] += c.y;
+            z[4 * q + 2] += c.z;
+            z[4 * q + 3] += c.w;
+            }
+#pragma unroll
+        for (int c = 0; c < 32; c++)
+            {
+            const float sg = logistic(z[c]);
+            const float hv = z[c] * sg;
+            dzv[c] = sg * (1.0f + z[c] * (1.0f - sg)) * dzv[c];
+            z[c] = hv;
+            }
+#pragma unroll
+        for (int g = 0; g < 4; g++)
+            {
+            const uint32_t off = tc_off((int)row, 32 * (int)half + 8 * g, HID);
+            *reinterpret_cast<uint4*>(sm + TC_OP + 0 * 16384 + off) = bf16x8(z + 8 * g, false);
+            *reinterpret_cast<uint4*>(sm + TC_OP + 2 * 16384 + off) = bf16x8(dzv + 8 * g, false);
+            if (SPLIT)
+                {
+                *reinterpret_cast<uint4*>(sm + TC_OP + 1 * 16384 + off) = bf16x8(z + 8 * g, true);
+                *reinterpret_cast<uint4*>(sm + TC_OP + 3 * 16384 + off)
+                    = bf16x8(dzv + 8 * g, true);
+                }
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (tid == 0)
+            {
+#pragma unroll
+            for (int k = 0; k < HID / 16; k++)
+                {
+                const uint64_t bw = tc_desc(w2a + 256u * k, HID);
+                tc_mma(tmem + 128, tc_desc(op + 0 * 16384 + 256u * k, HID), bw, k > 0);
+                tc_mma(tmem + 192, tc_desc(op + 2 * 16384 + 256u * k, HID), bw, k > 0);
+                if (SPLIT)
+                    {
+                    tc_mma(tmem + 128, tc_desc(op + 1 * 16384 + 256u * k, HID), bw, 1u);
+                    tc_mma(tmem + 192, tc_desc(op + 3 * 16384 + 256u * k, HID), bw, 1u);
+                    }
+                }
+            tc_commit(mbar);
+            }
+        if (!__syncthreads_and(tc_wait(mbar, parity)))
+            {
+            if (tid == 0)
+                atomicExch(err, 1u);
+            break;
+            }
+        parity ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // layer 2 epilogue and the output layer: U = w3 . silu(z2) + b3, dU = w3 . silu'(z2) dz2
+        float u = 0.0f, du = 0.0f;
+        {
+        float z[32], dzv[32];
+        tc_ld32(t_lane + 128 + 32u * half, z);
+        tc_ld32(t_lane + 192 + 32u * half, dzv);
+#pragma unroll
+        for (int c = 0; c < 32; c++)
+            {
+            const int k = 32 * (int)half + c;
+            const float zz = z[c] + b2[k];
+            const float sg = logistic(zz);
+            u += w3[k] * (zz * sg);
+            du += w3[k] * (sg * (1.0f + zz * (1.0f - sg)) * dzv[c]);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        if (half == 1)
+            part[row] = make_float2(u, du);
+        __syncthreads();
+        if (half == 0 && v)
+            {
+            const float2 o = part[row];
+            const float U = u + o.x + *b3s, D = du + o.y;
+            const float fd = -D / r;
+            const float4 f = make_float4(fd * dx, fd * dy, fd * dz, 0.5f * U);
+            atomicAdd(force + pr.x, f);
+            atomicAdd(force + pr.y, make_float4(-f.x, -f.y, -f.z, f.w));
+            }
+        }
+    // every thread has finished its tensor-memory loads (or left the loop together)
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                     ::"r"(tmem), "r"(TC_TMEM_COLS));
+    }
 } // namespace
 } // namespace gb
 
@@ -754,7 +1112,7 @@ extern "C"
     int gb_mlp_prepare(const float* d_theta, uint32_t n_pairs, void* d_infer, void* stream)
         {
         GB_REQUIRE(d_theta && d_infer && n_pairs > 0, "gb_mlp_prepare: bad argument");
-        const unsigned int work = n_pairs * HID > 1024 ? n_pairs * HID : 1024;
+        const unsigned int work = n_pairs * HID > HID * HID ? n_pairs * HID : HID * HID;
         k_prepare<<<div_up(work, 256), 256, 0, (cudaStream_t)stream>>>(
             d_theta, n_pairs, static_cast<unsigned char*>(d_infer));
         return check_launch("gb_mlp_prepare");
@@ -798,7 +1156,8 @@ extern "C"
         unsigned char* sc = static_cast<unsigned char*>(a->d_scratch);
         unsigned int* count = reinterpret_cast<unsigned int*>(sc);
         uint2* pairs = reinterpret_cast<uint2*>(sc + 256);
-        if (cudaMemsetAsync(count, 0, sizeof(unsigned int), s) != cudaSuccess
+        // count word, then the tensor-core path's error word
+        if (cudaMemsetAsync(count, 0, 2 * sizeof(unsigned int), s) != cudaSuccess
             || cudaMemsetAsync(a->d_force, 0, (size_t)a->N * 16, s) != cudaSuccess)
             return fail(GB_ERR_CUDA, "gb_mlp_forces: memset");
         if (a->N == 0)
@@ -807,9 +1166,30 @@ extern "C"
         k_pair_list<<<div_up(a->N, 256), 256, 0, s>>>(
             pos, a->N, a->box, a->d_n_neigh, reinterpret_cast<const uint4*>(a->d_nlist),
             a->stride, a->r_min * a->r_min, a->r_cut * a->r_cut, pairs, count);
-        const unsigned int grid = 152u * 16u;
         const unsigned char* inf = static_cast<const unsigned char*>(a->d_infer);
         float4* force = reinterpret_cast<float4*>(a->d_force);
+        if (a->mma_sync == 0)
+            {
+            // tcgen05 tiles: two CTAs per SM (256 tensor-memory columns each)
+            static int sms = 0;
+            if (sms == 0)
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+            auto kern = a->act_split ? k_mlp_forces_tc<true> : k_mlp_forces_tc<false>;
+            static bool attr = false;
+            if (!attr)
+                {
+                cudaFuncSetAttribute(k_mlp_forces_tc<true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+                cudaFuncSetAttribute(k_mlp_forces_tc<false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+                attr = true;
+                }
+            kern<<<2u * (unsigned)sms, TC_THREADS, TC_SMEM, s>>>(
+                inf, pos, a->box, a->ntypes, n_pairs, a->r_min, a->r_cut, pairs, count, force,
+                count + 1);
+            return check_launch("gb_mlp_forces (tcgen05)");
+            }
+        const unsigned int grid = 152u * 16u;
         if (a->act_split)
             k_mlp_forces<true><<<grid, 128, 0, s>>>(inf, pos, a->box, a->ntypes, n_pairs,
                                                     a->r_min, a->r_cut, pairs, count, force);

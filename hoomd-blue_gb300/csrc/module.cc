@@ -773,6 +773,14 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def_readonly("r_min", &MlpSurrogate::r_min)
         .def_readonly("r_cut", &MlpSurrogate::r_cut)
         .def_readwrite("act_split", &MlpSurrogate::act_split)
+        .def_property(
+            "tensor_kernel",
+            [](const MlpSurrogate& s) { return std::string(s.mma_sync ? "mma.sync" : "tcgen05"); },
+            [](MlpSurrogate& s, const std::string& k) {
+                if (k != "tcgen05" && k != "mma.sync")
+                    throw py::value_error("tensor_kernel: 'tcgen05' or 'mma.sync'");
+                s.mma_sync = k == "mma.sync" ? 1 : 0;
+            })
         .def_readonly("train_steps", &MlpSurrogate::train_steps)
         .def_readonly("train_ms", &MlpSurrogate::train_ms)
         .def("setParams", [fvec](MlpSurrogate& s, farr th) { s.set_params(fvec(th)); })

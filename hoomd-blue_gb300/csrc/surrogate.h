@@ -43,6 +43,7 @@ class MlpSurrogate
     unsigned int ntypes;
     float r_min, r_cut;
     int act_split = 1;
+    int mma_sync = 0; // 0: tcgen05 tiles of 128 pairs, 1: mma.sync tiles of 16 pairs
     uint64_t train_steps = 0;
     double train_ms = 0.0;
     cudaStream_t stream = nullptr;

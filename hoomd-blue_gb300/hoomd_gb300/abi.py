@@ -95,7 +95,7 @@ class MlpForceArgs(ctypes.Structure):
     _fields_ = [("d_force", c_void), ("d_pos", c_void), ("N", c_uint), ("box", Box),
                 ("d_n_neigh", c_void), ("d_nlist", c_void), ("stride", c_u64), ("Nmax", c_uint),
                 ("ntypes", c_uint), ("r_min", c_float), ("r_cut", c_float), ("act_split", c_int),
-                ("d_infer", c_void), ("d_scratch", c_void)]
+                ("d_infer", c_void), ("d_scratch", c_void), ("mma_sync", c_int)]
 
 
 _P = ctypes.POINTER

@@ -826,6 +826,11 @@ typedef struct gb_mlp_force_args
     int act_split;
     const void* d_infer;
     void* d_scratch;
+    /* 0: tcgen05 tiles of 128 pairs (operands in shared memory, FP32 accumulators in tensor
+       memory, one CTA of 256 threads per tile, two per SM); 1: the mma.sync path (one warp per
+       tile of 16 pairs, accumulators in registers). The tcgen05 path writes 1 to the second
+       word of d_scratch when a wait for its products ran out (the forces are then incomplete). */
+    int mma_sync;
     } gb_mlp_force_args;
 size_t gb_mlp_forces_scratch_bytes(unsigned int N, unsigned int Nmax);
 int gb_mlp_forces(const gb_mlp_force_args* args, void* stream);

@@ -96,6 +96,67 @@ def test_tensor_core_forward_matches_oracle(split):
     assert err < (0.01 if split else 0.05)
 
 
+def _surrogate_forces(mma_sync, split, N=600, Lb=9.0, seed=3):
+    """Forces of a random 3-type system through gb_mlp_forces on the chosen tensor-core path,
+    the oracle's forces and energies, and the path's error word."""
+    rng = np.random.default_rng(seed)
+    ntypes = 3
+    pos = rng.uniform(-Lb / 2, Lb / 2, (N, 3))
+    types = rng.integers(0, ntypes, N)
+    n_pairs = ntypes * (ntypes + 1) // 2
+    th = params(n_pairs, 11)
+    pos4 = np.zeros((N, 4), np.float32)
+    pos4[:, :3] = pos
+    pos4[:, 3] = types.astype(np.uint32).view(np.float32)
+    box = (Lb, Lb, Lb, 0, 0, 0)
+    nl = GpuNlist(pos4, box, np.full((ntypes, ntypes), RCUT), 0.3, layout="col4")
+    inf = prepared(th, n_pairs)
+    L = abi.load()
+    Nmax = int(nl.Nmax.max())
+    force = torch.zeros(4 * N, dtype=torch.float32, device="cuda")
+    scr = torch.empty(L.gb_mlp_forces_scratch_bytes(N, Nmax), dtype=torch.uint8, device="cuda")
+    a = abi.MlpForceArgs(d_force=p(force), d_pos=p(nl.pos), N=N, box=nl.box,
+                         d_n_neigh=p(nl.n_neigh), d_nlist=p(nl.nlist), stride=nl.stride,
+                         Nmax=Nmax, ntypes=ntypes, r_min=RMIN, r_cut=RCUT, act_split=split,
+                         d_infer=p(inf), d_scratch=p(scr), mma_sync=mma_sync)
+    abi.check(L.gb_mlp_forces(ctypes.byref(a), stream()), "forces")
+    F = host(force).reshape(N, 4)
+    words = host(scr[:8]).view(np.uint32)
+    Fo, Eo = M.pair_forces(th, pos4[:, :3].astype(np.float64), types, (Lb, Lb, Lb), ntypes, RMIN,
+                           RCUT, quant="bf16x2" if split else "bf16")
+    return F, Fo, Eo, int(words[0]), int(words[1])
+
+
+@pytest.mark.parametrize("split", [0, 1])
+@pytest.mark.parametrize("mma_sync", [0, 1])
+def test_surrogate_forces_both_tensor_paths_match_oracle(mma_sync, split):
+    """The tcgen05 path (128-pair tiles, accumulators in tensor memory) and the mma.sync path
+    against the oracle's network with the same bfloat16 rounding; no wait ran out."""
+    F, Fo, Eo, npairs, err = _surrogate_forces(mma_sync, split, N=2000, Lb=13.0, seed=5)
+    assert err == 0
+    assert npairs > 128 * 40  # many tiles, the last one partial
+    scale = np.abs(Fo).max()
+    tol = 3e-3 if split else 3e-2
+    assert np.abs(F[:, :3] - Fo).max() <= tol * scale
+    assert np.abs(F[:, 3] - Eo).max() <= tol * max(1.0, np.abs(Eo).max())
+    assert abs(F[:, :3].sum(0)).max() < 1e-3 * scale  # Newton's third law
+
+
+@pytest.mark.parametrize("split", [0, 1])
+def test_tcgen05_path_equals_mma_sync_path(split):
+    """Same bfloat16 weights and features on both tensor paths: the results differ by the FP32
+    accumulation order inside the products, the point where the layer-1 offsets and b2 join the
+    sums and the order of the force atomics. With one-term activations such a difference can
+    move a hidden activation across a bfloat16 rounding boundary (2^-8 relative), hence the
+    wider bound there."""
+    Ft, _, _, _, _ = _surrogate_forces(0, split)
+    Fm, _, _, _, _ = _surrogate_forces(1, split)
+    tol = 2e-5 if split else 4e-4
+    scale = np.abs(Fm[:, :3]).max()
+    assert np.abs(Ft[:, :3] - Fm[:, :3]).max() <= tol * scale
+    assert np.abs(Ft[:, 3] - Fm[:, 3]).max() <= tol * max(1.0, np.abs(Fm[:, 3]).max())
+
+
 def test_pair_forces_match_oracle():
     rng = np.random.default_rng(3)
     ntypes, N, Lb = 3, 600, 9.0
