@@ -1,9 +1,11 @@
 // Radial MLP surrogate of the Table pair potential (EvaluatorPairTable,
 // hoomd/md/EvaluatorPairTable.h): training kernels (FP32, one thread per sample, then batch
-// reductions and Adam) and inference kernels (BF16 tensor cores through mma.sync m16n8k16 with
-// FP32 accumulation, one warp per tile of 16 pairs).
+// reductions and Adam) and two inference paths on the BF16 tensor cores with FP32 accumulation:
+// tcgen05 tiles of 128 pairs with the accumulators in tensor memory (k_mlp_forces_tc, the
+// default, at the end of this file) and warp-level mma.sync m16n8k16 tiles of 16 pairs
+// (k_mlp_forces, k_eval).
 //
-// Inference tile: the 16 pairs of a tile are the 16 rows of the A operand. Layer 1 multiplies the
+// mma.sync tile: the 16 pairs of a tile are the 16 rows of the A operand. Layer 1 multiplies the
 // 32 radial features (and, for the derivative, their r-derivatives) by W1r^T; its FP32
 // accumulator starts from the per-type-pair offset C[p] = W1e E[p] + b1. The accumulator
 // fragment of one layer (rows g and g+8, columns 2t and 2t+1 of each 8-column tile) is exactly the
