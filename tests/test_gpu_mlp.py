@@ -217,9 +217,10 @@ def test_training_reduces_the_loss():
     assert losses[1] < 0.05 * losses[0], losses
 
 
-def test_surrogate_pipeline_learns_the_table():
-    """Plain-Table NVT frames -> pair samples -> GPU training -> TableSurrogate run; per-particle
-    forces of the trained surrogate against the FP64 oracle's Table forces on a fresh frame."""
+@pytest.fixture(scope="module")
+def trained_pipeline():
+    """Plain-Table NVT frames of a 4096-particle 3-type system -> pair samples -> GPU training
+    -> a TableSurrogate simulation on the last frame; the FP64 oracle's Table forces there."""
     import hoomd_gb300 as hoomd
     from hoomd_gb300 import md, workloads
     from hoomd_gb300.surrogate import Surrogate
@@ -251,9 +252,6 @@ def test_surrogate_pipeline_learns_the_table():
     before = sur._cpp.loss(8192, 0.1, 1)
     sur.fit(samples, steps=3000, batch=4096, report=1000)
     after = sur._cpp.loss(8192, 0.1, 1)
-    assert after < 0.1 * before, (before, after)
-    # per-particle forces on the held-out frame: surrogate (GPU) vs Table (FP64 oracle)
-    pos, typeid, _ = frames[3]
     s2 = hoomd.Simulation(device=hoomd.device.GPU(), seed=1)
     snap2 = sim.state.get_snapshot()
     s2.create_state_from_snapshot(snap2)
@@ -264,7 +262,6 @@ def test_surrogate_pipeline_learns_the_table():
     s2.run(0)
     Fs = sf.forces
     from oracle import oracle as O
-    N = len(pos)
     pos64 = O.make_pos4(snap2.particles.position, snap2.particles.typeid, 64)
     tp, _, opar, odata = __import__("gpu_util").table_params(
         ntypes, {k: (v["r_min"], v["U"], v["F"]) for k, v in tabs.items()})
@@ -273,8 +270,46 @@ def test_surrogate_pipeline_learns_the_table():
     fo, _ = O.pair_forces("table", pos64, tuple(snap2.configuration.box), opar,
                           np.full((ntypes, ntypes), RCUT * RCUT), n, l, h, third_law=True,
                           compute_virial=False, tdata=odata, prec=64)
-    rmse = np.sqrt(np.mean((Fs - fo[:, :3]) ** 2))
-    frms = np.sqrt(np.mean(fo[:, :3] ** 2))
+    return dict(sim=sim, s2=s2, Fs=Fs, fo=fo, before=before, after=after)
+
+
+def test_surrogate_pipeline_learns_the_table(trained_pipeline):
+    """The training reduces the loss tenfold, the trained surrogate's per-particle forces follow
+    the FP64 oracle's Table forces on a fresh frame, and it drives dynamics."""
+    t = trained_pipeline
+    assert t["after"] < 0.1 * t["before"], (t["before"], t["after"])
+    rmse = np.sqrt(np.mean((t["Fs"] - t["fo"][:, :3]) ** 2))
+    frms = np.sqrt(np.mean(t["fo"][:, :3] ** 2))
     assert rmse < 0.1 * frms, (rmse, frms)
-    s2.run(20)  # the surrogate drives dynamics through the unfused integrator path
-    assert np.isfinite(s2.state.get_snapshot().particles.position).all()
+    t["s2"].run(20)  # the surrogate drives dynamics through the unfused integrator path
+    assert np.isfinite(t["s2"].state.get_snapshot().particles.position).all()
+
+
+def test_surrogate_against_its_targets(trained_pipeline, record_property):
+    """The surrogate's two targets, recorded whichever way they go: per-particle force RMSE
+    within 1e-3 epsilon/sigma of the FP64 oracle's Table forces, and more timesteps/s than the
+    plain Table path on the same system. The measured values are attached to the test report;
+    the test is marked as an expected failure (with the numbers) while a target is missed."""
+    import torch
+    t = trained_pipeline
+    rmse = float(np.sqrt(np.mean((t["Fs"] - t["fo"][:, :3]) ** 2)))
+
+    def tps(sim, steps=300):
+        sim.run(10)
+        torch.cuda.synchronize()
+        import time
+        t0 = time.perf_counter()
+        sim.run(steps)
+        torch.cuda.synchronize()
+        return steps / (time.perf_counter() - t0)
+
+    tps_table = tps(t["sim"])
+    tps_mlp = tps(t["s2"])
+    record_property("force_rmse", rmse)
+    record_property("force_rmse_target", 1e-3)
+    record_property("tps_surrogate", tps_mlp)
+    record_property("tps_table", tps_table)
+    assert np.isfinite(rmse) and tps_mlp > 0 and tps_table > 0
+    if rmse > 1e-3 or tps_mlp <= tps_table:
+        pytest.xfail(f"surrogate targets missed: force RMSE {rmse:.3g} (target 1e-3), "
+                     f"{tps_mlp:.0f} timesteps/s against {tps_table:.0f} for plain Table")
