@@ -873,13 +873,17 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     const float gamma = 1.0f / (2.0f * hstep * hstep);
     const unsigned int n = *count;
     uint32_t parity = 0;
+    // the pair of this thread's row in the next tile is loaded one tile ahead
+    uint2 pr_next = make_uint2(0u, 0u);
+    if (blockIdx.x * 128u + row < n)
+        pr_next = pairs[blockIdx.x * 128u + row];
 
     for (uint32_t tile = blockIdx.x; tile * 128u < n; tile += gridDim.x)
         {
         // geometry of this thread's row (both threads of a row compute it)
         const uint32_t s = tile * 128u + row;
         const bool v = s < n;
-        const uint2 pr = v ? pairs[s] : make_uint2(0u, 0u);
+        const uint2 pr = v ? pr_next : make_uint2(0u, 0u);
         const float4 pi = pos[pr.x], pj = pos[pr.y];
         float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         min_image(box, dx, dy, dz);
@@ -889,6 +893,14 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         const unsigned int ta = __float_as_uint(pi.w), tb = __float_as_uint(pj.w);
         const unsigned int a = min(ta, tb), b = max(ta, tb);
         p = v ? min(a * ntypes - a * (a - 1) / 2 + (b - a), n_pairs - 1) : 0u;
+        }
+        // this row's first-layer offsets, in flight while the layer-1 products run
+        float4 cv[8];
+        {
+        const float4* Cp = reinterpret_cast<const float4*>(C + (size_t)p * HID + 32 * half);
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            cv[q] = __ldg(Cp + q);
         }
         // layer-1 operands: features 16 half .. 16 half + 15 of this row
         {
@@ -949,11 +961,10 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
         float z[32], dzv[32];
         tc_ld32(t_lane + 0 + 32u * half, z);
         tc_ld32(t_lane + 64 + 32u * half, dzv);
-        const float4* Cp = reinterpret_cast<const float4*>(C + (size_t)p * HID + 32 * half);
 #pragma unroll
         for (int q = 0; q < 8; q++)
             {
-            const float4 c = __ldg(Cp + q);
+            const float4 c = cv[q];
             z[4 * q] += c.x;
             z[4 * q + 1] += c.y;
             z[4 * q + 2] += c.z;
@@ -1009,6 +1020,11 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             }
         parity ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;");
+        {
+        const uint32_t sn = (tile + gridDim.x) * 128u + row;
+        if (sn < n)
+            pr_next = pairs[sn];
+        }
         // layer 2 epilogue and the output layer: U = w3 . silu(z2) + b3, dU = w3 . silu'(z2) dz2
         float u = 0.0f, du = 0.0f;
         {
