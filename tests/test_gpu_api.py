@@ -334,6 +334,38 @@ def test_rebuild_check_schedule(r_buff, delay, dist_check, builds, dangerous, ca
         assert cell.shortest_rebuild == delay
 
 
+@pytest.mark.parametrize("method", ["langevin", "constant_volume"])
+def test_rebuild_check_schedule_on_the_unfused_path(method):
+    """Two pair forces summed take the unfused step, which advances the device step counter too
+    (the Langevin half itself, a separate kernel after ConstantVolume's), so the rebuild schedule
+    and the build statistics follow the steps there as well."""
+    from test_oracle import sc_lattice
+    pos, (L, _, _) = sc_lattice(8, 1.2, 0.05, seed=3)
+    snap = hoomd.Snapshot()
+    snap.configuration.box = [L, L, L, 0, 0, 0]
+    snap.particles.N = len(pos)
+    snap.particles.types = ["A"]
+    snap.particles.position[:] = np.asarray(pos, np.float32)
+    sim = make_sim(snap)
+    sim.state.thermalize_particle_momenta(hoomd.filter.All(), 1.5)
+    cell = md.nlist.Cell(buffer=0.002, rebuild_check_delay=4, check_dist=False)
+    lj = md.pair.LJ(nlist=cell, default_r_cut=2.5)
+    lj.params[("A", "A")] = dict(epsilon=1.0, sigma=1.0)
+    g = md.pair.Gaussian(nlist=cell, default_r_cut=2.0)
+    g.params[("A", "A")] = dict(epsilon=0.1, sigma=0.5)
+    forces = [lj, g]
+    if method == "constant_volume":
+        m = md.methods.ConstantVolume(hoomd.filter.All())
+    else:
+        m = md.methods.Langevin(hoomd.filter.All(), kT=1.5)
+    sim.operations.integrator = md.Integrator(dt=0.005, forces=forces, methods=[m])
+    sim.run(40)
+    assert cell.num_builds == 10 and cell.dangerous_builds == 0
+    assert cell.shortest_rebuild == 4
+    assert sim._cpp_integrator.status()["last_update"] == 40
+    assert sim._cpp_integrator.status()["timestep"] == 40
+
+
 def test_delayed_check_matches_oracle():
     """A check every third step with the 0.4 buffer: the GPU builds as often as the oracle from
     the same state, never dangerously, and the trajectory follows the oracle's."""
