@@ -207,12 +207,16 @@ class ClockSampler:
 
 
 def dist_init():
+    """Rank, world size and local rank from the launcher's environment; for N > 1 the process
+    group (NCCL on GPUs, gloo where CUDA is absent). The ranks exchange only the barrier and the
+    largest elapsed time: each runs its own independent system."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, world, local
 
 
@@ -227,7 +231,8 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
