@@ -321,7 +321,8 @@ def run_gb300(args):
         sim._needs_prep = True
     # the reference tunes its kernels' launch parameters during its first steps
     # (hoomd/Autotuner.h); here the search runs once, on the warmed-up state, before the timing
-    sim.operations.tune_kernel_parameters()
+    if not args.no_kernel_search:
+        sim.operations.tune_kernel_parameters()
     sim.run(3)
     kernel_parameters = {**force.kernel_parameters, **cell.kernel_parameters}
     integ = sim._cpp_integrator
@@ -848,6 +849,9 @@ def main():
     ap.add_argument("--mlp-anchors", type=int, default=20000)
     ap.add_argument("--replicas", type=int, default=256,
                     help="replica count of replicas_256 (256 = the benchmark; fewer for profiling)")
+    ap.add_argument("--no-kernel-search", action="store_true",
+                    help="keep the default kernel parameters (profiling captures: the launch "
+                         "sequence then has no search launches)")
     ap.add_argument("--no-tune", action="store_true",
                     help="replicas_256: fixed 1024-thread launch instead of the tuner (profiling)")
     ap.add_argument("--mlp-act-split", type=int, default=1, choices=[0, 1],
