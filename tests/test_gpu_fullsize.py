@@ -131,11 +131,12 @@ def test_fullsize_nlist_and_forces_vs_oracle(systems, case):
                           (f[:, :3], f[:, 3], v), (f32[:, :3], f32[:, 3], v32), case)
 
 
-def check_against_oracles(kind, pos64, box6, oparams, rc, r_buff, odata, got, f32, case):
+def check_against_oracles(kind, pos64, box6, oparams, rc, r_buff, odata, got, f32, case, ndim=3):
     """got / f32: (forces (N, 3), energies (N,), virials (6, N)) of the GPU and of the FP32
     oracle; the FP64 oracle's values, the sums of term magnitudes and the cut-off band terms are
     computed here."""
-    n6, l6, h6, _ = O.build_nlist(pos64, box6, rc, r_buff, full=True, prec=64, nthreads=CORES)
+    n6, l6, h6, _ = O.build_nlist(pos64, box6, rc, r_buff, full=True, ndim=ndim, prec=64,
+                                  nthreads=CORES)
     kw = dict(third_law=False, compute_virial=True, tdata=odata, prec=64, nthreads=CORES)
     fo, vo = O.pair_forces(kind, pos64, box6, oparams, rc ** 2, n6, l6, h6, **kw)
     fa, va = O.pair_forces(kind, pos64, box6, oparams, rc ** 2, n6, l6, h6, abs_terms=1, **kw)
@@ -191,3 +192,61 @@ def test_fullsize_fcc_after_run_vs_oracle():
     pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
     check_against_oracles("lj", pos64, box6, [[1.0, 1.0]], rc, 0.4, None,
                           (F, E, W.T), (f32[:, :3], f32[:, 3], v32), "fcc after 200 steps")
+
+
+def _plane_system(N, L, seed):
+    """N particles on a jittered square lattice in the plane z = 0 (a 2D box, Lz = 1)."""
+    rng = np.random.default_rng(seed)
+    n = int(round(np.sqrt(N)))
+    g = (np.arange(n) + 0.5) / n - 0.5
+    f = np.stack(np.meshgrid(g, g, indexing="ij"), -1).reshape(-1, 2)
+    f = f + rng.uniform(-0.1 / n, 0.1 / n, f.shape)
+    pos = np.zeros((len(f), 3))
+    pos[:, :2] = f * L
+    return O.make_pos4(pos, np.zeros(len(f)), 32), (L, L, 1.0, 0.0, 0.0, 0.0)
+
+
+@pytest.mark.parametrize("case", ["triclinic_110k", "plane_250k"])
+def test_medium_tilted_and_planar_systems_vs_oracle(case):
+    """The boxes the benchmark configurations leave out, at a size where every cell of the grid
+    is exercised many times: a two-type system of 110,592 particles in a triclinic box (tilts
+    0.2, -0.15, 0.1; the builds' tilted image arithmetic) and a 2D system of 250,000 particles
+    (the 2D cell grid and stencil). Neighbour sets bit-exact against the FP32 oracle, forces,
+    energies and virials held to the FP32 and FP64 oracles as for the benchmark systems."""
+    if case == "triclinic_110k":
+        rng = np.random.default_rng(4)
+        n = 48
+        g = (np.arange(n) + 0.5) / n - 0.5
+        f = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        f = f + rng.uniform(-0.1 / n, 0.1 / n, f.shape)
+        L, (xy, xz, yz) = 52.0, (0.2, -0.15, 0.1)
+        x = f[:, 0] * L + xy * f[:, 1] * L + xz * f[:, 2] * L
+        y = f[:, 1] * L + yz * f[:, 2] * L
+        z = f[:, 2] * L
+        types = rng.integers(0, 2, len(f))
+        pos4 = O.make_pos4(np.stack([x, y, z], 1), types, 32)
+        box6 = (L, L, L, xy, xz, yz)
+        rc, par = np.array([[2.5, 2.0], [2.0, 2.2]]), np.array([[1.0, 1.0], [0.8, 1.5],
+                                                                 [0.8, 1.5], [0.88, 0.5]])
+        ndim, r_buff = 3, 0.4
+    else:
+        pos4, box6 = _plane_system(250000, 560.0, seed=6)
+        rc, par = np.array([[2.5]]), np.array([[1.0, 1.0]])
+        ndim, r_buff = 2, 0.4
+    nl = GpuNlist(pos4, box6, rc, r_buff, layout="col4", ndim=ndim)
+    n_o, l_o, h_o, info = O.build_nlist(pos4, box6, rc, r_buff, full=True, ndim=ndim, prec=32,
+                                        nthreads=CORES)
+    assert nl.dim == info["dim"].tolist()
+    nn_g = nl.n_neigh.cpu().numpy().view(np.uint32)
+    nl_g = nl.nlist.cpu().numpy().view(np.uint32)
+    ho = h_o.astype(np.int64)
+    bad = compare_neighbor_sets(nn_g, nl_g, nl.word_index(), n_o, l_o, lambda i, k: ho[i] + k)
+    assert len(bad) == 0, f"{case}: {len(bad)} particles' sets differ, first {bad[:5]}"
+    assert int(n_o.astype(np.int64).sum()) > 10 * len(pos4)
+    f, v = gpu_pair_forces(nl, "lj", par, rc, virial=True)
+    f32, v32 = O.pair_forces("lj", pos4, box6, par, (rc ** 2).astype(np.float32), n_o, l_o, h_o,
+                             third_law=False, compute_virial=True, prec=32, nthreads=CORES)
+    pos64 = pos4.astype(np.float64)
+    pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
+    check_against_oracles("lj", pos64, box6, par, rc, r_buff, None, (f[:, :3], f[:, 3], v),
+                          (f32[:, :3], f32[:, 3], v32), case, ndim=ndim)
