@@ -409,12 +409,17 @@ def test_kernel_parameters_and_tuning():
     sim.run(10)
     assert sim.operations.is_tuning_complete
     samples = sim._cpp_integrator.lastTuning()
-    pair = [s for s in samples if s[0] == "pair"]
-    nl = [s for s in samples if s[0] == "nlist"]
+    pair = {(s[1], s[2]): s[3] for s in samples if s[0] == "pair"}
+    nl = {(s[1],): s[3] for s in samples if s[0] == "nlist"}
     assert len(pair) == 6 and len(nl) == 3 and all(s[3] > 0 for s in samples)
-    best = min(pair, key=lambda s: s[3])
-    assert lj.kernel_parameters["pair"] == (best[1], best[2])
-    assert cell.kernel_parameters["nlist"] == (min(nl, key=lambda s: s[3])[1],)
+
+    def kept_rule(times, kept, default):
+        # the fastest, unless it is within 2 % of the default, which then stays
+        fastest = min(times, key=times.get)
+        return kept == fastest or (kept == default and times[fastest] >= 0.98 * times[default])
+
+    assert kept_rule(pair, lj.kernel_parameters["pair"], (256, 8))
+    assert kept_rule(nl, cell.kernel_parameters["nlist"], (128,))
 
     sim2, lj2, cell2, _ = lj_sim(snap, kT=None, thermalize=1.5)
     sim2.run(0)
