@@ -395,6 +395,10 @@ def run_gb300(args):
     achieved_pn = (bytes_pair + per_build * bytes_nl) / t_pn / 1e9
     roofline["pair_nlist"] = {"achieved": achieved_pn, "frac": achieved_pn / peak,
                               "builds_per_step": per_build, "nlist_bytes_per_build": bytes_nl}
+    # the build alone (cell list + neighbour list, one forced build of timePhases)
+    achieved_nl = bytes_nl / (phases[1] / 1e3) / 1e9
+    roofline["nlist_build"] = {"achieved": achieved_nl, "frac": achieved_nl / peak,
+                               "bound": "issue (exact-rounding candidate tests)"}
 
     line = {"metric": wl.metric, "value": tps * world, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
