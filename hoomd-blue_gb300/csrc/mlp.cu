@@ -725,10 +725,10 @@ __global__ void __launch_bounds__(128)
 // parts accumulated into the same FP32 accumulator) into tensor memory and commits them to an
 // mbarrier; after the wait every thread reads its row's accumulators with tcgen05.ld, adds C[p],
 // applies SiLU and its derivative and writes the layer-2 operands (K = 64) over the layer-1 ones;
-// the layer-2 products go to four more accumulator columns; the output layer, the radial
-// derivative and the forces follow in registers, and each pair adds its force to both particles
-// with float4 atomics. Tensor memory: 4 accumulators x 64 FP32 columns = 256 columns per CTA,
-// two CTAs per SM. Every wait on the mbarrier is bounded; a wait that runs out records an error
+// the layer-2 products go to the other two accumulators; the output layer, the radial derivative
+// and the forces follow in registers, and each pair adds its force to both particles with float4
+// atomics. C[p] is loaded before the layer-1 products and the next tile's pair one tile ahead.
+// Tensor memory: 4 accumulators x 64 FP32 columns = 256 columns per CTA, two CTAs per SM. Every wait on the mbarrier is bounded; a wait that runs out records an error
 // and all threads leave the tile loop together, free the tensor memory and return.
 constexpr int TC_THREADS = 256;
 constexpr uint32_t TC_OP = 0;                        // operands: 4 x (128 x 64) bf16 = 64 KB
