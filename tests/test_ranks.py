@@ -24,8 +24,9 @@ def _free_port():
 
 
 def _rank_main(rank, world, port, out):
+    # CPU ranks even where a GPU is visible (gloo, as the two-rank test of the host logic)
     os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank),
-                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), CUDA_VISIBLE_DEVICES="")
     sys.path.insert(0, str(REPO))
     import bench
     r, w, local = bench.dist_init()
