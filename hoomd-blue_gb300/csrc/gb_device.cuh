@@ -104,20 +104,21 @@ __device__ __forceinline__ float dot3(float x, float y, float z)
     return fadd(fadd(fmul(x, x), fmul(y, y)), fmul(z, z));
     }
 
-// dot3 of both halves of packed differences. The squares and sums are scalar __fmul_rn /
-// __fadd_rn, which are never contracted into fused multiply-adds; the same sequence written
-// with packed mul.rn/add.rn.f32x2 was measured to round differently from the scalar sequence on
-// a share of inputs (a list membership decided at r_list^2 then differs from the reference's by
-// one pair in a million particles), so only the subtractions stay packed.
+// dot3 of both halves of packed differences. The squares are packed mul.rn.f32x2 (each half an
+// IEEE round-to-nearest product) and the sums scalar __fadd_rn, which is never merged into a
+// multiply-add, so each sum adds the rounded squares exactly as the scalar sequence does. The
+// sums written as packed add.rn.f32x2 were measured to round differently from the scalar
+// sequence on a share of inputs (as if merged with the products; a list membership decided at
+// r_list^2 then differed from the reference's by one pair in a million particles).
 __device__ __forceinline__ void f2dot3(uint64_t dx, uint64_t dy, uint64_t dz, float& r0,
                                        float& r1)
     {
     float x0, x1, y0, y1, z0, z1;
-    f2unpack(dx, x0, x1);
-    f2unpack(dy, y0, y1);
-    f2unpack(dz, z0, z1);
-    r0 = dot3(x0, y0, z0);
-    r1 = dot3(x1, y1, z1);
+    f2unpack(f2mul(dx, dx), x0, x1);
+    f2unpack(f2mul(dy, dy), y0, y1);
+    f2unpack(f2mul(dz, dz), z0, z1);
+    r0 = fadd(fadd(x0, y0), z0);
+    r1 = fadd(fadd(x1, y1), z1);
     }
 
 // BoxDim::makeFraction with no ghost layer: hoomd/BoxDim.h:276-284.

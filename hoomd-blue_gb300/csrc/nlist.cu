@@ -579,8 +579,8 @@ __global__ void __launch_bounds__(TILE_WARPS_MAX * 32)
 // particle ob + l in registers. The nine cells of each stencil plane are staged in shared memory
 // as structure-of-arrays (x, y, z, index[, type]), every cell starting at an even slot, so two
 // consecutive candidates load as one 8-byte packed pair. Every lane tests its own particle
-// against the staged candidates two at a time: packed FP32 differences (each half rounds as the
-// scalar subtraction) and scalar rounded squares and sums (f2dot3), so the decisions are
+// against the staged candidates two at a time: packed FP32 differences and squares (each half
+// rounds as the scalar operation) and scalar rounded sums (f2dot3), so the decisions are
 // bit-identical to the minImage sequence, and writes its hits straight into
 // its own row; a cell's exact image shift is applied only when the stencil wraps there (it is
 // zero otherwise, and x - 0 is exact). Hits come in the order (plane, cell, slot) of the

@@ -260,8 +260,8 @@ __device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint
             cnt++;
         };
         // candidates [s_start[c0], s_start[c1]) shifted by (sx, sy, sz); two per step: packed
-        // FP32 differences (each half rounds as the scalar subtraction) and scalar rounded
-        // squares and sums (f2dot3)
+        // FP32 differences and squares (each half rounds as the scalar operation) and scalar
+        // rounded sums (f2dot3)
         auto run = [&](uint32_t c0, uint32_t c1, float sx, float sy, float sz) {
             const uint32_t e = s_start[c1];
             uint32_t a = s_start[c0];
