@@ -403,6 +403,7 @@ void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count
     a.ntypes = pd.ntypes;
     a.d_gate = d_gate;
     a.block_size = kp_block;
+    a.threads_per_particle = kp_tpp;
     a.nlist_capacity = nlist.size();
     check(gb_nlist_build_binned(&a, s), "gb_nlist_build_binned");
     if (ex_pitch > 0)
@@ -1872,9 +1873,15 @@ std::vector<Integrator::TuneSample> Integrator::autotune()
         if (nlist->tune_requested)
             {
             // a build at the current positions, as the forced build before the run made
-            std::vector<Candidate> cand = {{32u, 1u, 0.0}, {64u, 1u, 0.0}, {128u, 1u, 0.0}};
+            // (block size, threads per own particle); the default is the first
+            std::vector<Candidate> cand = {{128u, 32u, 0.0}, {64u, 32u, 0.0}, {32u, 32u, 0.0},
+                                           {128u, 1u, 0.0},  {64u, 1u, 0.0},  {32u, 1u, 0.0}};
             const size_t pick = search(
-                cand, 2, [&](const Candidate& c) { nlist->kp_block = c.block; },
+                cand, 0,
+                [&](const Candidate& c) {
+                    nlist->kp_block = c.block;
+                    nlist->kp_tpp = c.tpp;
+                },
                 [&] {
                     cuda_check(cudaMemsetAsync(ds->cell_cond, 0, sizeof(ds->cell_cond), s),
                                "cond");
@@ -1882,8 +1889,9 @@ std::vector<Integrator::TuneSample> Integrator::autotune()
                     nlist->enqueue_build(nullptr, nullptr, ds->cell_cond, ds->nl_cond, s);
                 });
             for (const auto& c : cand)
-                out.push_back({"nlist", c.block, 1u, c.ms});
+                out.push_back({"nlist", c.block, c.tpp, c.ms});
             nlist->kp_block = cand[pick].block;
+            nlist->kp_tpp = cand[pick].tpp;
             nlist->tune_requested = false;
             }
         const bool fused_path = forces.size() == 1 && !compute_virial

@@ -229,9 +229,10 @@ class NeighborList
     bool allocated = false;
     bool dirty = true; // r_cut or capacities changed: graphs must be rebuilt
     bool capacity_fixed = false; // start from exactly Nmax_cell / Nmax (tests of the growth path)
-    // kernel parameters (Autotuner): threads per block of the lane build (0 = default); a
-    // search on the live state runs at the next run when requested
-    unsigned int kp_block = 0;
+    // kernel parameters (Autotuner): threads per block of the tiled build and threads testing
+    // each own particle (32 = candidate stream, 1 = lane per particle; 0 = defaults); a search on
+    // the live state runs at the next run when requested
+    unsigned int kp_block = 0, kp_tpp = 0;
     bool tune_requested = false;
     // exclusions (NeighborList::addExclusion / filterNlist): unordered tag pairs, and per
     // particle index the excluded indices (rebuilt when a sort permutes the indices)

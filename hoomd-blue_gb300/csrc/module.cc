@@ -431,7 +431,8 @@ PYBIND11_MODULE(_hoomd_gb300, m)
         .def("getAutotunerParameters",
              [](NeighborList& n) {
                  py::dict d;
-                 d["nlist"] = py::make_tuple(n.kp_block ? n.kp_block : 128u);
+                 d["nlist"] = py::make_tuple(n.kp_block ? n.kp_block : 128u,
+                                             n.kp_tpp ? n.kp_tpp : 32u);
                  return d;
              })
         .def("setAutotunerParameters",
@@ -441,9 +442,12 @@ PYBIND11_MODULE(_hoomd_gb300, m)
                      if (py::str(kv.first).cast<std::string>() != "nlist")
                          throw py::key_error("no kernel " + py::str(kv.first).cast<std::string>());
                      auto t = kv.second.cast<std::vector<unsigned int>>();
-                     if (t.size() != 1 || (t[0] != 32 && t[0] != 64 && t[0] != 128))
-                         throw py::value_error("nlist: (block size 32, 64 or 128)");
+                     if (t.size() != 2 || (t[0] != 32 && t[0] != 64 && t[0] != 128)
+                         || (t[1] != 1 && t[1] != 32))
+                         throw py::value_error(
+                             "nlist: (block size 32, 64 or 128, threads per particle 1 or 32)");
                      n.kp_block = t[0];
+                     n.kp_tpp = t[1];
                      }
                  n.tune_requested = false;
              })

@@ -6,13 +6,15 @@
 // (hoomd/CellListGPU.cu:478-540 does the same with a global thrust sort).
 //
 // Neighbour list (replaces gpu_compute_nlist_binned, hoomd/md/NeighborListGPUBinned.cu:52-298):
-// one warp per cell. The warp's lanes own the cell's particles; for each of the 27 (or fewer,
-// deduplicated) adjacent cells the warp stages 32 candidates at a time in shared memory with one
-// coalesced load, then every lane tests its particle against every staged candidate. All lanes
-// walk the same candidate sequence, so there is no divergence in the search (the reference's
-// thread-per-particle search diverges whenever a warp straddles cells). Hits are written in the
-// column-major layout nlist[k * stride + i] (coalesced across particles in SFC order) or the
-// reference's flat head-list layout.
+// one warp per cell in every form. The default (k_nlist_stream) puts 32 candidates of the
+// cell's stencil in the lanes and tests them against one own particle at a time, a ballot per own
+// particle; the other forms put the own particles in the lanes. In the first of those, for each
+// of the 27 (or fewer, deduplicated) adjacent cells the warp stages 32 candidates at a time in
+// shared memory with one coalesced load, then every lane tests its particle against every staged
+// candidate. All lanes walk the same candidate sequence, so there is no divergence in the search
+// (the reference's thread-per-particle search diverges whenever a warp straddles cells). Hits are
+// written in the column-major layout nlist[k * stride + i] (coalesced across particles in SFC
+// order), the same interleaved by four, or the reference's flat head-list layout.
 #include <cstdint>
 #include <type_traits>
 
@@ -795,6 +797,297 @@ __global__ void __launch_bounds__(LANE_WARPS * 32)
         }
     }
 
+// Candidate-stream build (same cases as k_nlist_lane): one warp per cell, the lanes holding
+// candidates instead of own particles, so every lane works whatever the cell's occupancy. The
+// own particles (the cell's, 32 per pass) sit in shared memory. Each stencil plane's nine cells
+// form one stream of candidates in the order (cell, slot); the warp takes 32 of them into its
+// lanes' registers, walks the own particles, and records each own particle's test of the 32 as
+// one ballot mask. After the plane, lane p takes own particle p and appends the candidates of its
+// masks in stream order, so its list is the lane build's list, entry for entry. Distances use the
+// lane build's operation order (minImage's, with the cell's exact image shift only where the
+// stencil wraps), so the decisions are bit-identical.
+constexpr int STREAM_WARPS = 4;
+
+// 32-candidate blocks of one plane's stream, at most
+__host__ __device__ inline unsigned int stream_nb(unsigned int Nmax_cell)
+    {
+    return (9u * Nmax_cell + 31u) / 32u;
+    }
+
+// per-warp shared memory (words): own x, y, z, index and type row [32 each], plane record
+// [32], candidate indices [32 nb], masks [32 nb]
+__host__ __device__ inline size_t stream_warp_bytes(unsigned int Nmax_cell)
+    {
+    return 4u * 32u * 6u + 2u * 4u * 32u * (size_t)stream_nb(Nmax_cell);
+    }
+
+template<bool MULTI, int LAYOUT, bool ORTHO>
+__global__ void __launch_bounds__(STREAM_WARPS * 32)
+    k_nlist_stream(unsigned int* __restrict__ nlist, unsigned int* __restrict__ n_neigh,
+                   float4* __restrict__ last_pos, unsigned int* __restrict__ cond,
+                   uint64_t stride, const unsigned int* __restrict__ Nmax_t,
+                   const unsigned int* __restrict__ cell_size, const float4* __restrict__ xyzf,
+                   const unsigned int* __restrict__ cell_type, uint3 dim, unsigned int ncell,
+                   unsigned int Nmax_cell, gb_box box, const float* __restrict__ r_cut,
+                   const float* __restrict__ r_listsq, unsigned int ntypes, const uint32_t* gate)
+    {
+    if (gate && *gate == 0)
+        return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int wpb = blockDim.x / 32;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    // r_list^2 per type pair (own row, candidate column), -1 where r_cut is off (MULTI only)
+    float* s_tab = reinterpret_cast<float*>(smem);
+    const size_t tab_bytes = MULTI ? ((sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
+    if (MULTI)
+        {
+        for (unsigned int t = threadIdx.x; t < ntypes * ntypes; t += blockDim.x)
+            s_tab[t] = r_cut[t] > 0.0f ? r_listsq[t] : -1.0f;
+        __syncthreads();
+        }
+    const unsigned int nb_max = stream_nb(Nmax_cell);
+    unsigned char* base = smem + tab_bytes + (size_t)warp * stream_warp_bytes(Nmax_cell);
+    float* s_ox = reinterpret_cast<float*>(base);
+    float* s_oy = s_ox + 32;
+    float* s_oz = s_oy + 32;
+    unsigned int* s_oi = reinterpret_cast<unsigned int*>(s_oz + 32);
+    unsigned int* s_orow = s_oi + 32;
+    unsigned int* s_plane = s_orow + 32; // [0, 10) offsets, [10, 19) cells, [19, 28) images
+    unsigned int* s_cj = s_plane + 32;
+    unsigned int* s_mask = s_cj + 32 * nb_max;
+
+    const unsigned int cell = blockIdx.x * wpb + warp;
+    if (cell >= ncell)
+        return;
+    const int ci = cell % dim.x, cj = (cell / dim.x) % dim.y, ck = cell / (dim.x * dim.y);
+    const unsigned int csize = min(cell_size[cell], Nmax_cell);
+    if (csize == 0)
+        return;
+    const size_t row4 = (size_t)stride * 4u;
+    const float rl_single = (!MULTI && __ldg(r_cut) > 0.0f) ? __ldg(r_listsq) : -1.0f;
+    const float inf = __int_as_float(0x7f800000);
+
+    for (unsigned int ob = 0; ob < csize; ob += 32)
+        {
+        const unsigned int n_pass = min(csize - ob, 32u);
+        const bool active = lane < n_pass;
+        float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+        unsigned int ti = 0;
+        if (active)
+            {
+            pi = __ldg(xyzf + (size_t)cell * Nmax_cell + ob + lane);
+            if (MULTI)
+                ti = __ldg(cell_type + (size_t)cell * Nmax_cell + ob + lane);
+            s_ox[lane] = pi.x;
+            s_oy[lane] = pi.y;
+            s_oz[lane] = pi.z;
+            s_oi[lane] = __float_as_uint(pi.w);
+            if (MULTI)
+                s_orow[lane] = ti * ntypes;
+            }
+        const unsigned int i = __float_as_uint(pi.w);
+        const unsigned int nmax_i = active ? __ldg(Nmax_t + (MULTI ? ti : 0u)) : 0u;
+        unsigned int wo = LAYOUT == 4 ? i * 4u : i;
+        const unsigned int jump = LAYOUT == 4 ? (unsigned int)row4 - 3u : (unsigned int)stride;
+        unsigned int cnt = 0;
+
+        for (int pz = -1; pz <= 1; pz++)
+            {
+            // the plane's nine cells: offsets of their runs in the stream, cell, image
+            unsigned int q_n = 0;
+            bool q_wrap = false;
+            if (lane < 9)
+                {
+                const int ox = lane % 3 - 1, oy = lane / 3 - 1;
+                const unsigned int q_cell
+                    = (wrap_cell(ck + pz, dim.z) * dim.y + wrap_cell(cj + oy, dim.y)) * dim.x
+                      + wrap_cell(ci + ox, dim.x);
+                q_n = min(__ldg(cell_size + q_cell), Nmax_cell);
+                const int ix = (ci + ox >= (int)dim.x) ? 1 : (ci + ox < 0 ? -1 : 0);
+                const int iy = (cj + oy >= (int)dim.y) ? 1 : (cj + oy < 0 ? -1 : 0);
+                const int iz = (ck + pz >= (int)dim.z) ? 1 : (ck + pz < 0 ? -1 : 0);
+                q_wrap = ix != 0 || iy != 0 || iz != 0;
+                s_plane[10 + lane] = q_cell;
+                s_plane[19 + lane] = (unsigned int)((ix + 1) | ((iy + 1) << 2) | ((iz + 1) << 4));
+                }
+            unsigned int incl = q_n;
+#pragma unroll
+            for (int o = 1; o < 16; o <<= 1)
+                {
+                const unsigned int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                    incl += y;
+                }
+            if (lane < 9)
+                s_plane[lane] = incl - q_n;
+            const unsigned int total = __shfl_sync(0xffffffffu, incl, 8);
+            if (lane == 9)
+                s_plane[9] = total;
+            const bool plane_wraps = __any_sync(0xffffffffu, q_wrap);
+            __syncwarp();
+            const unsigned int nb = (total + 31u) / 32u;
+            unsigned int q = 0;
+            for (unsigned int b = 0; b < nb; b++)
+                {
+                // this lane's candidate: stream entry 32 b + lane
+                const unsigned int k = 32u * b + lane;
+                float cx = inf, cy = inf, cz = inf;
+                unsigned int cjdx = 0xffffffffu, ct = 0;
+                float sx = 0.f, sy = 0.f, sz = 0.f, syz = 0.f, sxz = 0.f, sxy = 0.f;
+                if (k < total)
+                    {
+                    while (k >= s_plane[q + 1])
+                        q++;
+                    const unsigned int qc = s_plane[10 + q];
+                    const unsigned int slot = k - s_plane[q];
+                    const float4 c = __ldg(xyzf + (size_t)qc * Nmax_cell + slot);
+                    cx = c.x;
+                    cy = c.y;
+                    cz = c.z;
+                    cjdx = __float_as_uint(c.w);
+                    if (MULTI)
+                        ct = __ldg(cell_type + (size_t)qc * Nmax_cell + slot);
+                    const unsigned int img = s_plane[19 + q];
+                    const float ix = (float)((int)(img & 3u) - 1);
+                    const float iy = (float)((int)((img >> 2) & 3u) - 1);
+                    const float iz = (float)((int)((img >> 4) & 3u) - 1);
+                    sz = fmul(box.L[2], iz);
+                    sy = fmul(box.L[1], iy);
+                    sx = fmul(box.L[0], ix);
+                    if (!ORTHO)
+                        {
+                        syz = fmul(fmul(box.L[2], box.yz), iz);
+                        sxz = fmul(fmul(box.L[2], box.xz), iz);
+                        sxy = fmul(fmul(box.L[1], box.xy), iy);
+                        }
+                    }
+                s_cj[k] = cjdx;
+                unsigned int* mrow = s_mask + b;
+                auto test = [&](auto wrap_tag) {
+                    constexpr bool wrapped = decltype(wrap_tag)::value;
+                    unsigned int p = 0;
+                    // two own particles per step: packed FP32 differences and squares (each half
+                    // rounds as the scalar operation), scalar rounded sums (f2dot3)
+                    const uint64_t cx2 = f2pack(cx, cx), cy2 = f2pack(cy, cy), cz2 = f2pack(cz, cz);
+                    for (; p + 1 < n_pass; p += 2)
+                        {
+                        uint64_t dx = f2sub(*reinterpret_cast<const uint64_t*>(s_ox + p), cx2);
+                        uint64_t dy = f2sub(*reinterpret_cast<const uint64_t*>(s_oy + p), cy2);
+                        uint64_t dz = f2sub(*reinterpret_cast<const uint64_t*>(s_oz + p), cz2);
+                        if (wrapped)
+                            {
+                            dz = f2sub(dz, f2pack(sz, sz));
+                            if (!ORTHO)
+                                {
+                                dy = f2sub(dy, f2pack(syz, syz));
+                                dx = f2sub(dx, f2pack(sxz, sxz));
+                                }
+                            dy = f2sub(dy, f2pack(sy, sy));
+                            if (!ORTHO)
+                                dx = f2sub(dx, f2pack(sxy, sxy));
+                            dx = f2sub(dx, f2pack(sx, sx));
+                            }
+                        float r0, r1;
+                        f2dot3(dx, dy, dz, r0, r1);
+                        const uint2 oi = *reinterpret_cast<const uint2*>(s_oi + p);
+                        float rl0 = rl_single, rl1 = rl_single;
+                        if (MULTI)
+                            {
+                            const uint2 orow = *reinterpret_cast<const uint2*>(s_orow + p);
+                            rl0 = s_tab[orow.x + ct];
+                            rl1 = s_tab[orow.y + ct];
+                            }
+                        const unsigned int m0 = __ballot_sync(0xffffffffu, r0 <= rl0 && cjdx != oi.x);
+                        const unsigned int m1 = __ballot_sync(0xffffffffu, r1 <= rl1 && cjdx != oi.y);
+                        if (lane == 0)
+                            {
+                            mrow[p * nb_max] = m0;
+                            mrow[(p + 1) * nb_max] = m1;
+                            }
+                        }
+                    for (; p < n_pass; p++)
+                        {
+                        const float4 o = make_float4(s_ox[p], s_oy[p], s_oz[p],
+                                                     __uint_as_float(s_oi[p]));
+                        float dx = fsub(o.x, cx), dy = fsub(o.y, cy), dz = fsub(o.z, cz);
+                        if (wrapped)
+                            {
+                            dz = fsub(dz, sz);
+                            if (!ORTHO)
+                                {
+                                dy = fsub(dy, syz);
+                                dx = fsub(dx, sxz);
+                                }
+                            dy = fsub(dy, sy);
+                            if (!ORTHO)
+                                dx = fsub(dx, sxy);
+                            dx = fsub(dx, sx);
+                            }
+                        const float rsq = dot3(dx, dy, dz);
+                        const float rl = MULTI ? s_tab[s_orow[p] + ct] : rl_single;
+                        const bool hit = rsq <= rl && cjdx != __float_as_uint(o.w);
+                        const unsigned int m = __ballot_sync(0xffffffffu, hit);
+                        if (lane == 0)
+                            mrow[p * nb_max] = m;
+                        }
+                };
+                if (plane_wraps)
+                    test(std::true_type {});
+                else
+                    test(std::false_type {});
+                }
+            __syncwarp();
+            // lane p appends own particle p's hits of this plane in stream order
+            if (active)
+                {
+                for (unsigned int b = 0; b < nb; b++)
+                    {
+                    unsigned int m = s_mask[lane * nb_max + b];
+                    const unsigned int* cjb = s_cj + 32u * b;
+                    auto put = [&](unsigned int j) {
+                        if (cnt < nmax_i)
+                            nlist[wo] = j;
+                        cnt++;
+                        if (LAYOUT == 4)
+                            wo += (cnt & 3u) ? 1u : jump;
+                        else
+                            wo += jump;
+                    };
+                    // two hits per iteration: both candidate loads issue before the stores
+                    while (m)
+                        {
+                        const unsigned int t0 = __ffs(m) - 1;
+                        m &= m - 1u;
+                        const unsigned int t1 = m ? __ffs(m) - 1 : t0;
+                        const bool two = m != 0u;
+                        m &= m - 1u;
+                        const unsigned int j0 = cjb[t0], j1 = cjb[t1];
+                        put(j0);
+                        if (two)
+                            put(j1);
+                        }
+                    }
+                }
+            __syncwarp();
+            }
+        if (active)
+            {
+            n_neigh[i] = min(cnt, nmax_i);
+            if (cnt > nmax_i)
+                atomicMax(&cond[MULTI ? ti : 0u], cnt);
+            if (last_pos)
+                last_pos[i] = make_float4(pi.x, pi.y, pi.z, 0.0f);
+            }
+        __syncwarp();
+        }
+    }
+
+size_t stream_smem_bytes(unsigned int Nmax_cell, unsigned int ntypes, bool multi, int wpb)
+    {
+    const size_t tab = multi ? ((sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
+    return tab + (size_t)wpb * stream_warp_bytes(Nmax_cell);
+    }
+
 size_t lane_smem_bytes(unsigned int Nmax_cell, unsigned int ntypes, bool multi, int wpb)
     {
     const size_t tab = multi ? ((2 * sizeof(float) * ntypes * ntypes + 15) / 16) * 16 : 0;
@@ -815,6 +1108,29 @@ bool launch_nlist_tile(const gb_nlist_args& a, unsigned int ncell, cudaStream_t 
     const bool ortho = a.box.xy == 0.0f && a.box.xz == 0.0f && a.box.yz == 0.0f;
     if (a.nlist_capacity != 0 && a.nlist_capacity <= 0xffffffffull)
         {
+        if (a.threads_per_particle != 1)
+            {
+            // the candidate stream (32 lanes test each own particle), the default
+            int wpb2 = a.block_size ? (int)(a.block_size / 32) : STREAM_WARPS;
+            size_t smem2 = stream_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, wpb2);
+            while (smem2 > 96 * 1024 && wpb2 > 1)
+                smem2 = stream_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, --wpb2);
+            if (smem2 <= 200 * 1024)
+                {
+                auto kern2 = ortho ? k_nlist_stream<MULTI, LAYOUT, true>
+                                   : k_nlist_stream<MULTI, LAYOUT, false>;
+                if (smem2 > 48 * 1024)
+                    cudaFuncSetAttribute(kern2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem2);
+                kern2<<<div_up(ncell, wpb2), wpb2 * 32, smem2, s>>>(
+                    a.d_nlist, a.d_n_neigh, reinterpret_cast<float4*>(a.d_last_pos),
+                    a.d_conditions, a.stride, a.d_Nmax, a.d_cell_size,
+                    reinterpret_cast<const float4*>(a.d_xyzf), a.d_cell_type,
+                    make_uint3(a.dim[0], a.dim[1], a.dim[2]), ncell, a.Nmax_cell, a.box, a.d_r_cut,
+                    a.d_r_listsq, a.ntypes, a.d_gate);
+                return true;
+                }
+            }
         int wpb = a.block_size ? (int)(a.block_size / 32) : LANE_WARPS;
         size_t smem = lane_smem_bytes(a.Nmax_cell, a.ntypes, MULTI, wpb);
         while (smem > 96 * 1024 && wpb > 1)
@@ -1080,6 +1396,9 @@ extern "C"
         GB_REQUIRE(a->block_size == 0 || a->block_size == 32 || a->block_size == 64
                        || a->block_size == 128,
                    "gb_nlist_build_binned: block_size must be 32, 64 or 128");
+        GB_REQUIRE(a->threads_per_particle == 0 || a->threads_per_particle == 1
+                       || a->threads_per_particle == 32,
+                   "gb_nlist_build_binned: threads_per_particle must be 1 or 32");
         const unsigned int ncell = a->dim[0] * a->dim[1] * a->dim[2];
         if (ncell == 0 || a->N == 0)
             return GB_OK;

@@ -43,7 +43,8 @@ class NlistArgs(ctypes.Structure):
                 ("d_xyzf", c_void), ("d_cell_type", c_void), ("d_cell_adj", c_void),
                 ("dim", c_uint * 3), ("Nmax_cell", c_uint), ("adj_width", c_uint), ("box", Box),
                 ("d_r_cut", c_void), ("d_r_listsq", c_void), ("ntypes", c_uint),
-                ("d_gate", c_void), ("block_size", ctypes.c_uint32), ("nlist_capacity", c_u64)]
+                ("d_gate", c_void), ("block_size", ctypes.c_uint32), ("nlist_capacity", c_u64),
+                ("threads_per_particle", ctypes.c_uint32)]
 
 
 class PairArgs(ctypes.Structure):

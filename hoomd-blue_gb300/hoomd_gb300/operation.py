@@ -16,7 +16,8 @@ class AutotunedObject:
     @property
     def kernel_parameters(self):
         """dict[str, tuple[int]]: kernel name -> launch parameters in use ("pair": (block size,
-        threads per particle); "nlist": (block size,))."""
+        threads per particle); "nlist": (block size, threads per particle), where 32 threads per
+        particle is the candidate-stream build and 1 the lane-per-particle build)."""
         if getattr(self, "_cpp_obj", None) is None:
             raise DataAccessError("kernel_parameters")
         return self._cpp_obj.getAutotunerParameters()

@@ -150,13 +150,17 @@ typedef struct gb_nlist_args
     const float* d_r_listsq;          /* [ntypes^2] (r_cut + r_buff)^2, 0 where r_cut <= 0 */
     unsigned int ntypes;
     const uint32_t* d_gate;           /* optional no-op gate, as for the cell list */
-    /* threads per block of the lane-per-particle build: 32, 64 or 128 (0 = 128), a warp per cell
-       (the kernel parameter the reference's Autotuner varies, hoomd/md/NeighborListGPUBinned.h) */
+    /* threads per block of the tiled builds: 32, 64 or 128 (0 = 128), a warp per cell (the
+       kernel parameters the reference's Autotuner varies, block size and threads per particle,
+       hoomd/md/NeighborListGPUBinned.cc:39-44) */
     uint32_t block_size;
     uint64_t nlist_capacity;          /* words allocated at d_nlist, or 0 when unknown; below 2^32
-                                         the tiled build addresses slots with 32-bit offsets
-                                         (one lane per particle), else it uses the warp-per-cell
-                                         form */
+                                         the tiled builds address slots with 32-bit offsets,
+                                         else the warp-per-cell form runs */
+    /* threads testing each own particle in the tiled build: 32 = candidate stream (a warp's
+       lanes hold 32 candidates and test them against one own particle at a time; the default,
+       0 means 32), 1 = one lane per own particle. Both give the same lists, entry for entry. */
+    uint32_t threads_per_particle;
     } gb_nlist_args;
 
 int gb_nlist_build_binned(const gb_nlist_args* args, void* stream);

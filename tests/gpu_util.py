@@ -48,8 +48,12 @@ class GpuNlist:
     def __init__(self, pos4, box6, r_cut, r_buff, layout="col", deterministic=False, ndim=3):
         """layout: "col", "col4" (column-major, interleaved by 4), "flat" (head list); a trailing
         "w" ("colw", "col4w") withholds the list capacity, which selects the warp-per-cell form
-        of the tiled build instead of the lane-per-particle one."""
+        of the tiled build, and a trailing "_lane" ("col_lane", "col4_lane") asks for the
+        lane-per-particle form (one thread per own particle) instead of the default candidate
+        stream."""
         L = abi.load()
+        self.tpp = 1 if layout.endswith("_lane") else 0
+        layout = layout[:-5] if self.tpp else layout
         self.warp_build = layout.endswith("w")
         layout = layout[:-1] if self.warp_build else layout
         self.N = N = len(pos4)
@@ -115,7 +119,8 @@ class GpuNlist:
                               d_cell_adj=p(self.adj), dim=(ctypes.c_uint32 * 3)(*self.dim),
                               Nmax_cell=self.Nmax_cell, adj_width=self.adj_w, box=self.box,
                               d_r_cut=p(self.d_rc), d_r_listsq=p(self.d_rl), ntypes=nt,
-                              nlist_capacity=0 if self.warp_build else self.nlist.numel())
+                              nlist_capacity=0 if self.warp_build else self.nlist.numel(),
+                              threads_per_particle=self.tpp)
             abi.check(L.gb_nlist_build_binned(ctypes.byref(a), stream()), "nlist")
             cond = host(self.ncond)
             over = cond > Nmax

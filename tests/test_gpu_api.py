@@ -394,7 +394,7 @@ def test_kernel_parameters_and_tuning():
         _ = lj.kernel_parameters
     sim.run(0)
     assert lj.kernel_parameters == {"pair": (256, 8)}  # 4096 particles: 8 lanes per particle
-    assert cell.kernel_parameters == {"nlist": (128,)}
+    assert cell.kernel_parameters == {"nlist": (128, 32)}
     assert lj.is_tuning_complete and cell.is_tuning_complete
     assert sim.operations.is_tuning_complete
     with pytest.raises(ValueError):
@@ -410,8 +410,8 @@ def test_kernel_parameters_and_tuning():
     assert sim.operations.is_tuning_complete
     samples = sim._cpp_integrator.lastTuning()
     pair = {(s[1], s[2]): s[3] for s in samples if s[0] == "pair"}
-    nl = {(s[1],): s[3] for s in samples if s[0] == "nlist"}
-    assert len(pair) == 6 and len(nl) == 3 and all(s[3] > 0 for s in samples)
+    nl = {(s[1], s[2]): s[3] for s in samples if s[0] == "nlist"}
+    assert len(pair) == 6 and len(nl) == 6 and all(s[3] > 0 for s in samples)
 
     def kept_rule(times, kept, default):
         # the fastest, unless it is within 2 % of the default, which then stays
@@ -419,11 +419,12 @@ def test_kernel_parameters_and_tuning():
         return kept == fastest or (kept == default and times[fastest] >= 0.98 * times[default])
 
     assert kept_rule(pair, lj.kernel_parameters["pair"], (256, 8))
-    assert kept_rule(nl, cell.kernel_parameters["nlist"], (128,))
+    assert kept_rule(nl, cell.kernel_parameters["nlist"], (128, 32))
 
     sim2, lj2, cell2, _ = lj_sim(snap, kT=None, thermalize=1.5)
     sim2.run(0)
-    for pcfg, ncfg in [((128, 1), (32,)), ((256, 4), (64,)), ((128, 8), (128,))]:
+    for pcfg, ncfg in [((128, 1), (32, 1)), ((256, 4), (64, 32)), ((128, 8), (128, 1)),
+                       ((256, 1), (32, 32))]:
         lj2.kernel_parameters = {"pair": pcfg}
         cell2.kernel_parameters = {"nlist": ncfg}
         sim2.run(0)

@@ -100,7 +100,8 @@ NLIST_CASES = {
 
 
 @pytest.mark.parametrize("case", sorted(NLIST_CASES))
-@pytest.mark.parametrize("layout", ["col", "col4", "colw", "col4w", "flat"])
+@pytest.mark.parametrize("layout", ["col", "col4", "col_lane", "col4_lane", "colw", "col4w",
+                                    "flat"])
 def test_nlist_bitexact_vs_oracle(case, layout):
     pos4, box6, rc, rb = NLIST_CASES[case]()
     nl = GpuNlist(pos4, box6, rc, rb, layout=layout)
@@ -473,17 +474,15 @@ def test_bussi_predrawn_ring_gives_the_same_factor():
 @pytest.mark.parametrize("case", ["lj4096", "binary3000", "triclinic1728", "random60k",
                                   "hi_face4096"])
 @pytest.mark.parametrize("layout", ["col", "col4"])
-def test_lane_and_warp_builds_are_identical(case, layout):
-    """The lane-per-particle and warp-per-cell tiled builds write the same neighbours in the same
-    order (so the force sums, and with them trajectories, do not depend on which one ran). The
-    cell lists are built in the deterministic (sorted) mode, so both read the same cell order."""
+def test_tiled_builds_are_identical(case, layout):
+    """The candidate-stream, lane-per-particle and warp-per-cell tiled builds write the same
+    neighbours in the same order (so the force sums, and with them trajectories, do not depend on
+    which one ran). The cell lists are built in the deterministic (sorted) mode, so all three read
+    the same cell order."""
     pos4, box6, rc, rb = NLIST_CASES[case]()
     a = GpuNlist(pos4, box6, rc, rb, layout=layout, deterministic=True)
-    b = GpuNlist(pos4, box6, rc, rb, layout=layout + "w", deterministic=True)
-    na, nb = host(a.n_neigh), host(b.n_neigh)
-    assert np.array_equal(na, nb)
-    la, lb = host(a.nlist), host(b.nlist)
     N = len(pos4)
+    na, la = host(a.n_neigh), host(a.nlist)
     k = np.arange(int(na.max()))[None, :]
     i = np.arange(N)[:, None]
     if layout == "col4":
@@ -491,4 +490,8 @@ def test_lane_and_warp_builds_are_identical(case, layout):
     else:
         idx = k * a.stride + i
     valid = k < na[:, None]
-    assert np.array_equal(la[idx][valid], lb[idx][valid])
+    for form in ("_lane", "w"):
+        b = GpuNlist(pos4, box6, rc, rb, layout=layout + form, deterministic=True)
+        nb, lb = host(b.n_neigh), host(b.nlist)
+        assert np.array_equal(na, nb), form
+        assert np.array_equal(la[idx][valid], lb[idx][valid]), form
