@@ -822,7 +822,7 @@ __host__ __device__ inline size_t stream_warp_bytes(unsigned int Nmax_cell)
     }
 
 template<bool MULTI, int LAYOUT, bool ORTHO>
-__global__ void __launch_bounds__(STREAM_WARPS * 32)
+__global__ void __launch_bounds__(STREAM_WARPS * 32, 6)
     k_nlist_stream(unsigned int* __restrict__ nlist, unsigned int* __restrict__ n_neigh,
                    float4* __restrict__ last_pos, unsigned int* __restrict__ cond,
                    uint64_t stride, const unsigned int* __restrict__ Nmax_t,
@@ -962,13 +962,14 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32)
                         }
                     }
                 s_cj[k] = cjdx;
-                unsigned int* mrow = s_mask + b;
+                unsigned int* mrow = s_mask + 32u * b;
                 auto test = [&](auto wrap_tag) {
                     constexpr bool wrapped = decltype(wrap_tag)::value;
                     unsigned int p = 0;
                     // two own particles per step: packed FP32 differences and squares (each half
                     // rounds as the scalar operation), scalar rounded sums (f2dot3)
                     const uint64_t cx2 = f2pack(cx, cx), cy2 = f2pack(cy, cy), cz2 = f2pack(cz, cz);
+#pragma unroll 2
                     for (; p + 1 < n_pass; p += 2)
                         {
                         uint64_t dx = f2sub(*reinterpret_cast<const uint64_t*>(s_ox + p), cx2);
@@ -1000,10 +1001,7 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32)
                         const unsigned int m0 = __ballot_sync(0xffffffffu, r0 <= rl0 && cjdx != oi.x);
                         const unsigned int m1 = __ballot_sync(0xffffffffu, r1 <= rl1 && cjdx != oi.y);
                         if (lane == 0)
-                            {
-                            mrow[p * nb_max] = m0;
-                            mrow[(p + 1) * nb_max] = m1;
-                            }
+                            *reinterpret_cast<uint2*>(mrow + p) = make_uint2(m0, m1);
                         }
                     for (; p < n_pass; p++)
                         {
@@ -1028,7 +1026,7 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32)
                         const bool hit = rsq <= rl && cjdx != __float_as_uint(o.w);
                         const unsigned int m = __ballot_sync(0xffffffffu, hit);
                         if (lane == 0)
-                            mrow[p * nb_max] = m;
+                            mrow[p] = m;
                         }
                 };
                 if (plane_wraps)
@@ -1042,7 +1040,7 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32)
                 {
                 for (unsigned int b = 0; b < nb; b++)
                     {
-                    unsigned int m = s_mask[lane * nb_max + b];
+                    unsigned int m = s_mask[32u * b + lane];
                     const unsigned int* cjb = s_cj + 32u * b;
                     auto put = [&](unsigned int j) {
                         if (cnt < nmax_i)
