@@ -847,11 +847,11 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32, 6)
         }
     const unsigned int nb_max = stream_nb(Nmax_cell);
     unsigned char* base = smem + tab_bytes + (size_t)warp * stream_warp_bytes(Nmax_cell);
-    float* s_ox = reinterpret_cast<float*>(base);
-    float* s_oy = s_ox + 32;
-    float* s_oz = s_oy + 32;
-    unsigned int* s_oi = reinterpret_cast<unsigned int*>(s_oz + 32);
-    unsigned int* s_orow = s_oi + 32;
+    // own particles by pairs: s_oa[q] = (x, x', y, y') and s_ob[q] = (z, z', index, index') of own
+    // particles 2q and 2q + 1, so one 16-byte load gives a packed pair of two coordinates
+    float4* s_oa = reinterpret_cast<float4*>(base);
+    float4* s_ob = s_oa + 16;
+    unsigned int* s_orow = reinterpret_cast<unsigned int*>(s_ob + 16);
     unsigned int* s_plane = s_orow + 32; // [0, 10) offsets, [10, 19) cells, [19, 28) images
     unsigned int* s_cj = s_plane + 32;
     unsigned int* s_mask = s_cj + 32 * nb_max;
@@ -878,10 +878,12 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32, 6)
             pi = __ldg(xyzf + (size_t)cell * Nmax_cell + ob + lane);
             if (MULTI)
                 ti = __ldg(cell_type + (size_t)cell * Nmax_cell + ob + lane);
-            s_ox[lane] = pi.x;
-            s_oy[lane] = pi.y;
-            s_oz[lane] = pi.z;
-            s_oi[lane] = __float_as_uint(pi.w);
+            float* a = reinterpret_cast<float*>(s_oa + lane / 2) + (lane & 1);
+            float* bz = reinterpret_cast<float*>(s_ob + lane / 2) + (lane & 1);
+            a[0] = pi.x;
+            a[2] = pi.y;
+            bz[0] = pi.z;
+            bz[2] = pi.w;
             if (MULTI)
                 s_orow[lane] = ti * ntypes;
             }
@@ -972,9 +974,10 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32, 6)
 #pragma unroll 2
                     for (; p + 1 < n_pass; p += 2)
                         {
-                        uint64_t dx = f2sub(*reinterpret_cast<const uint64_t*>(s_ox + p), cx2);
-                        uint64_t dy = f2sub(*reinterpret_cast<const uint64_t*>(s_oy + p), cy2);
-                        uint64_t dz = f2sub(*reinterpret_cast<const uint64_t*>(s_oz + p), cz2);
+                        const float4 oa = s_oa[p / 2], obz = s_ob[p / 2];
+                        uint64_t dx = f2sub(f2pack(oa.x, oa.y), cx2);
+                        uint64_t dy = f2sub(f2pack(oa.z, oa.w), cy2);
+                        uint64_t dz = f2sub(f2pack(obz.x, obz.y), cz2);
                         if (wrapped)
                             {
                             dz = f2sub(dz, f2pack(sz, sz));
@@ -990,7 +993,7 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32, 6)
                             }
                         float r0, r1;
                         f2dot3(dx, dy, dz, r0, r1);
-                        const uint2 oi = *reinterpret_cast<const uint2*>(s_oi + p);
+                        const uint2 oi = make_uint2(__float_as_uint(obz.z), __float_as_uint(obz.w));
                         float rl0 = rl_single, rl1 = rl_single;
                         if (MULTI)
                             {
@@ -1005,8 +1008,9 @@ __global__ void __launch_bounds__(STREAM_WARPS * 32, 6)
                         }
                     for (; p < n_pass; p++)
                         {
-                        const float4 o = make_float4(s_ox[p], s_oy[p], s_oz[p],
-                                                     __uint_as_float(s_oi[p]));
+                        const float* a = reinterpret_cast<const float*>(s_oa + p / 2) + (p & 1);
+                        const float* bz = reinterpret_cast<const float*>(s_ob + p / 2) + (p & 1);
+                        const float4 o = make_float4(a[0], a[2], bz[0], bz[2]);
                         float dx = fsub(o.x, cx), dy = fsub(o.y, cy), dz = fsub(o.z, cz);
                         if (wrapped)
                             {
