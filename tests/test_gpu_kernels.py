@@ -50,6 +50,19 @@ def random_system(N, L, ntypes=1, seed=0, tilts=(0, 0, 0), lattice=False):
     return O.make_pos4(np.stack([x, y, z], 1), types, 32), (Lx, Ly, Lz, xy, xz, yz)
 
 
+def dense_system():
+    """Cells holding more than 32 particles (the tiled builds take own particles in passes of 32):
+    2600 uniform particles in a 14^3 box (4^3 cells of 3.5, ≈ 41 a cell) and a cluster of 120 in
+    one cell at a corner of the box, two types."""
+    rng = np.random.default_rng(11)
+    L = 14.0
+    uni = rng.uniform(-L / 2, L / 2, (2600, 3))
+    clu = rng.uniform(-L / 2, -L / 2 + 3.0, (120, 3))
+    pos = np.concatenate([uni, clu])
+    types = rng.integers(0, 2, len(pos))
+    return O.make_pos4(pos, types, 32), (L, L, L, 0.0, 0.0, 0.0)
+
+
 def snap_pos4(snap):
     return O.make_pos4(snap.particles.position, snap.particles.typeid, 32), \
         tuple(snap.configuration.box)
@@ -96,6 +109,7 @@ NLIST_CASES = {
     + ([[2.5, 1.5], [1.5, 2.0]], 0.4),
     "random60k": lambda: random_system(60000, (41.0, 41.0, 41.0), seed=7) + ([[2.5]], 0.4),
     "hi_face4096": lambda: hi_face_system() + ([[2.5]], 0.4),
+    "dense2720": lambda: dense_system() + ([[2.5, 2.0], [2.0, 2.2]], 0.4),
 }
 
 
@@ -472,7 +486,7 @@ def test_bussi_predrawn_ring_gives_the_same_factor():
 
 
 @pytest.mark.parametrize("case", ["lj4096", "binary3000", "triclinic1728", "random60k",
-                                  "hi_face4096"])
+                                  "hi_face4096", "dense2720"])
 @pytest.mark.parametrize("layout", ["col", "col4"])
 def test_tiled_builds_are_identical(case, layout):
     """The candidate-stream, lane-per-particle and warp-per-cell tiled builds write the same
