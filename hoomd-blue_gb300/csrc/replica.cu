@@ -62,10 +62,22 @@ constexpr size_t scratch_chunk(uint64_t n)
     return ((n + 31) / 32 * 16 + 255) / 256 * 256;
     }
 
-__host__ __device__ inline size_t smem_bytes(uint32_t max_cells, uint32_t block)
+// Candidate-stream search (stream_search): cells of at most STREAM_OCC particles; per warp
+// the own particles by pairs (512 B), the plane record (128 B), and the candidate indices and
+// ballot masks of up to STREAM_NB blocks of 32 candidates (one plane's stream).
+constexpr uint32_t STREAM_OCC = 40;
+constexpr uint32_t STREAM_NB = (9 * STREAM_OCC + 31) / 32;
+constexpr size_t STREAM_WARP_BYTES = 512 + 128 + 2 * 4 * 32 * STREAM_NB;
+
+__host__ __device__ inline size_t smem_cells_bytes(uint32_t max_cells, uint32_t block)
     {
     // Bussi draws (double2 per thread), cell starts (max_cells + 1), cell counters (max_cells)
     return ((size_t)block * 16 + (size_t)(2 * max_cells + 1) * 4 + 15) / 16 * 16;
+    }
+
+__host__ __device__ inline size_t smem_bytes(uint32_t max_cells, uint32_t block)
+    {
+    return smem_cells_bytes(max_cells, block) + (size_t)(block / 32) * STREAM_WARP_BYTES;
     }
 
 struct RepShared
@@ -76,6 +88,7 @@ struct RepShared
     uint32_t rebuild;   // set by step one when a particle moved far enough
     uint32_t err;       // status bits raised during a build
     uint32_t maxcnt;    // largest neighbour count found by the last build
+    uint32_t maxocc;    // most particles in one cell at the last build
     uint32_t wtot[32];  // scan scratch
     long long clk[4];   // cycles in step one, builds, pair step, Bussi draws (thread 0)
     long long t0;       // last phase boundary (thread 0)
@@ -146,10 +159,214 @@ __device__ __forceinline__ uint32_t wrap_index(int c, int n)
     return (uint32_t)(c < 0 ? c + n : (c >= n ? c - n : c));
     }
 
+// Candidate-stream search of one replica (the main build's k_nlist_stream): a warp per cell, the lanes holding 32 candidates of one stencil
+// plane's stream (nine cells in the order (row, column), each a run of the cell-ordered array),
+// the own particles tested two at a time against them (packed differences and squares, scalar
+// sums: the per-thread search's roundings), one ballot mask per own particle and block, then lane
+// p appends own particle p's hits in stream order, which is the per-thread search's order. Used
+// for orthorhombic replicas with at least four cells a side, stencil 1 and at most STREAM_OCC
+// particles a cell (cell images then come from the cell offsets, as in the per-thread search).
+// Returns the warp's largest neighbour count.
+__device__ __noinline__ uint32_t stream_search(const gb_replica& R, const RepArrays& A,
+                                               const uint32_t* s_start, unsigned char* s_stream,
+                                               float rlsq)
+    {
+    const uint32_t lane = threadIdx.x % 32, warp = threadIdx.x / 32, nwarps = blockDim.x / 32;
+    const uint32_t dims[3] = {R.dim[0], R.dim[1], R.dim[2]};
+    const uint32_t ncell = dims[0] * dims[1] * dims[2];
+    const gb_box box = R.box;
+    const float4* sorted = A.sorted + R.first;
+    uint32_t* nlist = A.nlist + R.nlist_offset;
+    const uint32_t Nmax = R.Nmax;
+    const uint32_t stride = R.stride;
+    const float inf = __int_as_float(0x7f800000);
+    unsigned char* base = s_stream + (size_t)warp * STREAM_WARP_BYTES;
+    float4* s_oa = reinterpret_cast<float4*>(base);     // (x, x', y, y') of own pairs
+    float4* s_ob = s_oa + 16;                           // (z, z', index, index')
+    uint32_t* s_plane = reinterpret_cast<uint32_t*>(s_ob + 16); // [0, 10) offsets, [10, 19)
+                                                        // run starts, [19, 28) images
+    uint32_t* s_cj = s_plane + 32;
+    uint32_t* s_mask = s_cj + 32 * STREAM_NB;
+    uint32_t my_max = 0;
+
+    for (uint32_t cell = warp; cell < ncell; cell += nwarps)
+        {
+        const uint32_t c0 = s_start[cell], csize = s_start[cell + 1] - c0;
+        const int ci = cell % dims[0], cj = (cell / dims[0]) % dims[1],
+                  ck = cell / (dims[0] * dims[1]);
+        for (uint32_t ob = 0; ob < csize; ob += 32)
+            {
+            const uint32_t n_pass = min(csize - ob, 32u);
+            const bool active = lane < n_pass;
+            float4 pi = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (active)
+                {
+                pi = sorted[c0 + ob + lane];
+                float* a = reinterpret_cast<float*>(s_oa + lane / 2) + (lane & 1);
+                float* bz = reinterpret_cast<float*>(s_ob + lane / 2) + (lane & 1);
+                a[0] = pi.x;
+                a[2] = pi.y;
+                bz[0] = pi.z;
+                bz[2] = pi.w;
+                }
+            const uint32_t i = __float_as_uint(pi.w);
+            uint32_t wo = i * 4u;
+            const uint32_t jump = stride * 4u - 3u;
+            uint32_t cnt = 0;
+            for (int pz = -1; pz <= 1; pz++)
+                {
+                uint32_t q_n = 0;
+                bool q_wrap = false;
+                if (lane < 9)
+                    {
+                    const int ox = lane % 3 - 1, oy = lane / 3 - 1;
+                    const int x = ci + ox, y = cj + oy, z = ck + pz;
+                    const uint32_t q_cell = (wrap_index(z, (int)dims[2]) * dims[1]
+                                             + wrap_index(y, (int)dims[1])) * dims[0]
+                                            + wrap_index(x, (int)dims[0]);
+                    const uint32_t qs = s_start[q_cell];
+                    q_n = s_start[q_cell + 1] - qs;
+                    const int ix = x >= (int)dims[0] ? 1 : (x < 0 ? -1 : 0);
+                    const int iy = y >= (int)dims[1] ? 1 : (y < 0 ? -1 : 0);
+                    const int iz = z >= (int)dims[2] ? 1 : (z < 0 ? -1 : 0);
+                    q_wrap = ix != 0 || iy != 0 || iz != 0;
+                    s_plane[10 + lane] = qs;
+                    s_plane[19 + lane] = (uint32_t)((ix + 1) | ((iy + 1) << 2) | ((iz + 1) << 4));
+                    }
+                uint32_t incl = q_n;
+#pragma unroll
+                for (int o = 1; o < 16; o <<= 1)
+                    {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if ((int)lane >= o)
+                        incl += y;
+                    }
+                if (lane < 9)
+                    s_plane[lane] = incl - q_n;
+                const uint32_t total = __shfl_sync(0xffffffffu, incl, 8);
+                if (lane == 9)
+                    s_plane[9] = total;
+                const bool plane_wraps = __any_sync(0xffffffffu, q_wrap);
+                __syncwarp();
+                const uint32_t nb = (total + 31u) / 32u;
+                uint32_t q = 0;
+                for (uint32_t b = 0; b < nb; b++)
+                    {
+                    const uint32_t k = 32u * b + lane;
+                    float cx = inf, cy = inf, cz = inf, sx = 0.f, sy = 0.f, sz = 0.f;
+                    uint32_t cjdx = 0xffffffffu;
+                    if (k < total)
+                        {
+                        while (k >= s_plane[q + 1])
+                            q++;
+                        const float4 c = sorted[s_plane[10 + q] + (k - s_plane[q])];
+                        cx = c.x;
+                        cy = c.y;
+                        cz = c.z;
+                        cjdx = __float_as_uint(c.w);
+                        const uint32_t img = s_plane[19 + q];
+                        sx = fmul(box.L[0], (float)((int)(img & 3u) - 1));
+                        sy = fmul(box.L[1], (float)((int)((img >> 2) & 3u) - 1));
+                        sz = fmul(box.L[2], (float)((int)((img >> 4) & 3u) - 1));
+                        }
+                    s_cj[k] = cjdx;
+                    uint32_t* mrow = s_mask + 32u * b;
+                    auto test = [&](auto wrap_tag) {
+                        constexpr bool wrapped = decltype(wrap_tag)::value;
+                        const uint64_t cx2 = f2pack(cx, cx), cy2 = f2pack(cy, cy),
+                                       cz2 = f2pack(cz, cz);
+                        uint32_t p = 0;
+#pragma unroll 2
+                        for (; p + 1 < n_pass; p += 2)
+                            {
+                            const float4 oa = s_oa[p / 2], obz = s_ob[p / 2];
+                            uint64_t dx = f2sub(f2pack(oa.x, oa.y), cx2);
+                            uint64_t dy = f2sub(f2pack(oa.z, oa.w), cy2);
+                            uint64_t dz = f2sub(f2pack(obz.x, obz.y), cz2);
+                            if (wrapped)
+                                {
+                                dx = f2sub(dx, f2pack(sx, sx));
+                                dy = f2sub(dy, f2pack(sy, sy));
+                                dz = f2sub(dz, f2pack(sz, sz));
+                                }
+                            float r0, r1;
+                            f2dot3(dx, dy, dz, r0, r1);
+                            const uint32_t m0 = __ballot_sync(
+                                0xffffffffu, r0 <= rlsq && cjdx != __float_as_uint(obz.z));
+                            const uint32_t m1 = __ballot_sync(
+                                0xffffffffu, r1 <= rlsq && cjdx != __float_as_uint(obz.w));
+                            if (lane == 0)
+                                *reinterpret_cast<uint2*>(mrow + p) = make_uint2(m0, m1);
+                            }
+                        for (; p < n_pass; p++)
+                            {
+                            const float* a = reinterpret_cast<const float*>(s_oa + p / 2) + (p & 1);
+                            const float* bz = reinterpret_cast<const float*>(s_ob + p / 2) + (p & 1);
+                            float dx = fsub(a[0], cx), dy = fsub(a[2], cy), dz = fsub(bz[0], cz);
+                            if (wrapped)
+                                {
+                                dx = fsub(dx, sx);
+                                dy = fsub(dy, sy);
+                                dz = fsub(dz, sz);
+                                }
+                            const bool hit = dot3(dx, dy, dz) <= rlsq
+                                             && cjdx != __float_as_uint(bz[2]);
+                            const uint32_t m = __ballot_sync(0xffffffffu, hit);
+                            if (lane == 0)
+                                mrow[p] = m;
+                            }
+                    };
+                    if (plane_wraps)
+                        test(std::true_type {});
+                    else
+                        test(std::false_type {});
+                    }
+                __syncwarp();
+                if (active)
+                    {
+                    for (uint32_t b = 0; b < nb; b++)
+                        {
+                        uint32_t m = s_mask[32u * b + lane];
+                        const uint32_t* cjb = s_cj + 32u * b;
+                        auto put = [&](uint32_t j) {
+                            if (cnt < Nmax)
+                                nlist[wo] = j;
+                            cnt++;
+                            wo += (cnt & 3u) ? 1u : jump;
+                        };
+                        while (m)
+                            {
+                            const uint32_t t0 = __ffs(m) - 1;
+                            m &= m - 1u;
+                            const uint32_t t1 = m ? __ffs(m) - 1 : t0;
+                            const bool two = m != 0u;
+                            m &= m - 1u;
+                            const uint32_t j0 = cjb[t0], j1 = cjb[t1];
+                            put(j0);
+                            if (two)
+                                put(j1);
+                            }
+                        }
+                    }
+                __syncwarp();
+                }
+            if (active)
+                {
+                A.n_neigh[R.first + i] = min(cnt, Nmax);
+                A.last_pos[R.first + i] = make_float4(pi.x, pi.y, pi.z, 0.0f);
+                my_max = max(my_max, cnt);
+                }
+            __syncwarp();
+            }
+        }
+    return my_max;
+    }
+
 // Cell list + neighbour list of the replica in sh.rep. Sets sh.err / sh.maxcnt; ends synced.
 // Not inlined (nor are the other phases): each phase gets its own register allocation.
 template<int MAXT>
-__device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint32_t* s_start, uint32_t* s_cnt)
+__device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint32_t* s_start,
+                                         uint32_t* s_cnt, unsigned char* s_stream)
     {
     const gb_replica& R = sh.rep;
     const uint32_t T = blockDim.x, t = threadIdx.x;
@@ -167,6 +384,7 @@ __device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint
         {
         sh.err = 0u;
         sh.maxcnt = 0u;
+        sh.maxocc = 0u;
         }
     __syncthreads();
     // bin (hoomd/CellListGPU.cu:42-170, without a slot limit)
@@ -197,9 +415,11 @@ __device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint
         }
     __syncthreads();
     // slots of a cell in particle-index order (nlist.Cell(deterministic=True))
+    uint32_t occ = 0;
     for (uint32_t c = t; c < ncell; c += T)
         {
         const uint32_t b = s_start[c], e = s_start[c + 1];
+        occ = max(occ, e - b);
         for (uint32_t a = b + 1; a < e; a++)
             {
             const float4 v = sorted[a];
@@ -213,6 +433,9 @@ __device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint
             sorted[k] = v;
             }
         }
+    occ = __reduce_max_sync(0xffffffffu, occ);
+    if (t % 32 == 0)
+        atomicMax(&sh.maxocc, occ);
     __syncthreads();
 
     // binned search: lanes walk consecutive cell-ordered slots, so a warp mostly shares a
@@ -236,6 +459,9 @@ __device__ __noinline__ void build_lists(RepShared& sh, const RepArrays& A, uint
     // every pair within r_list; otherwise each candidate goes through min_image.
     const bool shifts = ortho && dims[0] >= span + 1 && dims[1] >= span + 1 && dims[2] >= span + 1;
     uint32_t my_max = 0;
+    if (shifts && S == 1 && sh.maxocc <= STREAM_OCC)
+        my_max = stream_search(R, A, s_start, s_stream, rlsq);
+    else
     for (uint32_t s = t; s < N; s += T)
         {
         const float4 pi = sorted[s];
@@ -562,7 +788,7 @@ __device__ __noinline__ void finish_step(RepShared& sh, const double2* s_draws, 
 
 template<int MAXT>
 __device__ void run_replica(RepShared& sh, const RepArrays& A, double2* s_draws,
-                            uint32_t* s_start, uint32_t* s_cnt)
+                            uint32_t* s_start, uint32_t* s_cnt, unsigned char* s_stream)
     {
     gb_replica& R = sh.rep;
     const uint32_t T = blockDim.x, t = threadIdx.x;
@@ -582,7 +808,7 @@ __device__ void run_replica(RepShared& sh, const RepArrays& A, double2* s_draws,
         {
         // IntegratorTwoStep::prepRun: lists, forces and a = F/m at the current step, thermo,
         // and the factor of the first step (hoomd/md/IntegratorTwoStep.cc:226-298)
-        build_lists<MAXT>(sh, A, s_start, s_cnt);
+        build_lists<MAXT>(sh, A, s_start, s_cnt, s_stream);
         stamp(sh, 1);
         if (sh.err)
             {
@@ -666,7 +892,7 @@ __device__ void run_replica(RepShared& sh, const RepArrays& A, double2* s_draws,
             }
         if (R.pending_build)
             {
-            build_lists<MAXT>(sh, A, s_start, s_cnt);
+            build_lists<MAXT>(sh, A, s_start, s_cnt, s_stream);
             stamp(sh, 1);
             if (sh.err)
                 {
@@ -703,6 +929,7 @@ __global__ void __launch_bounds__(MAXT, 1)
     double2* s_draws = reinterpret_cast<double2*>(smem);
     uint32_t* s_start = reinterpret_cast<uint32_t*>(s_draws + blockDim.x);
     uint32_t* s_cnt = s_start + max_cells + 1;
+    unsigned char* s_stream = smem + smem_cells_bytes(max_cells, blockDim.x);
     constexpr uint32_t WORDS = sizeof(gb_replica) / 4;
     for (;;)
         {
@@ -733,7 +960,7 @@ __global__ void __launch_bounds__(MAXT, 1)
                 }
             else
                 {
-                run_replica<MAXT>(sh, A, s_draws, s_start, s_cnt);
+                run_replica<MAXT>(sh, A, s_draws, s_start, s_cnt, s_stream);
                 if (A.clocks && threadIdx.x == 0)
                     for (int k = 0; k < 4; k++)
                         A.clocks[4 * (size_t)r + k] += (uint64_t)sh.clk[k];

@@ -94,6 +94,8 @@ def test_replica_host_helpers():
     n = 1000
     assert lib.gb_replica_scratch_bytes(n) >= n * (4 + 16) + (n + 31) // 32 * 16
     # double2 Bussi draws per thread, cell starts and counters, 16-byte rounded
-    assert lib.gb_replica_smem_bytes(1000, 512) == (512 * 16 + 2001 * 4 + 15) // 16 * 16
+    # Bussi draws, cell starts and counters, and per warp the candidate-stream scratch
+    assert lib.gb_replica_smem_bytes(1000, 512) == ((512 * 16 + 2001 * 4 + 15) // 16 * 16
+                                                    + 16 * (512 + 128 + 2 * 4 * 32 * 12))
     assert lib.gb_replica_smem_bytes(100000, 1024) == 0  # beyond 227 KB of shared memory
     assert lib.gb_replicas_run(None, None) == abi.GB_ERR_INVALID
