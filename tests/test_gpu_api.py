@@ -762,11 +762,15 @@ def test_particles_on_the_hi_face_keep_their_neighbours():
     p32 = O.make_pos4(pos, np.zeros(len(pos)), 32)
     n, l, h, _ = O.build_nlist(p32, box, [[2.5]], 0.4, full=True, prec=32)
     f32, _ = O.pair_forces("lj", p32, box, [[1.0, 1.0]], np.float32([[6.25]]), n, l, h, prec=32)
+    # cut-off band at FP32 too: across the boundary the FP32 r^2 can sit a few 1e-6 from FP64's
+    fb32, _ = O.pair_forces("lj", p32, box, [[1.0, 1.0]], np.float32([[6.25]]), n, l, h,
+                            prec=32, abs_terms=2)
     p64 = O.make_pos4(pos, np.zeros(len(pos)), 64)
     n, l, h, _ = O.build_nlist(p64, box, [[2.5]], 0.4, full=True, prec=64)
     fa, _ = O.pair_forces("lj", p64, box, [[1.0, 1.0]], [[6.25]], n, l, h, prec=64, abs_terms=1)
     fb, _ = O.pair_forces("lj", p64, box, [[1.0, 1.0]], [[6.25]], n, l, h, prec=64, abs_terms=2)
-    assert_close_cond(lj.forces, f32[:, :3], fa[:, :3], band=fb[:, :3], what="hi-face forces")
+    assert_close_cond(lj.forces, f32[:, :3], fa[:, :3], band=fb[:, :3] + fb32[:, :3],
+                      what="hi-face forces")
 
 
 def test_params_changed_between_runs_recompute_forces():

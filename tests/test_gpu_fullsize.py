@@ -7,16 +7,16 @@ Each system is built from the same seeds as the benchmark:
 * the 524,288-particle 32-type system with 528 tabulated potentials (density 0.8, r_cut 3.0,
   buffer 0.4).
 
-For each, the GPU neighbour list (cell list + lane-per-particle build through the C ABI, the
-layout the engine runs) must equal the FP32 oracle's full list as per-particle sorted sets, bit
+For each, the GPU neighbour list (cell list + the candidate-stream build through the C ABI, the
+layout and build the engine runs) must equal the FP32 oracle's full list as per-particle sorted sets, bit
 for bit. One evaluation of the pair forces, per-particle energies and virials over that list is
 then held to two bars:
 
 * against the FP32 oracle (the reference's arithmetic at HOOMD_LONGREAL_SIZE=32 on the same
   FP32 positions): within 1e-5 of the sum of the magnitudes of the terms of each value (the
   only differences left are the evaluator's reciprocal and the summation order), plus the terms
-  of pairs within 1e-6 relative of r_cut^2 (LJ does not vanish at r_cut in mode "none", and
-  whether such a pair counts turns on the last bit of r^2);
+  of pairs within 1e-6 relative of r_cut^2 at FP64 or at FP32 (LJ does not vanish at r_cut in
+  mode "none", and whether such a pair counts turns on the last bit of r^2);
 * against the FP64 oracle: no worse than the FP32 oracle itself (largest error at most 1.5x
   the FP32 oracle's; values outside 1e-5 relative at most twice as many as the FP32 oracle's,
   plus 1e-4 of the values).
@@ -134,13 +134,26 @@ def test_fullsize_nlist_and_forces_vs_oracle(systems, case):
 def check_against_oracles(kind, pos64, box6, oparams, rc, r_buff, odata, got, f32, case, ndim=3):
     """got / f32: (forces (N, 3), energies (N,), virials (6, N)) of the GPU and of the FP32
     oracle; the FP64 oracle's values, the sums of term magnitudes and the cut-off band terms are
-    computed here."""
+    computed here. The band is taken both at FP64 and at FP32: for a pair across a periodic
+    boundary the FP32 difference x_i - x_j of coordinates near +-L/2 carries a rounding of up to
+    ~L 2^-24, so its FP32 r^2 can sit several 1e-6 (relative) from the FP64 one, and the pairs
+    that the two FP32 evaluations may count differently are those whose FP32 r^2 is near r_cut^2."""
     n6, l6, h6, _ = O.build_nlist(pos64, box6, rc, r_buff, full=True, ndim=ndim, prec=64,
                                   nthreads=CORES)
     kw = dict(third_law=False, compute_virial=True, tdata=odata, prec=64, nthreads=CORES)
     fo, vo = O.pair_forces(kind, pos64, box6, oparams, rc ** 2, n6, l6, h6, **kw)
     fa, va = O.pair_forces(kind, pos64, box6, oparams, rc ** 2, n6, l6, h6, abs_terms=1, **kw)
     fb, vb = O.pair_forces(kind, pos64, box6, oparams, rc ** 2, n6, l6, h6, abs_terms=2, **kw)
+    del n6, l6, h6
+    pos32 = O.make_pos4(pos64[:, :3], O.pos_index_bits(pos64[:, 3], 64), 32)
+    n3, l3, h3, _ = O.build_nlist(pos32, box6, rc, r_buff, full=True, ndim=ndim, prec=32,
+                                  nthreads=CORES)
+    kw32 = dict(kw, prec=32)
+    fb32, vb32 = O.pair_forces(kind, pos32, box6, oparams, np.float32(rc ** 2), n3, l3, h3,
+                               abs_terms=2, **kw32)
+    del n3, l3, h3
+    fb = fb + fb32.astype(np.float64)
+    vb = vb + vb32.astype(np.float64)
     ref = (fo[:, :3], fo[:, 3], vo)
     absref = (fa[:, :3], fa[:, 3], va)
     bands = (fb[:, :3], fb[:, 3], vb)
