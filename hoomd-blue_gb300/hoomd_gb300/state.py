@@ -91,10 +91,14 @@ class State:
         if list(snapshot.configuration.box) != list(self._cpp_pdata.getBox()):
             raise RuntimeError("set_snapshot: box changes are not supported")
         snapshot.validate()
-        topology = _copy_topology(snapshot)
-        if not _same_topology(topology, self._topology):
-            self._topology = topology
-            self._topology_version += 1
+        # no bonds, angles, ... before or after: the topology (and the exclusions built from it)
+        # stays as it is without copying the empty sections
+        if not (all(getattr(snapshot, k).N == 0 for k in _SECTIONS)
+                and all(self._topology[k].N == 0 for k in _SECTIONS)):
+            topology = _copy_topology(snapshot)
+            if not _same_topology(topology, self._topology):
+                self._topology = topology
+                self._topology_version += 1
         self._passive = _copy_passive(snapshot)
         self._upload(snapshot)
 
