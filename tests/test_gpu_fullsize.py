@@ -31,9 +31,10 @@ This follows the reference's CPU-vs-GPU list comparison
 (hoomd/md/pytest/test_potential.py:952-1058), at full size. The oracle runs on every host core
 (OpenMP); the comparisons are vectorised over particle chunks.
 
-The 1M-particle fluid is also checked after 200 steps of the product's own run (Bussi at
-kT 1.5, Hilbert sort every 100 steps): the engine's forces, energies and virials through the
-Python API against the oracles at the resulting positions, with the same bars.
+The 1M-particle fluid and the Kob-Andersen mixture are also checked after 200 steps of the
+product's own run (Bussi, Hilbert sort every 100 steps, the benchmark's settings): the engine's
+forces, energies and virials through the Python API against the oracles at the resulting
+positions, with the same bars.
 """
 
 import os
@@ -205,6 +206,47 @@ def test_fullsize_fcc_after_run_vs_oracle():
     pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
     check_against_oracles("lj", pos64, box6, [[1.0, 1.0]], rc, 0.4, None,
                           (F, E, W.T), (f32[:, :3], f32[:, 3], v32), "fcc after 200 steps")
+
+
+def test_fullsize_ka_after_run_vs_oracle():
+    """The 262,144-particle Kob-Andersen mixture after 200 steps of the product's own run (Bussi
+    at kT 0.8, dt 0.003, Hilbert sort every 100 steps, the benchmark's settings): the engine's
+    forces, energies and virials through the Python API against the oracles at the resulting
+    positions, with the per-type-pair cut-offs and parameters of the mixture."""
+    import hoomd_gb300 as hoomd
+    from hoomd_gb300 import md
+    from hoomd_gb300.workloads import to_snapshot
+
+    system = S.binary_mixture(N=262144, density=1.2, seed=1)
+    sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=1)
+    sim.create_state_from_snapshot(to_snapshot(system))
+    sim.state.thermalize_particle_momenta(hoomd.filter.All(), 0.8)
+    cell = md.nlist.Cell(buffer=0.3)
+    lj = md.pair.LJ(nlist=cell, default_r_cut=2.5)
+    pairs = {("A", "A"): (1.0, 1.0, 2.5), ("A", "B"): (1.5, 0.8, 2.0),
+             ("B", "B"): (0.5, 0.88, 2.2)}
+    for key, (eps, sig, r) in pairs.items():
+        lj.params[key] = dict(epsilon=eps, sigma=sig)
+        lj.r_cut[key] = r
+    sim.operations.integrator = md.Integrator(dt=0.003, forces=[lj], methods=[
+        md.methods.ConstantVolume(hoomd.filter.All(), md.methods.thermostats.Bussi(kT=0.8))])
+    sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=100))
+    sim.run(200)
+    F, E, W = lj.forces, lj.energies, lj.virials
+    snap = sim.state.get_snapshot()
+    box6 = tuple(snap.configuration.box)
+    pos4 = O.make_pos4(snap.particles.position, snap.particles.typeid, 32)
+    rc, par = _lj_case(system, {(0, 0): (1.0, 1.0, 2.5), (0, 1): (1.5, 0.8, 2.0),
+                                (1, 1): (0.5, 0.88, 2.2)})
+    n, l, h, _ = O.build_nlist(pos4, box6, rc, 0.3, full=True, prec=32, nthreads=CORES)
+    f32, v32 = O.pair_forces("lj", pos4, box6, par, (rc ** 2).astype(np.float32), n, l, h,
+                             third_law=False, compute_virial=True, prec=32, nthreads=CORES)
+    del l, h
+    assert cell.num_builds >= 2
+    pos64 = pos4.astype(np.float64)
+    pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
+    check_against_oracles("lj", pos64, box6, par, rc, 0.3, None,
+                          (F, E, W.T), (f32[:, :3], f32[:, 3], v32), "ka after 200 steps")
 
 
 def _plane_system(N, L, seed):
