@@ -31,8 +31,8 @@ This follows the reference's CPU-vs-GPU list comparison
 (hoomd/md/pytest/test_potential.py:952-1058), at full size. The oracle runs on every host core
 (OpenMP); the comparisons are vectorised over particle chunks.
 
-The 1M-particle fluid and the Kob-Andersen mixture are also checked after 200 steps of the
-product's own run (Bussi, Hilbert sort every 100 steps, the benchmark's settings): the engine's
+The 1M-particle fluid, the Kob-Andersen mixture and the 32-type Table system are also checked
+after 200 steps of the product's own run (Bussi, Hilbert sort every 100 steps, the benchmark's settings): the engine's
 forces, energies and virials through the Python API against the oracles at the resulting
 positions, with the same bars.
 """
@@ -105,7 +105,7 @@ def test_fullsize_nlist_and_forces_vs_oracle(systems, case):
         rc = np.full((nt, nt), 3.0)
         par = None
 
-    # neighbour sets: GPU (interleaved column-major list, lane-per-particle build) vs FP32 oracle
+    # neighbour sets: GPU (interleaved column-major list, candidate-stream build) vs FP32 oracle
     nl = GpuNlist(pos4, box6, rc, r_buff, layout="col4")
     n_o, l_o, h_o, info = O.build_nlist(pos4, box6, rc, r_buff, full=True, prec=32,
                                         nthreads=CORES)
@@ -247,6 +247,49 @@ def test_fullsize_ka_after_run_vs_oracle():
     pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
     check_against_oracles("lj", pos64, box6, par, rc, 0.3, None,
                           (F, E, W.T), (f32[:, :3], f32[:, 3], v32), "ka after 200 steps")
+
+
+def test_fullsize_table32_after_run_vs_oracle():
+    """The 524,288-particle 32-type system after 200 steps of the product's own run with its 528
+    tabulated potentials (Bussi at kT 1.5, dt 0.004, Hilbert sort every 100 steps, the
+    benchmark's settings): forces, energies and virials against the oracles at the resulting
+    positions."""
+    import hoomd_gb300 as hoomd
+    from hoomd_gb300 import md
+    from hoomd_gb300.workloads import to_snapshot
+
+    system = S.multitype_system(N=524288, ntypes=32, density=0.8, seed=1)
+    tabs = S.mixture_tables(32, r_min=0.8, r_cut=3.0, width=1000, seed=2)
+    sim = hoomd.Simulation(device=hoomd.device.GPU(), seed=1)
+    sim.create_state_from_snapshot(to_snapshot(system))
+    sim.state.thermalize_particle_momenta(hoomd.filter.All(), 1.5)
+    cell = md.nlist.Cell(buffer=0.4)
+    tab = md.pair.Table(nlist=cell, default_r_cut=3.0)
+    types = system.particles.types
+    for (i, j), v in tabs.items():
+        tab.params[(types[i], types[j])] = dict(r_min=v["r_min"], U=v["U"], F=v["F"])
+    sim.operations.integrator = md.Integrator(dt=0.004, forces=[tab], methods=[
+        md.methods.ConstantVolume(hoomd.filter.All(), md.methods.thermostats.Bussi(kT=1.5))])
+    sim.operations.tuners.append(hoomd.tune.ParticleSorter(trigger=100))
+    sim.run(200)
+    F, E, W = tab.forces, tab.energies, tab.virials
+    snap = sim.state.get_snapshot()
+    box6 = tuple(snap.configuration.box)
+    pos4 = O.make_pos4(snap.particles.position, snap.particles.typeid, 32)
+    nt = len(types)
+    _, _, opar, odata = table_params(nt, {k: (v["r_min"], v["U"], v["F"])
+                                          for k, v in tabs.items()})
+    rc = np.full((nt, nt), 3.0)
+    n, l, h, _ = O.build_nlist(pos4, box6, rc, 0.4, full=True, prec=32, nthreads=CORES)
+    f32, v32 = O.pair_forces("table", pos4, box6, opar, (rc ** 2).astype(np.float32), n, l, h,
+                             third_law=False, compute_virial=True,
+                             tdata=odata.astype(np.float32), prec=32, nthreads=CORES)
+    del l, h
+    assert cell.num_builds >= 2
+    pos64 = pos4.astype(np.float64)
+    pos64[:, 3] = O.types_as_w(O.pos_index_bits(pos4[:, 3], 32), 64)
+    check_against_oracles("table", pos64, box6, opar, rc, 0.4, odata,
+                          (F, E, W.T), (f32[:, :3], f32[:, 3], v32), "table32 after 200 steps")
 
 
 def _plane_system(N, L, seed):
