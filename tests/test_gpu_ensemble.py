@@ -223,3 +223,50 @@ def test_errors():
     small = system(100, 0.9, 1.0, 3)  # L = 4.8 < 2 r_list
     with pytest.raises(ValueError, match="too small"):
         hoomd.ReplicaEnsemble(dt=0.005).add_replica(small, kT=1.0)
+
+
+def test_benchmark_ensemble_first_lists_and_forces():
+    """All 256 replicas of the benchmark ensemble (N 500-20,000, density 0.7-0.9, 2.6 M particles,
+    the seeded systems of the replicas_256 configuration): after the first build every replica's
+    neighbour sets equal the FP32 oracle's, and its forces are no worse against the FP64 oracle
+    than the FP32 oracle's (largest error at most 1.5x the FP32 oracle's, values outside 1e-5
+    relative at most twice as many, plus the terms of pairs at the cut-off). The replica kernel
+    shifts particle i by its image before subtracting, which is closer to FP64 than the
+    reference's subtract-then-shift order at FP32, so the FP64 oracle is the reference here."""
+    import os
+
+    cores = os.cpu_count() or 1
+    systems = workloads.replica_systems(count=256, n_min=500, n_max=20000, seed=4)
+    ens = hoomd.ReplicaEnsemble(dt=0.005, r_cut=2.5, buffer=0.4)
+    for snap, kT, seed in systems:
+        ens.add_replica(snap, kT=kT, seed=seed)
+    ens.run(0)
+    for r, (s, _, _) in enumerate(systems):
+        N = s.particles.N
+        box = tuple(s.configuration.box)
+        pos32 = O.make_pos4(s.particles.position, np.zeros(N), 32)
+        n, l, h, _ = O.build_nlist(pos32, box, [[2.5]], 0.4, full=True, prec=32, nthreads=cores)
+        ref = O.neighbor_sets(n, l, h)
+        got = ens.neighbor_sets(r)
+        assert [len(x) for x in got] == [len(x) for x in ref], r
+        assert np.array_equal(np.concatenate(got), np.concatenate(ref)), r
+        kw = dict(third_law=False, compute_virial=False, nthreads=cores)
+        f32, _ = O.pair_forces("lj", pos32, box, [[1.0, 1.0]], np.float32([[6.25]]), n, l, h,
+                               prec=32, **kw)
+        b32, _ = O.pair_forces("lj", pos32, box, [[1.0, 1.0]], np.float32([[6.25]]), n, l, h,
+                               prec=32, abs_terms=2, **kw)
+        pos64 = O.make_pos4(pos32[:, :3].astype(np.float64), np.zeros(N), 64)
+        n, l, h, _ = O.build_nlist(pos64, box, [[2.5]], 0.4, full=True, prec=64, nthreads=cores)
+        f64, _ = O.pair_forces("lj", pos64, box, [[1.0, 1.0]], [[6.25]], n, l, h, prec=64, **kw)
+        b64, _ = O.pair_forces("lj", pos64, box, [[1.0, 1.0]], [[6.25]], n, l, h, prec=64,
+                               abs_terms=2, **kw)
+        _, _, _, F = state(ens, r)
+        ref = f64[:, :3]
+        band = b64[:, :3] + b32[:, :3].astype(np.float64)
+        e_gpu = np.abs(F[:, :3] - ref)
+        e_32 = np.abs(f32[:, :3].astype(np.float64) - ref)
+        assert (e_gpu <= 1.5 * e_32.max() + band + 1e-7 * np.abs(ref).max()).all(), (
+            r, float(e_gpu.max()), float(e_32.max()))
+        plain = 1e-5 * np.abs(ref) + 1e-5 * np.abs(ref).max() + band
+        out_gpu, out_32 = int((e_gpu > plain).sum()), int((e_32 > plain).sum())
+        assert out_gpu <= 2 * out_32 + 1e-4 * e_gpu.size, (r, out_gpu, out_32)
