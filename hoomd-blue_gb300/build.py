@@ -1,7 +1,7 @@
 """Build the GB300 extension in-tree.
 
-Outputs (git-ignored, rebuilt on every host because the GPU machine is aarch64 and this container
-x86-64):
+Outputs (git-ignored, rebuilt on every host, since GB300 hosts are aarch64 and build hosts may
+be x86-64):
   hoomd-blue_gb300/hoomd_gb300/libhoomd_gb300.so   CUDA kernels + the C ABI (include/hoomd_gb300.h)
   hoomd-blue_gb300/hoomd_gb300/_hoomd_gb300*.so    C++ host engine behind pybind11; calls the
                                                    kernels only through the C ABI

@@ -1,5 +1,5 @@
-"""Generate the golden fixtures in tests/golden/ from the reference (run in a container that has
-the HOOMD-blue source tree; the fixtures are committed so the GPU machine never needs that tree).
+"""Generate the golden fixtures in tests/golden/ from the reference (run where the HOOMD-blue
+source tree is present; the fixtures are committed so that test hosts never need that tree).
 
 Outputs
 -------
