@@ -1,7 +1,8 @@
 // ORACLE — test infrastructure only.
 //
 // A CPU restatement of HOOMD-blue 4.8.2's short-range MD step, written for this project and used
-// only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker. It is
+// only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg, as the reference the
+// GPU results are compared with or the timed CPU baseline. It is
 // never linked into, loaded by or called from the product (hoomd-blue_gb300/). Every routine cites
 // the reference file:line it follows (paths relative to the HOOMD-blue source tree).
 //

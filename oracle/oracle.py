@@ -2,7 +2,8 @@
 
 ctypes front end for the CPU restatement in ``oracle/md_oracle.cc`` (built by ``oracle/build.py``
 into ``oracle/_build/``). Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
-``bench.py`` import this module, and only as the checker or the timed CPU baseline; the product
+``bench.py`` import this module, and only as the reference the GPU results are compared with or
+the timed CPU baseline; the product
 package never does.
 
 Precision: every entry point exists at FP32 (``prec=32``, HOOMD built with
