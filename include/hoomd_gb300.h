@@ -98,7 +98,7 @@ typedef struct gb_cell_list_args
     const uint64_t* d_timestep;
     uint64_t* d_build_steps;
     /* optional, with d_build_steps: dangerous builds. When check_dist is set, check_delay > 1 and
-     * this build's step is exactly d_build_steps[0] + check_delay (the first check after the
+     * the step of the list build is exactly d_build_steps[0] + check_delay (the first check after the
      * delay found the list stale), *d_dangerous is incremented (hoomd/md/NeighborList.cc:
      * 1349-1356, 1405-1414). */
     uint64_t* d_dangerous;
