@@ -73,6 +73,16 @@ def test_c_abi_rejects_bad_arguments_without_gpu():
     assert lib.gb_pair_forces_lj(ctypes.byref(args), None, None) == abi.GB_ERR_INVALID
     b = abi.make_box((10, 10, 10))
     assert lib.gb_cell_dims(ctypes.byref(b), 3, 0.0, (ctypes.c_uint32 * 3)()) == abi.GB_ERR_INVALID
+    # kernel parameters of the tiled builds are checked before anything runs (the pointers below
+    # are never dereferenced)
+    fake = ctypes.c_void_p(0x1000)
+    nl = abi.NlistArgs(d_nlist=fake, d_n_neigh=fake, d_conditions=fake, d_Nmax=fake,
+                       d_cell_size=fake, d_xyzf=fake, d_cell_adj=fake, d_r_cut=fake,
+                       d_r_listsq=fake, ntypes=1, N=8, stride=8, adj_width=27)
+    for block, tpp in ((96, 0), (128, 2), (128, 16)):
+        nl.block_size, nl.threads_per_particle = block, tpp
+        assert lib.gb_nlist_build_binned(ctypes.byref(nl), None) == abi.GB_ERR_INVALID
+    assert b"threads_per_particle" in lib.gb_last_error()
 
 
 def test_table_pack_layout():
