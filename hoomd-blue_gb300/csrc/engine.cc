@@ -355,7 +355,7 @@ void NeighborList::allocate()
 void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count,
                                  uint32_t* d_cell_cond, uint32_t* d_nl_cond, cudaStream_t s,
                                  const uint64_t* d_timestep, uint64_t* d_build_steps,
-                                 uint64_t* d_dangerous)
+                                 uint64_t* d_dangerous, bool counts_zeroed)
     {
     ParticleData& pd = *pdata;
     gb_cell_list_args c {};
@@ -377,6 +377,7 @@ void NeighborList::enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count
     c.d_build_count = d_build_count;
     c.d_timestep = d_timestep;
     c.d_build_steps = d_build_steps;
+    c.counts_zeroed = counts_zeroed ? 1 : 0;
     check(gb_cell_list_build(&c, s), "gb_cell_list_build");
     gb_nlist_args a {};
     a.d_nlist = nlist.get();
@@ -1376,10 +1377,13 @@ void Integrator::enqueue_step_fused(cudaStream_t s)
     {
     ParticleData& pd = *pdata;
     DevStatus* ds = d_status.get();
-    const gb_step_one_args o = step_one_args(ds);
+    // step one also zeroes the cell counts, so the build's gated launches are two, not three
+    gb_step_one_args o = step_one_args(ds);
+    o.d_zero_words = nlist->cell_size.get();
+    o.n_zero_words = (uint32_t)nlist->cell_size.size();
     check(gb_md_step_one(&o, s), "gb_md_step_one");
     nlist->enqueue_build(&ds->rebuild, &ds->n_builds, ds->cell_cond, ds->nl_cond, s, &ds->timestep,
-                         ds->build_steps, &ds->n_dangerous);
+                         ds->build_steps, &ds->n_dangerous, true);
     PairForce& f = *forces[0];
     gb_pair_args a = f.pair_args(false);
     const gb_step_fuse fu = fuse_args(ds);

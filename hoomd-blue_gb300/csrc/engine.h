@@ -205,7 +205,8 @@ class NeighborList
     void build_sync();          // forced build with host-side overflow retry
     void enqueue_build(const uint32_t* d_gate, uint64_t* d_build_count, uint32_t* d_cell_cond,
                        uint32_t* d_nl_cond, cudaStream_t s, const uint64_t* d_timestep = nullptr,
-                       uint64_t* d_build_steps = nullptr, uint64_t* d_dangerous = nullptr);
+                       uint64_t* d_build_steps = nullptr, uint64_t* d_dangerous = nullptr,
+                       bool counts_zeroed = false);
     bool grow(const DevStatus& st); // returns true when a capacity grew
     // pairs of the list as tags (or as the current particle indices with local = true)
     std::vector<uint32_t> pair_list(bool full, bool local = false);

@@ -115,6 +115,8 @@ struct StepOneExtra
     const uint64_t* d_timestep; // BD: current step on the device, or NULL to use timestep
     uint64_t timestep;
     int noiseless;            // OverdampedViscous: no random force, v = F / gamma
+    uint32_t* zero;           // words set to zero on the way (the next build's cell counts)
+    unsigned int n_zero;
     };
 
 // MTTK thermostat state and the reduction scratch of step one.
@@ -135,6 +137,8 @@ __global__ void k_step_one(float4* __restrict__ pos, float4* __restrict__ vel,
                            StepOneExtra ex)
     {
     const unsigned int j = blockIdx.x * blockDim.x + threadIdx.x;
+    for (unsigned int w = j; w < ex.n_zero; w += gridDim.x * blockDim.x)
+        ex.zero[w] = 0u;
     bool moved = false;
     __shared__ float s_mttk;
     if (MTTK)
@@ -692,6 +696,8 @@ extern "C"
         ex.d_timestep = a->d_timestep;
         ex.timestep = a->timestep;
         ex.noiseless = a->noiseless;
+        ex.zero = a->d_zero_words;
+        ex.n_zero = a->d_zero_words ? a->n_zero_words : 0u;
         using K = void (*)(float4*, float4*, const float*, int*, unsigned int, gb_box, float,
                            float, const double*, StepOneCheck, MttkStep, StepOneExtra);
         K kern;

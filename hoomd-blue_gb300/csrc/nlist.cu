@@ -35,39 +35,49 @@ struct BuildRecord
     int dist_check;
     };
 
+// build statistics of one (non-gated-off) build; one thread
+__device__ void record_build(uint64_t* count, const uint64_t* timestep, uint64_t* build_steps,
+                             const BuildRecord& rec)
+    {
+    if (count)
+        *count += 1;
+    if (timestep && build_steps)
+        {
+        // NeighborList::needsUpdating (hoomd/md/NeighborList.cc:1349-1356, 1388-1414) for the
+        // step whose forces follow
+        const uint64_t T = *timestep + 1, last = build_steps[0];
+        if (last != ~0ull && T > last)
+            build_steps[1] = min(build_steps[1], min(T - last, (uint64_t)99));
+        if (rec.dangerous && rec.dist_check && rec.delay > 1 && last != ~0ull
+            && T == last + rec.delay)
+            *rec.dangerous += 1;
+        build_steps[0] = T;
+        }
+    }
+
 __global__ void k_zero_u32(unsigned int* p, size_t n, const uint32_t* gate, uint64_t* count,
                            const uint64_t* timestep, uint64_t* build_steps, BuildRecord rec)
     {
     if (gate && *gate == 0)
         return;
     if (blockIdx.x == 0 && threadIdx.x == 0)
-        {
-        if (count)
-            *count += 1;
-        if (timestep && build_steps)
-            {
-            // NeighborList::needsUpdating (hoomd/md/NeighborList.cc:1349-1356, 1388-1414) for the
-            // step whose forces follow
-            const uint64_t T = *timestep + 1, last = build_steps[0];
-            if (last != ~0ull && T > last)
-                build_steps[1] = min(build_steps[1], min(T - last, (uint64_t)99));
-            if (rec.dangerous && rec.dist_check && rec.delay > 1 && last != ~0ull
-                && T == last + rec.delay)
-                *rec.dangerous += 1;
-            build_steps[0] = T;
-            }
-        }
+        record_build(count, timestep, build_steps, rec);
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x)
         p[i] = 0;
     }
 
+// stats: the build statistics are kept here (the counts were zeroed by the caller's step)
 __global__ void k_cell_bin(const float4* __restrict__ pos, unsigned int N, gb_box box, uint3 dim,
                            unsigned int Nmax, unsigned int* cell_size, float4* xyzf,
-                           unsigned int* cell_type, unsigned int* cond, const uint32_t* gate)
+                           unsigned int* cell_type, unsigned int* cond, const uint32_t* gate,
+                           bool stats, uint64_t* count, const uint64_t* timestep,
+                           uint64_t* build_steps, BuildRecord rec)
     {
     if (gate && *gate == 0)
         return;
+    if (stats && blockIdx.x == 0 && threadIdx.x == 0)
+        record_build(count, timestep, build_steps, rec);
     const unsigned int dims[3] = {dim.x, dim.y, dim.z};
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
         {
@@ -1341,15 +1351,18 @@ extern "C"
                    "gb_cell_list_build: the build statistics need both the step and the record");
         const int sms = num_sms();
         const BuildRecord rec {a->d_dangerous, a->check_delay, a->check_dist};
-        k_zero_u32<<<min(div_up(ncell, 256), (unsigned)sms * 8), 256, 0, s>>>(
-            a->d_cell_size, ncell, a->d_gate, a->d_build_count, a->d_timestep, a->d_build_steps,
-            rec);
+        // with counts_zeroed the binning launch keeps the statistics (and there must be one)
+        const bool stats_in_bin = a->counts_zeroed && a->N > 0;
+        if (!stats_in_bin)
+            k_zero_u32<<<min(div_up(ncell, 256), (unsigned)sms * 8), 256, 0, s>>>(
+                a->counts_zeroed ? nullptr : a->d_cell_size, a->counts_zeroed ? 0 : ncell,
+                a->d_gate, a->d_build_count, a->d_timestep, a->d_build_steps, rec);
         if (a->N > 0)
             k_cell_bin<<<min(div_up(a->N, 256), (unsigned)sms * 16), 256, 0, s>>>(
                 reinterpret_cast<const float4*>(a->d_pos), a->N, a->box,
                 make_uint3(a->dim[0], a->dim[1], a->dim[2]), a->Nmax, a->d_cell_size,
                 reinterpret_cast<float4*>(a->d_xyzf), a->d_cell_type, a->d_conditions,
-                a->d_gate);
+                a->d_gate, stats_in_bin, a->d_build_count, a->d_timestep, a->d_build_steps, rec);
         if (a->deterministic)
             {
             const int wpb = 4;

@@ -33,7 +33,8 @@ class CellListArgs(ctypes.Structure):
                 ("d_cell_type", c_void), ("d_conditions", c_void), ("d_gate", c_void),
                 ("deterministic", c_int), ("d_build_count", c_void), ("d_timestep", c_void),
                 ("d_build_steps", c_void), ("d_dangerous", c_void),
-                ("check_delay", ctypes.c_uint32), ("check_dist", c_int)]
+                ("check_delay", ctypes.c_uint32), ("check_dist", c_int),
+                ("counts_zeroed", c_int)]
 
 
 class NlistArgs(ctypes.Structure):
@@ -68,7 +69,7 @@ class StepOneArgs(ctypes.Structure):
                 ("ndim", ctypes.c_uint32), ("seed", ctypes.c_uint32), ("d_timestep", c_void),
                 ("timestep", c_u64), ("noiseless", c_int), ("d_check_step", c_void),
                 ("d_last_update", c_void), ("check_delay", ctypes.c_uint32),
-                ("check_dist", c_int)]
+                ("check_dist", c_int), ("d_zero_words", c_void), ("n_zero_words", ctypes.c_uint32)]
 
 
 class StepFuse(ctypes.Structure):

@@ -104,6 +104,9 @@ typedef struct gb_cell_list_args
     uint64_t* d_dangerous;
     uint32_t check_delay;
     int check_dist;
+    /* the caller has zeroed d_cell_size (gb_step_one_args.d_zero_words in the same step): the
+       call does not zero it again, and the build statistics are kept by the binning launch */
+    int counts_zeroed;
     } gb_cell_list_args;
 
 int gb_cell_list_build(const gb_cell_list_args* args, void* stream);
@@ -544,6 +547,10 @@ typedef struct gb_step_one_args
     const uint64_t* d_last_update;
     uint32_t check_delay;
     int check_dist;
+    /* optional: n_zero_words words at d_zero_words are set to zero by the same launch (the cell
+       counts of the build that may follow, gb_cell_list_args.counts_zeroed) */
+    uint32_t* d_zero_words;
+    uint32_t n_zero_words;
     } gb_step_one_args;
 
 int gb_md_step_one(const gb_step_one_args* args, void* stream);
